@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""(T) wall-seconds at o=60, v=500 on GB300: split precision vs plain FP64.
+
+Workload (the shape the headline metric is quoted on): closed-shell (T), o=60 occupied,
+v=500 virtual orbitals, seed 3, tile extents drawn per index range from {16,24,32,40,48},
+synthetic inputs from exachem_gb300.generator (built on the GPU, ovvv 60 GB in HBM).
+
+A step is one batch of occupied triplets (i <= j <= k) of that workload, run through the
+C ABI on inputs already resident in HBM.  ``value`` is the wall time of the whole (T)
+call: with --mode ozaki the K timed steps cover every triplet once (timed_fraction 1);
+with --mode fp64 (hours at this size) the timed steps cover a fixed, evenly spread sample
+of triplets and the whole-call time is projected from it (timed_fraction < 1, stated).
+
+--impl reference times the reference's CPU (T) on the host cores (the C restatement of
+the oracle where the reference's own build is not present) on a bounded sample of the
+same workload and projects the whole-call time the same way.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "(T) wall-s at o=60,v=500: split-prec vs plain FP64 on GB300, |dE|<=1e-6 Eh"
+UNIT = "s"
+
+
+def workload_tiles(o, v, seed):
+    from exachem_gb300.generator import tiles_ragged
+    rng = np.random.default_rng([seed, 7])
+    return tiles_ragged(o, rng), tiles_ragged(v, rng)
+
+
+def triplet_list(o):
+    return np.array([(i, j, k) for i in range(o) for j in range(i, o) for k in range(j, o) if i != k],
+                    dtype=np.int32)
+
+
+def spread_sample(tri, n, offset=0):
+    """n triplets evenly spread over the list (deterministic)."""
+    idx = (np.arange(n) * len(tri)) // n + offset
+    return tri[np.clip(idx, 0, len(tri) - 1)]
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def dgemm_peak_tflops(torch):
+    """cuBLAS DGEMM 8192^3 (best of 3) - the FP64 denominator, measured in this run."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def profile_traffic(kernel):
+    """dram bytes per launch of `kernel` from a committed ncu summary, if present."""
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get(kernel)
+        except json.JSONDecodeError:
+            return None
+    return None
+
+
+def cpu_baseline_port(d_host_slabs, tri, reps=1):
+    """Times the oracle's C restatement on the host cores for one sample triplet."""
+    import oracle
+    best = 1e30
+    out = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = oracle.triplets_slabs(d_host_slabs, tri)
+        best = min(best, time.perf_counter() - t0)
+    return best, out, oracle.num_threads()
+
+
+def host_slabs_from_device(dev, tri):
+    """Host copies of what the sample triplets read (for the CPU baseline / checks)."""
+    need = sorted(set(int(x) for x in np.asarray(tri).ravel()))
+    h = {k: dev[k].cpu().numpy() for k in ("eps_occ", "eps_vir", "t1", "t2", "oovv", "ooov")}
+    h.update(o=dev["o"], v=dev["v"], seed=dev["seed"], ovvv_slabs={i: dev["ovvv"][i].cpu().numpy() for i in need})
+    return h
+
+
+def run_reference(args):
+    """CPU (T) of the reference on the host cores (bounded sample, projected)."""
+    import oracle
+    from exachem_gb300.generator import generate_host_slabs
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    o, v, seed = args.o, args.v, args.seed
+    tri_all = triplet_list(o)
+    sample = spread_sample(tri_all, 1, offset=len(tri_all) // 2)
+    t0 = time.perf_counter()
+    d = generate_host_slabs(o, v, seed, sample.ravel())
+    t_gen = time.perf_counter() - t0
+    # ExaChem's own CPU kernel materialises two ts^6 t3 blocks per task (ccsd_t_all_fused_cpu.hpp:
+    # 103-108), far beyond host memory at these tile sizes, and its build needs the reference
+    # tree; the timed CPU (T) is therefore the oracle's C restatement ("port").
+    kind = "port"
+    for _ in range(args.warmup):
+        oracle.triplets_slabs(d, sample)
+    times = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        oracle.triplets_slabs(d, sample)
+        times.append(time.perf_counter() - t1)
+    per_trip = statistics.mean(times) / len(sample)
+    value = per_trip * len(tri_all)
+    cores = oracle.num_threads()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator; no dataset)",
+        "config": {"workload": f"closed-shell (T) o={o} v={v} seed={seed}", "o": o, "v": v,
+                   "timed_fraction": len(sample) / len(tri_all), "projection": "per-triplet CPU time x triplets",
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"triplet {tuple(int(x) for x in sample[0])} of {len(tri_all)} "
+                                   f"(C restatement, OpenMP {cores} threads), projected to the whole call"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "host_generation_s": t_gen,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="auto", choices=["auto", "fp64", "ozaki", "learned"])
+    ap.add_argument("--slices", type=int, default=4)
+    ap.add_argument("--o", type=int, default=60)
+    ap.add_argument("--v", type=int, default=500)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--fp64-batch", type=int, default=2, help="triplets per step in fp64 mode")
+    ap.add_argument("--cpu-sample", type=int, default=1, help="triplets timed on the CPU baseline (0: skip)")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from exachem_gb300 import ccsd_t as ct
+    from exachem_gb300.generator import generate_device
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    mode = args.mode
+    if mode == "auto":
+        mode = "ozaki" if os.environ.get("CCSDT_SPLIT_READY", "0") == "1" else "fp64"
+    o, v, seed = args.o, args.v, args.seed
+    occ_tiles, vir_tiles = workload_tiles(o, v, seed)
+
+    t0 = time.perf_counter()
+    dev = generate_device(o, v, seed, device="cuda")
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    fp64_peak = dgemm_peak_tflops(torch)
+
+    ft = ct.FusedTriples(o, v, occ_tiles, vir_tiles, device=local)
+    ft.upload_dict(dev)
+    stream = torch.cuda.current_stream()
+    ft.set_stream(stream.cuda_stream)
+
+    tri_all = triplet_list(o)
+    mine = tri_all[rank::world]                       # independent triplets, no data-path collective
+    kw = {"slices": args.slices} if mode != "fp64" else {}
+    if mode == "fp64":
+        batches = [spread_sample(mine, args.fp64_batch, offset=s) for s in range(args.steps)]
+        warm = [spread_sample(mine, 1, offset=len(mine) // 3 + s) for s in range(args.warmup)]
+    else:
+        batches = np.array_split(mine, args.steps)
+        warm = [mine[: max(1, len(mine) // (4 * args.steps))] for _ in range(args.warmup)]
+    for b in warm:
+        ft.triplet_energies(b, mode, **kw)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches = 0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    esum4, esum5 = 0.0, 0.0
+    for b in batches:
+        g4, g5 = ft.triplet_energies(b, mode, **kw)
+        esum4 += float(g4.sum())
+        esum5 += float(g5.sum())
+        launches += ft.launch_count()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    elapsed = e0.elapsed_time(e1) * 1e-3
+    timed_trip = sum(len(b) for b in batches)
+    if dist:
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    frac = timed_trip / len(mine)
+    value = elapsed / frac                               # whole call (all triplets) on N GPUs
+
+    # per-phase device times of one representative triplet -> roofline of the d-sum GEMMs
+    i, j, k = (int(x) for x in mine[len(mine) // 2])
+    prof = [ft.profile_triplet(i, j, k, mode, **kw) for _ in range(3)]
+    gemm_ms = statistics.median(p[1] for p in prof)
+    gemm_flops = 12.0 * float(v) ** 4                      # 3 arrays x 2 terms x 2 v^4
+    achieved = gemm_flops / (gemm_ms * 1e-3) / 1e12
+    peaks = measured_peaks()
+    if mode == "fp64":
+        peak, peak_src = fp64_peak, "measured (cuBLAS DGEMM 8192^3 in this run; FP64 is not in MEASURED_PEAKS.json)"
+        kernel = "dmma_gemm_kernel"
+    else:
+        peak, peak_src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (burst)"
+        kernel = "ozaki_gemm_kernel"
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": profile_traffic(kernel), "kernel": kernel,
+            "per_launch_flops": gemm_flops, "launch_ms": gemm_ms, "peak_source": peak_src,
+            "phase_ms": dict(zip(["l_sum", "d_sum", "energy", "reduce"], prof[1]))}
+
+    # end to end through the C ABI with host (pinned) buffers: upload + one batch + readback
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        keys = ["eps_occ", "eps_vir", "t1", "t2", "oovv", "ooov", "ovvv"]
+        try:
+            host = {k: torch.empty(dev[k].shape, dtype=torch.float64, pin_memory=True) for k in keys}
+        except RuntimeError:
+            host = {k: torch.empty(dev[k].shape, dtype=torch.float64) for k in keys}
+        for k in keys:
+            host[k].copy_(dev[k])
+        harr = {k: host[k].numpy() for k in keys}
+        h2d = sum(a.nbytes for a in harr.values())
+        b = batches[0]
+        up, comp = [], []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            ta = time.perf_counter()
+            ft.upload(*[harr[k] for k in keys])
+            torch.cuda.synchronize()
+            tb = time.perf_counter()
+            ft.triplet_energies(b, mode, **kw)
+            tc = time.perf_counter()
+            up.append(tb - ta)
+            comp.append(tc - tb)
+        per_trip = min(comp) / len(b)
+        e2e_val = min(up) + per_trip * len(tri_all) / world
+        e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16 * len(b),
+               "upload_s": min(up), "projection": "one upload + per-triplet API time x triplets per GPU"}
+        del host, harr
+        ft.upload_dict(dev)
+
+    # CPU baseline: the oracle's C restatement on this host, one triplet of this workload
+    cpu = None
+    dE = None
+    if rank == 0 and args.cpu_sample > 0:
+        samp = spread_sample(tri_all, args.cpu_sample, offset=len(tri_all) // 2)
+        hs = host_slabs_from_device(dev, samp)
+        t_cpu, (c4, c5), cores = cpu_baseline_port(hs, samp)
+        g4, g5 = ft.triplet_energies(samp, mode, **kw)
+        dE = {"sample_triplets": samp.tolist(), "gpu_e_paren": g5.tolist(), "oracle_e_paren": c5.tolist(),
+              "max_rel": float(np.max(np.abs(g5 - c5) / np.maximum(np.abs(c5), 1e-300)))}
+        cpu = {"value": t_cpu / len(samp) * len(tri_all), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{len(samp)} triplet(s) {samp.tolist()} of {len(tri_all)} at o={o} v={v} "
+                         f"(oracle C restatement, {cores} OpenMP threads, {t_cpu:.1f} s), projected to the whole call"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / max(1, len(batches)),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if mode == "fp64" else "bf16-slices/f64", "data": "synthetic (seeded generator, built on GPU)",
+            "config": {"workload": f"closed-shell (T) o={o} v={v} seed={seed} ragged tiles", "o": o, "v": v,
+                       "mode": mode, "slices": args.slices if mode != "fp64" else None,
+                       "occ_tiles": occ_tiles, "vir_tiles": vir_tiles, "triplets_total": int(len(tri_all)),
+                       "triplets_timed": int(timed_trip), "timed_fraction": frac,
+                       "projection": None if frac >= 1 else "value = timed seconds / timed_fraction",
+                       "l2": "inputs (75 GB) and per-triplet scratch (3 GB) exceed L2; no flush"},
+            "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "energy_sample": dE, "partial_energy_timed": {"e_bracket_T": esum4, "e_paren_T": esum5},
+            "setup": {"generate_s": t_gen, "fp64_dgemm_tflops": fp64_peak},
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,211 @@
+"""Python binding of the C ABI in include/ccsdt.h (ctypes; no torch types cross it).
+
+Mirrors the call ExaChem makes, ``CCSD_T_Fused_Driver<T>::execute``
+(exachem/cc/ccsd_t/ccsd_t_fused_driver.hpp:91-546), which returns
+(E[T], E(T), work seconds, total seconds): ``FusedTriples.execute`` returns the same
+tuple.  The CUDA library must be built (``exachem_gb300.build.build_library``); if it is
+missing, loading fails loudly - there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIB
+
+_lib = None
+
+MODES = {"fp64": 0, "ozaki": 1, "learned": 2}
+
+
+class CCSDTError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"ccsdt status {status}: {msg}")
+        self.status = status
+
+
+class Layout(ctypes.Structure):
+    _fields_ = [("o", ctypes.c_int), ("v", ctypes.c_int), ("n_occ_tiles", ctypes.c_int),
+                ("occ_tiles", ctypes.POINTER(ctypes.c_int)), ("n_vir_tiles", ctypes.c_int),
+                ("vir_tiles", ctypes.POINTER(ctypes.c_int))]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("slices", ctypes.c_int), ("energy_budget", ctypes.c_double),
+                ("use_graph", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("e_bracket_T", ctypes.c_double), ("e_paren_T", ctypes.c_double),
+                ("abs_err_bound", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("flops_executed", ctypes.c_double), ("flops_ref_equiv", ctypes.c_double),
+                ("n_triplets", ctypes.c_long), ("n_tasks_ref", ctypes.c_long)]
+
+
+EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
+            "ccsdt_last_launch_count", "ccsdt_reference_op_count", "ccsdt_destroy",
+            "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet"]
+
+
+def load_library(path: str | os.PathLike | None = None):
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: build it with exachem_gb300.build.build_library()")
+    lib = ctypes.CDLL(str(p))
+    vp, ip, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)
+    lib.ccsdt_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Layout), ctypes.c_int]
+    lib.ccsdt_upload.argtypes = [vp] + [vp] * 7 + [ctypes.c_int]
+    lib.ccsdt_energy.argtypes = [vp, ctypes.POINTER(Opts), ctypes.POINTER(Result)]
+    lib.ccsdt_triplet_energies.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp]
+    lib.ccsdt_last_launch_count.argtypes = [vp]
+    lib.ccsdt_last_launch_count.restype = ctypes.c_long
+    lib.ccsdt_reference_op_count.argtypes = [ctypes.POINTER(Layout), dp, ctypes.POINTER(ctypes.c_long)]
+    lib.ccsdt_set_stream.argtypes = [vp, vp]
+    lib.ccsdt_profile_triplet.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    lib.ccsdt_destroy.argtypes = [vp]
+    lib.ccsdt_destroy.restype = None
+    lib.ccsdt_last_error.argtypes = [vp]
+    lib.ccsdt_last_error.restype = ctypes.c_char_p
+    lib.ccsdt_status_string.argtypes = [ctypes.c_int]
+    lib.ccsdt_status_string.restype = ctypes.c_char_p
+    for name in ("ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
+                 "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet"):
+        getattr(lib, name).restype = ctypes.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _tiles(n: int, tiles) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(tiles, dtype=np.int32))
+
+
+def make_layout(o: int, v: int, occ_tiles, vir_tiles):
+    ot, vt = _tiles(o, occ_tiles), _tiles(v, vir_tiles)
+    L = Layout(o, v, len(ot), ot.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(vt),
+               vt.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    return L, (ot, vt)
+
+
+def reference_op_count(o: int, v: int, occ_tiles, vir_tiles) -> tuple[float, int]:
+    """The reference's spin-orbital op count and task count for a tile layout."""
+    lib = load_library()
+    L, keep = make_layout(o, v, occ_tiles, vir_tiles)
+    ops, nt = ctypes.c_double(), ctypes.c_long()
+    st = lib.ccsdt_reference_op_count(ctypes.byref(L), ctypes.byref(ops), ctypes.byref(nt))
+    if st:
+        raise CCSDTError(st, lib.ccsdt_status_string(st).decode())
+    return ops.value, nt.value
+
+
+def _ptr(x) -> int:
+    """Host numpy array (C-contiguous float64) or a CUDA tensor -> raw address."""
+    if isinstance(x, np.ndarray):
+        if x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise TypeError("host inputs must be C-contiguous float64 arrays")
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        if not x.is_contiguous() or str(x.dtype) != "torch.float64":
+            raise TypeError("device inputs must be contiguous float64 tensors")
+        return x.data_ptr()
+    raise TypeError(f"unsupported input type {type(x)}")
+
+
+class FusedTriples:
+    """One (T) problem resident on one GPU."""
+
+    def __init__(self, o: int, v: int, occ_tiles=None, vir_tiles=None, ts: int = 40, device: int = 0):
+        from .generator import tiles_uniform
+        self.lib = load_library()
+        self.o, self.v = o, v
+        self.occ_tiles = list(occ_tiles) if occ_tiles is not None else tiles_uniform(o, ts)
+        self.vir_tiles = list(vir_tiles) if vir_tiles is not None else tiles_uniform(v, ts)
+        L, keep = make_layout(o, v, self.occ_tiles, self.vir_tiles)
+        h = ctypes.c_void_p()
+        st = self.lib.ccsdt_create(ctypes.byref(h), ctypes.byref(L), device)
+        if st:
+            raise CCSDTError(st, self.lib.ccsdt_status_string(st).decode())
+        self.h = h
+
+    def _check(self, st: int):
+        if st:
+            raise CCSDTError(st, self.lib.ccsdt_last_error(self.h).decode())
+
+    def upload(self, eps_occ, eps_vir, t1, t2, oovv, ooov, ovvv):
+        arrs = [eps_occ, eps_vir, t1, t2, oovv, ooov, ovvv]
+        on_dev = 0 if isinstance(arrs[0], np.ndarray) else 1
+        if any((isinstance(a, np.ndarray)) != (on_dev == 0) for a in arrs):
+            raise TypeError("pass all inputs on the host or all on the device")
+        self._keep = arrs
+        self._check(self.lib.ccsdt_upload(self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs], on_dev))
+
+    def upload_dict(self, d: dict):
+        self.upload(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], d["oovv"], d["ooov"], d["ovvv"])
+
+    @staticmethod
+    def opts(mode="fp64", slices=4, energy_budget=1e-9, use_graph=0) -> Opts:
+        o = Opts()
+        o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
+        o.slices = slices
+        o.energy_budget = energy_budget
+        o.use_graph = use_graph
+        return o
+
+    def energy(self, mode="fp64", **kw) -> dict:
+        op = self.opts(mode, **kw)
+        r = Result()
+        self._check(self.lib.ccsdt_energy(self.h, ctypes.byref(op), ctypes.byref(r)))
+        return {k: getattr(r, k) for k, _ in Result._fields_} | {"launches": self.launch_count()}
+
+    def triplet_energies(self, triplets, mode="fp64", **kw):
+        tri = np.ascontiguousarray(np.asarray(triplets, dtype=np.int32).reshape(-1, 3))
+        n = tri.shape[0]
+        e4, e5 = np.zeros(n), np.zeros(n)
+        op = self.opts(mode, **kw)
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self.lib.ccsdt_triplet_energies(self.h, ctypes.byref(op), n,
+                                                    tri.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                    e4.ctypes.data_as(dp), e5.ctypes.data_as(dp)))
+        return e4, e5
+
+    def set_stream(self, stream_handle: int | None):
+        """Run on an external cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(self.lib.ccsdt_set_stream(self.h, ctypes.c_void_p(stream_handle or 0)))
+
+    def profile_triplet(self, i: int, j: int, k: int, mode="fp64", **kw) -> list[float]:
+        """Device ms of [l-sum GEMMs, d-sum GEMMs, energy, reduction] for one triplet."""
+        out = (ctypes.c_double * 4)()
+        op = self.opts(mode, **kw)
+        self._check(self.lib.ccsdt_profile_triplet(self.h, ctypes.byref(op), i, j, k, out))
+        return list(out)
+
+    def launch_count(self) -> int:
+        return int(self.lib.ccsdt_last_launch_count(self.h))
+
+    def execute(self, mode="fp64", **kw):
+        """(E[T], E(T), work seconds, total seconds), as the reference driver returns."""
+        import time
+        t0 = time.perf_counter()
+        r = self.energy(mode, **kw)
+        return r["e_bracket_T"], r["e_paren_T"], r["seconds"], time.perf_counter() - t0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ccsdt_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def all_triplets(o: int) -> np.ndarray:
+    return np.array([(i, j, k) for i in range(o) for j in range(i, o) for k in range(j, o)], dtype=np.int32)

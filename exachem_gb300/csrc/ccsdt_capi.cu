@@ -1,0 +1,394 @@
+// C ABI of the GB300 closed-shell (T) library: handle, upload, energy.
+//
+// Replaces the per-task orchestration of ExaChem's fused driver
+// (exachem/cc/ccsd_t/ccsd_t_fused_driver.hpp:91-546 and ccsd_t_all_fused.hpp:77-286):
+// instead of gathering spin-orbital blocks on the host and copying them per task, every
+// input stays resident in HBM and each occupied triplet i <= j <= k is one unit of work.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ccsdt.h"
+#include "ccsdt_internal.cuh"
+#include "fp64_kernels.cuh"
+
+using namespace ccsdt;
+
+namespace {
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e__ = (call);                                                                      \
+    if(e__ != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+  } while(0)
+
+int multiplicity(int i, int j, int k) {
+  if(i == j && j == k) return 1;
+  if(i == j || j == k || i == k) return 3;
+  return 6;
+}
+
+} // namespace
+
+ccsdt_status ccsdt_handle::fail(ccsdt_status s, const std::string& msg) {
+  err = msg;
+  return s;
+}
+
+ccsdt_status ccsdt_handle::alloc(double** p, size_t n) {
+  if(n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**) p, n * sizeof(double));
+  if(e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(CCSDT_E_OOM, std::string("cudaMalloc of ") + std::to_string(n * sizeof(double)) +
+                               " bytes failed: " + cudaGetErrorString(e));
+  }
+  owned.push_back(*p);
+  return CCSDT_OK;
+}
+
+ccsdt_handle::~ccsdt_handle() {
+  cudaSetDevice(device);
+  for(void* p: owned) cudaFree(p);
+  for(void* p: owned_bytes) cudaFree(p);
+  for(void* p: slice_bufs) cudaFree(p);
+  if(ev0) cudaEventDestroy(ev0);
+  if(ev1) cudaEventDestroy(ev1);
+  for(auto& e: prof_ev)
+    if(e) cudaEventDestroy(e);
+  if(own_stream) cudaStreamDestroy(own_stream);
+}
+
+extern "C" {
+
+const char* ccsdt_status_string(ccsdt_status s) {
+  switch(s) {
+    case CCSDT_OK: return "ok";
+    case CCSDT_E_INVALID: return "invalid argument";
+    case CCSDT_E_BAD_LAYOUT: return "bad tile layout";
+    case CCSDT_E_OOM: return "out of memory";
+    case CCSDT_E_NONFINITE: return "non-finite value";
+    case CCSDT_E_TIMEOUT: return "device wait timed out";
+    case CCSDT_E_CUDA: return "CUDA error";
+    case CCSDT_E_STATE: return "call out of order";
+  }
+  return "unknown status";
+}
+
+const char* ccsdt_last_error(const ccsdt_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+long ccsdt_last_launch_count(const ccsdt_handle* h) { return h ? h->launches : -1; }
+
+ccsdt_status ccsdt_create(ccsdt_handle** out, const ccsdt_layout* L, int device) {
+  if(!out || !L) return CCSDT_E_INVALID;
+  *out = nullptr;
+  if(L->o <= 0 || L->v <= 0 || L->n_occ_tiles <= 0 || L->n_vir_tiles <= 0 || !L->occ_tiles ||
+     !L->vir_tiles)
+    return CCSDT_E_INVALID;
+  long so = 0, sv = 0;
+  for(int t = 0; t < L->n_occ_tiles; t++) {
+    if(L->occ_tiles[t] <= 0) return CCSDT_E_BAD_LAYOUT;
+    so += L->occ_tiles[t];
+  }
+  for(int t = 0; t < L->n_vir_tiles; t++) {
+    if(L->vir_tiles[t] <= 0) return CCSDT_E_BAD_LAYOUT;
+    sv += L->vir_tiles[t];
+  }
+  if(so != L->o || sv != L->v) return CCSDT_E_BAD_LAYOUT;
+  int ndev = 0;
+  if(cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
+    cudaGetLastError();
+    return CCSDT_E_CUDA;
+  }
+  ccsdt_handle* h = new ccsdt_handle();
+  h->device       = device;
+  h->o            = L->o;
+  h->v            = L->v;
+  h->occ_tiles.assign(L->occ_tiles, L->occ_tiles + L->n_occ_tiles);
+  h->vir_tiles.assign(L->vir_tiles, L->vir_tiles + L->n_vir_tiles);
+  if(cudaSetDevice(device) != cudaSuccess ||
+     cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+     cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return CCSDT_E_CUDA;
+  }
+  for(auto& e: h->prof_ev)
+    if(cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      delete h;
+      return CCSDT_E_CUDA;
+    }
+  h->stream = h->own_stream;
+  *out      = h;
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_set_stream(ccsdt_handle* h, void* stream) {
+  if(!h) return CCSDT_E_INVALID;
+  h->stream = stream ? (cudaStream_t) stream : h->own_stream;
+  return CCSDT_OK;
+}
+
+void ccsdt_destroy(ccsdt_handle* h) { delete h; }
+
+ccsdt_status ccsdt_upload(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
+                          const double* t1, const double* t2, const double* oovv,
+                          const double* ooov, const double* ovvv, int on_device) {
+  if(!h) return CCSDT_E_INVALID;
+  if(!eps_occ || !eps_vir || !t1 || !t2 || !oovv || !ooov || !ovvv)
+    return h->fail(CCSDT_E_INVALID, "ccsdt_upload: null input pointer");
+  CK(cudaSetDevice(h->device));
+  const size_t o = h->o, v = h->v;
+  const size_t n_eo = o, n_ev = v, n_t1 = o * v, n_t2 = o * o * v * v, n_oovv = n_t2,
+               n_ooov = o * o * o * v, n_ovvv = o * v * v * v;
+  if(!h->eo) {
+    ccsdt_status s;
+    if((s = h->alloc(&h->eo, n_eo)) || (s = h->alloc(&h->ev, n_ev)) || (s = h->alloc(&h->t1, n_t1)) ||
+       (s = h->alloc(&h->t2, n_t2)) || (s = h->alloc(&h->oovv, n_oovv)) ||
+       (s = h->alloc(&h->ooov, n_ooov)) || (s = h->alloc(&h->ovvv, n_ovvv)) ||
+       (s = h->alloc(&h->t2h, n_t2)) || (s = h->alloc(&h->ooovh, n_ooov)))
+      return s;
+    if(cudaMalloc((void**) &h->d_count, sizeof(unsigned long long)) != cudaSuccess) {
+      cudaGetLastError();
+      return h->fail(CCSDT_E_OOM, "cudaMalloc of the error counter failed");
+    }
+    h->owned_bytes.push_back(h->d_count);
+  }
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  struct {
+    double*       dst;
+    const double* src;
+    size_t        n;
+  } cp[] = {{h->eo, eps_occ, n_eo},  {h->ev, eps_vir, n_ev},     {h->t1, t1, n_t1},
+            {h->t2, t2, n_t2},       {h->oovv, oovv, n_oovv},    {h->ooov, ooov, n_ooov},
+            {h->ovvv, ovvv, n_ovvv}};
+  for(auto& c: cp) CK(cudaMemcpyAsync(c.dst, c.src, c.n * sizeof(double), kind, h->stream));
+  // finiteness of every input
+  CK(cudaMemsetAsync(h->d_count, 0, sizeof(unsigned long long), h->stream));
+  for(auto& c: cp) {
+    nonfinite_count_kernel<<<1024, 256, 0, h->stream>>>(c.dst, (long long) c.n, h->d_count);
+    CK(cudaGetLastError());
+  }
+  // kappa-contiguous copies for the l-sum contractions
+  transpose_mid_kernel<<<2048, 256, 0, h->stream>>>(h->t2, h->t2h, (int) o, (int) o, (long long) (v * v));
+  CK(cudaGetLastError());
+  transpose_mid_kernel<<<1024, 256, 0, h->stream>>>(h->ooov, h->ooovh, (int) o, (int) o, (long long) (o * v));
+  CK(cudaGetLastError());
+  unsigned long long bad = 0;
+  CK(cudaMemcpyAsync(&bad, h->d_count, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  h->uploaded = false;
+  if(bad) return h->fail(CCSDT_E_NONFINITE, "ccsdt_upload: " + std::to_string(bad) + " non-finite input values");
+  h->uploaded = true;
+  h->slices_ready = 0;
+  return CCSDT_OK;
+}
+
+} // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// FP64 path: per triplet, hole GEMMs (initialise P12/P34/P56), particle GEMMs (accumulate),
+// energy, partial reduction.
+
+ccsdt_status ccsdt_handle::ensure_scratch() {
+  const size_t v = this->v;
+  ccsdt_status s;
+  if(!P12) {
+    if((s = alloc(&P12, v * v * v)) || (s = alloc(&P34, v * v * v)) || (s = alloc(&P56, v * v * v)))
+      return s;
+    if((s = alloc(&part, 4 * (size_t) kEnergyBlocks)) || (s = alloc(&res, 2))) return s;
+  }
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_handle::ensure_triplet_slots(long n) {
+  if(etrip_cap >= n) return CCSDT_OK;
+  double*      p = nullptr;
+  ccsdt_status s = alloc(&p, 2 * (size_t) n);
+  if(s) return s;
+  etrip     = p;
+  etrip_cap = n;
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
+  const long long o = this->o, v = this->v, v2 = v * v, v3 = v2 * v;
+  // ---- l-sum (hole) contractions: C[(pair)][single] = -sum_l t(pair, l) (..l|..)
+  GemmBatch hb{};
+  auto      t2h_of = [&](int x) { return t2h + (long long) x * v2 * o; };                // [(a,b)][l]
+  auto      ooh_of = [&](int y, int z) { return ooovh + ((long long) y * o + z) * v * o; }; // [c][l]
+  const RowMap pair_nat = plain_rows(o), pair_swp = swapped_pair_rows((int) v, o), single = plain_rows(o);
+  // P12[(a,c)][b]: -t_il^{ac} (kl|jb) - t_kl^{ca} (il|jb)
+  hb.job[0] = GemmJob{{GemmTerm{t2h_of(i), pair_nat, ooh_of(k, j), single, (int) o, -1.0},
+                       GemmTerm{t2h_of(k), pair_swp, ooh_of(i, j), single, (int) o, -1.0}},
+                      2, P12, v2, v, 0.0};
+  // P34[(b,a)][c]: -t_il^{ab} (jl|kc) - t_jl^{ba} (il|kc)
+  hb.job[1] = GemmJob{{GemmTerm{t2h_of(i), pair_swp, ooh_of(j, k), single, (int) o, -1.0},
+                       GemmTerm{t2h_of(j), pair_nat, ooh_of(i, k), single, (int) o, -1.0}},
+                      2, P34, v2, v, 0.0};
+  // P56[(c,b)][a]: -t_jl^{bc} (kl|ia) - t_kl^{cb} (jl|ia)
+  hb.job[2] = GemmJob{{GemmTerm{t2h_of(j), pair_swp, ooh_of(k, i), single, (int) o, -1.0},
+                       GemmTerm{t2h_of(k), pair_nat, ooh_of(j, i), single, (int) o, -1.0}},
+                      2, P56, v2, v, 0.0};
+  if(profiling) cudaEventRecord(prof_ev[0], stream);
+  {
+    long long tiles = ((v2 + D_BM - 1) / D_BM) * ((v + D_BN - 1) / D_BN);
+    if(tiles > 0x7fffffffLL) return fail(CCSDT_E_INVALID, "too many GEMM tiles");
+    dmma_gemm_kernel<<<dim3((unsigned) tiles, 1, 3), D_THREADS, 0, stream>>>(hb);
+    launches++;
+  }
+  // ---- d-sum (particle) contractions: C[single][(pair)] += sum_d t(single, d) (pair|d)
+  GemmBatch pb{};
+  auto      t2_of   = [&](int x, int y) { return t2 + ((long long) x * o + y) * v2; }; // [a][d]
+  auto      ovvv_of = [&](int z) { return ovvv + (long long) z * v3; };                 // [(g,b)][d]
+  const RowMap arow = plain_rows(v), bnat = plain_rows(v), bswp = swapped_pair_rows((int) v, v);
+  // P12[a][(c,b)] += t_ij^{ad} (kc|bd) + t_ik^{ad} (jb|cd)
+  pb.job[0] = GemmJob{{GemmTerm{t2_of(i, j), arow, ovvv_of(k), bnat, (int) v, 1.0},
+                       GemmTerm{t2_of(i, k), arow, ovvv_of(j), bswp, (int) v, 1.0}},
+                      2, P12, v, v2, 1.0};
+  // P34[b][(a,c)] += t_ji^{bd} (kc|ad) + t_jk^{bd} (ia|cd)
+  pb.job[1] = GemmJob{{GemmTerm{t2_of(j, i), arow, ovvv_of(k), bswp, (int) v, 1.0},
+                       GemmTerm{t2_of(j, k), arow, ovvv_of(i), bnat, (int) v, 1.0}},
+                      2, P34, v, v2, 1.0};
+  // P56[c][(b,a)] += t_ki^{cd} (jb|ad) + t_kj^{cd} (ia|bd)
+  pb.job[2] = GemmJob{{GemmTerm{t2_of(k, i), arow, ovvv_of(j), bnat, (int) v, 1.0},
+                       GemmTerm{t2_of(k, j), arow, ovvv_of(i), bswp, (int) v, 1.0}},
+                      2, P56, v, v2, 1.0};
+  if(profiling) cudaEventRecord(prof_ev[1], stream);
+  {
+    long long tiles = ((v + D_BM - 1) / D_BM) * ((v2 + D_BN - 1) / D_BN);
+    dmma_gemm_kernel<<<dim3((unsigned) tiles, 1, 3), D_THREADS, 0, stream>>>(pb);
+    launches++;
+  }
+  if(profiling) cudaEventRecord(prof_ev[2], stream);
+  EnergyArgs ea{P12, P34, P56, oovv, t1, eo, ev, (int) o, (int) v, i, j, k, part};
+  energy_fp64_kernel<<<kEnergyBlocks, E_THREADS, 0, stream>>>(ea);
+  if(profiling) cudaEventRecord(prof_ev[3], stream);
+  reduce_parts_kernel<<<1, 32, 0, stream>>>(part, kEnergyBlocks, multiplicity(i, j, k) / 9.0, eout);
+  if(profiling) cudaEventRecord(prof_ev[4], stream);
+  launches += 2;
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("launch: ") + cudaGetErrorString(e));
+  return CCSDT_OK;
+}
+
+static bool valid_opts(const ccsdt_opts* o) {
+  return o && (o->mode == CCSDT_MODE_FP64 || o->mode == CCSDT_MODE_OZAKI || o->mode == CCSDT_MODE_LEARNED);
+}
+
+ccsdt_status ccsdt_handle::run_list(const ccsdt_opts* opts, long n, const int* tri_host) {
+  ccsdt_status s;
+  if((s = ensure_scratch()) || (s = ensure_triplet_slots(n))) return s;
+  launches = 0;
+  if(opts->mode != CCSDT_MODE_FP64) return run_split(opts, n, tri_host);
+  for(long t = 0; t < n; t++) {
+    const int i = tri_host[3 * t], j = tri_host[3 * t + 1], k = tri_host[3 * t + 2];
+    if(i == k) {
+      // i = j = k: W is symmetric in (a, b, c), so Z Y vanishes identically
+      cudaError_t e = cudaMemsetAsync(etrip + 2 * t, 0, 2 * sizeof(double), stream);
+      if(e != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e));
+      continue;
+    }
+    if((s = run_triplet_fp64(i, j, k, etrip + 2 * t))) return s;
+  }
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_triplet_energies(ccsdt_handle* h, const ccsdt_opts* opts, long n,
+                                               const int* tri, double* e_bracket, double* e_paren) {
+  if(!h) return CCSDT_E_INVALID;
+  if(!valid_opts(opts) || n < 0 || (n > 0 && (!tri || !e_bracket || !e_paren)))
+    return h->fail(CCSDT_E_INVALID, "ccsdt_triplet_energies: bad arguments");
+  if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_triplet_energies before a successful ccsdt_upload");
+  for(long t = 0; t < n; t++) {
+    const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
+    if(!(0 <= i && i <= j && j <= k && k < h->o))
+      return h->fail(CCSDT_E_INVALID, "triplet " + std::to_string(t) + " is not 0 <= i <= j <= k < o");
+  }
+  CK(cudaSetDevice(h->device));
+  ccsdt_status s = h->run_list(opts, n, tri);
+  if(s) return s;
+  std::vector<double> buf(2 * (size_t) n);
+  if(n) CK(cudaMemcpyAsync(buf.data(), h->etrip, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for(long t = 0; t < n; t++) {
+    e_bracket[t] = buf[2 * t];
+    e_paren[t]   = buf[2 * t + 1];
+  }
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, ccsdt_result* out) {
+  if(!h) return CCSDT_E_INVALID;
+  if(!valid_opts(opts) || !out) return h->fail(CCSDT_E_INVALID, "ccsdt_energy: bad arguments");
+  if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_energy before a successful ccsdt_upload");
+  CK(cudaSetDevice(h->device));
+  const int        o = h->o;
+  std::vector<int> tri;
+  for(int i = 0; i < o; i++)
+    for(int j = i; j < o; j++)
+      for(int k = j; k < o; k++) {
+        tri.push_back(i);
+        tri.push_back(j);
+        tri.push_back(k);
+      }
+  const long n = (long) tri.size() / 3;
+  CK(cudaEventRecord(h->ev0, h->stream));
+  ccsdt_status s = h->run_list(opts, n, tri.data());
+  if(s) return s;
+  reduce_triplets_kernel<<<1, 32, 0, h->stream>>>(h->etrip, n, h->res);
+  h->launches++;
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->ev1, h->stream));
+  double r[2];
+  CK(cudaMemcpyAsync(r, h->res, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+  std::memset(out, 0, sizeof(*out));
+  out->e_bracket_T    = r[0];
+  out->e_paren_T      = r[1];
+  out->abs_err_bound  = h->last_err_bound;
+  out->seconds        = ms * 1e-3;
+  const double vv     = h->v;
+  out->flops_executed = (double) (n - o) * 12.0 * vv * vv * vv * (vv + o); // i = j = k skipped
+  out->n_triplets     = n;
+  ccsdt_layout L{h->o, h->v, (int) h->occ_tiles.size(), h->occ_tiles.data(), (int) h->vir_tiles.size(),
+                 h->vir_tiles.data()};
+  double ops = 0;
+  long   nt  = 0;
+  if(ccsdt_reference_op_count(&L, &ops, &nt) == CCSDT_OK) {
+    out->flops_ref_equiv = ops;
+    out->n_tasks_ref     = nt;
+  }
+  if(!std::isfinite(r[0]) || !std::isfinite(r[1])) return h->fail(CCSDT_E_NONFINITE, "non-finite energy");
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_profile_triplet(ccsdt_handle* h, const ccsdt_opts* opts, int i, int j,
+                                              int k, double* out_ms) {
+  if(!h) return CCSDT_E_INVALID;
+  if(!valid_opts(opts) || !out_ms || !(0 <= i && i <= j && j <= k && k < h->o) || i == k)
+    return h->fail(CCSDT_E_INVALID, "ccsdt_profile_triplet: bad arguments (needs i <= j <= k, i < k)");
+  if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_profile_triplet before ccsdt_upload");
+  CK(cudaSetDevice(h->device));
+  const int tri[3] = {i, j, k};
+  h->profiling     = true;
+  ccsdt_status s   = h->run_list(opts, 1, tri);
+  h->profiling     = false;
+  if(s) return s;
+  CK(cudaStreamSynchronize(h->stream));
+  for(int q = 0; q < 4; q++) {
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, h->prof_ev[q], h->prof_ev[q + 1]));
+    out_ms[q] = ms;
+  }
+  return CCSDT_OK;
+}

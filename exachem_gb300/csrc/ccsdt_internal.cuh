@@ -1,0 +1,59 @@
+// Handle internals shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/ccsdt.h"
+
+constexpr int kEnergyBlocks = 1216; // 8 x 152 SMs
+
+struct ccsdt_handle {
+  int              device = 0, o = 0, v = 0;
+  std::vector<int> occ_tiles, vir_tiles;
+  cudaStream_t     stream = nullptr, own_stream = nullptr;
+  cudaEvent_t      prof_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  bool             profiling  = false;
+  cudaEvent_t      ev0 = nullptr, ev1 = nullptr;
+
+  // resident inputs (C-ABI layouts) and kappa-contiguous copies
+  double *eo = nullptr, *ev = nullptr, *t1 = nullptr, *t2 = nullptr, *oovv = nullptr,
+         *ooov = nullptr, *ovvv = nullptr, *t2h = nullptr, *ooovh = nullptr;
+  unsigned long long* d_count = nullptr;
+  bool                uploaded = false;
+  int                 slices_ready = 0;
+
+  // per-triplet scratch
+  double *P12 = nullptr, *P34 = nullptr, *P56 = nullptr, *part = nullptr, *res = nullptr;
+  double* etrip     = nullptr;
+  long    etrip_cap = 0;
+
+  // split-precision state: digit planes (BF16 or INT8), exponents, FP32 copies, ff scratch
+  std::vector<void*> slice_bufs;
+  int                slice_variant = -1, kp_v = 0, kp_o = 0;
+  void *             sl_t2 = nullptr, *sl_t2h = nullptr, *sl_ovvv = nullptr, *sl_ooovh = nullptr;
+  int *              ex_t2 = nullptr, *ex_t2h = nullptr, *ex_ovvv = nullptr, *ex_ooovh = nullptr;
+  long long          pl_t2 = 0, pl_t2h = 0, pl_ovvv = 0, pl_ooovh = 0;
+  float *            oovv_f = nullptr, *t1_f = nullptr;
+  float2 *           F12 = nullptr, *F34 = nullptr, *F56 = nullptr;
+
+  long        launches       = 0;
+  double      last_err_bound = 0.0;
+  std::string err;
+
+  std::vector<double*> owned;
+  std::vector<void*>   owned_bytes;
+
+  ~ccsdt_handle();
+  ccsdt_status fail(ccsdt_status s, const std::string& msg);
+  ccsdt_status alloc(double** p, size_t n);
+  ccsdt_status ensure_scratch();
+  ccsdt_status ensure_triplet_slots(long n);
+  ccsdt_status run_triplet_fp64(int i, int j, int k, double* eout);
+  ccsdt_status run_list(const ccsdt_opts* opts, long n, const int* tri_host);
+  ccsdt_status run_split(const ccsdt_opts* opts, long n, const int* tri_host);
+  ccsdt_status ensure_slices(int S, int variant);
+  ccsdt_status run_triplet_split(int i, int j, int k, int S, int variant, double* eout);
+};

@@ -1,0 +1,144 @@
+// Split-precision (Ozaki) contractions: slicing, slice GEMMs, float-float recombination.
+//
+// Every operand row r (length K along the contraction) is scaled by 2^-e_r, with e_r the
+// smallest exponent such that max_k |x[r,k]| (1 + 2^-7) < 2^e_r, and written as
+//   x[r,k] = 2^e_r  sum_{p=1..S} 2^{-7p} sigma_p[r,k],   sigma_p integer,
+//   |sigma_1| <= 127, |sigma_p| <= 64 (p > 1)   (round-to-nearest digit extraction).
+// Each digit is exact in BF16 and in INT8.  The product of two rows is then
+//   sum_k x y = 2^{e_x + e_y} sum_{l=2..S+1} 2^{-7l} L_l,   L_l = sum_{p+q=l} sum_k sigma_p tau_q.
+// For K <= 512 every L_l (l <= 7) is an integer below 2^24, so it is EXACT in an FP32
+// tensor-core accumulator (and in INT32 for the INT8 variant); the levels are combined in
+// float-float (pairs of FP32, ~48 bits), not FP64, because FP64 issue on GB300 is 1/64 of FP32.
+// Products with p + q > S + 1 are dropped; that truncation is the method's only error.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace ccsdt {
+
+constexpr int OZ_BITS = 7;
+constexpr int OZ_MAX_SLICES = 8;
+
+// ---------------------------------------------------------------------------------- float-float
+struct ff {
+  float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+  float s = a + b, z = s - a;
+  return ff{s, (a - (s - z)) + (b - z)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = ff_two_sum(a.hi, b.hi);
+  float lo = s.lo + a.lo + b.lo;
+  float hi = s.hi + lo;
+  return ff{hi, lo - (hi - s.hi)};
+}
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+  ff s = ff_two_sum(a.hi, b);
+  float lo = s.lo + a.lo;
+  float hi = s.hi + lo;
+  return ff{hi, lo - (hi - s.hi)};
+}
+__device__ __forceinline__ ff ff_scale(ff a, float s) { return ff{a.hi * s, a.lo * s}; } // s = small integer or 2^k
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  float hi = p + e;
+  return ff{hi, e - (hi - p)};
+}
+// a / b, one correction step
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+  float q1 = a.hi / b.hi;
+  ff    r  = ff_add(a, ff_scale(ff_mul(ff{q1, 0.f}, b), -1.f));
+  float q2 = r.hi / b.hi;
+  ff    s  = ff_two_sum(q1, q2);
+  return s;
+}
+__device__ __forceinline__ ff ff_from_double(double x) {
+  float hi = (float) x;
+  return ff{hi, (float) (x - (double) hi)};
+}
+
+// ---------------------------------------------------------------------------------- slicing
+// Rows of a dense FP64 array [R][K] -> S digit planes [S][R][Kp] (Kp >= K, zero padded) and
+// exponents e[R].  One warp per row.
+template<typename T>
+__device__ __forceinline__ T oz_digit(double d);
+template<>
+__device__ __forceinline__ __nv_bfloat16 oz_digit<__nv_bfloat16>(double d) {
+  return __float2bfloat16_rn((float) d);
+}
+template<>
+__device__ __forceinline__ int8_t oz_digit<int8_t>(double d) {
+  return (int8_t) (int) d;
+}
+
+template<typename T>
+__global__ void oz_slice_rows_kernel(const double* __restrict__ x, long long R, int K, int Kp, int S,
+                                     T* __restrict__ out, long long plane, int* __restrict__ exps) {
+  const int       lane = threadIdx.x & 31;
+  const long long warps = (long long) gridDim.x * (blockDim.x >> 5);
+  for(long long r = (long long) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < R; r += warps) {
+    const double* row = x + r * K;
+    double        mx  = 0.0;
+    for(int k = lane; k < K; k += 32) mx = fmax(mx, fabs(row[k]));
+#pragma unroll
+    for(int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    int e = 0;
+    if(mx > 0.0) frexp(mx * (1.0 + 1.0 / 128.0), &e); // mx (1 + 2^-7) < 2^e
+    if(lane == 0) exps[r] = e;
+    for(int k = lane; k < Kp; k += 32) {
+      double y = k < K ? ldexp(row[k], -e) : 0.0;
+      for(int p = 0; p < S; p++) {
+        y        = y * 128.0;
+        double d = rint(y);
+        y        = y - d;
+        out[(long long) p * plane + r * Kp + k] = oz_digit<T>(d);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------- GEMM
+// One term: sum over kappa of A(m, kappa) B(n, kappa), each operand given as digit planes.
+// Row r of an operand lives at plane base + rid(r) * Kp, rid(r) = (r / q) * h + (r % q) * l.
+struct OzRows {
+  long long h, l;
+  int       q;
+};
+__host__ __device__ inline long long oz_rid(const OzRows& m, long long r) { return (r / m.q) * m.h + (r % m.q) * m.l; }
+inline OzRows oz_plain() { return OzRows{0, 1, 1 << 30}; }
+inline OzRows oz_swapped(int q) { return OzRows{1, q, q}; } // r = x q + y -> y q + x
+
+struct OzTerm {
+  const void* A;       // digit planes of A: plane stride planeA elements
+  const int*  eA;      // exponents, indexed by rid
+  OzRows      ma;
+  long long   planeA;
+  const void* B;
+  const int*  eB;
+  OzRows      mb;
+  long long   planeB;
+  int         Kp;      // padded contraction length (multiple of the k chunk)
+  float       sign;
+};
+
+struct OzJob {
+  OzTerm    t[2];
+  int       nterms;
+  float2*   C; // ff output [M][N]
+  long long M, N;
+  int       accumulate; // 0: C = result, 1: C += result
+};
+
+struct OzBatch {
+  OzJob job[3];
+  int   S; // slices used (<= planes stored)
+};
+
+} // namespace ccsdt

@@ -1,0 +1,417 @@
+// Split-precision (T): Ozaki slice contractions on the tensor cores, float-float
+// recombination and a float-float energy.  Same contraction plan as the FP64 path
+// (three partial arrays P12 / P34 / P56 per triplet; l-sum GEMMs initialise them, d-sum
+// GEMMs accumulate), with every GEMM run on digit planes.
+//
+// Two tensor-core variants of the slice products, selected by opts->reserved[0]:
+//   0: BF16 digits, mma.sync m16n8k16 with FP32 accumulation (exact per level, K <= 512)
+//   1: INT8 digits, mma.sync m16n8k32 with INT32 accumulation (exact per level)
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+
+#include "ccsdt_internal.cuh"
+#include "fp64_kernels.cuh"
+#include "ozaki.cuh"
+
+using namespace ccsdt;
+
+namespace {
+
+constexpr int OZ_BM = 64, OZ_BN = 64, OZ_THREADS = 256, OZ_LEVELS = 4, OZ_KWIN = 512;
+
+template<typename T>
+struct OzTraits;
+template<>
+struct OzTraits<__nv_bfloat16> {
+  static constexpr int KC = 32;        // contraction elements per smem chunk
+  static constexpr int KSTEP = 16;     // per mma
+  using Acc = float;
+};
+template<>
+struct OzTraits<int8_t> {
+  static constexpr int KC = 64;
+  static constexpr int KSTEP = 32;
+  using Acc = int;
+};
+
+__device__ __forceinline__ void mma_k(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+               "{%8,%9}, {%0,%1,%2,%3};\n"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+__device__ __forceinline__ void mma_k(int (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile("mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+               "{%8,%9}, {%0,%1,%2,%3};\n"
+               : "+r"(c[0]), "+r"(c[1]), "+r"(c[2]), "+r"(c[3])
+               : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Fragment loads from a [rows][ROWB bytes] smem tile.  For both variants the 32-bit word
+// at (row, word w) holds 2 bf16 / 4 int8 consecutive along k; the m16n8k16 (bf16) and
+// m16n8k32 (s8) fragments use words: a0 (g, t) a1 (g+8, t) a2 (g, t+4) a3 (g+8, t+4);
+// b0 (n = g, t) b1 (g, t+4), with k-step offset ks words.
+__device__ __forceinline__ uint32_t lds32(const unsigned char* base, int row, int word) {
+  return *reinterpret_cast<const uint32_t*>(base + row * 80 + word * 4);
+}
+
+template<typename T>
+__global__ void __launch_bounds__(OZ_THREADS) oz_gemm_kernel(const __grid_constant__ OzBatch batch) {
+  using Tr  = OzTraits<T>;
+  using Acc = typename Tr::Acc;
+  const OzJob&    J       = batch.job[blockIdx.z];
+  const int       S       = batch.S;
+  const long long tiles_n = (J.N + OZ_BN - 1) / OZ_BN;
+  const long long m0 = (long long) (blockIdx.x / tiles_n) * OZ_BM, n0 = (long long) (blockIdx.x % tiles_n) * OZ_BN;
+  if(m0 >= J.M || n0 >= J.N) return;
+
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned char* As = smem;                               // [S][64 rows][80 B]
+  unsigned char* Bs = smem + (size_t) S * OZ_BM * 80;     // [S][64 rows][80 B]
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp >> 2) * 32, wn = (warp & 3) * 16; // 2 x 4 warps, warp tile 32 x 16
+  const int g = lane >> 2, t = lane & 3;
+
+  ff out[2][2][4];
+#pragma unroll
+  for(int x = 0; x < 2; x++)
+#pragma unroll
+    for(int y = 0; y < 2; y++)
+#pragma unroll
+      for(int z = 0; z < 4; z++) out[x][y][z] = ff{0.f, 0.f};
+
+  for(int term = 0; term < J.nterms; term++) {
+    const OzTerm& T_ = J.t[term];
+    // exponents of this thread's output rows / columns
+    int ea[2][2], eb[2][2];
+#pragma unroll
+    for(int x = 0; x < 2; x++)
+#pragma unroll
+      for(int h = 0; h < 2; h++) {
+        long long m = m0 + wm + x * 16 + g + h * 8;
+        ea[x][h]    = m < J.M ? T_.eA[oz_rid(T_.ma, m)] : 0;
+      }
+#pragma unroll
+    for(int y = 0; y < 2; y++)
+#pragma unroll
+      for(int e = 0; e < 2; e++) {
+        long long n = n0 + wn + y * 8 + 2 * t + e;
+        eb[y][e]    = n < J.N ? T_.eB[oz_rid(T_.mb, n)] : 0;
+      }
+    const T* Ab = static_cast<const T*>(T_.A);
+    const T* Bb = static_cast<const T*>(T_.B);
+    // loader: thread -> (row = tid / 4, 16-byte word group (tid % 4)) per plane
+    const int       lr = tid >> 2, lq = tid & 3;
+    const long long ma = m0 + lr, nb = n0 + lr;
+    const bool      va = ma < J.M, vb = nb < J.N;
+    const long long ra = va ? oz_rid(T_.ma, ma) * T_.Kp : 0, rb = vb ? oz_rid(T_.mb, nb) * T_.Kp : 0;
+
+    for(int lvl0 = 2; lvl0 <= S + 1; lvl0 += OZ_LEVELS) {
+      for(int kw = 0; kw < T_.Kp; kw += OZ_KWIN) {
+        const int kend = min(T_.Kp, kw + OZ_KWIN);
+        Acc       acc[OZ_LEVELS][2][2][4];
+#pragma unroll
+        for(int l = 0; l < OZ_LEVELS; l++)
+#pragma unroll
+          for(int x = 0; x < 2; x++)
+#pragma unroll
+            for(int y = 0; y < 2; y++)
+#pragma unroll
+              for(int z = 0; z < 4; z++) acc[l][x][y][z] = 0;
+        for(int k0 = kw; k0 < kend; k0 += Tr::KC) {
+          __syncthreads();
+          for(int p = 0; p < S; p++) {
+            // 64 bytes of row data per plane: 4 x 16 B, one per thread
+            uint4 va4 = make_uint4(0, 0, 0, 0), vb4 = make_uint4(0, 0, 0, 0);
+            if(va) va4 = *reinterpret_cast<const uint4*>(Ab + p * T_.planeA + ra + k0 + lq * (16 / sizeof(T)));
+            if(vb) vb4 = *reinterpret_cast<const uint4*>(Bb + p * T_.planeB + rb + k0 + lq * (16 / sizeof(T)));
+            *reinterpret_cast<uint4*>(As + ((size_t) p * OZ_BM + lr) * 80 + lq * 16) = va4;
+            *reinterpret_cast<uint4*>(Bs + ((size_t) p * OZ_BN + lr) * 80 + lq * 16) = vb4;
+          }
+          __syncthreads();
+#pragma unroll
+          for(int ks = 0; ks < Tr::KC / Tr::KSTEP; ks++) {
+            const int w0 = ks * 8; // 8 words (32 B) per k-step
+            for(int q = 1; q <= S; q++) {
+              const unsigned char* Bq = Bs + (size_t) (q - 1) * OZ_BN * 80;
+              uint32_t             bf[2][2];
+#pragma unroll
+              for(int y = 0; y < 2; y++) {
+                bf[y][0] = lds32(Bq, wn + y * 8 + g, w0 + t);
+                bf[y][1] = lds32(Bq, wn + y * 8 + g, w0 + t + 4);
+              }
+              for(int p = 1; p <= S; p++) {
+                const int l = p + q - lvl0;
+                if(l < 0 || l >= OZ_LEVELS) continue;
+                const unsigned char* Ap = As + (size_t) (p - 1) * OZ_BM * 80;
+#pragma unroll
+                for(int x = 0; x < 2; x++) {
+                  uint32_t af[4];
+                  af[0] = lds32(Ap, wm + x * 16 + g, w0 + t);
+                  af[1] = lds32(Ap, wm + x * 16 + g + 8, w0 + t);
+                  af[2] = lds32(Ap, wm + x * 16 + g, w0 + t + 4);
+                  af[3] = lds32(Ap, wm + x * 16 + g + 8, w0 + t + 4);
+#pragma unroll
+                  for(int y = 0; y < 2; y++) {
+                    // select the level accumulator without dynamic register indexing
+#pragma unroll
+                    for(int ll = 0; ll < OZ_LEVELS; ll++)
+                      if(ll == l) mma_k(acc[ll][x][y], af, bf[y]);
+                  }
+                }
+              }
+            }
+          }
+        }
+        // fold this window's levels into the float-float output (exact power-of-two scaling)
+#pragma unroll
+        for(int ll = 0; ll < OZ_LEVELS; ll++) {
+          const int lev = lvl0 + ll;
+          if(lev > S + 1) break;
+#pragma unroll
+          for(int x = 0; x < 2; x++)
+#pragma unroll
+            for(int y = 0; y < 2; y++)
+#pragma unroll
+              for(int z = 0; z < 4; z++) {
+                const int   h = z >> 1, e = z & 1;
+                const float sc = ldexpf(T_.sign, ea[x][h] + eb[y][e] - OZ_BITS * lev);
+                out[x][y][z]   = ff_add_f(out[x][y][z], (float) acc[ll][x][y][z] * sc);
+              }
+        }
+      }
+    }
+  }
+  // C (+)= out
+#pragma unroll
+  for(int x = 0; x < 2; x++)
+#pragma unroll
+    for(int y = 0; y < 2; y++)
+#pragma unroll
+      for(int z = 0; z < 4; z++) {
+        const int       h = z >> 1, e = z & 1;
+        const long long m = m0 + wm + x * 16 + g + h * 8, n = n0 + wn + y * 8 + 2 * t + e;
+        if(m >= J.M || n >= J.N) continue;
+        float2* cp = J.C + m * J.N + n;
+        ff      r  = out[x][y][z];
+        if(J.accumulate) {
+          float2 old = *cp;
+          r          = ff_add(r, ff{old.x, old.y});
+        }
+        *cp = make_float2(r.hi, r.lo);
+      }
+}
+
+// ----------------------------------------------------------------------------- energy (ff)
+struct SplitEnergyArgs {
+  const float2 *P12, *P34, *P56;
+  const float * oovv, *t1; // FP32 copies
+  const double *eo, *ev;
+  int           o, v, i, j, k;
+  double*       part;
+};
+
+__global__ void __launch_bounds__(E_THREADS) energy_split_kernel(const __grid_constant__ SplitEnergyArgs A) {
+  const int       v = A.v, o = A.o;
+  const long long v2 = (long long) v * v, n = v2 * v;
+  const int       i = A.i, j = A.j, k = A.k;
+  const ff        eijk = ff_add(ff_add(ff_from_double(A.eo[i]), ff_from_double(A.eo[j])), ff_from_double(A.eo[k]));
+  const float *   Ojk = A.oovv + ((long long) j * o + k) * v2, *Oik = A.oovv + ((long long) i * o + k) * v2,
+              *Oij = A.oovv + ((long long) i * o + j) * v2;
+  const float *ti = A.t1 + (long long) i * v, *tj = A.t1 + (long long) j * v, *tk = A.t1 + (long long) k * v;
+  ff           s4{0.f, 0.f}, s5{0.f, 0.f};
+  for(long long e = (long long) blockIdx.x * blockDim.x + threadIdx.x; e < n;
+      e += (long long) gridDim.x * blockDim.x) {
+    const int a = (int) (e / v2), b = (int) ((e / v) % v), c = (int) (e % v);
+    auto      W = [&](int x, int y, int z) {
+      float2 p = A.P12[((long long) x * v + z) * v + y], q = A.P34[((long long) y * v + x) * v + z],
+             r = A.P56[((long long) z * v + y) * v + x];
+      return ff_add(ff_add(ff{p.x, p.y}, ff{q.x, q.y}), ff{r.x, r.y});
+    };
+    auto SG = [&](int x, int y, int z) {
+      return Ojk[(long long) y * v + z] * ti[x] + Oik[(long long) x * v + z] * tj[y] + Oij[(long long) x * v + y] * tk[z];
+    };
+    const ff wabc = W(a, b, c), wbca = W(b, c, a), wcab = W(c, a, b);
+    const ff wacb = W(a, c, b), wbac = W(b, a, c), wcba = W(c, b, a);
+    const ff z    = ff_add(ff_add(ff_scale(wabc, 4.f), wbca), wcab);
+    const ff y4   = ff_add(ff_add(ff_scale(wabc, 3.f), ff_scale(wacb, -1.f)),
+                           ff_add(ff_scale(wbac, -1.f), ff_scale(wcba, -1.f)));
+    const float sgl = 3.f * SG(a, b, c) - SG(a, c, b) - SG(b, a, c) - SG(c, b, a);
+    const ff    y5  = ff_add_f(y4, sgl);
+    const ff    d   = ff_add(ff_add(ff_add(eijk, ff_from_double(-A.ev[a])), ff_from_double(-A.ev[b])),
+                        ff_from_double(-A.ev[c]));
+    s4 = ff_add(s4, ff_div(ff_mul(z, y4), d));
+    s5 = ff_add(s5, ff_div(ff_mul(z, y5), d));
+  }
+  CSum c4, c5;
+  c4.add((double) s4.hi);
+  c4.add((double) s4.lo);
+  c5.add((double) s5.hi);
+  c5.add((double) s5.lo);
+  block_reduce_csum(c4, c5, A.part + 4 * (long long) blockIdx.x);
+}
+
+__global__ void to_float_kernel(const double* x, float* y, long long n) {
+  for(long long e = (long long) blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long) gridDim.x * blockDim.x)
+    y[e] = (float) x[e];
+}
+
+int multiplicity(int i, int j, int k) {
+  if(i == j && j == k) return 1;
+  if(i == j || j == k || i == k) return 3;
+  return 6;
+}
+
+template<typename T>
+size_t oz_smem(int S) {
+  return (size_t) S * (OZ_BM + OZ_BN) * 80;
+}
+
+} // namespace
+
+// ------------------------------------------------------------------------------------ host
+ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
+  if(S < 1 || S > OZ_MAX_SLICES) return fail(CCSDT_E_INVALID, "slices must be in 1..8");
+  if(slices_ready >= S && slice_variant == variant) return CCSDT_OK;
+  const long long o = this->o, v = this->v;
+  const size_t    esz = variant == 0 ? 2 : 1;
+  const int       kc  = variant == 0 ? 32 : 64;
+  const int       Kpv = (int) ((v + kc - 1) / kc * kc), Kpo = (int) ((o + kc - 1) / kc * kc);
+  // drop old planes
+  for(void* p: slice_bufs) cudaFree(p);
+  slice_bufs.clear();
+  slices_ready = 0;
+  auto grab = [&](void** p, size_t bytes) -> ccsdt_status {
+    cudaError_t e = cudaMalloc(p, bytes ? bytes : 1);
+    if(e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(CCSDT_E_OOM, "slice planes: cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+    }
+    slice_bufs.push_back(*p);
+    return CCSDT_OK;
+  };
+  struct Src {
+    const double* x;
+    long long     R;
+    int           K, Kp;
+    void**        planes;
+    int**         exps;
+    long long*    plane;
+  } src[4] = {{t2, o * o * v, (int) v, Kpv, &sl_t2, &ex_t2, &pl_t2},
+              {t2h, o * v * v, (int) o, Kpo, &sl_t2h, &ex_t2h, &pl_t2h},
+              {ovvv, o * v * v, (int) v, Kpv, &sl_ovvv, &ex_ovvv, &pl_ovvv},
+              {ooovh, o * o * v, (int) o, Kpo, &sl_ooovh, &ex_ooovh, &pl_ooovh}};
+  ccsdt_status s;
+  for(auto& q: src) {
+    *q.plane = q.R * q.Kp;
+    if((s = grab(q.planes, (size_t) S * q.R * q.Kp * esz)) || (s = grab((void**) q.exps, (size_t) q.R * sizeof(int))))
+      return s;
+    if(variant == 0)
+      oz_slice_rows_kernel<__nv_bfloat16><<<4096, 256, 0, stream>>>(q.x, q.R, q.K, q.Kp, S, (__nv_bfloat16*) *q.planes, *q.plane, *q.exps);
+    else
+      oz_slice_rows_kernel<int8_t><<<4096, 256, 0, stream>>>(q.x, q.R, q.K, q.Kp, S, (int8_t*) *q.planes, *q.plane, *q.exps);
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("slicing: ") + cudaGetErrorString(e));
+  }
+  kp_v = Kpv;
+  kp_o = Kpo;
+  // FP32 copies for the energy's singles terms; ff scratch
+  if((s = grab((void**) &oovv_f, (size_t) o * o * v * v * sizeof(float))) ||
+     (s = grab((void**) &t1_f, (size_t) o * v * sizeof(float))) ||
+     (s = grab((void**) &F12, (size_t) v * v * v * sizeof(float2))) ||
+     (s = grab((void**) &F34, (size_t) v * v * v * sizeof(float2))) ||
+     (s = grab((void**) &F56, (size_t) v * v * v * sizeof(float2))))
+    return s;
+  to_float_kernel<<<2048, 256, 0, stream>>>(oovv, oovv_f, o * o * v * v);
+  to_float_kernel<<<64, 256, 0, stream>>>(t1, t1_f, o * v);
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("to_float: ") + cudaGetErrorString(e));
+  slices_ready  = S;
+  slice_variant = variant;
+  return CCSDT_OK;
+}
+
+template<typename T>
+static ccsdt_status launch_oz(ccsdt_handle* h, const OzBatch& b, long long M, long long N) {
+  const long long tiles = ((M + OZ_BM - 1) / OZ_BM) * ((N + OZ_BN - 1) / OZ_BN);
+  const size_t    sm    = oz_smem<T>(b.S);
+  cudaError_t     e     = cudaFuncSetAttribute(oz_gemm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+  if(e != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string("smem attr: ") + cudaGetErrorString(e));
+  oz_gemm_kernel<T><<<dim3((unsigned) tiles, 1, 3), OZ_THREADS, sm, h->stream>>>(b);
+  h->launches++;
+  e = cudaGetLastError();
+  if(e != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string("oz_gemm launch: ") + cudaGetErrorString(e));
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int variant, double* eout) {
+  const long long o = this->o, v = this->v, v2 = v * v;
+  const size_t    esz = variant == 0 ? 2 : 1;
+  auto at = [&](const void* base, long long elems) { return (const void*) ((const char*) base + elems * esz); };
+  // l-sum: rows of t2h are (x, (a, b)), rows of ooovh are (y, z, c)
+  auto t2h_t = [&](int x, OzRows m) {
+    return std::make_tuple(at(sl_t2h, (long long) x * v2 * kp_o), ex_t2h + (long long) x * v2, m);
+  };
+  auto ooh_t = [&](int y, int z) {
+    return std::make_tuple(at(sl_ooovh, ((long long) y * o + z) * v * kp_o), ex_ooovh + ((long long) y * o + z) * v);
+  };
+  auto hole = [&](int xa, OzRows ma, int yb, int zb) {
+    auto [A, eA, mA] = t2h_t(xa, ma);
+    auto [B, eB]     = ooh_t(yb, zb);
+    return OzTerm{A, eA, mA, pl_t2h, B, eB, oz_plain(), pl_ooovh, kp_o, -1.f};
+  };
+  const OzRows nat = oz_plain(), swp = oz_swapped((int) v);
+  OzBatch      hb{};
+  hb.S      = S;
+  hb.job[0] = OzJob{{hole(i, nat, k, j), hole(k, swp, i, j)}, 2, F12, v2, v, 0};
+  hb.job[1] = OzJob{{hole(i, swp, j, k), hole(j, nat, i, k)}, 2, F34, v2, v, 0};
+  hb.job[2] = OzJob{{hole(j, swp, k, i), hole(k, nat, j, i)}, 2, F56, v2, v, 0};
+  ccsdt_status s;
+  if(profiling) cudaEventRecord(prof_ev[0], stream);
+  if((s = variant == 0 ? launch_oz<__nv_bfloat16>(this, hb, v2, v) : launch_oz<int8_t>(this, hb, v2, v))) return s;
+  // d-sum: rows of t2 are (x, y, a), rows of ovvv are (z, c, b)
+  auto part_t = [&](int x, int y, int z, OzRows mb) {
+    const long long ra = ((long long) x * o + y) * v, rb = (long long) z * v2;
+    return OzTerm{at(sl_t2, ra * kp_v), ex_t2 + ra, nat, pl_t2, at(sl_ovvv, rb * kp_v), ex_ovvv + rb, mb, pl_ovvv, kp_v, 1.f};
+  };
+  OzBatch pb{};
+  pb.S      = S;
+  pb.job[0] = OzJob{{part_t(i, j, k, nat), part_t(i, k, j, swp)}, 2, F12, v, v2, 1};
+  pb.job[1] = OzJob{{part_t(j, i, k, swp), part_t(j, k, i, nat)}, 2, F34, v, v2, 1};
+  pb.job[2] = OzJob{{part_t(k, i, j, nat), part_t(k, j, i, swp)}, 2, F56, v, v2, 1};
+  if(profiling) cudaEventRecord(prof_ev[1], stream);
+  if((s = variant == 0 ? launch_oz<__nv_bfloat16>(this, pb, v, v2) : launch_oz<int8_t>(this, pb, v, v2))) return s;
+  if(profiling) cudaEventRecord(prof_ev[2], stream);
+  SplitEnergyArgs ea{F12, F34, F56, oovv_f, t1_f, eo, ev, (int) o, (int) v, i, j, k, part};
+  energy_split_kernel<<<kEnergyBlocks, E_THREADS, 0, stream>>>(ea);
+  if(profiling) cudaEventRecord(prof_ev[3], stream);
+  reduce_parts_kernel<<<1, 32, 0, stream>>>(part, kEnergyBlocks, multiplicity(i, j, k) / 9.0, eout);
+  if(profiling) cudaEventRecord(prof_ev[4], stream);
+  launches += 2;
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("split launch: ") + cudaGetErrorString(e));
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
+  const int S       = opts->slices;
+  const int variant = opts->reserved[0];
+  if(variant != 0 && variant != 1) return fail(CCSDT_E_INVALID, "unknown slice variant");
+  if(v > OZ_KWIN * 64) return fail(CCSDT_E_INVALID, "v too large for the split path");
+  ccsdt_status s;
+  if((s = ensure_slices(S, variant))) return s;
+  for(long t = 0; t < n; t++) {
+    const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
+    if(i == k) {
+      cudaError_t e = cudaMemsetAsync(etrip + 2 * t, 0, 2 * sizeof(double), stream);
+      if(e != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e));
+      continue;
+    }
+    if((s = run_triplet_split(i, j, k, S, variant, etrip + 2 * t))) return s;
+  }
+  return CCSDT_OK;
+}

@@ -138,13 +138,19 @@ def generate_device(o: int, v: int, seed: int, Q: int | None = None, device="cud
         scale = QUANT * QUANT
         oovv = (_exact_gemm_tf32(ov, ov) * scale).reshape(o, v, o, v).permute(0, 2, 1, 3).contiguous()
         ooov = (_exact_gemm_tf32(oo, ov) * scale).reshape(o, o, o, v).contiguous()
-        ovvv = torch.empty((o * v, v * v), dtype=torch.float64, device=device)
-        vv = Bi[:, o:, o:].reshape(Qn, v * v)
-        for c0 in range(0, v * v, vv_chunk):
-            c1 = min(v * v, c0 + vv_chunk)
-            ovvv[:, c0:c1] = _exact_gemm_tf32(ov, vv[:, c0:c1].contiguous()) * scale
+        # (ia|bc) = (ia|cb): compute the b <= c half by row blocks of b, mirror the rest
+        ovvv = torch.empty((o * v, v, v), dtype=torch.float64, device=device)
+        vvm = Bi[:, o:, o:]
+        nb = max(1, min(v, vv_chunk // max(1, v)))
+        for b0 in range(0, v, nb):
+            b1 = min(v, b0 + nb)
+            blk = vvm[:, b0:b1, b0:].reshape(Qn, -1).contiguous()
+            r = (_exact_gemm_tf32(ov, blk) * scale).reshape(o * v, b1 - b0, v - b0)
+            ovvv[:, b0:b1, b0:] = r
+            ovvv[:, b0:, b0:b1] = r.transpose(1, 2)
+            del r, blk
         ovvv = ovvv.reshape(o, v, v, v)
-        del Bi, ov, oo, vv
+        del Bi, ov, oo, vvm
         eo = torch.from_numpy(eps_occ).to(device)
         ev = torch.from_numpy(eps_vir).to(device)
         d = ((eo[:, None, None, None] + eo[None, :, None, None]) - ev[None, None, :, None]) - ev[None, None, None, :]
@@ -155,3 +161,22 @@ def generate_device(o: int, v: int, seed: int, Q: int | None = None, device="cud
         torch.backends.cuda.matmul.allow_tf32 = old
     return dict(o=o, v=v, seed=seed, eps_occ=eo, eps_vir=ev, t1=torch.from_numpy(t1).to(device),
                 t2=t2.contiguous(), oovv=oovv, ooov=ooov, ovvv=ovvv)
+
+
+def generate_host_slabs(o: int, v: int, seed: int, slabs, Q: int | None = None) -> dict:
+    """Host inputs for a sample of triplets: everything except ovvv in full, and the
+    (ia|bc) slabs only for the occupied indices in ``slabs`` (key ``ovvv_slabs``:
+    {i: array[v][v][v]}).  Same values as ``generate``."""
+    eps_occ, eps_vir, B, t1 = draw_host(o, v, seed, Q)
+    Qn = B.shape[0]
+    Bo = B[:, :o, o:]
+    ov = np.ascontiguousarray(Bo.reshape(Qn, o * v))
+    oovv = (ov.T @ ov).reshape(o, v, o, v).transpose(0, 2, 1, 3).copy()
+    ooov = (np.ascontiguousarray(B[:, :o, :o].reshape(Qn, o * o)).T @ ov).reshape(o, o, o, v)
+    vv = np.ascontiguousarray(B[:, o:, o:].reshape(Qn, v * v))
+    sl = {int(i): np.ascontiguousarray((np.ascontiguousarray(Bo[:, i, :]).T @ vv).reshape(v, v, v))
+          for i in sorted(set(int(x) for x in slabs))}
+    t2 = mp2_t2(oovv, eps_occ, eps_vir)
+    return dict(o=o, v=v, seed=seed, eps_occ=eps_occ, eps_vir=eps_vir, t1=np.ascontiguousarray(t1),
+                t2=np.ascontiguousarray(t2), oovv=np.ascontiguousarray(oovv),
+                ooov=np.ascontiguousarray(ooov), ovvv_slabs=sl)

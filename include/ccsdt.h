@@ -1,0 +1,131 @@
+/*
+ * ccsdt.h - C ABI of the GB300 closed-shell CCSD(T) perturbative-triples library.
+ *
+ * This is the drop-in boundary for ExaChem's fused (T) driver:
+ *
+ *   std::tuple<T,T,double,double> CCSD_T_Fused_Driver<T>::execute(
+ *       ChemEnv&, ExecutionContext&, std::vector<int>& k_spin, const TiledIndexSpace& MO,
+ *       Tensor<T>& d_t1, Tensor<T>& d_t2, V2Tensors<T>& d_v2, std::vector<T>& k_evl_sorted,
+ *       T hf_ccsd_energy, bool is_restricted, LRUCache x6, bool seq_h3b, bool tilesize_opt)
+ *   (exachem/cc/ccsd_t/ccsd_t_fused_driver.hpp:73-81, 91-546; called from ccsd_t.cpp:253-256)
+ *
+ * which takes T1/T2, the V2 integral blocks, orbital energies and the triples tile
+ * layout and returns (E[T], E(T), work seconds, total seconds).  The C++ adapter in
+ * include/exachem_compat/ccsd_t_fused_driver.hpp keeps that signature and calls the
+ * functions below.  Everything here uses plain pointers and sizes; no exceptions,
+ * no exit(): every call returns a ccsdt_status and ccsdt_last_error() explains it.
+ *
+ * Closed-shell spatial layouts (row-major, chemist notation; o occupied, v virtual):
+ *   eps_occ[o], eps_vir[v]                 orbital energies (Eh)
+ *   t1[o][v]          t1[i][a]             = t_i^a
+ *   t2[o][o][v][v]    t2[i][j][a][b]       = t_ij^ab        (ExaChem t2_abab(a,b,i,j))
+ *   oovv[o][o][v][v]  oovv[i][j][a][b]     = (ia|jb)        (alpha-beta block of v2ijab)
+ *   ooov[o][o][o][v]  ooov[i][j][k][a]     = (ij|ka)        (Coulomb part of v2ijka)
+ *   ovvv[o][v][v][v]  ovvv[i][a][b][c]     = (ia|bc)        (Coulomb part of v2iabc)
+ * The spin-orbital blocks ExaChem passes are the antisymmetrised combinations of these
+ * (exachem/cholesky/v2tensors.cpp:67-86, exachem/cc/ccsd/cd_ccsd_cs_ann.cpp:949-973).
+ */
+#ifndef CCSDT_GB300_H
+#define CCSDT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  CCSDT_OK           = 0,
+  CCSDT_E_INVALID    = 1, /* bad argument (null pointer, negative size, unknown mode)      */
+  CCSDT_E_BAD_LAYOUT = 2, /* tile layout inconsistent with o / v                            */
+  CCSDT_E_OOM        = 3, /* device or host allocation failed                               */
+  CCSDT_E_NONFINITE  = 4, /* NaN or Inf in the inputs or in the result                      */
+  CCSDT_E_TIMEOUT    = 5, /* a bounded device-side wait gave up                             */
+  CCSDT_E_CUDA       = 6, /* CUDA runtime / driver error                                    */
+  CCSDT_E_STATE      = 7  /* call out of order (e.g. energy before upload)                  */
+} ccsdt_status;
+
+/* Precision of the triples contractions. */
+typedef enum {
+  CCSDT_MODE_FP64    = 0, /* FP64 DMMA tensor-core contractions, FP64 energy (the drop-in) */
+  CCSDT_MODE_OZAKI   = 1, /* split-precision: BF16 slices on tcgen05, FP64-exact recombination */
+  CCSDT_MODE_LEARNED = 2  /* split-precision with a per-block slice count from the MLP     */
+} ccsdt_mode;
+
+/* The triples tile layout: occupied and virtual tile extents (ragged allowed).
+ * ExaChem's MO space repeats these for alpha and beta (cholesky_2e.cpp:230-285). */
+typedef struct {
+  int        o, v;
+  int        n_occ_tiles;
+  const int* occ_tiles; /* extents, sum == o */
+  int        n_vir_tiles;
+  const int* vir_tiles; /* extents, sum == v */
+} ccsdt_layout;
+
+typedef struct {
+  int    mode;          /* ccsdt_mode                                                        */
+  int    slices;        /* Ozaki slices per operand (2..8) for CCSDT_MODE_OZAKI              */
+  double energy_budget; /* per-block |dE| budget (Eh, relative to |E| scale) for LEARNED     */
+  int    use_graph;     /* capture the per-call launch sequence in a CUDA graph              */
+  int    reserved[8];
+} ccsdt_opts;
+
+typedef struct {
+  double e_bracket_T;      /* E[T]                                                            */
+  double e_paren_T;        /* E(T)                                                            */
+  double abs_err_bound;    /* a-posteriori bound on |E(T) - E(T)_fp64| (0 in FP64 mode)        */
+  double seconds;          /* device time of the call                                         */
+  double flops_executed;   /* 2 x multiply-adds of the contractions (FP64-equivalent)         */
+  double flops_ref_equiv;  /* the reference's own spin-orbital op count for this layout       */
+  long   n_triplets;       /* occupied triplets i <= j <= k processed                         */
+  long   n_tasks_ref;      /* tile-block tasks the reference would run for this layout        */
+} ccsdt_result;
+
+typedef struct ccsdt_handle ccsdt_handle;
+
+/* Create a handle bound to CUDA device `device` for the given layout. */
+ccsdt_status ccsdt_create(ccsdt_handle** out, const ccsdt_layout* layout, int device);
+
+/* Copy the inputs into handle-owned device memory.  `on_device` = 0: host pointers
+ * (pinned or pageable), 1: device pointers on the handle's device.  Checks finiteness. */
+ccsdt_status ccsdt_upload(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
+                          const double* t1, const double* t2, const double* oovv,
+                          const double* ooov, const double* ovvv, int on_device);
+
+/* Full (T): E[T] and E(T) over every occupied triplet.  Blocking. */
+ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, ccsdt_result* out);
+
+/* Per-triplet contributions for an explicit list tri[3n] (each i <= j <= k < o):
+ * e_bracket[t], e_paren[t] receive host doubles.  Used for sampled parity checks. */
+ccsdt_status ccsdt_triplet_energies(ccsdt_handle* h, const ccsdt_opts* opts, long n,
+                                    const int* tri, double* e_bracket, double* e_paren);
+
+/* Launch all further work of this handle on `stream` (a cudaStream_t on the handle's
+ * device; NULL restores the handle's own stream).  Lets a caller time the calls with
+ * CUDA events on its own stream.  No counterpart in the reference (it used one pooled
+ * stream per rank, ccsd_t_all_fused.hpp:108). */
+ccsdt_status ccsdt_set_stream(ccsdt_handle* h, void* stream);
+
+/* Device milliseconds of each phase of one triplet (i <= j <= k), measured with CUDA
+ * events on the handle's stream: out_ms[0] l-sum contractions, [1] d-sum contractions,
+ * [2] energy, [3] reduction.  Profiling aid; no counterpart in the reference. */
+ccsdt_status ccsdt_profile_triplet(ccsdt_handle* h, const ccsdt_opts* opts, int i, int j, int k,
+                                   double* out_ms);
+
+/* Number of kernel launches issued by the last ccsdt_energy / ccsdt_triplet_energies. */
+long ccsdt_last_launch_count(const ccsdt_handle* h);
+
+/* Reference-equivalent op count and task count for a layout (restricted, i.e. RHF):
+ * the sum over tile-block tasks of 2 x product of sizes per enabled contraction, as
+ * exachem/cc/ccsd_t/fused_common.hpp:34-261 counts it.  Pure host arithmetic. */
+ccsdt_status ccsdt_reference_op_count(const ccsdt_layout* layout, double* ops, long* tasks);
+
+void        ccsdt_destroy(ccsdt_handle* h);
+const char* ccsdt_last_error(const ccsdt_handle* h);
+const char* ccsdt_status_string(ccsdt_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CCSDT_GB300_H */

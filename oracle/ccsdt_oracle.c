@@ -43,8 +43,9 @@
 #endif
 
 typedef struct {
-  int           o, v;
-  const double *eo, *ev, *t1, *t2, *oovv, *ooov, *ovvv;
+  int                  o, v;
+  const double *       eo, *ev, *t1, *t2, *oovv, *ooov;
+  const double* const* slab; /* slab[z] = ovvv + z v^3 (only the triplet's z are read) */
 } sys_t;
 
 /* Neumaier compensated accumulation */
@@ -65,7 +66,7 @@ static void add_perm(const sys_t* S, double* W, int x, int y, int z, const int p
   const int     o = S->o, v = S->v;
   const size_t  v2 = (size_t) v * v;
   const double* T   = S->t2 + ((size_t) x * o + y) * v2; /* T[alpha][d] */
-  const double* I   = S->ovvv + (size_t) z * v * v2;     /* I[gamma][beta][d] */
+  const double* I   = S->slab[z];                        /* I[gamma][beta][d] */
   const size_t  st[3] = {v2, (size_t) v, 1};
   const size_t  sa = st[pos[0]], sb = st[pos[1]], sc = st[pos[2]];
 #pragma omp parallel for schedule(static)
@@ -163,18 +164,38 @@ static void triplet_energy(const sys_t* S, const double* W, int i, int j, int k,
   *e5      = m * (s5.s + s5.c);
 }
 
+int oracle_triplets_slabs(int o, int v, const double* eo, const double* ev, const double* t1,
+                          const double* t2, const double* oovv, const double* ooov,
+                          const double* const* slab, long n, const int* tri, double* out4,
+                          double* out5);
+
 /* Per-triplet energies for a list of triplets (tri[3 n], each i <= j <= k).
  * out4 / out5 receive E[T] / E(T) contributions; returns 0 or an error code. */
 int oracle_triplets(int o, int v, const double* eo, const double* ev, const double* t1,
                     const double* t2, const double* oovv, const double* ooov, const double* ovvv,
                     long n, const int* tri, double* out4, double* out5) {
   if(o <= 0 || v <= 0) return 1;
-  sys_t   S = {o, v, eo, ev, t1, t2, oovv, ooov, ovvv};
+  const double** slab = (const double**) malloc(sizeof(double*) * (size_t) o);
+  if(!slab) return 2;
+  for(int z = 0; z < o; z++) slab[z] = ovvv + (size_t) z * v * v * v;
+  int rc = oracle_triplets_slabs(o, v, eo, ev, t1, t2, oovv, ooov, slab, n, tri, out4, out5);
+  free(slab);
+  return rc;
+}
+
+/* As oracle_triplets, with the (ia|bc) integrals given as one v^3 slab per occupied i
+ * (slab[i] may be NULL for any i that no listed triplet contains). */
+int oracle_triplets_slabs(int o, int v, const double* eo, const double* ev, const double* t1,
+                          const double* t2, const double* oovv, const double* ooov,
+                          const double* const* slab, long n, const int* tri, double* out4,
+                          double* out5) {
+  if(o <= 0 || v <= 0) return 1;
+  sys_t   S = {o, v, eo, ev, t1, t2, oovv, ooov, slab};
   double* W = (double*) malloc(sizeof(double) * (size_t) v * v * v);
   if(!W) return 2;
   for(long t = 0; t < n; t++) {
     int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
-    if(!(0 <= i && i <= j && j <= k && k < o)) {
+    if(!(0 <= i && i <= j && j <= k && k < o) || !slab[i] || !slab[j] || !slab[k]) {
       free(W);
       return 3;
     }

@@ -1,0 +1,108 @@
+"""GPU parity of the plain FP64 path (the drop-in) through the C ABI.
+
+Tolerances: the reference's own CPU (T) (golden fixtures) and the CPU oracle are FP64;
+with these synthetic inputs |E(T)| reaches 1e2..1e11 Eh, so absolute bounds such as
+1e-9 Eh are below one FP64 ulp of E.  Parity is therefore stated relative to |E|:
+1e-12 for full energies (reassociation of ~1e7..1e13 FP64 terms), 1e-11 per triplet.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_close
+
+pytestmark = pytest.mark.gpu
+
+RTOL_FULL = 1e-12
+RTOL_TRIPLET = 1e-11
+
+
+def _ft(d, occ_tiles=None, vir_tiles=None, ts=40):
+    from exachem_gb300.ccsd_t import FusedTriples
+    ft = FusedTriples(d["o"], d["v"], occ_tiles, vir_tiles, ts=ts)
+    ft.upload_dict(d)
+    return ft
+
+
+def test_fp64_matches_reference_goldens(built, golden):
+    from exachem_gb300.generator import generate
+    for c in golden["cases"]:
+        d = generate(c["o"], c["v"], c["seed"], t2_scale=c["t2_scale"])
+        ft = _ft(d, c["occ_tiles"], c["vir_tiles"])
+        r = ft.energy("fp64")
+        assert rel_close(r["e_bracket_T"], c["e_bracket_T"], RTOL_FULL, 1e-20), (c["name"], r)
+        assert rel_close(r["e_paren_T"], c["e_paren_T"], RTOL_FULL, 1e-20), (c["name"], r)
+        assert r["flops_ref_equiv"] == c["ref_ops"] and r["n_tasks_ref"] == c["ref_tasks"]
+        assert r["launches"] > 0
+        ft.close()
+
+
+def test_fp64_triplets_vs_oracle_medium(built):
+    import oracle
+    from exachem_gb300.generator import generate
+    d = generate(12, 70, seed=21)
+    rng = np.random.default_rng(5)
+    tri = {(0, 0, 0), (0, 0, 11), (3, 7, 7), (11, 11, 11), (2, 5, 9)}
+    while len(tri) < 14:
+        t = tuple(sorted(rng.integers(0, 12, 3)))
+        tri.add(t)
+    tri = np.array(sorted(tri), dtype=np.int32)
+    g4, g5 = _ft(d).triplet_energies(tri, "fp64")
+    o4, o5 = oracle.triplets(d, tri)
+    # i = j = k contributes exactly zero (W is then symmetric in a, b, c, so Y vanishes):
+    # compare on the scale of the sample, not relative to a roundoff-sized value
+    for g, w in ((g4, o4), (g5, o5)):
+        np.testing.assert_allclose(g, w, rtol=RTOL_TRIPLET, atol=RTOL_TRIPLET * np.abs(w).max())
+    for t in range(len(tri)):
+        if tri[t][0] == tri[t][2]:
+            assert g4[t] == 0.0 and g5[t] == 0.0 and abs(o5[t]) < 1e-12 * np.abs(o5).max()
+
+
+def test_fp64_cfg1_shape_sampled_triplets(built):
+    """o=21, v=180 (ts=40 layout, ragged 20-wide last virtual tile), seed 1: a sample of
+    triplets, incl. the degenerate ones, against the oracle."""
+    import oracle
+    from exachem_gb300.generator import generate
+    d = generate(21, 180, seed=1)
+    tri = np.array([(0, 0, 0), (0, 0, 20), (0, 20, 20), (4, 9, 17), (20, 20, 20), (7, 8, 9)], dtype=np.int32)
+    g4, g5 = _ft(d).triplet_energies(tri, "fp64")
+    o4, o5 = oracle.triplets(d, tri)
+    np.testing.assert_allclose(g4, o4, rtol=RTOL_TRIPLET, atol=RTOL_TRIPLET * np.abs(o4).max())
+    np.testing.assert_allclose(g5, o5, rtol=RTOL_TRIPLET, atol=RTOL_TRIPLET * np.abs(o5).max())
+
+
+def test_fp64_deterministic_and_tiling_invariant(built):
+    from exachem_gb300.generator import generate
+    d = generate(7, 33, seed=9)
+    r1 = _ft(d, [7], [33]).energy("fp64")
+    r2 = _ft(d, [7], [33]).energy("fp64")
+    assert r1["e_paren_T"] == r2["e_paren_T"] and r1["e_bracket_T"] == r2["e_bracket_T"]
+    r3 = _ft(d, [3, 3, 1], [16, 16, 1]).energy("fp64")
+    assert rel_close(r3["e_paren_T"], r1["e_paren_T"], 1e-14)
+
+
+def test_device_inputs_and_device_generator(built):
+    import torch
+    from exachem_gb300.generator import generate, generate_device
+    d = generate(5, 21, seed=3)
+    dd = generate_device(5, 21, seed=3, device="cuda")
+    for k in ("oovv", "ooov", "ovvv", "t2"):
+        assert np.array_equal(dd[k].cpu().numpy(), d[k]), k
+    r_host = _ft(d).energy("fp64")
+    r_dev = _ft(dd).energy("fp64")
+    assert r_host["e_paren_T"] == r_dev["e_paren_T"]
+    torch.cuda.synchronize()
+
+
+def test_nonfinite_inputs_rejected(built):
+    from exachem_gb300.ccsd_t import CCSDTError, FusedTriples
+    from exachem_gb300.generator import generate
+    d = generate(3, 6, seed=1)
+    d["ovvv"] = d["ovvv"].copy()
+    d["ovvv"][1, 2, 3, 4] = np.nan
+    ft = FusedTriples(3, 6, ts=40)
+    with pytest.raises(CCSDTError) as e:
+        ft.upload_dict(d)
+    assert e.value.status == 4
+    with pytest.raises(CCSDTError) as e:
+        ft.energy("fp64")
+    assert e.value.status == 7

@@ -1,0 +1,88 @@
+"""CPU tests: the oracle against the reference's own outputs, host logic, C-ABI exports."""
+import ctypes
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, rel_close
+
+
+def _case_inputs(c):
+    from exachem_gb300.generator import generate
+    return generate(c["o"], c["v"], c["seed"], t2_scale=c["t2_scale"])
+
+
+def test_port_oracle_matches_reference_goldens(built, golden):
+    import oracle
+    for c in golden["cases"]:
+        d = _case_inputs(c)
+        e4, e5 = oracle.energy(d)
+        assert rel_close(e4, c["e_bracket_T"], 1e-12, 1e-20), c["name"]
+        assert rel_close(e5, c["e_paren_T"], 1e-12, 1e-20), c["name"]
+
+
+def test_per_triplet_sum_equals_total(built):
+    import oracle
+    from exachem_gb300.ccsd_t import all_triplets
+    from exachem_gb300.generator import generate
+    d = generate(5, 13, 4)
+    e4, e5 = oracle.triplets(d, all_triplets(5))
+    t4, t5 = oracle.energy(d)
+    assert rel_close(e4.sum(), t4, 1e-13) and rel_close(e5.sum(), t5, 1e-13)
+
+
+@pytest.mark.skipif(not (ROOT / "oracle" / "_ref" / "libccsdt_ref.so").exists(), reason="reference tree not built here")
+def test_reference_reruns_its_golden(golden):
+    import oracle
+    c = next(c for c in golden["cases"] if c["name"] == "o6_v24_ts5")
+    r = oracle.reference_energy(_case_inputs(c), c["occ_tiles"], c["vir_tiles"])
+    assert rel_close(r["e_paren_T"], c["e_paren_T"], 1e-14)
+    assert r["ops"] == c["ref_ops"] and r["tasks"] == c["ref_tasks"]
+
+
+def test_reference_op_count_matches(built, golden):
+    from exachem_gb300.ccsd_t import reference_op_count
+    from exachem_gb300.generator import tiles_uniform
+    for c in golden["cases"]:
+        ops, nt = reference_op_count(c["o"], c["v"], c["occ_tiles"], c["vir_tiles"])
+        assert ops == c["ref_ops"] and nt == c["ref_tasks"], c["name"]
+    for c in golden["ci_ops"]:
+        ops, _ = reference_op_count(c["o"], c["v"], tiles_uniform(c["o"], c["ts"]), tiles_uniform(c["v"], c["ts"]))
+        assert ops == c["total_num_ops"], c["file"]
+
+
+def test_generator_integrals_are_exact_and_symmetric():
+    from exachem_gb300.generator import generate
+    d = generate(4, 9, 3)
+    for k in ("oovv", "ooov", "ovvv"):
+        x = d[k] * 2.0 ** 24
+        assert np.array_equal(x, np.rint(x)), k
+    assert np.array_equal(d["ovvv"], d["ovvv"].transpose(0, 1, 3, 2))
+    assert np.array_equal(d["oovv"], d["oovv"].transpose(1, 0, 3, 2))
+    # the same draw twice is bit-identical
+    assert np.array_equal(generate(4, 9, 3)["ovvv"], d["ovvv"])
+
+
+def test_library_exports_every_declared_symbol(built):
+    from exachem_gb300.build import LIB
+    hdr = (ROOT / "include" / "ccsdt.h").read_text()
+    names = set(re.findall(r"\b(ccsdt_[a-z_]+)\s*\(", hdr))
+    assert len(names) >= 9
+    lib = ctypes.CDLL(str(LIB))
+    for n in sorted(names):
+        assert hasattr(lib, n), n
+
+
+def test_capi_rejects_bad_layouts_without_gpu(built):
+    from exachem_gb300 import ccsd_t as ct
+    lib = ct.load_library()
+    L, keep = ct.make_layout(8, 40, [4, 4], [16, 16])        # vir tiles sum 32 != 40
+    h = ctypes.c_void_p()
+    assert lib.ccsdt_create(ctypes.byref(h), ctypes.byref(L), 0) == 2    # CCSDT_E_BAD_LAYOUT
+    L2, keep2 = ct.make_layout(8, 40, [8, 0], [40])                      # empty tile
+    assert lib.ccsdt_create(ctypes.byref(h), ctypes.byref(L2), 0) == 2
+    assert lib.ccsdt_create(None, ctypes.byref(L), 0) == 1              # CCSDT_E_INVALID
+    with pytest.raises(ct.CCSDTError):
+        ct.reference_op_count(8, 40, [8], [30])
+    assert lib.ccsdt_status_string(5) == b"device wait timed out"
