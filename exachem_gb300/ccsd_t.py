@@ -34,8 +34,9 @@ class Layout(ctypes.Structure):
 
 
 class Opts(ctypes.Structure):
-    _fields_ = [("mode", ctypes.c_int), ("slices", ctypes.c_int), ("energy_budget", ctypes.c_double),
-                ("use_graph", ctypes.c_int), ("reserved", ctypes.c_int * 8)]
+    _fields_ = [("mode", ctypes.c_int), ("slices", ctypes.c_int), ("slice_kind", ctypes.c_int),
+                ("use_graph", ctypes.c_int), ("shard_index", ctypes.c_int), ("shard_count", ctypes.c_int),
+                ("energy_budget", ctypes.c_double), ("reserved", ctypes.c_int * 6)]
 
 
 class Result(ctypes.Structure):
@@ -149,12 +150,15 @@ class FusedTriples:
         self.upload(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], d["oovv"], d["ooov"], d["ovvv"])
 
     @staticmethod
-    def opts(mode="fp64", slices=4, energy_budget=1e-9, use_graph=0) -> Opts:
+    def opts(mode="fp64", slices=4, slice_kind="bf16", energy_budget=1e-9, use_graph=0,
+             shard_index=0, shard_count=1) -> Opts:
         o = Opts()
         o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
         o.slices = slices
+        o.slice_kind = {"bf16": 0, "int8": 1}[slice_kind] if isinstance(slice_kind, str) else int(slice_kind)
         o.energy_budget = energy_budget
         o.use_graph = use_graph
+        o.shard_index, o.shard_count = shard_index, shard_count
         return o
 
     def energy(self, mode="fp64", **kw) -> dict:

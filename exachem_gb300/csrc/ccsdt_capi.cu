@@ -331,10 +331,15 @@ extern "C" ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, cc
   if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_energy before a successful ccsdt_upload");
   CK(cudaSetDevice(h->device));
   const int        o = h->o;
+  const int        nsh = opts->shard_count > 1 ? opts->shard_count : 1;
+  if(opts->shard_index < 0 || opts->shard_index >= nsh)
+    return h->fail(CCSDT_E_INVALID, "ccsdt_energy: shard_index outside [0, shard_count)");
   std::vector<int> tri;
+  long             tcount = 0;
   for(int i = 0; i < o; i++)
     for(int j = i; j < o; j++)
-      for(int k = j; k < o; k++) {
+      for(int k = j; k < o; k++, tcount++) {
+        if(tcount % nsh != opts->shard_index) continue;
         tri.push_back(i);
         tri.push_back(j);
         tri.push_back(k);
@@ -358,7 +363,9 @@ extern "C" ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, cc
   out->abs_err_bound  = h->last_err_bound;
   out->seconds        = ms * 1e-3;
   const double vv     = h->v;
-  out->flops_executed = (double) (n - o) * 12.0 * vv * vv * vv * (vv + o); // i = j = k skipped
+  long nzero = 0; // i = j = k triplets are skipped (they contribute exactly zero)
+  for(long t = 0; t < n; t++) nzero += tri[3 * t] == tri[3 * t + 2];
+  out->flops_executed = (double) (n - nzero) * 12.0 * vv * vv * vv * (vv + o);
   out->n_triplets     = n;
   ccsdt_layout L{h->o, h->v, (int) h->occ_tiles.size(), h->occ_tiles.data(), (int) h->vir_tiles.size(),
                  h->vir_tiles.data()};

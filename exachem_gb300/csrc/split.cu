@@ -3,7 +3,7 @@
 // (three partial arrays P12 / P34 / P56 per triplet; l-sum GEMMs initialise them, d-sum
 // GEMMs accumulate), with every GEMM run on digit planes.
 //
-// Two tensor-core variants of the slice products, selected by opts->reserved[0]:
+// Two tensor-core variants of the slice products, selected by opts->slice_kind:
 //   0: BF16 digits, mma.sync m16n8k16 with FP32 accumulation (exact per level, K <= 512)
 //   1: INT8 digits, mma.sync m16n8k32 with INT32 accumulation (exact per level)
 #include <cuda_bf16.h>
@@ -399,7 +399,7 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
   const int S       = opts->slices;
-  const int variant = opts->reserved[0];
+  const int variant = opts->slice_kind;
   if(variant != 0 && variant != 1) return fail(CCSDT_E_INVALID, "unknown slice variant");
   if(v > OZ_KWIN * 64) return fail(CCSDT_E_INVALID, "v too large for the split path");
   ccsdt_status s;

@@ -64,11 +64,15 @@ typedef struct {
 } ccsdt_layout;
 
 typedef struct {
-  int    mode;          /* ccsdt_mode                                                        */
-  int    slices;        /* Ozaki slices per operand (2..8) for CCSDT_MODE_OZAKI              */
-  double energy_budget; /* per-block |dE| budget (Eh, relative to |E| scale) for LEARNED     */
-  int    use_graph;     /* capture the per-call launch sequence in a CUDA graph              */
-  int    reserved[8];
+  int    mode;          /* ccsdt_mode                                                         */
+  int    slices;        /* Ozaki digit planes per operand (1..8) for CCSDT_MODE_OZAKI         */
+  int    slice_kind;    /* 0: BF16 digits on the tensor cores (FP32 accumulation),            */
+                        /* 1: INT8 digits (INT32 accumulation)                                */
+  int    use_graph;     /* capture the per-call launch sequence in a CUDA graph               */
+  int    shard_index;   /* process triplets t with t % shard_count == shard_index; the        */
+  int    shard_count;   /* caller sums the partial energies (0 or 1 = every triplet)          */
+  double energy_budget; /* LEARNED: per-triplet |dE| budget relative to |E_triplet|           */
+  int    reserved[6];
 } ccsdt_opts;
 
 typedef struct {

@@ -1,0 +1,191 @@
+// Drop-in replacement for ExaChem's fused (T) driver entry point
+//   std::tuple<T,T,double,double> CCSD_T_Fused_Driver<T>::execute(...)
+//   (exachem/cc/ccsd_t/ccsd_t_fused_driver.hpp:73-81, 91-546; called from ccsd_t.cpp:253-256)
+// backed by the GB300 library (include/ccsdt.h).
+//
+// Two layers:
+//  * gather_closed_shell(): reads the spin-orbital tiled blocks ExaChem holds - d_t1 {V,O},
+//    d_t2 {V,V,O,O}, v2ijab {O,O,V,V}, v2ijka {O,O,O,V}, v2iabc {O,V,V,V}, k_evl_sorted in MO
+//    order occ_a | occ_b | virt_a | virt_b - with Tensor::get(block ids, buffer), the same call
+//    the reference's gathers make (ccsd_t_all_fused_singles.hpp:200,304,
+//    doubles1.hpp:222,237,282, doubles2.hpp:215,230,335), and returns the closed-shell spatial
+//    arrays of include/ccsdt.h.  Only alpha / alpha-beta blocks are read:
+//        t_ij^ab = t2(a_alpha, b_beta, i_alpha, j_beta)         (cd_ccsd_cs_ann.cpp:949-973)
+//        (ia|jb) = v2ijab(i_alpha, j_beta, a_alpha, b_beta)     (v2tensors.cpp:67-70)
+//        (ij|ka) = v2ijka(i_alpha, k_beta, j_alpha, a_beta)     (v2tensors.cpp:76-78)
+//        (ia|bc) = v2iabc(i_alpha, b_beta, a_alpha, c_beta)     (v2tensors.cpp:84-86)
+//    (in each the exchange part of the antisymmetrised block vanishes by spin).
+//    It is a template over the tensor types, so it needs only Tensor<T>::get.
+//  * CCSD_T_Fused_Driver<T>::execute(): the reference's signature, compiled when
+//    EXACHEM_GB300_WITH_TAMM is defined (inside an ExaChem build).  Each rank of the process
+//    group takes every size-th occupied triplet on its own GPU and returns its partial
+//    energies; ccsd_t.cpp:262-263 already sums them with pg().reduce.
+#pragma once
+
+#include <chrono>
+#include <cstddef>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../ccsdt.h"
+
+namespace exachem_gb300 {
+
+struct SpatialInputs {
+  int                 o = 0, v = 0;
+  std::vector<int>    occ_tiles, vir_tiles; // alpha tile extents
+  std::vector<double> eps_occ, eps_vir, t1, t2, oovv, ooov, ovvv;
+};
+
+namespace detail {
+inline std::vector<size_t> offsets(const std::vector<size_t>& ext) {
+  std::vector<size_t> off;
+  size_t              s = 0;
+  for(auto e: ext) {
+    off.push_back(s);
+    s += e;
+  }
+  return off;
+}
+} // namespace detail
+
+// mo_tiles: extents of the MO tiles in the order occ_a, occ_b, virt_a, virt_b (as
+// TiledIndexSpace::input_tile_sizes() returns them); noa / nva: alpha occupied / virtual tiles.
+template<typename T, typename TensorT, typename V2T>
+SpatialInputs gather_closed_shell(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva,
+                                  TensorT& d_t1, TensorT& d_t2, V2T& d_v2,
+                                  const std::vector<T>& k_evl_sorted) {
+  if(mo_tiles.size() != 2 * noa + 2 * nva) throw std::invalid_argument("MO tiles != 2 noa + 2 nva");
+  std::vector<size_t> ot(mo_tiles.begin(), mo_tiles.begin() + noa);
+  std::vector<size_t> vt(mo_tiles.begin() + 2 * noa, mo_tiles.begin() + 2 * noa + nva);
+  for(size_t t = 0; t < noa; t++)
+    if(mo_tiles[noa + t] != ot[t]) throw std::invalid_argument("closed shell needs equal alpha/beta tiles");
+  for(size_t t = 0; t < nva; t++)
+    if(mo_tiles[2 * noa + nva + t] != vt[t]) throw std::invalid_argument("closed shell needs equal alpha/beta tiles");
+  const auto   oo = detail::offsets(ot), vo = detail::offsets(vt);
+  const size_t o = oo.empty() ? 0 : oo.back() + ot.back(), v = vo.empty() ? 0 : vo.back() + vt.back();
+  SpatialInputs S;
+  S.o = (int) o;
+  S.v = (int) v;
+  for(auto x: ot) S.occ_tiles.push_back((int) x);
+  for(auto x: vt) S.vir_tiles.push_back((int) x);
+  if(k_evl_sorted.size() < 2 * o + 2 * v) throw std::invalid_argument("k_evl_sorted too short");
+  S.eps_occ.assign(k_evl_sorted.begin(), k_evl_sorted.begin() + o);
+  S.eps_vir.assign(k_evl_sorted.begin() + 2 * o, k_evl_sorted.begin() + 2 * o + v);
+  S.t1.assign(o * v, 0.0);
+  S.t2.assign(o * o * v * v, 0.0);
+  S.oovv.assign(o * o * v * v, 0.0);
+  S.ooov.assign(o * o * o * v, 0.0);
+  S.ovvv.assign(o * v * v * v, 0.0);
+  std::vector<T> buf;
+  // block ids: O tiles 0..2noa-1 (beta = alpha + noa), V tiles 0..2nva-1 (beta = alpha + nva)
+  for(size_t A = 0; A < nva; A++)
+    for(size_t I = 0; I < noa; I++) {
+      d_t1.get({A, I}, buf); // [a][i]
+      for(size_t a = 0; a < vt[A]; a++)
+        for(size_t i = 0; i < ot[I]; i++) S.t1[(oo[I] + i) * v + vo[A] + a] = buf[a * ot[I] + i];
+    }
+  for(size_t A = 0; A < nva; A++)
+    for(size_t B = 0; B < nva; B++)
+      for(size_t I = 0; I < noa; I++)
+        for(size_t J = 0; J < noa; J++) {
+          d_t2.get({A, B + nva, I, J + noa}, buf); // [a][b][i][j], a,i alpha / b,j beta
+          for(size_t a = 0; a < vt[A]; a++)
+            for(size_t b = 0; b < vt[B]; b++)
+              for(size_t i = 0; i < ot[I]; i++)
+                for(size_t j = 0; j < ot[J]; j++)
+                  S.t2[(((oo[I] + i) * o + oo[J] + j) * v + vo[A] + a) * v + vo[B] + b] =
+                    buf[((a * vt[B] + b) * ot[I] + i) * ot[J] + j];
+          d_v2.v2ijab.get({I, J + noa, A, B + nva}, buf); // [i][j][a][b]
+          for(size_t i = 0; i < ot[I]; i++)
+            for(size_t j = 0; j < ot[J]; j++)
+              for(size_t a = 0; a < vt[A]; a++)
+                for(size_t b = 0; b < vt[B]; b++)
+                  S.oovv[(((oo[I] + i) * o + oo[J] + j) * v + vo[A] + a) * v + vo[B] + b] =
+                    buf[((i * ot[J] + j) * vt[A] + a) * vt[B] + b];
+        }
+  for(size_t I = 0; I < noa; I++)
+    for(size_t K = 0; K < noa; K++)
+      for(size_t J = 0; J < noa; J++)
+        for(size_t A = 0; A < nva; A++) {
+          d_v2.v2ijka.get({I, K + noa, J, A + nva}, buf); // [i][k][j][a] = (ij|ka)
+          for(size_t i = 0; i < ot[I]; i++)
+            for(size_t k = 0; k < ot[K]; k++)
+              for(size_t j = 0; j < ot[J]; j++)
+                for(size_t a = 0; a < vt[A]; a++)
+                  S.ooov[(((oo[I] + i) * o + oo[J] + j) * o + oo[K] + k) * v + vo[A] + a] =
+                    buf[((i * ot[K] + k) * ot[J] + j) * vt[A] + a];
+        }
+  for(size_t I = 0; I < noa; I++)
+    for(size_t B = 0; B < nva; B++)
+      for(size_t A = 0; A < nva; A++)
+        for(size_t C = 0; C < nva; C++) {
+          d_v2.v2iabc.get({I, B + nva, A, C + nva}, buf); // [i][b][a][c] = (ia|bc)
+          for(size_t i = 0; i < ot[I]; i++)
+            for(size_t b = 0; b < vt[B]; b++)
+              for(size_t a = 0; a < vt[A]; a++)
+                for(size_t c = 0; c < vt[C]; c++)
+                  S.ovvv[(((oo[I] + i) * v + vo[A] + a) * v + vo[B] + b) * v + vo[C] + c] =
+                    buf[((i * vt[B] + b) * vt[A] + a) * vt[C] + c];
+        }
+  return S;
+}
+
+// Runs (T) on the spatial inputs through the C ABI: returns (E[T], E(T), device seconds).
+inline std::tuple<double, double, double> run_closed_shell(const SpatialInputs& S, int device,
+                                                           const ccsdt_opts& opts) {
+  ccsdt_layout  L{S.o, S.v, (int) S.occ_tiles.size(), S.occ_tiles.data(), (int) S.vir_tiles.size(),
+                 S.vir_tiles.data()};
+  ccsdt_handle* h  = nullptr;
+  ccsdt_status  st = ccsdt_create(&h, &L, device);
+  if(st != CCSDT_OK) throw std::runtime_error(std::string("ccsdt_create: ") + ccsdt_status_string(st));
+  st = ccsdt_upload(h, S.eps_occ.data(), S.eps_vir.data(), S.t1.data(), S.t2.data(), S.oovv.data(),
+                    S.ooov.data(), S.ovvv.data(), 0);
+  ccsdt_result r{};
+  if(st == CCSDT_OK) st = ccsdt_energy(h, &opts, &r);
+  if(st != CCSDT_OK) {
+    std::string msg = ccsdt_last_error(h);
+    ccsdt_destroy(h);
+    throw std::runtime_error("ccsdt: " + msg);
+  }
+  ccsdt_destroy(h);
+  return {r.e_bracket_T, r.e_paren_T, r.seconds};
+}
+
+} // namespace exachem_gb300
+
+#ifdef EXACHEM_GB300_WITH_TAMM
+// Inside an ExaChem build: same class name and signature as the reference driver.
+template<typename T>
+class CCSD_T_Fused_Driver {
+public:
+  virtual ~CCSD_T_Fused_Driver() = default;
+  virtual std::tuple<T, T, double, double>
+  execute(ChemEnv& chem_env, ExecutionContext& ec, std::vector<int>& k_spin, const TiledIndexSpace& MO,
+          Tensor<T>& d_t1, Tensor<T>& d_t2, exachem::cholesky_2e::V2Tensors<T>& d_v2,
+          std::vector<T>& k_evl_sorted, T hf_ccsd_energy, bool is_restricted,
+          LRUCache<Index, std::vector<T>>& cache_s1t, LRUCache<Index, std::vector<T>>& cache_s1v,
+          LRUCache<Index, std::vector<T>>& cache_d1t, LRUCache<Index, std::vector<T>>& cache_d1v,
+          LRUCache<Index, std::vector<T>>& cache_d2t, LRUCache<Index, std::vector<T>>& cache_d2v,
+          bool seq_h3b = false, bool tilesize_opt = true) {
+    (void) chem_env, (void) k_spin, (void) hf_ccsd_energy, (void) cache_s1t, (void) cache_s1v;
+    (void) cache_d1t, (void) cache_d1v, (void) cache_d2t, (void) cache_d2v, (void) seq_h3b, (void) tilesize_opt;
+    if(!is_restricted) throw std::invalid_argument("the GB300 (T) path is closed-shell (RHF) only");
+    auto                t0 = std::chrono::steady_clock::now();
+    std::vector<size_t> mo;
+    for(auto x: MO.input_tile_sizes()) mo.push_back((size_t) x);
+    const size_t noa = MO("occ_alpha").num_tiles(), nva = MO("virt_alpha").num_tiles();
+    auto         S   = exachem_gb300::gather_closed_shell<T>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl_sorted);
+    ccsdt_opts   op{};
+    op.mode        = CCSDT_MODE_FP64;
+    op.shard_index = (int) ec.pg().rank().value();
+    op.shard_count = (int) ec.pg().size().value();
+    int dev        = 0;
+    auto [e4, e5, work] = exachem_gb300::run_closed_shell(S, dev, op);
+    double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return {(T) e4, (T) e5, work, total};
+  }
+};
+#endif

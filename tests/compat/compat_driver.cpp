@@ -1,0 +1,64 @@
+// Exercises include/exachem_compat/ccsd_t_fused_driver.hpp the way ExaChem would feed it:
+// spin-orbital tiled tensors (built with the oracle's spin_orbital.hpp on the TAMM stand-in)
+// -> gather_closed_shell() -> spatial arrays, and optionally run_closed_shell() on the GPU.
+//
+//   compat_driver <in.bin> <out.bin> [--run]
+// in.bin : int32 o, v, noa, nva, occ tiles[noa], vir tiles[nva]; float64 eps_occ[o] eps_vir[v]
+//          t1 t2 oovv ooov ovvv (C-ABI layouts)
+// out.bin: the gathered float64 arrays in the same order; with --run also E[T], E(T).
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <vector>
+
+#include "spin_orbital.hpp"
+#include "exachem_compat/ccsd_t_fused_driver.hpp"
+
+template<typename X>
+static void rd(std::ifstream& f, X* p, size_t n) {
+  f.read(reinterpret_cast<char*>(p), sizeof(X) * n);
+}
+
+int main(int argc, char** argv) {
+  if(argc < 3) return 2;
+  std::ifstream f(argv[1], std::ios::binary);
+  int           hdr[4];
+  rd(f, hdr, 4);
+  const int o = hdr[0], v = hdr[1], noa = hdr[2], nva = hdr[3];
+  std::vector<int> ot(noa), vt(nva);
+  rd(f, ot.data(), noa);
+  rd(f, vt.data(), nva);
+  std::vector<double> eo(o), ev(v), t1((size_t) o * v), t2((size_t) o * o * v * v), oovv(t2.size()),
+    ooov((size_t) o * o * o * v), ovvv((size_t) o * v * v * v);
+  for(auto* a: {&eo, &ev, &t1, &t2, &oovv, &ooov, &ovvv}) rd(f, a->data(), a->size());
+  if(!f) return 3;
+
+  // MO space occ_a | occ_b | virt_a | virt_b, as ExaChem tiles it
+  std::vector<size_t> mo, OT, VT;
+  for(int s = 0; s < 2; s++)
+    for(int x: ot) OT.push_back(x);
+  for(int s = 0; s < 2; s++)
+    for(int x: vt) VT.push_back(x);
+  mo.insert(mo.end(), OT.begin(), OT.end());
+  mo.insert(mo.end(), VT.begin(), VT.end());
+  std::vector<double> k_evl;
+  for(int s = 0; s < 2; s++) k_evl.insert(k_evl.end(), eo.begin(), eo.end());
+  for(int s = 0; s < 2; s++) k_evl.insert(k_evl.end(), ev.begin(), ev.end());
+  tamm::Tensor<double>                    d_t1, d_t2;
+  exachem::cholesky_2e::V2Tensors<double> d_v2;
+  build_spin_orbital(o, v, OT, VT, t1.data(), t2.data(), oovv.data(), ooov.data(), ovvv.data(), d_t1, d_t2, d_v2);
+
+  auto S = exachem_gb300::gather_closed_shell<double>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl);
+  std::ofstream g(argv[2], std::ios::binary);
+  for(auto* a: {&S.eps_occ, &S.eps_vir, &S.t1, &S.t2, &S.oovv, &S.ooov, &S.ovvv})
+    g.write(reinterpret_cast<const char*>(a->data()), sizeof(double) * a->size());
+  if(argc > 3 && std::string(argv[3]) == "--run") {
+    ccsdt_opts op{};
+    op.mode = CCSDT_MODE_FP64;
+    auto [e4, e5, secs] = exachem_gb300::run_closed_shell(S, 0, op);
+    g.write(reinterpret_cast<const char*>(&e4), sizeof(double));
+    g.write(reinterpret_cast<const char*>(&e5), sizeof(double));
+    std::printf("E[T] %.17g E(T) %.17g (%.3f s)\n", e4, e5, secs);
+  }
+  return 0;
+}
