@@ -125,6 +125,25 @@ long ccsdt_last_launch_count(const ccsdt_handle* h);
  * exachem/cc/ccsd_t/fused_common.hpp:34-261 counts it.  Pure host arithmetic. */
 ccsdt_status ccsdt_reference_op_count(const ccsdt_layout* layout, double* ops, long* tasks);
 
+/* Allocation-free FP64 (T) for small problems.  No counterpart in the reference: it is
+ * for callers that cannot call cudaMalloc - a host runtime whose device memory is owned
+ * by a pooled allocator (ExaChem's TAMM reserves the device through its RMM pool), code
+ * running inside a CUDA stream capture, or a service held to a fixed device budget.
+ * All pointers are device pointers on the current device: the inputs in the layouts
+ * above and `energies`, which receives {E[T], E(T)}.  Work is queued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream) and is complete when that stream is.
+ * Every intermediate lives in one fixed device array of about 6.0 MB defined in the
+ * library, which each GPU that loads the library keeps until the process exits; sizes
+ * beyond o = 12 or v = 48 are rejected with CCSDT_E_INVALID.  The first call on a device
+ * looks up that array's device address (make that first call before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race and give wrong results,
+ * so order them on one stream or synchronise between them.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine. */
+ccsdt_status ccsdt_energy_noalloc(int o, int v, const double* eps_occ, const double* eps_vir,
+                                  const double* t1, const double* t2, const double* oovv,
+                                  const double* ooov, const double* ovvv, double* energies,
+                                  void* stream);
+
 void        ccsdt_destroy(ccsdt_handle* h);
 const char* ccsdt_last_error(const ccsdt_handle* h);
 const char* ccsdt_status_string(ccsdt_status s);
