@@ -71,7 +71,7 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
             if verbose:
                 sys.stdout.write(r.stdout + r.stderr)
     if force or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcuda"])
+        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)])
     return LIB
 
 

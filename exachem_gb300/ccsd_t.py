@@ -48,7 +48,8 @@ class Result(ctypes.Structure):
 
 EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
             "ccsdt_last_launch_count", "ccsdt_reference_op_count", "ccsdt_destroy",
-            "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet"]
+            "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet",
+            "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc"]
 
 
 def load_library(path: str | os.PathLike | None = None):
@@ -69,6 +70,8 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_reference_op_count.argtypes = [ctypes.POINTER(Layout), dp, ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_set_stream.argtypes = [vp, vp]
     lib.ccsdt_profile_triplet.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    lib.ccsdt_debug_triplet_w.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    lib.ccsdt_debug_triplet_w.restype = ctypes.c_int
     lib.ccsdt_destroy.argtypes = [vp]
     lib.ccsdt_destroy.restype = None
     lib.ccsdt_last_error.argtypes = [vp]
@@ -151,7 +154,7 @@ class FusedTriples:
 
     @staticmethod
     def opts(mode="fp64", slices=4, slice_kind="bf16", energy_budget=1e-9, use_graph=0,
-             shard_index=0, shard_count=1) -> Opts:
+             shard_index=0, shard_count=1, legacy_mma=0) -> Opts:
         o = Opts()
         o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
         o.slices = slices
@@ -159,6 +162,7 @@ class FusedTriples:
         o.energy_budget = energy_budget
         o.use_graph = use_graph
         o.shard_index, o.shard_count = shard_index, shard_count
+        o.reserved[0] = legacy_mma   # 1: mma.sync slice kernel instead of tcgen05 (testing)
         return o
 
     def energy(self, mode="fp64", **kw) -> dict:
@@ -188,6 +192,14 @@ class FusedTriples:
         op = self.opts(mode, **kw)
         self._check(self.lib.ccsdt_profile_triplet(self.h, ctypes.byref(op), i, j, k, out))
         return list(out)
+
+    def triplet_w(self, i: int, j: int, k: int, mode="fp64", **kw) -> np.ndarray:
+        """W_abc of one triplet (verification aid), shape (v, v, v)."""
+        w = np.empty((self.v, self.v, self.v))
+        op = self.opts(mode, **kw)
+        self._check(self.lib.ccsdt_debug_triplet_w(self.h, ctypes.byref(op), i, j, k,
+                                                   w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return w
 
     def launch_count(self) -> int:
         return int(self.lib.ccsdt_last_launch_count(self.h))

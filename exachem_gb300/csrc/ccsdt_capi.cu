@@ -318,6 +318,7 @@ extern "C" ccsdt_status ccsdt_triplet_energies(ccsdt_handle* h, const ccsdt_opts
   std::vector<double> buf(2 * (size_t) n);
   if(n) CK(cudaMemcpyAsync(buf.data(), h->etrip, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  if(opts->mode != CCSDT_MODE_FP64 && (s = h->check_device_error())) return s;
   for(long t = 0; t < n; t++) {
     e_bracket[t] = buf[2 * t];
     e_paren[t]   = buf[2 * t + 1];
@@ -355,6 +356,7 @@ extern "C" ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, cc
   double r[2];
   CK(cudaMemcpyAsync(r, h->res, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  if(opts->mode != CCSDT_MODE_FP64 && (s = h->check_device_error())) return s;
   float ms = 0;
   CK(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
   std::memset(out, 0, sizeof(*out));
@@ -397,5 +399,39 @@ extern "C" ccsdt_status ccsdt_profile_triplet(ccsdt_handle* h, const ccsdt_opts*
     CK(cudaEventElapsedTime(&ms, h->prof_ev[q], h->prof_ev[q + 1]));
     out_ms[q] = ms;
   }
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts* opts, int i, int j, int k,
+                                              double* w_host) {
+  if(!h) return CCSDT_E_INVALID;
+  if(!valid_opts(opts) || !w_host || !(0 <= i && i <= j && j <= k && k < h->o) || i == k)
+    return h->fail(CCSDT_E_INVALID, "ccsdt_debug_triplet_w: bad arguments (needs i <= j <= k, i < k)");
+  if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_debug_triplet_w before ccsdt_upload");
+  CK(cudaSetDevice(h->device));
+  const int    tri[3] = {i, j, k};
+  ccsdt_status s      = h->run_list(opts, 1, tri);
+  if(s) return s;
+  CK(cudaStreamSynchronize(h->stream));
+  if(opts->mode != CCSDT_MODE_FP64 && (s = h->check_device_error())) return s;
+  const size_t        v = h->v, n = v * v * v;
+  std::vector<double> a(n), b(n), c(n);
+  if(opts->mode == CCSDT_MODE_FP64) {
+    CK(cudaMemcpy(a.data(), h->P12, n * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(b.data(), h->P34, n * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(c.data(), h->P56, n * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float2> f(n);
+    for(int q = 0; q < 3; q++) {
+      CK(cudaMemcpy(f.data(), q == 0 ? h->F12 : q == 1 ? h->F34 : h->F56, n * sizeof(float2), cudaMemcpyDeviceToHost));
+      std::vector<double>& d = q == 0 ? a : q == 1 ? b : c;
+      for(size_t e = 0; e < n; e++) d[e] = (double) f[e].x + (double) f[e].y;
+    }
+  }
+  // W_xyz = P12[x][z][y] + P34[y][x][z] + P56[z][y][x]
+  for(size_t x = 0; x < v; x++)
+    for(size_t y = 0; y < v; y++)
+      for(size_t z = 0; z < v; z++)
+        w_host[(x * v + y) * v + z] = a[(x * v + z) * v + y] + b[(y * v + x) * v + z] + c[(z * v + y) * v + x];
   return CCSDT_OK;
 }

@@ -1,6 +1,7 @@
 // Handle internals shared by the C-ABI translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -9,6 +10,7 @@
 #include "../../include/ccsdt.h"
 
 constexpr int kEnergyBlocks = 1216; // 8 x 152 SMs
+constexpr int kTiledBlocks  = 1216; // persistent grid of the tiled energy
 
 struct ccsdt_handle {
   int              device = 0, o = 0, v = 0;
@@ -38,6 +40,13 @@ struct ccsdt_handle {
   long long          pl_t2 = 0, pl_t2h = 0, pl_ovvv = 0, pl_ooovh = 0;
   float *            oovv_f = nullptr, *t1_f = nullptr;
   float2 *           F12 = nullptr, *F34 = nullptr, *F56 = nullptr;
+  // tcgen05 path: TMA maps over the digit planes (built once per slicing) and an error flag
+  CUtensorMap        tmaps[6];
+  bool               tmaps_ready = false;
+  int*               d_err       = nullptr;
+  int*               e_tiles     = nullptr; // sorted virtual block triples of the tiled energy
+  int                e_ntiles    = 0;
+  double*            e_part      = nullptr;
 
   long        launches       = 0;
   double      last_err_bound = 0.0;
@@ -56,4 +65,11 @@ struct ccsdt_handle {
   ccsdt_status run_split(const ccsdt_opts* opts, long n, const int* tri_host);
   ccsdt_status ensure_slices(int S, int variant);
   ccsdt_status run_triplet_split(int i, int j, int k, int S, int variant, double* eout);
+  ccsdt_status ensure_tmaps(int S);
+  ccsdt_status run_triplet_tc(int i, int j, int k, int S, double* eout);
+  bool         tc_eligible(int S, int variant) const;
+  double*      part_buf() { return part; }
+  ccsdt_status launch_energy_tiled(int i, int j, int k, double* eout);
+  ccsdt_status check_device_error();
+  bool         force_mma_sync = false; // use the mma.sync slice kernel even where tcgen05 applies
 };

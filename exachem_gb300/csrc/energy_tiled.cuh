@@ -1,0 +1,188 @@
+// Tiled float-float energy of one occupied triplet (split-precision path).
+//
+// Restates the energy of ccsd_t_all_fused_cpu.hpp:597-619 in the closed-shell form
+//   e = Z Y / D,  Z = 4 W_abc + W_bca + W_cab,  Y = 3 V_abc - V_acb - V_bac - V_cba,
+//   W_xyz = P12[x][z][y] + P34[y][x][z] + P56[z][y][x]
+// for every (a, b, c).  The virtual range is cut into blocks of 8; one work item is a sorted
+// block triple X <= Y <= Z.  Its six ordered block cubes (the permutations of (X, Y, Z)) are
+// summed from P12 / P34 / P56 into shared memory - each array read once, in runs of 8
+// contiguous elements - so every permuted W an element needs is on chip.  The singles'
+// integrals and amplitudes of the three blocks are staged too.  Work items are walked by a
+// persistent grid in a fixed order; per-CTA float-float sums are written for a fixed-order
+// reduction, so the result is deterministic.
+#pragma once
+
+#include "ozaki.cuh"
+
+namespace ccsdt {
+
+constexpr int ET_B = 8, ET_THREADS = 256;
+
+struct TiledEnergyArgs {
+  const float2 *P12, *P34, *P56;
+  const float * oovv, *t1; // FP32 copies
+  const double *eo, *ev;
+  const int3*   tiles;     // sorted block triples
+  int           ntiles;
+  int           o, v, i, j, k;
+  double*       part;      // 4 doubles per CTA
+};
+
+// slot s <-> permutation (p0, p1, p2) of the block positions
+__device__ __constant__ int c_perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+
+__device__ __forceinline__ int perm_slot(int p0, int p1, int p2) {
+  // (0,1,2)=0 (0,2,1)=1 (1,0,2)=2 (1,2,0)=3 (2,0,1)=4 (2,1,0)=5
+  return p0 * 2 + (p1 > p2 ? 1 : 0);
+}
+
+__global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_constant__ TiledEnergyArgs A) {
+  constexpr int B = ET_B, B3 = B * B * B;
+  __shared__ float2 W[6][B3];            // [slot][a'][b'][c'] (a', b', c' local to the slot's blocks)
+  __shared__ float  Ojk[3][3][B * B], Oik[3][3][B * B], Oij[3][3][B * B];
+  __shared__ float  ti[3][B], tj[3][B], tk[3][B];
+  __shared__ float2 evs[3][B];
+  __shared__ int    blk0[3], blkn[3];
+  __shared__ int    slot_on[6];
+
+  const int       v = A.v, o = A.o, i = A.i, j = A.j, k = A.k, tid = threadIdx.x;
+  const long long v2 = (long long) v * v;
+  const ff        eijk = ff_add(ff_add(ff_from_double(A.eo[i]), ff_from_double(A.eo[j])), ff_from_double(A.eo[k]));
+  const float *   gOjk = A.oovv + ((long long) j * o + k) * v2, *gOik = A.oovv + ((long long) i * o + k) * v2,
+              *gOij = A.oovv + ((long long) i * o + j) * v2;
+  ff s4{0.f, 0.f}, s5{0.f, 0.f};
+
+  for(int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+    __syncthreads();
+    if(tid < 3) {
+      const int3 t = A.tiles[tile];
+      const int  b = tid == 0 ? t.x : tid == 1 ? t.y : t.z;
+      blk0[tid]    = b * B;
+      blkn[tid]    = min(B, v - b * B);
+    }
+    __syncthreads();
+    if(tid < 6) { // a slot counts once per distinct ordered block triple
+      const int* P  = c_perm[tid];
+      int        on = 1;
+      for(int q = 0; q < tid; q++) {
+        const int* Q = c_perm[q];
+        if(blk0[P[0]] == blk0[Q[0]] && blk0[P[1]] == blk0[Q[1]] && blk0[P[2]] == blk0[Q[2]]) on = 0;
+      }
+      slot_on[tid] = on;
+    }
+    // singles data of the three blocks
+    for(int e = tid; e < 9 * B * B; e += ET_THREADS) {
+      const int u = e / (3 * B * B), w = (e / (B * B)) % 3, x = (e / B) % B, y = e % B;
+      const bool ok = x < blkn[u] && y < blkn[w];
+      const long long off = (long long) (blk0[u] + x) * v + blk0[w] + y;
+      Ojk[u][w][x * B + y] = ok ? gOjk[off] : 0.f;
+      Oik[u][w][x * B + y] = ok ? gOik[off] : 0.f;
+      Oij[u][w][x * B + y] = ok ? gOij[off] : 0.f;
+    }
+    if(tid < 3 * B) {
+      const int u = tid / B, x = tid % B;
+      const bool ok = x < blkn[u];
+      const int  a = blk0[u] + x;
+      ti[u][x] = ok ? A.t1[(long long) i * v + a] : 0.f;
+      tj[u][x] = ok ? A.t1[(long long) j * v + a] : 0.f;
+      tk[u][x] = ok ? A.t1[(long long) k * v + a] : 0.f;
+      const ff e = ok ? ff_from_double(A.ev[a]) : ff{0.f, 0.f};
+      evs[u][x] = make_float2(e.hi, e.lo);
+    }
+    // W of the six slots: three passes, each reading one array along its contiguous index
+#pragma unroll 1
+    for(int pass = 0; pass < 3; pass++) {
+      __syncthreads();
+      for(int e = tid; e < 6 * B3; e += ET_THREADS) {
+        const int  s = e / B3, r = e % B3;
+        const int  f = r % B, m = (r / B) % B, sl = r / (B * B); // fastest, middle, slowest local index
+        const int* P = c_perm[s];
+        int        la, lb, lc; // local (a', b', c') of this element within the slot
+        const float2* src;
+        long long     off;
+        // slot blocks: a in block P[0], b in P[1], c in P[2]
+        if(pass == 0) { // P12[a][c][b]: b fastest
+          la = sl, lc = m, lb = f;
+          src = A.P12;
+          off = ((long long) (blk0[P[0]] + la) * v + blk0[P[2]] + lc) * v + blk0[P[1]] + lb;
+        } else if(pass == 1) { // P34[b][a][c]: c fastest
+          lb = sl, la = m, lc = f;
+          src = A.P34;
+          off = ((long long) (blk0[P[1]] + lb) * v + blk0[P[0]] + la) * v + blk0[P[2]] + lc;
+        } else { // P56[c][b][a]: a fastest
+          lc = sl, lb = m, la = f;
+          src = A.P56;
+          off = ((long long) (blk0[P[2]] + lc) * v + blk0[P[1]] + lb) * v + blk0[P[0]] + la;
+        }
+        const bool ok = la < blkn[P[0]] && lb < blkn[P[1]] && lc < blkn[P[2]];
+        const float2 x = ok ? src[off] : make_float2(0.f, 0.f);
+        const int    w = (la * B + lb) * B + lc;
+        if(pass == 0) W[s][w] = x;
+        else {
+          const ff r = ff_add(ff{W[s][w].x, W[s][w].y}, ff{x.x, x.y});
+          W[s][w]    = make_float2(r.hi, r.lo);
+        }
+      }
+    }
+    __syncthreads();
+    // energies of the distinct ordered cubes
+    for(int e = tid; e < 6 * B3; e += ET_THREADS) {
+      const int s = e / B3, r = e % B3;
+      if(!slot_on[s]) continue;
+      const int* P = c_perm[s];
+      const int  p0 = P[0], p1 = P[1], p2 = P[2];
+      const int  a = r / (B * B), b = (r / B) % B, c = r % B;
+      if(a >= blkn[p0] || b >= blkn[p1] || c >= blkn[p2]) continue;
+      auto Wat = [&](int q0, int q1, int q2, int x, int y, int z) {
+        const float2 t = W[perm_slot(q0, q1, q2)][(x * B + y) * B + z];
+        return ff{t.x, t.y};
+      };
+      const ff wabc = Wat(p0, p1, p2, a, b, c), wbca = Wat(p1, p2, p0, b, c, a), wcab = Wat(p2, p0, p1, c, a, b);
+      const ff wacb = Wat(p0, p2, p1, a, c, b), wbac = Wat(p1, p0, p2, b, a, c), wcba = Wat(p2, p1, p0, c, b, a);
+      // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z, x in block qx ...
+      auto SG = [&](int qx, int qy, int qz, int x, int y, int z) {
+        return Ojk[qy][qz][y * B + z] * ti[qx][x] + Oik[qx][qz][x * B + z] * tj[qy][y] + Oij[qx][qy][x * B + y] * tk[qz][z];
+      };
+      const float sgl = 3.f * SG(p0, p1, p2, a, b, c) - SG(p0, p2, p1, a, c, b) - SG(p1, p0, p2, b, a, c) -
+                        SG(p2, p1, p0, c, b, a);
+      const ff z  = ff_add(ff_add(ff_scale(wabc, 4.f), wbca), wcab);
+      const ff y4 = ff_add(ff_add(ff_scale(wabc, 3.f), ff_scale(wacb, -1.f)),
+                           ff_add(ff_scale(wbac, -1.f), ff_scale(wcba, -1.f)));
+      const ff y5 = ff_add_f(y4, sgl);
+      const float2 ea = evs[p0][a], eb = evs[p1][b], ec = evs[p2][c];
+      const ff d = ff_add(ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y}), ff{-ec.x, -ec.y});
+      s4 = ff_add(s4, ff_div(ff_mul(z, y4), d));
+      s5 = ff_add(s5, ff_div(ff_mul(z, y5), d));
+    }
+  }
+  CSum c4, c5;
+  c4.add((double) s4.hi);
+  c4.add((double) s4.lo);
+  c5.add((double) s5.hi);
+  c5.add((double) s5.lo);
+  block_reduce_csum(c4, c5, A.part + 4 * (long long) blockIdx.x);
+}
+
+// Fixed-order parallel sum of per-CTA partials (4 doubles each) for one triplet -> out[2].
+__global__ void __launch_bounds__(256) reduce_parts_parallel_kernel(const double* part, int nparts, double scale,
+                                                                     double* out) {
+  CSum a, b;
+  const int per = (nparts + blockDim.x - 1) / blockDim.x;
+  const int q0 = threadIdx.x * per, q1 = min(nparts, q0 + per);
+  for(int q = q0; q < q1; q++) {
+    a.add(part[4 * q + 0]);
+    a.c += part[4 * q + 1];
+    b.add(part[4 * q + 2]);
+    b.c += part[4 * q + 3];
+  }
+  __shared__ double tmp[4];
+  // reuse the fixed-shape block reduction (its shared scratch is sized for 256 threads)
+  block_reduce_csum(a, b, tmp);
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    out[0] = scale * (tmp[0] + tmp[1]);
+    out[1] = scale * (tmp[2] + tmp[3]);
+  }
+}
+
+} // namespace ccsdt

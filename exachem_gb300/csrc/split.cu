@@ -8,12 +8,15 @@
 //   1: INT8 digits, mma.sync m16n8k32 with INT32 accumulation (exact per level)
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <cstring>
 #include <string>
 
 #include "ccsdt_internal.cuh"
 #include "fp64_kernels.cuh"
+#include "energy_tiled.cuh"
+#include "oz_tc.cuh"
 #include "ozaki.cuh"
 
 using namespace ccsdt;
@@ -279,12 +282,20 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
   if(slices_ready >= S && slice_variant == variant) return CCSDT_OK;
   const long long o = this->o, v = this->v;
   const size_t    esz = variant == 0 ? 2 : 1;
-  const int       kc  = variant == 0 ? 32 : 64;
+  const int       kc  = 64; // TMA box width of the tcgen05 path; the mma.sync path steps 32 / 64
   const int       Kpv = (int) ((v + kc - 1) / kc * kc), Kpo = (int) ((o + kc - 1) / kc * kc);
-  // drop old planes
+  // drop old planes (only what this function allocates below; persistent buffers stay)
+  cudaError_t se = cudaStreamSynchronize(stream);
+  if(se != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(se));
   for(void* p: slice_bufs) cudaFree(p);
   slice_bufs.clear();
+  sl_t2 = sl_t2h = sl_ovvv = sl_ooovh = nullptr;
+  ex_t2 = ex_t2h = ex_ovvv = ex_ooovh = nullptr;
+  oovv_f = t1_f = nullptr;
+  F12 = F34 = F56 = nullptr;
+  e_tiles = nullptr;
   slices_ready = 0;
+  tmaps_ready  = false;
   auto grab = [&](void** p, size_t bytes) -> ccsdt_status {
     cudaError_t e = cudaMalloc(p, bytes ? bytes : 1);
     if(e != cudaSuccess) {
@@ -330,8 +341,203 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
   to_float_kernel<<<64, 256, 0, stream>>>(t1, t1_f, o * v);
   cudaError_t e = cudaGetLastError();
   if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("to_float: ") + cudaGetErrorString(e));
+  // energy work items: sorted triples of 8-wide virtual blocks
+  {
+    const int        nb = (int) ((v + ET_B - 1) / ET_B);
+    std::vector<int> host;
+    for(int X = 0; X < nb; X++)
+      for(int Y = X; Y < nb; Y++)
+        for(int Z = Y; Z < nb; Z++) {
+          host.push_back(X);
+          host.push_back(Y);
+          host.push_back(Z);
+        }
+    e_ntiles = (int) (host.size() / 3);
+    if((s = grab((void**) &e_tiles, host.size() * sizeof(int)))) return s;
+    if(!e_part) {
+      cudaError_t ce = cudaMalloc((void**) &e_part, 4 * sizeof(double) * kTiledBlocks);
+      if(ce != cudaSuccess) {
+        e_part = nullptr;
+        cudaGetLastError();
+        return fail(CCSDT_E_OOM, "tiled energy partials: cudaMalloc failed");
+      }
+      owned_bytes.push_back(e_part);
+    }
+    cudaError_t ce = cudaMemcpyAsync(e_tiles, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
+    if(ce == cudaSuccess) ce = cudaStreamSynchronize(stream);
+    if(ce != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(ce));
+  }
+  if(!d_err) { // persistent: survives re-slicing
+    cudaError_t ce = cudaMalloc((void**) &d_err, sizeof(int));
+    if(ce != cudaSuccess) {
+      d_err = nullptr;
+      cudaGetLastError();
+      return fail(CCSDT_E_OOM, "error flag: cudaMalloc failed");
+    }
+    owned_bytes.push_back(d_err);
+  }
   slices_ready  = S;
   slice_variant = variant;
+  tmaps_ready   = false;
+  return CCSDT_OK;
+}
+
+namespace {
+
+enum { MAP_OVVV_NAT = 0, MAP_OVVV_SWP = 1, MAP_T2 = 2, MAP_T2H_NAT = 3, MAP_T2H_SWP = 4, MAP_OOOVH = 5 };
+
+// tcgen05 configurations: digit planes S -> columns per level NT (S NT <= 256, (S + 2) NT <= 512)
+template<int S>
+struct TcPick;
+template<>
+struct TcPick<1> {
+  static constexpr int NT = 128, ST = 4;
+};
+template<>
+struct TcPick<2> {
+  static constexpr int NT = 128, ST = 3;
+};
+template<>
+struct TcPick<3> {
+  static constexpr int NT = 80, ST = 2;
+};
+template<>
+struct TcPick<4> {
+  static constexpr int NT = 64, ST = 2;
+};
+template<>
+struct TcPick<5> {
+  static constexpr int NT = 48, ST = 2;
+};
+int tc_nt(int S) {
+  switch(S) {
+    case 1: return TcPick<1>::NT;
+    case 2: return TcPick<2>::NT;
+    case 3: return TcPick<3>::NT;
+    case 4: return TcPick<4>::NT;
+    case 5: return TcPick<5>::NT;
+  }
+  return 0;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point, so that the library
+// itself does not link libcuda (it must load on machines without a driver).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if(!fn) {
+    void*                           p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+       q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// 5-D BF16 map: dims (k, d1, d2, d3, plane), strides in elements for d1..d3 and plane.
+bool encode_map(CUtensorMap* m, const void* base, int Kp, long long d1, long long d2, long long d3, int planes,
+                long long s1, long long s2, long long s3, long long sp, int box1, int boxp) {
+  cuuint64_t dims[5]    = {(cuuint64_t) Kp, (cuuint64_t) d1, (cuuint64_t) d2, (cuuint64_t) d3, (cuuint64_t) planes};
+  cuuint64_t strides[4] = {(cuuint64_t) s1 * 2, (cuuint64_t) s2 * 2, (cuuint64_t) s3 * 2, (cuuint64_t) sp * 2};
+  cuuint32_t box[5]     = {64, (cuuint32_t) box1, 1, 1, (cuuint32_t) boxp};
+  cuuint32_t estr[5]    = {1, 1, 1, 1, 1};
+  auto fn = encode_fn();
+  if(!fn) return false;
+  CUresult   r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides,
+                                        box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+} // namespace
+
+ccsdt_status ccsdt_handle::ensure_tmaps(int S) {
+  if(tmaps_ready) return CCSDT_OK;
+  const long long o = this->o, v = this->v, S_ = S;
+  const int       NT = tc_nt(S);
+  if(!NT) return fail(CCSDT_E_INVALID, "no tcgen05 configuration for this slice count");
+  const long long Kv = kp_v, Ko = kp_o;
+  bool ok = true;
+  // A side (pair rows, 128-row boxes): rows (z, x, y) natural = z v^2 + x v + y, swapped = z v^2 + y v + x
+  ok &= encode_map(&tmaps[MAP_OVVV_NAT], sl_ovvv, (int) Kv, v, v, o, S, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OVVV_SWP], sl_ovvv, (int) Kv, v, v, o, S, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_T2H_NAT], sl_t2h, (int) Ko, v, v, o, S, Ko, v * Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_T2H_SWP], sl_t2h, (int) Ko, v, v, o, S, v * Ko, Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
+  // B side (single rows, NT-row boxes): t2 rows (xx, yy, a); ooovh rows (yy, zz, c)
+  ok &= encode_map(&tmaps[MAP_T2], sl_t2, (int) Kv, v, o, o, S, Kv, v * Kv, o * v * Kv, pl_t2, NT, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OOOVH], sl_ooovh, (int) Ko, v, o, o, S, Ko, v * Ko, o * v * Ko, pl_ooovh, NT, (int) S_);
+  if(!ok) return fail(CCSDT_E_CUDA, "cuTensorMapEncodeTiled failed for the digit planes");
+  tmaps_ready = true;
+  return CCSDT_OK;
+}
+
+template<int S>
+static ccsdt_status launch_tc(ccsdt_handle* h, TcBatch& b) {
+  constexpr int NT = TcPick<S>::NT, ST = TcPick<S>::ST;
+  using Cfg        = TcCfg<S, NT, ST>;
+  const int    v   = h->v;
+  const long long tiles = (long long) v * ((v + TC_BM - 1) / TC_BM) * ((v + NT - 1) / NT);
+  cudaError_t e = cudaFuncSetAttribute(oz_tc_gemm_kernel<S, NT, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
+  if(e != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string("tc smem attr: ") + cudaGetErrorString(e));
+  oz_tc_gemm_kernel<S, NT, ST><<<dim3((unsigned) tiles, 1, 3), TC_THREADS, Cfg::SMEM, h->stream>>>(b);
+  h->launches++;
+  e = cudaGetLastError();
+  if(e != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string("tc launch: ") + cudaGetErrorString(e));
+  return CCSDT_OK;
+}
+
+static ccsdt_status launch_tc_any(ccsdt_handle* h, TcBatch& b, int S) {
+  switch(S) {
+    case 1: return launch_tc<1>(h, b);
+    case 2: return launch_tc<2>(h, b);
+    case 3: return launch_tc<3>(h, b);
+    case 4: return launch_tc<4>(h, b);
+    case 5: return launch_tc<5>(h, b);
+  }
+  return h->fail(CCSDT_E_INVALID, "no tcgen05 configuration for this slice count");
+}
+
+bool ccsdt_handle::tc_eligible(int S, int variant) const {
+  return variant == 0 && S >= 1 && S <= 5 && kp_v <= 512 && kp_o <= 512 && !force_mma_sync;
+}
+
+ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eout) {
+  ccsdt_status s;
+  if((s = ensure_tmaps(S))) return s;
+  const long long o = this->o, v = this->v, v2 = v * v;
+  auto hole = [&](int xx, bool nat, int yy, int zz) {
+    return TcTerm{nat ? MAP_T2H_NAT : MAP_T2H_SWP, MAP_OOOVH, xx, zz, yy, ex_t2h, nat ? v : 1, nat ? 1 : v,
+                  xx * v2, ex_ooovh + ((long long) yy * o + zz) * v, kp_o, -1.f};
+  };
+  auto part = [&](int z, bool nat, int xx, int yy) {
+    return TcTerm{nat ? MAP_OVVV_NAT : MAP_OVVV_SWP, MAP_T2, z, yy, xx, ex_ovvv, nat ? v : 1, nat ? 1 : v,
+                  z * v2, ex_t2 + ((long long) xx * o + yy) * v, kp_v, 1.f};
+  };
+  TcBatch b;
+  std::memcpy(b.maps, tmaps, sizeof(tmaps));
+  b.v       = (int) v;
+  b.xblocks = (int) v;
+  b.err     = d_err;
+  // l-sum: F[(pair)][single], pairs (a,c) / (b,a) / (c,b)
+  b.job[0] = TcJob{{hole(i, true, k, j), hole(k, false, i, j)}, 2, F12, v, 1, 0};
+  b.job[1] = TcJob{{hole(i, false, j, k), hole(j, true, i, k)}, 2, F34, v, 1, 0};
+  b.job[2] = TcJob{{hole(j, false, k, i), hole(k, true, j, i)}, 2, F56, v, 1, 0};
+  if(profiling) cudaEventRecord(prof_ev[0], stream);
+  if((s = launch_tc_any(this, b, S))) return s;
+  // d-sum: F[single][(pair)], pairs (c,b) / (a,c) / (b,a)
+  b.job[0] = TcJob{{part(k, true, i, j), part(j, false, i, k)}, 2, F12, 1, v2, 1};
+  b.job[1] = TcJob{{part(k, false, j, i), part(i, true, j, k)}, 2, F34, 1, v2, 1};
+  b.job[2] = TcJob{{part(j, true, k, i), part(i, false, k, j)}, 2, F56, 1, v2, 1};
+  if(profiling) cudaEventRecord(prof_ev[1], stream);
+  if((s = launch_tc_any(this, b, S))) return s;
+  if(profiling) cudaEventRecord(prof_ev[2], stream);
+  if((s = launch_energy_tiled(i, j, k, eout))) return s;
+  if(profiling) cudaEventRecord(prof_ev[4], stream);
+  launches += 2;
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("tc energy launch: ") + cudaGetErrorString(e));
   return CCSDT_OK;
 }
 
@@ -386,10 +592,7 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
   if(profiling) cudaEventRecord(prof_ev[1], stream);
   if((s = variant == 0 ? launch_oz<__nv_bfloat16>(this, pb, v, v2) : launch_oz<int8_t>(this, pb, v, v2))) return s;
   if(profiling) cudaEventRecord(prof_ev[2], stream);
-  SplitEnergyArgs ea{F12, F34, F56, oovv_f, t1_f, eo, ev, (int) o, (int) v, i, j, k, part};
-  energy_split_kernel<<<kEnergyBlocks, E_THREADS, 0, stream>>>(ea);
-  if(profiling) cudaEventRecord(prof_ev[3], stream);
-  reduce_parts_kernel<<<1, 32, 0, stream>>>(part, kEnergyBlocks, multiplicity(i, j, k) / 9.0, eout);
+  if((s = launch_energy_tiled(i, j, k, eout))) return s;
   if(profiling) cudaEventRecord(prof_ev[4], stream);
   launches += 2;
   cudaError_t e = cudaGetLastError();
@@ -404,6 +607,11 @@ ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* 
   if(v > OZ_KWIN * 64) return fail(CCSDT_E_INVALID, "v too large for the split path");
   ccsdt_status s;
   if((s = ensure_slices(S, variant))) return s;
+  if(!d_err || !F12 || !F34 || !F56 || !e_tiles || !e_part || !oovv_f || !t1_f)
+    return fail(CCSDT_E_STATE, "split-precision buffers missing after slicing");
+  force_mma_sync = opts->reserved[0] != 0; // test knob: the mma.sync slice kernel everywhere
+  cudaError_t e0 = cudaMemsetAsync(d_err, 0, sizeof(int), stream);
+  if(e0 != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e0));
   for(long t = 0; t < n; t++) {
     const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
     if(i == k) {
@@ -411,7 +619,31 @@ ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* 
       if(e != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e));
       continue;
     }
-    if((s = run_triplet_split(i, j, k, S, variant, etrip + 2 * t))) return s;
+    if(tc_eligible(S, variant)) {
+      if((s = run_triplet_tc(i, j, k, S, etrip + 2 * t))) return s;
+    } else if((s = run_triplet_split(i, j, k, S, variant, etrip + 2 * t)))
+      return s;
   }
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_handle::check_device_error() {
+  if(!d_err) return fail(CCSDT_E_STATE, "device error flag missing");
+  int         flag = 0;
+  cudaError_t e    = cudaMemcpyAsync(&flag, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  if(e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e));
+  if(flag) return fail(CCSDT_E_TIMEOUT, "a bounded device-side wait of the tcgen05 contraction gave up");
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_handle::launch_energy_tiled(int i, int j, int k, double* eout) {
+  const int       G = e_ntiles < kTiledBlocks ? e_ntiles : kTiledBlocks;
+  TiledEnergyArgs ea{F12, F34, F56, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles, o, v, i, j, k, e_part};
+  energy_tiled_kernel<<<G, ET_THREADS, 0, stream>>>(ea);
+  if(profiling) cudaEventRecord(prof_ev[3], stream);
+  reduce_parts_parallel_kernel<<<1, 256, 0, stream>>>(e_part, G, multiplicity(i, j, k) / 9.0, eout);
+  cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("tiled energy launch: ") + cudaGetErrorString(e));
   return CCSDT_OK;
 }

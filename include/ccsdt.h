@@ -117,6 +117,12 @@ ccsdt_status ccsdt_set_stream(ccsdt_handle* h, void* stream);
 ccsdt_status ccsdt_profile_triplet(ccsdt_handle* h, const ccsdt_opts* opts, int i, int j, int k,
                                    double* out_ms);
 
+/* Connected triples W_abc (v^3 doubles, [a][b][c], host memory) of one triplet
+ * i <= j <= k, i < k, in the precision `opts` selects.  Verification aid: no counterpart
+ * in the reference, whose t3 blocks stay internal (ccsd_t_all_fused_cpu.hpp:103-170). */
+ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts* opts, int i, int j, int k,
+                                   double* w_host);
+
 /* Number of kernel launches issued by the last ccsdt_energy / ccsdt_triplet_energies. */
 long ccsdt_last_launch_count(const ccsdt_handle* h);
 
@@ -143,6 +149,30 @@ ccsdt_status ccsdt_energy_noalloc(int o, int v, const double* eps_occ, const dou
                                   const double* t1, const double* t2, const double* oovv,
                                   const double* ooov, const double* ovvv, double* energies,
                                   void* stream);
+
+/* ---- learned slice count (no counterpart in the reference) --------------------------
+ * A 12 -> 64 -> 64 -> 7 MLP (ReLU, softmax over slice counts 2..8) predicts, per occupied
+ * triplet, the smallest digit-plane count that keeps the triplet's energy error under a
+ * budget.  Parameters are CCSDT_MLP_NPARAM floats: W1[64][12] b1[64] W2[64][64] b2[64]
+ * W3[7][64] b3[7].  Training runs on the GPU in FP32 (hand-written forward/backward and
+ * Adam kernels); inference runs in BF16.  All pointers below are host pointers. */
+#define CCSDT_MLP_IN 12
+#define CCSDT_MLP_HIDDEN 64
+#define CCSDT_MLP_OUT 7
+#define CCSDT_MLP_NPARAM (64 * 12 + 64 + 64 * 64 + 64 + 7 * 64 + 7)
+
+/* grad = d(mean cross-entropy)/d(params) over n samples X[n][12] with labels 0..6 (slice
+ * count - 2); *loss = the mean cross-entropy. */
+ccsdt_status ccsdt_mlp_grad(const float* params, const float* X, const int* labels, int n, float* grad,
+                            float* loss);
+
+/* Adam training for `epochs` passes over shuffled minibatches of `batch`; init != 0 first
+ * draws a seeded He-uniform initialisation into params.  params is updated in place. */
+ccsdt_status ccsdt_mlp_train(const float* X, const int* labels, int n, int epochs, int batch, float lr,
+                             unsigned seed, int init, float* params, float* final_loss);
+
+/* BF16 inference: slices[s] = 2 + argmax of the logits (logits[n][7] optional). */
+ccsdt_status ccsdt_mlp_predict(const float* params, const float* X, int n, int* slices, float* logits);
 
 void        ccsdt_destroy(ccsdt_handle* h);
 const char* ccsdt_last_error(const ccsdt_handle* h);

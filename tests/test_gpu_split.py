@@ -1,0 +1,69 @@
+"""Split-precision (Ozaki) path on the GPU: the tcgen05 kernel against the mma.sync slice
+kernel (same exact level sums), INT8 against BF16 digits, and the error against the FP64
+path as the slice count grows.
+
+Tolerances are relative to |E(T)| (the synthetic energies are 1e-1 .. 1e11 Eh, so absolute
+Eh bounds do not transfer): digits carry 7 bits each, so S slices bound the contraction
+error near 2^(-7 S) of the operand scale; the observed |dE/E| is stated per S below.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# |dE(T)/E(T)| bounds vs FP64 per slice count, with headroom over what GB300 measured
+# (o=12, v=70: S=2 9.6e-7, S=3 9.2e-9, S=4 5.5e-11, S=5 3.5e-12)
+BOUND = {2: 5e-6, 3: 5e-8, 4: 5e-10, 5: 5e-11}
+
+
+def _ft(o, v, seed, **kw):
+    from exachem_gb300.ccsd_t import FusedTriples
+    from exachem_gb300.generator import generate
+    d = generate(o, v, seed, **kw)
+    ft = FusedTriples(o, v, ts=40)
+    ft.upload_dict(d)
+    return ft
+
+
+@pytest.mark.parametrize("o,v,seed", [(4, 16, 1), (6, 40, 0), (5, 130, 2)])
+def test_tcgen05_equals_mma_sync_levels(built, o, v, seed):
+    ft = _ft(o, v, seed)
+    for S in (1, 2, 3, 4, 5):
+        tc = ft.energy("ozaki", slices=S)
+        leg = ft.energy("ozaki", slices=S, legacy_mma=1)
+        assert tc["e_paren_T"] == pytest.approx(leg["e_paren_T"], rel=1e-13, abs=0)
+        assert tc["e_bracket_T"] == pytest.approx(leg["e_bracket_T"], rel=1e-13, abs=0)
+
+
+def test_int8_digits_equal_bf16_digits(built):
+    ft = _ft(6, 40, 3)
+    for S in (2, 4):
+        a = ft.energy("ozaki", slices=S, legacy_mma=1)["e_paren_T"]
+        b = ft.energy("ozaki", slices=S, slice_kind="int8")["e_paren_T"]
+        assert a == pytest.approx(b, rel=1e-13, abs=0)
+
+
+def test_split_error_shrinks_with_slices(built):
+    ft = _ft(12, 70, 21)
+    ref = ft.energy("fp64")["e_paren_T"]
+    errs = {}
+    for S in (2, 3, 4, 5):
+        errs[S] = abs(ft.energy("ozaki", slices=S)["e_paren_T"] - ref) / abs(ref)
+        assert errs[S] <= BOUND[S], (S, errs)
+    assert errs[3] < errs[2] and errs[4] < errs[3]
+
+
+def test_split_triplet_w_close_to_fp64(built):
+    ft = _ft(6, 40, 0)
+    for (i, j, k) in [(0, 1, 2), (1, 3, 3), (0, 0, 5)]:
+        wf = ft.triplet_w(i, j, k, "fp64")
+        ws = ft.triplet_w(i, j, k, "ozaki", slices=5)
+        assert np.abs(ws - wf).max() <= 1e-9 * np.abs(wf).max()
+
+
+def test_split_per_triplet_sum_equals_total(built):
+    from exachem_gb300.ccsd_t import all_triplets
+    ft = _ft(7, 33, 4)
+    tot = ft.energy("ozaki", slices=3)
+    e4, e5 = ft.triplet_energies(all_triplets(7), "ozaki", slices=3)
+    assert e5.sum() == pytest.approx(tot["e_paren_T"], rel=1e-13)
