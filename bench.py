@@ -211,11 +211,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="auto", choices=["auto", "fp64", "ozaki", "learned"])
-    ap.add_argument("--slices", type=int, default=4)
+    ap.add_argument("--slices", type=int, default=3)
     ap.add_argument("--o", type=int, default=60)
     ap.add_argument("--v", type=int, default=500)
     ap.add_argument("--seed", type=int, default=3)
     ap.add_argument("--fp64-batch", type=int, default=2, help="triplets per step in fp64 mode")
+    ap.add_argument("--batch", type=int, default=48, help="triplets per step in split mode")
     ap.add_argument("--cpu-sample", type=int, default=1, help="triplets timed on the CPU baseline (0: skip)")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -239,9 +240,10 @@ def main():
 
     mode = args.mode
     if mode == "auto":
-        mode = "ozaki" if os.environ.get("CCSDT_SPLIT_READY", "0") == "1" else "fp64"
+        mode = "ozaki"
     o, v, seed = args.o, args.v, args.seed
     occ_tiles, vir_tiles = workload_tiles(o, v, seed)
+    S = args.slices
 
     t0 = time.perf_counter()
     dev = generate_device(o, v, seed, device="cuda")
@@ -249,20 +251,31 @@ def main():
     t_gen = time.perf_counter() - t0
     fp64_peak = dgemm_peak_tflops(torch)
 
-    ft = ct.FusedTriples(o, v, occ_tiles, vir_tiles, device=local)
-    ft.upload_dict(dev)
-    stream = torch.cuda.current_stream()
-    ft.set_stream(stream.cuda_stream)
-
     tri_all = triplet_list(o)
     mine = tri_all[rank::world]                       # independent triplets, no data-path collective
-    kw = {"slices": args.slices} if mode != "fp64" else {}
-    if mode == "fp64":
-        batches = [spread_sample(mine, args.fp64_batch, offset=s) for s in range(args.steps)]
-        warm = [spread_sample(mine, 1, offset=len(mine) // 3 + s) for s in range(args.warmup)]
-    else:
-        batches = np.array_split(mine, args.steps)
-        warm = [mine[: max(1, len(mine) // (4 * args.steps))] for _ in range(args.warmup)]
+    cpu_samp = spread_sample(tri_all, max(1, args.cpu_sample), offset=len(tri_all) // 2)
+    host_slabs = host_slabs_from_device(dev, cpu_samp) if (rank == 0 and args.cpu_sample > 0) else None
+    keys = ["eps_occ", "eps_vir", "t1", "t2", "oovv", "ooov", "ovvv"]
+    host = None
+    if not args.no_e2e and rank == 0:
+        try:
+            host = {k: torch.empty(dev[k].shape, dtype=torch.float64, pin_memory=True) for k in keys}
+        except RuntimeError:
+            host = {k: torch.empty(dev[k].shape, dtype=torch.float64) for k in keys}
+        for k in keys:
+            host[k].copy_(dev[k])
+
+    ft = ct.FusedTriples(o, v, occ_tiles, vir_tiles, device=local)
+    ft.upload_dict(dev)
+    del dev
+    torch.cuda.empty_cache()
+    stream = torch.cuda.current_stream()
+    ft.set_stream(stream.cuda_stream)
+    kw = {"slices": S} if mode != "fp64" else {}
+
+    per_step = args.fp64_batch if mode == "fp64" else args.batch
+    batches = [spread_sample(mine, per_step, offset=s) for s in range(args.steps)]
+    warm = [spread_sample(mine, max(1, per_step // 4), offset=len(mine) // 3 + s) for s in range(args.warmup)]
     for b in warm:
         ft.triplet_energies(b, mode, **kw)
     torch.cuda.synchronize()
@@ -293,34 +306,45 @@ def main():
     frac = timed_trip / len(mine)
     value = elapsed / frac                               # whole call (all triplets) on N GPUs
 
-    # per-phase device times of one representative triplet -> roofline of the d-sum GEMMs
+    # per-phase device times of one representative triplet -> roofline of the d-sum contraction
     i, j, k = (int(x) for x in mine[len(mine) // 2])
     prof = [ft.profile_triplet(i, j, k, mode, **kw) for _ in range(3)]
     gemm_ms = statistics.median(p[1] for p in prof)
-    gemm_flops = 12.0 * float(v) ** 4                      # 3 arrays x 2 terms x 2 v^4
-    achieved = gemm_flops / (gemm_ms * 1e-3) / 1e12
+    fp64_eq = 12.0 * float(v) ** 4                         # 3 arrays x 2 terms x 2 v^4 multiply-adds
     peaks = measured_peaks()
     if mode == "fp64":
+        per_launch = fp64_eq
         peak, peak_src = fp64_peak, "measured (cuBLAS DGEMM 8192^3 in this run; FP64 is not in MEASURED_PEAKS.json)"
         kernel = "dmma_gemm_kernel"
     else:
-        peak, peak_src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (burst)"
-        kernel = "ozaki_gemm_kernel"
+        per_launch = fp64_eq * S * (S + 1) / 2             # BF16 digit-plane products actually required
+        peak, peak_src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (burst), of measured"
+        kernel = "oz_tc_gemm_kernel"
+    achieved = per_launch / (gemm_ms * 1e-3) / 1e12
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": profile_traffic(kernel), "kernel": kernel,
-            "per_launch_flops": gemm_flops, "launch_ms": gemm_ms, "peak_source": peak_src,
+            "per_launch_flops": per_launch, "launch_ms": gemm_ms, "peak_source": peak_src,
+            "fp64_equivalent_tflops": fp64_eq / (gemm_ms * 1e-3) / 1e12,
             "phase_ms": dict(zip(["l_sum", "d_sum", "energy", "reduce"], prof[1]))}
+
+    # plain FP64 on the same shape (projected from a few triplets) and |dE| on the CPU sample
+    fp64_proj, dE = None, None
+    if rank == 0 and mode != "fp64":
+        fb = spread_sample(mine, args.fp64_batch, offset=7)
+        ft.triplet_energies(fb[:1], "fp64")
+        torch.cuda.synchronize()
+        ta = time.perf_counter()
+        ft.triplet_energies(fb, "fp64")
+        torch.cuda.synchronize()
+        fp64_proj = (time.perf_counter() - ta) / len(fb) * len(tri_all) / world
+        f4, f5 = ft.triplet_energies(cpu_samp, "fp64")
+        s4, s5 = ft.triplet_energies(cpu_samp, mode, **kw)
+        dE = {"triplets": cpu_samp.tolist(), "rel_E(T)_vs_fp64": (np.abs(s5 - f5) / np.abs(f5)).tolist(),
+              "rel_E[T]_vs_fp64": (np.abs(s4 - f4) / np.abs(f4)).tolist()}
 
     # end to end through the C ABI with host (pinned) buffers: upload + one batch + readback
     e2e = None
-    if not args.no_e2e and rank == 0:
-        keys = ["eps_occ", "eps_vir", "t1", "t2", "oovv", "ooov", "ovvv"]
-        try:
-            host = {k: torch.empty(dev[k].shape, dtype=torch.float64, pin_memory=True) for k in keys}
-        except RuntimeError:
-            host = {k: torch.empty(dev[k].shape, dtype=torch.float64) for k in keys}
-        for k in keys:
-            host[k].copy_(dev[k])
+    if host is not None:
         harr = {k: host[k].numpy() for k in keys}
         h2d = sum(a.nbytes for a in harr.values())
         b = batches[0]
@@ -340,36 +364,33 @@ def main():
         e2e = {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 16 * len(b),
                "upload_s": min(up), "projection": "one upload + per-triplet API time x triplets per GPU"}
         del host, harr
-        ft.upload_dict(dev)
 
-    # CPU baseline: the oracle's C restatement on this host, one triplet of this workload
+    # CPU baseline: the oracle's C restatement on this host, on the sample triplet(s)
     cpu = None
-    dE = None
-    if rank == 0 and args.cpu_sample > 0:
-        samp = spread_sample(tri_all, args.cpu_sample, offset=len(tri_all) // 2)
-        hs = host_slabs_from_device(dev, samp)
-        t_cpu, (c4, c5), cores = cpu_baseline_port(hs, samp)
-        g4, g5 = ft.triplet_energies(samp, mode, **kw)
-        dE = {"sample_triplets": samp.tolist(), "gpu_e_paren": g5.tolist(), "oracle_e_paren": c5.tolist(),
-              "max_rel": float(np.max(np.abs(g5 - c5) / np.maximum(np.abs(c5), 1e-300)))}
-        cpu = {"value": t_cpu / len(samp) * len(tri_all), "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"{len(samp)} triplet(s) {samp.tolist()} of {len(tri_all)} at o={o} v={v} "
-                         f"(oracle C restatement, {cores} OpenMP threads, {t_cpu:.1f} s), projected to the whole call"}
+    if host_slabs is not None:
+        t_cpu, (c4, c5), cores = cpu_baseline_port(host_slabs, cpu_samp)
+        g4, g5 = ft.triplet_energies(cpu_samp, "fp64")
+        cpu = {"value": t_cpu / len(cpu_samp) * len(tri_all), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{len(cpu_samp)} triplet(s) {cpu_samp.tolist()} of {len(tri_all)} at o={o} v={v} "
+                         f"(oracle C restatement, {cores} OpenMP threads, {t_cpu:.1f} s), projected to the whole call",
+               "fp64_gpu_vs_cpu_max_rel": float(np.max(np.abs(g5 - c5) / np.abs(c5)))}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / max(1, len(batches)),
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if mode == "fp64" else "bf16-slices/f64", "data": "synthetic (seeded generator, built on GPU)",
+            "dtype": "f64" if mode == "fp64" else "bf16 digit planes (exact FP32 levels), float-float recombination",
+            "data": "synthetic (seeded generator, built on GPU)",
             "config": {"workload": f"closed-shell (T) o={o} v={v} seed={seed} ragged tiles", "o": o, "v": v,
-                       "mode": mode, "slices": args.slices if mode != "fp64" else None,
+                       "mode": mode, "slices": S if mode != "fp64" else None,
                        "occ_tiles": occ_tiles, "vir_tiles": vir_tiles, "triplets_total": int(len(tri_all)),
                        "triplets_timed": int(timed_trip), "timed_fraction": frac,
                        "projection": None if frac >= 1 else "value = timed seconds / timed_fraction",
                        "l2": "inputs (75 GB) and per-triplet scratch (3 GB) exceed L2; no flush"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "energy_sample": dE, "partial_energy_timed": {"e_bracket_T": esum4, "e_paren_T": esum5},
+            "fp64_projected_s": fp64_proj, "speedup_vs_fp64": (fp64_proj / value) if fp64_proj else None,
             "setup": {"generate_s": t_gen, "fp64_dgemm_tflops": fp64_peak},
         }
         print(json.dumps(line), flush=True)

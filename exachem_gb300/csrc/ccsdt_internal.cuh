@@ -43,10 +43,14 @@ struct ccsdt_handle {
   // tcgen05 path: TMA maps over the digit planes (built once per slicing) and an error flag
   CUtensorMap        tmaps[6];
   bool               tmaps_ready = false;
+  int                tmaps_S     = 0;
   int*               d_err       = nullptr;
   int*               e_tiles     = nullptr; // sorted virtual block triples of the tiled energy
   int                e_ntiles    = 0;
   double*            e_part      = nullptr;
+  // a-posteriori estimate slots of the triplet being run (nullptr: not collected)
+  float*             cur_tail    = nullptr;
+  double*            cur_sens    = nullptr;
 
   long        launches       = 0;
   double      last_err_bound = 0.0;
@@ -70,6 +74,19 @@ struct ccsdt_handle {
   bool         tc_eligible(int S, int variant) const;
   double*      part_buf() { return part; }
   ccsdt_status launch_energy_tiled(int i, int j, int k, double* eout);
+  ccsdt_status run_triplet_S(int i, int j, int k, int S, double* eout);
+  // learned slice count
+  ccsdt_status run_learned(const ccsdt_opts* opts, long n, const int* tri_host);
+  ccsdt_status features(long n, const int* tri_dev, float* feats_dev);
+  ccsdt_status ensure_stats();
+  std::vector<float> model;          // MLP parameters (host copy); empty = no model
+  void*              model_bf16 = nullptr;
+  int*               st_slab = nullptr, *st_pair = nullptr, *st_hole = nullptr; // exponent statistics
+  int                stats_for = -1;  // slicing generation the statistics belong to
+  int                slice_gen = 0;
+  // per-call statistics of the learned mode
+  double             learned_mean_slices = 0.0;
+  long               learned_fallbacks   = 0;
   ccsdt_status check_device_error();
   bool         force_mma_sync = false; // use the mma.sync slice kernel even where tcgen05 applies
 };

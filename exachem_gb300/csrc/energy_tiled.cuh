@@ -25,7 +25,7 @@ struct TiledEnergyArgs {
   const int3*   tiles;     // sorted block triples
   int           ntiles;
   int           o, v, i, j, k;
-  double*       part;      // 4 doubles per CTA
+  double*       part;      // 6 doubles per CTA: E[T] (s, c), E(T) (s, c), sum (|Z| + |Y|) / |D|, 0
 };
 
 // slot s <-> permutation (p0, p1, p2) of the block positions
@@ -50,7 +50,8 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
   const ff        eijk = ff_add(ff_add(ff_from_double(A.eo[i]), ff_from_double(A.eo[j])), ff_from_double(A.eo[k]));
   const float *   gOjk = A.oovv + ((long long) j * o + k) * v2, *gOik = A.oovv + ((long long) i * o + k) * v2,
               *gOij = A.oovv + ((long long) i * o + j) * v2;
-  ff s4{0.f, 0.f}, s5{0.f, 0.f};
+  ff    s4{0.f, 0.f}, s5{0.f, 0.f};
+  float sens = 0.f; // first-order sensitivity of the energy to errors in W (a-posteriori estimate)
 
   for(int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
     __syncthreads();
@@ -153,6 +154,7 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
       const ff d = ff_add(ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y}), ff{-ec.x, -ec.y});
       s4 = ff_add(s4, ff_div(ff_mul(z, y4), d));
       s5 = ff_add(s5, ff_div(ff_mul(z, y5), d));
+      sens += (fabsf(z.hi) + fabsf(y5.hi)) / fabsf(d.hi);
     }
   }
   CSum c4, c5;
@@ -160,20 +162,38 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
   c4.add((double) s4.lo);
   c5.add((double) s5.hi);
   c5.add((double) s5.lo);
-  block_reduce_csum(c4, c5, A.part + 4 * (long long) blockIdx.x);
+  block_reduce_csum(c4, c5, A.part + 6 * (long long) blockIdx.x);
+  // fixed-order block sum of the sensitivity
+  __shared__ float ssum[ET_THREADS / 32];
+#pragma unroll
+  for(int off = 16; off > 0; off >>= 1) sens += __shfl_down_sync(0xffffffffu, sens, off);
+  if((threadIdx.x & 31) == 0) ssum[threadIdx.x >> 5] = sens;
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    double t = 0.0;
+    for(int q = 0; q < ET_THREADS / 32; q++) t += ssum[q];
+    A.part[6 * (long long) blockIdx.x + 4] = t;
+    A.part[6 * (long long) blockIdx.x + 5] = 0.0;
+  }
 }
 
-// Fixed-order parallel sum of per-CTA partials (4 doubles each) for one triplet -> out[2].
+// Fixed-order parallel sum of per-CTA partials (6 doubles each) for one triplet -> out[2]
+// (energies); sens_out[0] (optional) receives scale * the summed sensitivity.
 __global__ void __launch_bounds__(256) reduce_parts_parallel_kernel(const double* part, int nparts, double scale,
-                                                                     double* out) {
+                                                                     double* out, double* sens_out) {
   CSum a, b;
   const int per = (nparts + blockDim.x - 1) / blockDim.x;
   const int q0 = threadIdx.x * per, q1 = min(nparts, q0 + per);
   for(int q = q0; q < q1; q++) {
-    a.add(part[4 * q + 0]);
-    a.c += part[4 * q + 1];
-    b.add(part[4 * q + 2]);
-    b.c += part[4 * q + 3];
+    a.add(part[6 * q + 0]);
+    a.c += part[6 * q + 1];
+    b.add(part[6 * q + 2]);
+    b.c += part[6 * q + 3];
+  }
+  if(sens_out && threadIdx.x == 0) {
+    double t = 0.0;
+    for(int q = 0; q < nparts; q++) t += part[6 * q + 4];
+    sens_out[0] = scale * t;
   }
   __shared__ double tmp[4];
   // reuse the fixed-shape block reduction (its shared scratch is sized for 256 threads)

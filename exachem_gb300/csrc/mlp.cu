@@ -256,3 +256,10 @@ extern "C" ccsdt_status ccsdt_mlp_predict(const float* params, const float* X, i
   if(logits && cudaMemcpy(logits, dl.p, (size_t) n * OUT * 4, cudaMemcpyDeviceToHost) != cudaSuccess) return CCSDT_E_CUDA;
   return CCSDT_OK;
 }
+
+// Device-side BF16 inference for the LEARNED mode (inputs already on the device).
+void ccsdt_mlp_infer_device(const void* params_bf16, const float* X, long n, int* slices, cudaStream_t st) {
+  if(n <= 0) return;
+  mlp_infer_kernel<<<(unsigned) ((n + 127) / 128), 128, 0, st>>>(static_cast<const __nv_bfloat16*>(params_bf16), X,
+                                                                 (int) n, slices, nullptr);
+}

@@ -51,6 +51,7 @@ struct TcBatch {
   int         v;        // pair rows per x and single rows
   int         xblocks;  // x values (= v)
   int*        err;      // device error flag (set on a wait timeout)
+  float*      tail;     // optional: max |contribution of the last kept level| (a-posteriori estimate)
 };
 
 template<int S, int NT, int STAGES>
@@ -185,6 +186,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
     const bool vrow = y < v;
     const long long m = (long long) x * v + y;
     const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
+    float          tmax      = 0.f; // largest |last-level term| seen by this thread
     for(int t = 0; t < J.nterms; t++) {
       const TcTerm& T = J.t[t];
       // warp-uniform decision: the tcgen05.ld / st below are .sync.aligned
@@ -222,10 +224,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
           sm100::tmem_wait_ld();
 #pragma unroll
           for(int e = 0; e < 16; e++) {
-            const float sc = ldexpf(T.sign, ea + eb[e] - OZ_BITS * (l + 2));
-            ff a = ff_add_f(ff{hi[e], lo[e]}, __uint_as_float(rv[e]) * sc);
+            const float sc   = ldexpf(T.sign, ea + eb[e] - OZ_BITS * (l + 2));
+            const float term = __uint_as_float(rv[e]) * sc;
+            ff a = ff_add_f(ff{hi[e], lo[e]}, term);
             hi[e] = a.hi;
             lo[e] = a.lo;
+            if(l == S - 1 && vrow) tmax = fmaxf(tmax, fabsf(term));
           }
         }
         if(!last) {
@@ -255,6 +259,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
       }
       sm100::tc_fence_before();
       sm100::mbar_arrive(tmem_free);
+    }
+    if(P.tail) {
+#pragma unroll
+      for(int off = 16; off > 0; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+      if(lane == 0 && tmax > 0.f) atomicMax(reinterpret_cast<int*>(P.tail), __float_as_int(tmax));
     }
   }
   sm100::tc_fence_before();

@@ -355,7 +355,7 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
     e_ntiles = (int) (host.size() / 3);
     if((s = grab((void**) &e_tiles, host.size() * sizeof(int)))) return s;
     if(!e_part) {
-      cudaError_t ce = cudaMalloc((void**) &e_part, 4 * sizeof(double) * kTiledBlocks);
+      cudaError_t ce = cudaMalloc((void**) &e_part, 6 * sizeof(double) * kTiledBlocks);
       if(ce != cudaSuccess) {
         e_part = nullptr;
         cudaGetLastError();
@@ -379,6 +379,7 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
   slices_ready  = S;
   slice_variant = variant;
   tmaps_ready   = false;
+  slice_gen++;
   return CCSDT_OK;
 }
 
@@ -439,6 +440,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 // 5-D BF16 map: dims (k, d1, d2, d3, plane), strides in elements for d1..d3 and plane.
 bool encode_map(CUtensorMap* m, const void* base, int Kp, long long d1, long long d2, long long d3, int planes,
                 long long s1, long long s2, long long s3, long long sp, int box1, int boxp) {
+  if(boxp > planes) return false;
   cuuint64_t dims[5]    = {(cuuint64_t) Kp, (cuuint64_t) d1, (cuuint64_t) d2, (cuuint64_t) d3, (cuuint64_t) planes};
   cuuint64_t strides[4] = {(cuuint64_t) s1 * 2, (cuuint64_t) s2 * 2, (cuuint64_t) s3 * 2, (cuuint64_t) sp * 2};
   cuuint32_t box[5]     = {64, (cuuint32_t) box1, 1, 1, (cuuint32_t) boxp};
@@ -454,22 +456,25 @@ bool encode_map(CUtensorMap* m, const void* base, int Kp, long long d1, long lon
 } // namespace
 
 ccsdt_status ccsdt_handle::ensure_tmaps(int S) {
-  if(tmaps_ready) return CCSDT_OK;
+  if(tmaps_ready && tmaps_S == S) return CCSDT_OK;
+  if(S > slices_ready) return fail(CCSDT_E_STATE, "tensor maps asked for more planes than were sliced");
   const long long o = this->o, v = this->v, S_ = S;
+  const int       P = slices_ready; // stored planes (extent); the box loads the first S
   const int       NT = tc_nt(S);
   if(!NT) return fail(CCSDT_E_INVALID, "no tcgen05 configuration for this slice count");
   const long long Kv = kp_v, Ko = kp_o;
   bool ok = true;
   // A side (pair rows, 128-row boxes): rows (z, x, y) natural = z v^2 + x v + y, swapped = z v^2 + y v + x
-  ok &= encode_map(&tmaps[MAP_OVVV_NAT], sl_ovvv, (int) Kv, v, v, o, S, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
-  ok &= encode_map(&tmaps[MAP_OVVV_SWP], sl_ovvv, (int) Kv, v, v, o, S, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
-  ok &= encode_map(&tmaps[MAP_T2H_NAT], sl_t2h, (int) Ko, v, v, o, S, Ko, v * Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
-  ok &= encode_map(&tmaps[MAP_T2H_SWP], sl_t2h, (int) Ko, v, v, o, S, v * Ko, Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OVVV_NAT], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OVVV_SWP], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_T2H_NAT], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_T2H_SWP], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
   // B side (single rows, NT-row boxes): t2 rows (xx, yy, a); ooovh rows (yy, zz, c)
-  ok &= encode_map(&tmaps[MAP_T2], sl_t2, (int) Kv, v, o, o, S, Kv, v * Kv, o * v * Kv, pl_t2, NT, (int) S_);
-  ok &= encode_map(&tmaps[MAP_OOOVH], sl_ooovh, (int) Ko, v, o, o, S, Ko, v * Ko, o * v * Ko, pl_ooovh, NT, (int) S_);
+  ok &= encode_map(&tmaps[MAP_T2], sl_t2, (int) Kv, v, o, o, P, Kv, v * Kv, o * v * Kv, pl_t2, NT, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OOOVH], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, NT, (int) S_);
   if(!ok) return fail(CCSDT_E_CUDA, "cuTensorMapEncodeTiled failed for the digit planes");
   tmaps_ready = true;
+  tmaps_S     = S;
   return CCSDT_OK;
 }
 
@@ -520,6 +525,7 @@ ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eo
   b.v       = (int) v;
   b.xblocks = (int) v;
   b.err     = d_err;
+  b.tail    = cur_tail;
   // l-sum: F[(pair)][single], pairs (a,c) / (b,a) / (c,b)
   b.job[0] = TcJob{{hole(i, true, k, j), hole(k, false, i, j)}, 2, F12, v, 1, 0};
   b.job[1] = TcJob{{hole(i, false, j, k), hole(j, true, i, k)}, 2, F34, v, 1, 0};
@@ -601,6 +607,7 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 }
 
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
+  if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
   const int S       = opts->slices;
   const int variant = opts->slice_kind;
   if(variant != 0 && variant != 1) return fail(CCSDT_E_INVALID, "unknown slice variant");
@@ -642,8 +649,13 @@ ccsdt_status ccsdt_handle::launch_energy_tiled(int i, int j, int k, double* eout
   TiledEnergyArgs ea{F12, F34, F56, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles, o, v, i, j, k, e_part};
   energy_tiled_kernel<<<G, ET_THREADS, 0, stream>>>(ea);
   if(profiling) cudaEventRecord(prof_ev[3], stream);
-  reduce_parts_parallel_kernel<<<1, 256, 0, stream>>>(e_part, G, multiplicity(i, j, k) / 9.0, eout);
+  reduce_parts_parallel_kernel<<<1, 256, 0, stream>>>(e_part, G, multiplicity(i, j, k) / 9.0, eout, cur_sens);
   cudaError_t e = cudaGetLastError();
   if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("tiled energy launch: ") + cudaGetErrorString(e));
   return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_handle::run_triplet_S(int i, int j, int k, int S, double* eout) {
+  if(tc_eligible(S, 0)) return run_triplet_tc(i, j, k, S, eout);
+  return run_triplet_split(i, j, k, S, 0, eout);
 }

@@ -1,0 +1,165 @@
+"""Training data, training and use of the per-triplet slice-count model.
+
+Labels: for an occupied triplet, the smallest digit-plane count S in 2..smax whose
+triplet energy E_t(S) satisfies |E_t(S) - E_t(FP64)| <= budget * |E_t(FP64)|, measured
+against the library's own FP64 path (the plain kernel judges the error).  Features come
+from the library (ccsdt_triplet_features, 12 per triplet).  Training runs on the GPU
+through ccsdt_mlp_train (hand-written FP32 forward / backward / Adam kernels).
+
+The budget is relative: with the synthetic generator triplet energies range over many
+decades (1e-6 .. 1e7 Eh), so a fixed absolute budget would be either unreachable or void.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+from pathlib import Path
+
+import numpy as np
+
+from . import ccsd_t as ct
+
+MODEL_PATH = Path(__file__).resolve().parent / "slice_model.json"
+NPARAM = 64 * 12 + 64 + 64 * 64 + 64 + 7 * 64 + 7
+_F = ctypes.POINTER(ctypes.c_float)
+_I = ctypes.POINTER(ctypes.c_int)
+
+
+def _lib():
+    lib = ct.load_library()
+    lib.ccsdt_mlp_grad.argtypes = [_F, _F, _I, ctypes.c_int, _F, _F]
+    lib.ccsdt_mlp_train.argtypes = [_F, _I, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                    ctypes.c_uint, ctypes.c_int, _F, _F]
+    lib.ccsdt_mlp_predict.argtypes = [_F, _F, ctypes.c_int, _I, _F]
+    lib.ccsdt_triplet_features.argtypes = [ctypes.c_void_p, ctypes.c_long, _I, _F]
+    lib.ccsdt_set_slice_model.argtypes = [ctypes.c_void_p, _F]
+    lib.ccsdt_learned_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                        ctypes.POINTER(ctypes.c_long)]
+    for n in ("ccsdt_mlp_grad", "ccsdt_mlp_train", "ccsdt_mlp_predict", "ccsdt_triplet_features",
+              "ccsdt_set_slice_model", "ccsdt_learned_stats"):
+        getattr(lib, n).restype = ctypes.c_int
+    return lib
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def mlp_grad(params, X, y):
+    """GPU gradient of the mean cross-entropy (labels y in 0..6)."""
+    p, X, y = _f32(params), _f32(X), np.ascontiguousarray(y, dtype=np.int32)
+    g, loss = np.zeros(NPARAM, np.float32), ctypes.c_float()
+    st = _lib().ccsdt_mlp_grad(p.ctypes.data_as(_F), X.ctypes.data_as(_F), y.ctypes.data_as(_I), len(y),
+                               g.ctypes.data_as(_F), ctypes.byref(loss))
+    if st:
+        raise ct.CCSDTError(st, "ccsdt_mlp_grad")
+    return g, loss.value
+
+
+def mlp_train(X, y, epochs=300, batch=64, lr=3e-3, seed=0, params=None):
+    p = _f32(params) if params is not None else np.zeros(NPARAM, np.float32)
+    X, y = _f32(X), np.ascontiguousarray(y, dtype=np.int32)
+    loss = ctypes.c_float()
+    st = _lib().ccsdt_mlp_train(X.ctypes.data_as(_F), y.ctypes.data_as(_I), len(y), epochs, batch, lr, seed,
+                                int(params is None), p.ctypes.data_as(_F), ctypes.byref(loss))
+    if st:
+        raise ct.CCSDTError(st, "ccsdt_mlp_train")
+    return p, loss.value
+
+
+def mlp_predict(params, X):
+    p, X = _f32(params), _f32(X)
+    s = np.zeros(len(X), np.int32)
+    st = _lib().ccsdt_mlp_predict(p.ctypes.data_as(_F), X.ctypes.data_as(_F), len(X), s.ctypes.data_as(_I), None)
+    if st:
+        raise ct.CCSDTError(st, "ccsdt_mlp_predict")
+    return s
+
+
+def features(ft: "ct.FusedTriples", tri) -> np.ndarray:
+    t = np.ascontiguousarray(np.asarray(tri, dtype=np.int32).reshape(-1, 3))
+    f = np.zeros((len(t), 12), np.float32)
+    ft._check(_lib().ccsdt_triplet_features(ft.h, len(t), t.ctypes.data_as(_I), f.ctypes.data_as(_F)))
+    return f
+
+
+def set_model(ft: "ct.FusedTriples", params):
+    p = _f32(params)
+    ft._keep_model = p
+    ft._check(_lib().ccsdt_set_slice_model(ft.h, p.ctypes.data_as(_F)))
+
+
+def learned_stats(ft: "ct.FusedTriples"):
+    m, f = ctypes.c_double(), ctypes.c_long()
+    _lib().ccsdt_learned_stats(ft.h, ctypes.byref(m), ctypes.byref(f))
+    return m.value, f.value
+
+
+def label_triplets(ft, tri, budget=1e-8, smax=7):
+    """Minimal S in 2..smax meeting the relative budget per triplet (smax if none does)."""
+    _, ref = ft.triplet_energies(tri, "fp64")
+    errs = []
+    for S in range(2, smax + 1):
+        _, e = ft.triplet_energies(tri, "ozaki", slices=S)
+        errs.append(np.abs(e - ref) / np.maximum(np.abs(ref), 1e-300))
+    errs = np.array(errs)                                   # [S-2][t]
+    ok = errs <= budget
+    lab = np.where(ok.any(0), ok.argmax(0) + 2, smax)
+    return lab, errs, ref
+
+
+def training_systems(n=20, seed0=100, o_range=(10, 30), v_range=(60, 200), scale_range=(0.5, 3.0)):
+    rng = np.random.default_rng(12345)
+    out = []
+    for s in range(seed0, seed0 + n):
+        o = int(rng.integers(o_range[0], o_range[1] + 1))
+        v = int(rng.integers(v_range[0], v_range[1] + 1))
+        sc = float(rng.uniform(*scale_range))
+        out.append((o, v, s, sc))
+    return out
+
+
+def build_training_set(systems, per_system=24, budget=1e-8, smax=7, log=print):
+    from .generator import generate
+    X, Y, meta = [], [], []
+    for (o, v, seed, sc) in systems:
+        d = generate(o, v, seed, t2_scale=sc)
+        ft = ct.FusedTriples(o, v, ts=40)
+        ft.upload_dict(d)
+        allt = ct.all_triplets(o)
+        allt = allt[allt[:, 0] != allt[:, 2]]
+        rng = np.random.default_rng(seed)
+        tri = allt[np.sort(rng.choice(len(allt), size=min(per_system, len(allt)), replace=False))]
+        lab, errs, _ = label_triplets(ft, tri, budget, smax)
+        X.append(features(ft, tri))
+        Y.append(lab - 2)
+        meta.append({"o": o, "v": v, "seed": seed, "t2_scale": sc, "labels": np.bincount(lab, minlength=smax + 1).tolist()})
+        log(f"system o={o} v={v} seed={seed} t2x{sc:.2f}: label histogram {meta[-1]['labels'][2:]}")
+        ft.close()
+    return np.concatenate(X), np.concatenate(Y).astype(np.int32), meta
+
+
+def save_model(params, meta, path=MODEL_PATH):
+    Path(path).write_text(json.dumps({"params": [float(x) for x in params], "meta": meta}) + "\n")
+
+
+def load_model(path=MODEL_PATH):
+    d = json.loads(Path(path).read_text())
+    return np.asarray(d["params"], np.float32), d.get("meta", {})
+
+
+def main():
+    """Train the shipped model on the GPU: python -m exachem_gb300.learned"""
+    import time
+    t0 = time.time()
+    systems = training_systems()
+    X, y, meta = build_training_set(systems)
+    params, loss = mlp_train(X, y, epochs=400, batch=64, lr=3e-3, seed=7)
+    acc = float((mlp_predict(params, X) - 2 == y).mean())
+    print(f"trained on {len(y)} triplets: loss {loss:.4f}, accuracy {acc:.3f}, {time.time() - t0:.0f} s")
+    save_model(params, {"systems": meta, "budget": 1e-8, "loss": loss, "train_accuracy": acc,
+                        "label_histogram": np.bincount(y + 2, minlength=9).tolist()})
+
+
+if __name__ == "__main__":
+    main()

@@ -174,6 +174,17 @@ ccsdt_status ccsdt_mlp_train(const float* X, const int* labels, int n, int epoch
 /* BF16 inference: slices[s] = 2 + argmax of the logits (logits[n][7] optional). */
 ccsdt_status ccsdt_mlp_predict(const float* params, const float* X, int n, int* slices, float* logits);
 
+/* The 12 features of each triplet (host array feats[n][12]) the slice-count model reads. */
+ccsdt_status ccsdt_triplet_features(ccsdt_handle* h, long n, const int* tri, float* feats);
+
+/* Install (params != NULL, CCSDT_MLP_NPARAM floats) or clear the model CCSDT_MODE_LEARNED uses.
+ * In that mode opts->slices is the full count used for the fallback (default 6) and
+ * opts->energy_budget the relative per-triplet budget of the a-posteriori check. */
+ccsdt_status ccsdt_set_slice_model(ccsdt_handle* h, const float* params);
+
+/* Mean predicted slice count and number of full-slice fallbacks of the last LEARNED call. */
+ccsdt_status ccsdt_learned_stats(const ccsdt_handle* h, double* mean_slices, long* fallbacks);
+
 void        ccsdt_destroy(ccsdt_handle* h);
 const char* ccsdt_last_error(const ccsdt_handle* h);
 const char* ccsdt_status_string(ccsdt_status s);
