@@ -49,7 +49,8 @@ class Result(ctypes.Structure):
 EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
             "ccsdt_last_launch_count", "ccsdt_reference_op_count", "ccsdt_destroy",
             "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet",
-            "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc"]
+            "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc", "ccsdt_shard_triplets",
+            "ccsdt_set_phase_timing", "ccsdt_phase_times"]
 
 
 def load_library(path: str | os.PathLike | None = None):
@@ -69,6 +70,9 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_last_launch_count.restype = ctypes.c_long
     lib.ccsdt_reference_op_count.argtypes = [ctypes.POINTER(Layout), dp, ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_set_stream.argtypes = [vp, vp]
+    lib.ccsdt_set_phase_timing.argtypes = [vp, ctypes.c_int]
+    lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
+    lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
     lib.ccsdt_profile_triplet.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     lib.ccsdt_debug_triplet_w.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     lib.ccsdt_debug_triplet_w.restype = ctypes.c_int
@@ -79,7 +83,8 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_status_string.argtypes = [ctypes.c_int]
     lib.ccsdt_status_string.restype = ctypes.c_char_p
     for name in ("ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
-                 "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet"):
+                 "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet",
+                 "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -200,6 +205,17 @@ class FusedTriples:
         self._check(self.lib.ccsdt_debug_triplet_w(self.h, ctypes.byref(op), i, j, k,
                                                    w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return w
+
+    def set_phase_timing(self, on: bool = True):
+        """Start (and zero) or stop live per-phase timing of the batched split-precision path."""
+        self._check(self.lib.ccsdt_set_phase_timing(self.h, int(on)))
+
+    def phase_times(self) -> dict:
+        """Accumulated device ms of the l-sum, d-sum and energy phases since set_phase_timing."""
+        ms = (ctypes.c_double * 3)()
+        b, t = ctypes.c_long(), ctypes.c_long()
+        self._check(self.lib.ccsdt_phase_times(self.h, ms, ctypes.byref(b), ctypes.byref(t)))
+        return {"l_sum_ms": ms[0], "d_sum_ms": ms[1], "energy_ms": ms[2], "batches": b.value, "triplets": t.value}
 
     def launch_count(self) -> int:
         return int(self.lib.ccsdt_last_launch_count(self.h))

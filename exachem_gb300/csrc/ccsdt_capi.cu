@@ -58,9 +58,13 @@ ccsdt_handle::~ccsdt_handle() {
   for(void* p: owned) cudaFree(p);
   for(void* p: owned_bytes) cudaFree(p);
   for(void* p: slice_bufs) cudaFree(p);
+  for(void* p: {(void*) bt_F, (void*) bt_part, (void*) bt_order, (void*) bt_order_partial, (void*) bt_ctrl, (void*) bt_tri})
+    if(p) cudaFree(p);
   if(ev0) cudaEventDestroy(ev0);
   if(ev1) cudaEventDestroy(ev1);
   for(auto& e: prof_ev)
+    if(e) cudaEventDestroy(e);
+  for(auto& e: tev)
     if(e) cudaEventDestroy(e);
   if(own_stream) cudaStreamDestroy(own_stream);
 }
@@ -102,6 +106,7 @@ ccsdt_status ccsdt_create(ccsdt_handle** out, const ccsdt_layout* L, int device)
   }
   if(so != L->o || sv != L->v) return CCSDT_E_BAD_LAYOUT;
   int ndev = 0;
+  if(device == -1 && cudaGetDevice(&device) != cudaSuccess) device = -2; // the caller's current device
   if(cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) {
     cudaGetLastError();
     return CCSDT_E_CUDA;
@@ -133,6 +138,22 @@ ccsdt_status ccsdt_create(ccsdt_handle** out, const ccsdt_layout* L, int device)
 ccsdt_status ccsdt_set_stream(ccsdt_handle* h, void* stream) {
   if(!h) return CCSDT_E_INVALID;
   h->stream = stream ? (cudaStream_t) stream : h->own_stream;
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_set_phase_timing(ccsdt_handle* h, int on) {
+  if(!h) return CCSDT_E_INVALID;
+  h->phase_timing = on != 0;
+  for(double& m: h->phase_ms) m = 0;
+  h->phase_batches = h->phase_triplets = 0;
+  return CCSDT_OK;
+}
+
+ccsdt_status ccsdt_phase_times(const ccsdt_handle* h, double* ms3, long* batches, long* triplets) {
+  if(!h || !ms3) return CCSDT_E_INVALID;
+  for(int q = 0; q < 3; q++) ms3[q] = h->phase_ms[q];
+  if(batches) *batches = h->phase_batches;
+  if(triplets) *triplets = h->phase_triplets;
   return CCSDT_OK;
 }
 
@@ -326,6 +347,24 @@ extern "C" ccsdt_status ccsdt_triplet_energies(ccsdt_handle* h, const ccsdt_opts
   return CCSDT_OK;
 }
 
+extern "C" ccsdt_status ccsdt_shard_triplets(int o, int shard_index, int shard_count, long* n, int* tri) {
+  if(o <= 0 || !n || shard_count < 1 || shard_index < 0 || shard_index >= shard_count) return CCSDT_E_INVALID;
+  long tcount = 0, m = 0;
+  for(int i = 0; i < o; i++)
+    for(int j = i; j < o; j++)
+      for(int k = j; k < o; k++, tcount++) {
+        if(tcount % shard_count != shard_index) continue;
+        if(tri) {
+          tri[3 * m]     = i;
+          tri[3 * m + 1] = j;
+          tri[3 * m + 2] = k;
+        }
+        m++;
+      }
+  *n = m;
+  return CCSDT_OK;
+}
+
 extern "C" ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, ccsdt_result* out) {
   if(!h) return CCSDT_E_INVALID;
   if(!valid_opts(opts) || !out) return h->fail(CCSDT_E_INVALID, "ccsdt_energy: bad arguments");
@@ -335,17 +374,10 @@ extern "C" ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, cc
   const int        nsh = opts->shard_count > 1 ? opts->shard_count : 1;
   if(opts->shard_index < 0 || opts->shard_index >= nsh)
     return h->fail(CCSDT_E_INVALID, "ccsdt_energy: shard_index outside [0, shard_count)");
-  std::vector<int> tri;
-  long             tcount = 0;
-  for(int i = 0; i < o; i++)
-    for(int j = i; j < o; j++)
-      for(int k = j; k < o; k++, tcount++) {
-        if(tcount % nsh != opts->shard_index) continue;
-        tri.push_back(i);
-        tri.push_back(j);
-        tri.push_back(k);
-      }
-  const long n = (long) tri.size() / 3;
+  long n = 0;
+  ccsdt_shard_triplets(o, opts->shard_index, nsh, &n, nullptr);
+  std::vector<int> tri(3 * (size_t) n);
+  ccsdt_shard_triplets(o, opts->shard_index, nsh, &n, tri.data());
   CK(cudaEventRecord(h->ev0, h->stream));
   ccsdt_status s = h->run_list(opts, n, tri.data());
   if(s) return s;
@@ -421,9 +453,13 @@ extern "C" ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts*
     CK(cudaMemcpy(b.data(), h->P34, n * sizeof(double), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(c.data(), h->P56, n * sizeof(double), cudaMemcpyDeviceToHost));
   } else {
+    // the persistent path keeps slot 0's P12, P34, P56 consecutively in the batch scratch
     std::vector<float2> f(n);
+    const float2*       src[3] = {h->F12, h->F34, h->F56};
+    if(h->last_batched)
+      for(int q = 0; q < 3; q++) src[q] = h->bt_F + q * n;
     for(int q = 0; q < 3; q++) {
-      CK(cudaMemcpy(f.data(), q == 0 ? h->F12 : q == 1 ? h->F34 : h->F56, n * sizeof(float2), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(f.data(), src[q], n * sizeof(float2), cudaMemcpyDeviceToHost));
       std::vector<double>& d = q == 0 ? a : q == 1 ? b : c;
       for(size_t e = 0; e < n; e++) d[e] = (double) f[e].x + (double) f[e].y;
     }

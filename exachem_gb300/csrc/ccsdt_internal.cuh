@@ -43,7 +43,7 @@ struct ccsdt_handle {
   // tcgen05 path: TMA maps over the digit planes (built once per slicing) and an error flag
   CUtensorMap        tmaps[6];
   bool               tmaps_ready = false;
-  int                tmaps_S     = 0;
+  int                tmaps_S     = 0, tmaps_NT = 0;
   int*               d_err       = nullptr;
   int*               e_tiles     = nullptr; // sorted virtual block triples of the tiled energy
   int                e_ntiles    = 0;
@@ -69,7 +69,7 @@ struct ccsdt_handle {
   ccsdt_status run_split(const ccsdt_opts* opts, long n, const int* tri_host);
   ccsdt_status ensure_slices(int S, int variant);
   ccsdt_status run_triplet_split(int i, int j, int k, int S, int variant, double* eout);
-  ccsdt_status ensure_tmaps(int S);
+  ccsdt_status ensure_tmaps(int S, int NT);
   ccsdt_status run_triplet_tc(int i, int j, int k, int S, double* eout);
   bool         tc_eligible(int S, int variant) const;
   double*      part_buf() { return part; }
@@ -84,9 +84,33 @@ struct ccsdt_handle {
   int*               st_slab = nullptr, *st_pair = nullptr, *st_hole = nullptr; // exponent statistics
   int                stats_for = -1;  // slicing generation the statistics belong to
   int                slice_gen = 0;
+  // batched persistent path
+  float2*   bt_F = nullptr;          // P arrays of the batch slots
+  bool      last_batched = false;    // the last split-precision call ran the persistent path
+  double*   bt_part = nullptr;
+  int       bt_B = 0, bt_order_key = -1;
+  unsigned* bt_order = nullptr, *bt_order_partial = nullptr;
+  unsigned  bt_nitems = 0;
+  int*      bt_ctrl = nullptr;       // queue counters and batch base
+  int*      bt_tri = nullptr;        // triplet table (i, j, k, output index)
+  long      bt_tri_cap = 0;
+  int       batch_slots = 4;         // triplets per batch
+  long      graph_replays = 0;
+  ccsdt_status ensure_batch(int S, int B);
+  ccsdt_status launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails, double* sens);
+  ccsdt_status run_batched(int S, long n, const int* tri, bool use_graph, float* tails, double* sens,
+                           const int* out_map = nullptr);
   // per-call statistics of the learned mode
   double             learned_mean_slices = 0.0;
   long               learned_fallbacks   = 0;
   ccsdt_status check_device_error();
   bool         force_mma_sync = false; // use the mma.sync slice kernel even where tcgen05 applies
+  // live per-phase timing of the batched path: 4 events per batch, read after the call
+  bool                     phase_timing = false, capturing = false;
+  std::vector<cudaEvent_t> tev;
+  size_t                   tev_used = 0;
+  std::vector<int>         tev_slots;
+  double                   phase_ms[3]   = {0, 0, 0}; // l-sum, d-sum, energy + reduction
+  long                     phase_batches = 0, phase_triplets = 0;
+  ccsdt_status collect_phase_times();
 };

@@ -12,6 +12,7 @@
 // reduction, so the result is deterministic.
 #pragma once
 
+#include "fp64_kernels.cuh"
 #include "ozaki.cuh"
 
 namespace ccsdt {
@@ -25,18 +26,20 @@ struct TiledEnergyArgs {
   const int3*   tiles;     // sorted block triples
   int           ntiles;
   int           o, v, i, j, k;
-  double*       part;      // 6 doubles per CTA: E[T] (s, c), E(T) (s, c), sum (|Z| + |Y|) / |D|, 0
+  double*       part;      // 6 doubles per CTA: E[T] (s, c), E(T) (s, c), sum ((|Z| + |Y|) / |D|)^2, 0
 };
 
 // slot s <-> permutation (p0, p1, p2) of the block positions
-__device__ __constant__ int c_perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+static __device__ __constant__ int c_perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 
 __device__ __forceinline__ int perm_slot(int p0, int p1, int p2) {
   // (0,1,2)=0 (0,2,1)=1 (1,0,2)=2 (1,2,0)=3 (2,0,1)=4 (2,1,0)=5
   return p0 * 2 + (p1 > p2 ? 1 : 0);
 }
 
-__global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_constant__ TiledEnergyArgs A) {
+__device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, const float2* P12, const float2* P34,
+                                                  const float2* P56, int i, int j, int k, double* part, int gblock,
+                                                  int gsize) {
   constexpr int B = ET_B, B3 = B * B * B;
   __shared__ float2 W[6][B3];            // [slot][a'][b'][c'] (a', b', c' local to the slot's blocks)
   __shared__ float  Ojk[3][3][B * B], Oik[3][3][B * B], Oij[3][3][B * B];
@@ -45,7 +48,7 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
   __shared__ int    blk0[3], blkn[3];
   __shared__ int    slot_on[6];
 
-  const int       v = A.v, o = A.o, i = A.i, j = A.j, k = A.k, tid = threadIdx.x;
+  const int       v = A.v, o = A.o, tid = threadIdx.x;
   const long long v2 = (long long) v * v;
   const ff        eijk = ff_add(ff_add(ff_from_double(A.eo[i]), ff_from_double(A.eo[j])), ff_from_double(A.eo[k]));
   const float *   gOjk = A.oovv + ((long long) j * o + k) * v2, *gOik = A.oovv + ((long long) i * o + k) * v2,
@@ -53,7 +56,7 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
   ff    s4{0.f, 0.f}, s5{0.f, 0.f};
   float sens = 0.f; // first-order sensitivity of the energy to errors in W (a-posteriori estimate)
 
-  for(int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+  for(int tile = gblock; tile < A.ntiles; tile += gsize) {
     __syncthreads();
     if(tid < 3) {
       const int3 t = A.tiles[tile];
@@ -104,15 +107,15 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
         // slot blocks: a in block P[0], b in P[1], c in P[2]
         if(pass == 0) { // P12[a][c][b]: b fastest
           la = sl, lc = m, lb = f;
-          src = A.P12;
+          src = P12;
           off = ((long long) (blk0[P[0]] + la) * v + blk0[P[2]] + lc) * v + blk0[P[1]] + lb;
         } else if(pass == 1) { // P34[b][a][c]: c fastest
           lb = sl, la = m, lc = f;
-          src = A.P34;
+          src = P34;
           off = ((long long) (blk0[P[1]] + lb) * v + blk0[P[0]] + la) * v + blk0[P[2]] + lc;
         } else { // P56[c][b][a]: a fastest
           lc = sl, lb = m, la = f;
-          src = A.P56;
+          src = P56;
           off = ((long long) (blk0[P[2]] + lc) * v + blk0[P[1]] + lb) * v + blk0[P[0]] + la;
         }
         const bool ok = la < blkn[P[0]] && lb < blkn[P[1]] && lc < blkn[P[2]];
@@ -154,7 +157,8 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
       const ff d = ff_add(ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y}), ff{-ec.x, -ec.y});
       s4 = ff_add(s4, ff_div(ff_mul(z, y4), d));
       s5 = ff_add(s5, ff_div(ff_mul(z, y5), d));
-      sens += (fabsf(z.hi) + fabsf(y5.hi)) / fabsf(d.hi);
+      const float g = (fabsf(z.hi) + fabsf(y5.hi)) / fabsf(d.hi); // |de / dW| up to a constant
+      sens += g * g;
     }
   }
   CSum c4, c5;
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
   c4.add((double) s4.lo);
   c5.add((double) s5.hi);
   c5.add((double) s5.lo);
-  block_reduce_csum(c4, c5, A.part + 6 * (long long) blockIdx.x);
+  block_reduce_csum(c4, c5, part);
   // fixed-order block sum of the sensitivity
   __shared__ float ssum[ET_THREADS / 32];
 #pragma unroll
@@ -172,14 +176,37 @@ __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_c
   if(threadIdx.x == 0) {
     double t = 0.0;
     for(int q = 0; q < ET_THREADS / 32; q++) t += ssum[q];
-    A.part[6 * (long long) blockIdx.x + 4] = t;
-    A.part[6 * (long long) blockIdx.x + 5] = 0.0;
+    part[4] = t;
+    part[5] = 0.0;
   }
+}
+
+static __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_constant__ TiledEnergyArgs A) {
+  energy_tiled_body(A, A.P12, A.P34, A.P56, A.i, A.j, A.k, A.part + 6 * (long long) blockIdx.x, blockIdx.x, gridDim.x);
+}
+
+// Batched form: blockIdx.y = triplet slot; the triplet and its P arrays come from the batch
+// tables (4 ints per triplet: i, j, k, output index; P arrays of slot s at F + s * 3 v^3).
+struct BatchEnergyArgs {
+  TiledEnergyArgs base_args; // P12/P34/P56/i/j/k/part unused
+  const int*      tri;
+  const int*      base;
+  const float2*   F;
+  double*         part;      // [slot][gridDim.x][6]
+};
+
+static __global__ void __launch_bounds__(ET_THREADS) energy_tiled_batch_kernel(const __grid_constant__ BatchEnergyArgs A) {
+  const int       slot = blockIdx.y, b0 = A.base ? *A.base : 0;
+  const int*      tp   = A.tri + 4 * (b0 + slot);
+  const long long v3   = (long long) A.base_args.v * A.base_args.v * A.base_args.v;
+  const float2*   F    = A.F + (long long) slot * 3 * v3;
+  energy_tiled_body(A.base_args, F, F + v3, F + 2 * v3, tp[0], tp[1], tp[2],
+                    A.part + 6 * ((long long) slot * gridDim.x + blockIdx.x), blockIdx.x, gridDim.x);
 }
 
 // Fixed-order parallel sum of per-CTA partials (6 doubles each) for one triplet -> out[2]
 // (energies); sens_out[0] (optional) receives scale * the summed sensitivity.
-__global__ void __launch_bounds__(256) reduce_parts_parallel_kernel(const double* part, int nparts, double scale,
+static __global__ void __launch_bounds__(256) reduce_parts_parallel_kernel(const double* part, int nparts, double scale,
                                                                      double* out, double* sens_out) {
   CSum a, b;
   const int per = (nparts + blockDim.x - 1) / blockDim.x;
@@ -190,10 +217,10 @@ __global__ void __launch_bounds__(256) reduce_parts_parallel_kernel(const double
     b.add(part[6 * q + 2]);
     b.c += part[6 * q + 3];
   }
-  if(sens_out && threadIdx.x == 0) {
+  if(sens_out && threadIdx.x == 0) { // sensitivity of the scaled energy: scale^2 * sum of squares
     double t = 0.0;
     for(int q = 0; q < nparts; q++) t += part[6 * q + 4];
-    sens_out[0] = scale * t;
+    sens_out[0] = scale * scale * t;
   }
   __shared__ double tmp[4];
   // reuse the fixed-shape block reduction (its shared scratch is sized for 256 threads)
@@ -203,6 +230,43 @@ __global__ void __launch_bounds__(256) reduce_parts_parallel_kernel(const double
     out[0] = scale * (tmp[0] + tmp[1]);
     out[1] = scale * (tmp[2] + tmp[3]);
   }
+}
+
+// One block per slot: fixed-order sum of that slot's partials; writes etrip[2 out] (scaled by
+// m / 9) and, if given, sens[out].
+static __global__ void __launch_bounds__(256) reduce_parts_batch_kernel(const double* part, int nparts, const int* tri,
+                                                                 const int* base, double* etrip, double* sens) {
+  const int  slot = blockIdx.x, b0 = base ? *base : 0;
+  const int* tp   = tri + 4 * (b0 + slot);
+  const int  i = tp[0], j = tp[1], k = tp[2], out = tp[3];
+  const int  m = (i == j && j == k) ? 1 : ((i == j || j == k || i == k) ? 3 : 6);
+  const double* pp = part + 6 * (long long) slot * nparts;
+  CSum a, b;
+  const int per = (nparts + blockDim.x - 1) / blockDim.x;
+  const int q0 = threadIdx.x * per, q1 = min(nparts, q0 + per);
+  for(int q = q0; q < q1; q++) {
+    a.add(pp[6 * q + 0]);
+    a.c += pp[6 * q + 1];
+    b.add(pp[6 * q + 2]);
+    b.c += pp[6 * q + 3];
+  }
+  __shared__ double tmp[4];
+  block_reduce_csum(a, b, tmp);
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    const double sc = m / 9.0;
+    etrip[2 * out]     = sc * (tmp[0] + tmp[1]);
+    etrip[2 * out + 1] = sc * (tmp[2] + tmp[3]);
+    if(sens) {
+      double t = 0.0;
+      for(int q = 0; q < nparts; q++) t += pp[6 * q + 4];
+      sens[out] = sc * sc * t;
+    }
+  }
+}
+
+static __global__ void advance_base_kernel(int* base, int by) {
+  if(threadIdx.x == 0 && blockIdx.x == 0) *base += by;
 }
 
 } // namespace ccsdt

@@ -3,10 +3,12 @@
 // No counterpart in the reference.  For every occupied triplet a small MLP (mlp.cu) reads 12
 // features and predicts the digit-plane count S in 2..8 that keeps the triplet's energy error
 // under a budget.  After the run an a-posteriori estimate is formed per triplet,
-//     est = 6 * tail * 2^-6 * sum_abc (|Z| + |Y|) / |D|      (times m / 9)
+//     est = 6 * tail * 2^-6 * sqrt(sum_abc ((|Z| + |Y|) / |D|)^2)      (times m / 9)
 // with `tail` the largest contribution of the last kept digit level (the dropped levels are
 // each about 2^-7 of it) and the sum the first-order sensitivity of the energy to W.  A triplet
 // whose estimate exceeds budget * |E_triplet| is recomputed with the full slice count.
+// The element errors are treated as independent (a random walk): the sensitivity is the
+// root of the summed squares, sqrt(sum_abc ((|Z| + |Y|) / |D|)^2), not the plain sum.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -190,7 +192,7 @@ extern "C" ccsdt_status ccsdt_learned_stats(const ccsdt_handle* h, double* mean_
 
 ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int* tri) {
   if(model.size() != (size_t) CCSDT_MLP_NPARAM) return fail(CCSDT_E_STATE, "LEARNED mode needs ccsdt_set_slice_model");
-  const int Sfull = opts->slices >= 2 && opts->slices <= 8 ? opts->slices : 6;
+  const int Sfull = opts->slices >= 2 && opts->slices <= 8 ? opts->slices : 5;
   ccsdt_status s;
   if((s = ensure_slices(Sfull, 0))) return s;
   Scratch sc;
@@ -223,27 +225,45 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
   if(cudaMemcpyAsync(S.data(), dsl, sizeof(int) * n, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
      cudaStreamSynchronize(stream) != cudaSuccess)
     return fail(CCSDT_E_CUDA, "learned-mode slice readback");
-  // run each triplet at its predicted count, grouped by count (one tensor-map set per count)
+  // run the triplets at their predicted counts, one persistent batched pass per count (the
+  // tcgen05 path, S <= 5); results, tails and sensitivities land at each triplet's own index
   force_mma_sync = false;
-  double ssum    = 0;
-  for(int cnt = 2; cnt <= Sfull; cnt++)
-    for(long t = 0; t < n; t++) {
-      const int st = std::min(std::max(S[t], 2), Sfull);
-      if(st != cnt) continue;
-      ssum += st;
-      const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
+  const bool graph = opts->use_graph != 0;
+  double     ssum  = 0;
+  auto       group = [&](int cnt, const std::vector<long>& ids, bool with_est) -> ccsdt_status {
+    if(ids.empty()) return CCSDT_OK;
+    std::vector<int> sub(3 * ids.size()), out(ids.size());
+    for(size_t q = 0; q < ids.size(); q++) {
+      for(int c = 0; c < 3; c++) sub[3 * q + c] = tri[3 * ids[q] + c];
+      out[q] = (int) ids[q];
+    }
+    if(tc_eligible(cnt, 0))
+      return run_batched(cnt, (long) ids.size(), sub.data(), graph, with_est ? dtail : nullptr,
+                         with_est ? dsens : nullptr, out.data());
+    for(size_t q = 0; q < ids.size(); q++) { // counts above the tcgen05 range: per-triplet slices
+      const int i = sub[3 * q], j = sub[3 * q + 1], k = sub[3 * q + 2];
+      const long t = ids[q];
       if(i == k) {
         if(cudaMemsetAsync(etrip + 2 * t, 0, 2 * sizeof(double), stream) != cudaSuccess)
           return fail(CCSDT_E_CUDA, "memset");
         continue;
       }
-      cur_tail = dtail + t;
-      cur_sens = dsens + t;
-      s        = run_triplet_S(i, j, k, st, etrip + 2 * t);
+      cur_tail = with_est ? dtail + t : nullptr;
+      cur_sens = with_est ? dsens + t : nullptr;
+      ccsdt_status r = run_triplet_S(i, j, k, cnt, etrip + 2 * t);
       cur_tail = nullptr;
       cur_sens = nullptr;
-      if(s) return s;
+      if(r) return r;
     }
+    return CCSDT_OK;
+  };
+  for(int cnt = 2; cnt <= Sfull; cnt++) {
+    std::vector<long> ids;
+    for(long t = 0; t < n; t++)
+      if(std::min(std::max(S[t], 2), Sfull) == cnt) ids.push_back(t);
+    ssum += (double) cnt * (double) ids.size();
+    if((s = group(cnt, ids, cnt < Sfull))) return s;
+  }
   learned_mean_slices = n ? ssum / n : 0.0;
   // a-posteriori check and full-slice fallback
   std::vector<double> E(2 * n), sens(n);
@@ -255,18 +275,18 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
     return fail(CCSDT_E_CUDA, "learned-mode readback");
   const double budget = opts->energy_budget > 0 ? opts->energy_budget : 1e-8;
   learned_fallbacks   = 0;
-  double bound        = 0;
+  double            bound = 0;
+  std::vector<long> redo;
   for(long t = 0; t < n; t++) {
-    const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
+    const int i = tri[3 * t], k = tri[3 * t + 2];
     const int st = std::min(std::max(S[t], 2), Sfull);
     if(i == k || st >= Sfull) continue;
-    const double est = 6.0 * std::ldexp((double) tail[t], -6) * sens[t];
-    if(!(est <= budget * std::fabs(E[2 * t + 1]))) {
-      learned_fallbacks++;
-      if((s = run_triplet_S(i, j, k, Sfull, etrip + 2 * t))) return s;
-    } else
-      bound += est;
+    const double est = 6.0 * std::ldexp((double) tail[t], -6) * std::sqrt(sens[t]);
+    if(!(est <= budget * std::fabs(E[2 * t + 1]))) redo.push_back(t);
+    else bound += est;
   }
+  learned_fallbacks = (long) redo.size();
+  if((s = group(Sfull, redo, false))) return s;
   last_err_bound = bound;
   return CCSDT_OK;
 }

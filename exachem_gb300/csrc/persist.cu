@@ -1,0 +1,314 @@
+// Batched, persistent split-precision (T): host orchestration.
+//
+// The non-zero triplets of a call (i < k) go into a device table (i, j, k, output index).  A batch
+// of B triplets runs as: l-sum contraction (persistent, work queue), d-sum contraction (persistent),
+// tiled energy of the B triplets, per-triplet reduction, advance of the device batch base.  With
+// opts->use_graph that sequence is captured once per call into a CUDA graph and replayed for every
+// full batch; the remainder batch is launched directly.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "ccsdt_internal.cuh"
+#include "energy_tiled.cuh"
+#include "fp64_kernels.cuh"
+#include "oz_persist.cuh"
+
+using namespace ccsdt;
+
+namespace {
+
+template<int S>
+struct PzPick;
+template<>
+struct PzPick<1> {
+  static constexpr int NT = 64, ST = 4;
+};
+template<>
+struct PzPick<2> {
+  static constexpr int NT = 64, ST = 4;
+};
+template<>
+struct PzPick<3> {
+  static constexpr int NT = 64, ST = 3;
+};
+template<>
+struct PzPick<4> {
+  static constexpr int NT = 64, ST = 2;
+};
+template<>
+struct PzPick<5> {
+  static constexpr int NT = 32, ST = 2;
+};
+
+int pz_nt(int S) {
+  switch(S) {
+    case 1: return PzPick<1>::NT;
+    case 2: return PzPick<2>::NT;
+    case 3: return PzPick<3>::NT;
+    case 4: return PzPick<4>::NT;
+    case 5: return PzPick<5>::NT;
+  }
+  return 0;
+}
+
+template<int S>
+cudaError_t launch_pz(const PzParams& p, int grid, cudaStream_t st) {
+  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST;
+  using Cfg        = PzCfg<S, NT, ST>;
+  cudaError_t e = cudaFuncSetAttribute(oz_persist_kernel<S, NT, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
+  if(e != cudaSuccess) return e;
+  oz_persist_kernel<S, NT, ST><<<grid, PZ_THREADS, Cfg::SMEM, st>>>(p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pz_any(int S, const PzParams& p, int grid, cudaStream_t st) {
+  switch(S) {
+    case 1: return launch_pz<1>(p, grid, st);
+    case 2: return launch_pz<2>(p, grid, st);
+    case 3: return launch_pz<3>(p, grid, st);
+    case 4: return launch_pz<4>(p, grid, st);
+    case 5: return launch_pz<5>(p, grid, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Item ids of B slots sorted by estimated cost (rows x columns of the tile), largest first; ties
+// keep the natural order (n-block fastest) so concurrently running CTAs share A tiles in L2.
+std::vector<unsigned> cost_order(int B, int v, int NT) {
+  const int  yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT;
+  const long n  = (long) B * 3 * v * yb * nb;
+  std::vector<unsigned> ids(n);
+  std::iota(ids.begin(), ids.end(), 0u);
+  auto cost = [&](unsigned id) {
+    const int n_b = id % nb, y_b = (id / nb) % yb;
+    const int rows = std::min(PZ_BM, v - y_b * PZ_BM), cols = std::min(NT, v - n_b * NT);
+    return rows * cols;
+  };
+  std::stable_sort(ids.begin(), ids.end(), [&](unsigned a, unsigned b) { return cost(a) > cost(b); });
+  return ids;
+}
+
+} // namespace
+
+ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
+  const long long v3 = (long long) v * v * v;
+  const int       NT = pz_nt(S);
+  if(!NT) return fail(CCSDT_E_INVALID, "no persistent configuration for this slice count");
+  if(bt_B != B) {
+    if(bt_F) cudaFree(bt_F);
+    if(bt_part) cudaFree(bt_part);
+    bt_F = nullptr;
+    bt_part = nullptr;
+    if(cudaMalloc((void**) &bt_F, sizeof(float2) * 3 * v3 * B) != cudaSuccess ||
+       cudaMalloc((void**) &bt_part, sizeof(double) * 6 * kTiledBlocks * B) != cudaSuccess) {
+      cudaGetLastError();
+      if(bt_F) cudaFree(bt_F);
+      bt_F = nullptr;
+      return fail(CCSDT_E_OOM, "batch scratch: cudaMalloc failed");
+    }
+    bt_B = B;
+    bt_order_key = -1;
+  }
+  const int key = S * 100000 + B;
+  if(bt_order_key != key) {
+    auto ids = cost_order(B, v, NT);
+    if(bt_order) cudaFree(bt_order);
+    bt_order = nullptr;
+    if(cudaMalloc((void**) &bt_order, ids.size() * sizeof(unsigned)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(CCSDT_E_OOM, "work-queue table: cudaMalloc failed");
+    }
+    if(cudaMemcpy(bt_order, ids.data(), ids.size() * sizeof(unsigned), cudaMemcpyHostToDevice) != cudaSuccess)
+      return fail(CCSDT_E_CUDA, "work-queue table upload");
+    bt_nitems    = (unsigned) ids.size();
+    bt_order_key = key;
+  }
+  if(!bt_ctrl) { // [0] queue l-sum, [1] queue d-sum, [2] batch base
+    if(cudaMalloc((void**) &bt_ctrl, 4 * sizeof(int)) != cudaSuccess) {
+      bt_ctrl = nullptr;
+      cudaGetLastError();
+      return fail(CCSDT_E_OOM, "batch counters");
+    }
+  }
+  return CCSDT_OK;
+}
+
+// Launch the sequence of one batch of `nslots` triplets starting at the device base counter.
+ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails,
+                                        double* sens) {
+  // the B-side TMA box must be exactly the kernel's N tile, or the loads overrun the smem slot
+  if(!tmaps_ready || tmaps_S != S || tmaps_NT != pz_nt(S))
+    return fail(CCSDT_E_STATE, "tensor maps do not match the persistent kernel's tile");
+  int sm = 0;
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+  PzParams p;
+  std::memcpy(p.maps, tmaps, sizeof(tmaps));
+  p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
+  p.F = bt_F, p.ex_t2 = ex_t2, p.ex_t2h = ex_t2h, p.ex_ovvv = ex_ovvv, p.ex_ooovh = ex_ooovh;
+  p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
+  const int NT  = pz_nt(S);
+  const int per = 3 * v * ((v + PZ_BM - 1) / PZ_BM) * ((v + NT - 1) / NT);
+  if(nitems_override <= 0) p.nitems = (unsigned) (per * nslots);
+  // the cost-ordered table was built for bt_B slots; a smaller last batch has its own table
+  const bool partial = nslots != bt_B;
+  cudaError_t e = cudaSuccess;
+  if(partial) p.order = bt_order_partial;
+  cudaEvent_t tv[4] = {nullptr, nullptr, nullptr, nullptr};
+  if(phase_timing && !capturing && !profiling) {
+    while(tev.size() < tev_used + 4) {
+      cudaEvent_t ev = nullptr;
+      if(cudaEventCreate(&ev) != cudaSuccess) return fail(CCSDT_E_CUDA, "phase-timing event");
+      tev.push_back(ev);
+    }
+    for(int q = 0; q < 4; q++) tv[q] = tev[tev_used + q];
+    tev_used += 4;
+    tev_slots.push_back(nslots);
+  }
+  for(int phase = 0; phase < 2 && e == cudaSuccess; phase++) {
+    p.phase = phase;
+    p.queue = reinterpret_cast<unsigned*>(bt_ctrl + phase);
+    if(tv[phase]) cudaEventRecord(tv[phase], stream);
+    e       = cudaMemsetAsync(p.queue, 0, sizeof(unsigned), stream);
+    if(profiling) cudaEventRecord(prof_ev[phase], stream);
+    if(e == cudaSuccess) e = launch_pz_any(S, p, sm, stream);
+    launches++;
+  }
+  if(profiling) cudaEventRecord(prof_ev[2], stream);
+  if(tv[2]) cudaEventRecord(tv[2], stream);
+  if(e == cudaSuccess) {
+    BatchEnergyArgs ea;
+    ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
+                                   o, v, 0, 0, 0, nullptr};
+    ea.tri = bt_tri, ea.base = bt_ctrl + 2, ea.F = bt_F, ea.part = bt_part;
+    const int G = std::min(e_ntiles, kTiledBlocks);
+    energy_tiled_batch_kernel<<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
+    if(profiling) cudaEventRecord(prof_ev[3], stream);
+    reduce_parts_batch_kernel<<<nslots, 256, 0, stream>>>(bt_part, G, bt_tri, bt_ctrl + 2, etrip, sens);
+    if(advance) advance_base_kernel<<<1, 32, 0, stream>>>(bt_ctrl + 2, nslots);
+    if(profiling) cudaEventRecord(prof_ev[4], stream);
+    if(tv[3]) cudaEventRecord(tv[3], stream);
+    launches += 2 + (advance ? 1 : 0);
+    e = cudaGetLastError();
+  }
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  return CCSDT_OK;
+}
+
+// Run triplets tri[3 n] at S digit planes through the persistent kernels; results -> etrip.
+// out_map (optional): output index of each listed triplet (etrip, tails, sens); default t.
+ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_graph, float* tails, double* sens,
+                                       const int* out_map) {
+  ccsdt_status s;
+  tev_used = 0; // events of a batch that failed earlier are not read
+  tev_slots.clear();
+  if((s = ensure_slices(std::max(S, slices_ready), 0)) || (s = ensure_tmaps(S, pz_nt(S)))) return s;
+  // table of non-zero triplets (i < k); i = j = k contributes exactly zero
+  std::vector<int> tab;
+  for(long t = 0; t < n; t++) {
+    const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
+    const int out = out_map ? out_map[t] : (int) t;
+    if(i == k) {
+      if(cudaMemsetAsync(etrip + 2 * (long) out, 0, 2 * sizeof(double), stream) != cudaSuccess)
+        return fail(CCSDT_E_CUDA, "memset");
+      continue;
+    }
+    tab.insert(tab.end(), {i, j, k, out});
+  }
+  const long m = (long) tab.size() / 4;
+  if(m == 0) return CCSDT_OK;
+  const int B = (int) std::min<long>(batch_slots, m);
+  if((s = ensure_batch(S, B))) return s;
+  if(bt_tri_cap < m) {
+    if(bt_tri) cudaFree(bt_tri);
+    bt_tri = nullptr;
+    if(cudaMalloc((void**) &bt_tri, tab.size() * sizeof(int)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(CCSDT_E_OOM, "triplet table");
+    }
+    bt_tri_cap = m;
+  }
+  // natural-order table for a partial last batch
+  const int  NT  = pz_nt(S);
+  const long per = 3L * v * ((v + PZ_BM - 1) / PZ_BM) * ((v + NT - 1) / NT);
+  const long rem = m % B;
+  if(rem) {
+    auto ids = cost_order((int) rem, v, NT);
+    if(bt_order_partial) cudaFree(bt_order_partial);
+    bt_order_partial = nullptr;
+    if(cudaMalloc((void**) &bt_order_partial, ids.size() * sizeof(unsigned)) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(CCSDT_E_OOM, "partial work-queue table");
+    }
+    if(cudaMemcpyAsync(bt_order_partial, ids.data(), ids.size() * sizeof(unsigned), cudaMemcpyHostToDevice, stream) !=
+       cudaSuccess)
+      return fail(CCSDT_E_CUDA, "partial table upload");
+  }
+  if(cudaMemcpyAsync(bt_tri, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+     cudaMemsetAsync(bt_ctrl + 2, 0, sizeof(int), stream) != cudaSuccess)
+    return fail(CCSDT_E_CUDA, "triplet table upload");
+  // table upload must finish before the host vector goes away
+  if(cudaStreamSynchronize(stream) != cudaSuccess) return fail(CCSDT_E_CUDA, "sync");
+  const long full = m / B;
+  if(full > 0) {
+    if(use_graph && full > 1 && !profiling) {
+      cudaGraph_t     g  = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      if(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        return fail(CCSDT_E_CUDA, "stream capture begin");
+      capturing      = true;
+      s              = launch_batch(S, B, 0, true, tails, sens);
+      capturing      = false;
+      cudaError_t ce = cudaStreamEndCapture(stream, &g);
+      if(s) {
+        if(g) cudaGraphDestroy(g);
+        return s;
+      }
+      if(ce != cudaSuccess || cudaGraphInstantiate(&ge, g, 0) != cudaSuccess) {
+        if(g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return fail(CCSDT_E_CUDA, "graph capture / instantiate");
+      }
+      for(long b = 0; b < full; b++)
+        if(cudaGraphLaunch(ge, stream) != cudaSuccess) {
+          cudaGraphExecDestroy(ge);
+          cudaGraphDestroy(g);
+          return fail(CCSDT_E_CUDA, "graph launch");
+        }
+      launches += (full - 1) * 5;
+      graph_replays += full;
+      cudaGraphExecDestroy(ge);
+      cudaGraphDestroy(g);
+    } else {
+      for(long b = 0; b < full; b++)
+        if((s = launch_batch(S, B, 0, true, tails, sens))) return s;
+    }
+  }
+  if(rem) {
+    if((s = launch_batch(S, (int) rem, (int) (per * rem), true, tails, sens))) return s;
+  }
+  return collect_phase_times();
+}
+
+// Adds the timed batches' phase durations to the running totals (waits for the stream).
+ccsdt_status ccsdt_handle::collect_phase_times() {
+  if(tev_used == 0) return CCSDT_OK;
+  if(cudaStreamSynchronize(stream) != cudaSuccess) return fail(CCSDT_E_CUDA, "phase-timing sync");
+  for(size_t b = 0; b < tev_slots.size(); b++)
+    for(int q = 0; q < 3; q++) {
+      float ms = 0;
+      if(cudaEventElapsedTime(&ms, tev[4 * b + q], tev[4 * b + q + 1]) != cudaSuccess)
+        return fail(CCSDT_E_CUDA, "phase-timing elapsed time");
+      phase_ms[q] += ms;
+    }
+  phase_batches += (long) tev_slots.size();
+  for(int n: tev_slots) phase_triplets += n;
+  tev_used = 0;
+  tev_slots.clear();
+  return CCSDT_OK;
+}

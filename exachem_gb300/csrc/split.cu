@@ -455,13 +455,14 @@ bool encode_map(CUtensorMap* m, const void* base, int Kp, long long d1, long lon
 
 } // namespace
 
-ccsdt_status ccsdt_handle::ensure_tmaps(int S) {
-  if(tmaps_ready && tmaps_S == S) return CCSDT_OK;
+// Tensor maps for S planes whose B-side box is NT rows: NT must equal the N tile of the kernel
+// that will use them (its shared-memory B slot holds exactly S x NT rows of 128 bytes).
+ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT) {
+  if(tmaps_ready && tmaps_S == S && tmaps_NT == NT) return CCSDT_OK;
   if(S > slices_ready) return fail(CCSDT_E_STATE, "tensor maps asked for more planes than were sliced");
+  if(NT <= 0 || NT > 256 || NT % 16) return fail(CCSDT_E_INVALID, "bad N tile for the tensor maps");
   const long long o = this->o, v = this->v, S_ = S;
   const int       P = slices_ready; // stored planes (extent); the box loads the first S
-  const int       NT = tc_nt(S);
-  if(!NT) return fail(CCSDT_E_INVALID, "no tcgen05 configuration for this slice count");
   const long long Kv = kp_v, Ko = kp_o;
   bool ok = true;
   // A side (pair rows, 128-row boxes): rows (z, x, y) natural = z v^2 + x v + y, swapped = z v^2 + y v + x
@@ -475,12 +476,15 @@ ccsdt_status ccsdt_handle::ensure_tmaps(int S) {
   if(!ok) return fail(CCSDT_E_CUDA, "cuTensorMapEncodeTiled failed for the digit planes");
   tmaps_ready = true;
   tmaps_S     = S;
+  tmaps_NT    = NT;
   return CCSDT_OK;
 }
 
 template<int S>
 static ccsdt_status launch_tc(ccsdt_handle* h, TcBatch& b) {
   constexpr int NT = TcPick<S>::NT, ST = TcPick<S>::ST;
+  if(!h->tmaps_ready || h->tmaps_S != S || h->tmaps_NT != NT)
+    return h->fail(CCSDT_E_STATE, "tensor maps do not match the tcgen05 kernel's tile");
   using Cfg        = TcCfg<S, NT, ST>;
   const int    v   = h->v;
   const long long tiles = (long long) v * ((v + TC_BM - 1) / TC_BM) * ((v + NT - 1) / NT);
@@ -510,7 +514,7 @@ bool ccsdt_handle::tc_eligible(int S, int variant) const {
 
 ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eout) {
   ccsdt_status s;
-  if((s = ensure_tmaps(S))) return s;
+  if((s = ensure_tmaps(S, tc_nt(S)))) return s;
   const long long o = this->o, v = this->v, v2 = v * v;
   auto hole = [&](int xx, bool nat, int yy, int zz) {
     return TcTerm{nat ? MAP_T2H_NAT : MAP_T2H_SWP, MAP_OOOVH, xx, zz, yy, ex_t2h, nat ? v : 1, nat ? 1 : v,
@@ -607,6 +611,7 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 }
 
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
+  last_batched = false;
   if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
   const int S       = opts->slices;
   const int variant = opts->slice_kind;
@@ -616,9 +621,14 @@ ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* 
   if((s = ensure_slices(S, variant))) return s;
   if(!d_err || !F12 || !F34 || !F56 || !e_tiles || !e_part || !oovv_f || !t1_f)
     return fail(CCSDT_E_STATE, "split-precision buffers missing after slicing");
-  force_mma_sync = opts->reserved[0] != 0; // test knob: the mma.sync slice kernel everywhere
+  // test knob opts->reserved[0]: 0 persistent tcgen05 (default), 1 mma.sync slice kernel,
+  // 2 per-triplet (non-persistent) tcgen05 kernel
+  const int kernel_kind = opts->reserved[0];
+  force_mma_sync        = kernel_kind == 1;
   cudaError_t e0 = cudaMemsetAsync(d_err, 0, sizeof(int), stream);
   if(e0 != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e0));
+  last_batched = kernel_kind == 0 && tc_eligible(S, variant);
+  if(last_batched) return run_batched(S, n, tri, opts->use_graph != 0, nullptr, nullptr);
   for(long t = 0; t < n; t++) {
     const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
     if(i == k) {

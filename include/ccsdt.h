@@ -49,8 +49,8 @@ typedef enum {
 /* Precision of the triples contractions. */
 typedef enum {
   CCSDT_MODE_FP64    = 0, /* FP64 DMMA tensor-core contractions, FP64 energy (the drop-in) */
-  CCSDT_MODE_OZAKI   = 1, /* split-precision: BF16 slices on tcgen05, FP64-exact recombination */
-  CCSDT_MODE_LEARNED = 2  /* split-precision with a per-block slice count from the MLP     */
+  CCSDT_MODE_OZAKI   = 1, /* split-precision: BF16 slices on tcgen05, float-float recombination */
+  CCSDT_MODE_LEARNED = 2  /* split-precision with a per-triplet slice count from the MLP   */
 } ccsdt_mode;
 
 /* The triples tile layout: occupied and virtual tile extents (ragged allowed).
@@ -88,7 +88,8 @@ typedef struct {
 
 typedef struct ccsdt_handle ccsdt_handle;
 
-/* Create a handle bound to CUDA device `device` for the given layout. */
+/* Create a handle bound to CUDA device `device` for the given layout; -1 = the calling
+ * thread's current device (the one the host runtime selected for this rank). */
 ccsdt_status ccsdt_create(ccsdt_handle** out, const ccsdt_layout* layout, int device);
 
 /* Copy the inputs into handle-owned device memory.  `on_device` = 0: host pointers
@@ -97,7 +98,15 @@ ccsdt_status ccsdt_upload(ccsdt_handle* h, const double* eps_occ, const double* 
                           const double* t1, const double* t2, const double* oovv,
                           const double* ooov, const double* ovvv, int on_device);
 
-/* Full (T): E[T] and E(T) over every occupied triplet.  Blocking. */
+/* The occupied triplets i <= j <= k of one shard, in the order ccsdt_energy runs them: the
+ * t-th triplet of the lexicographic list belongs to shard t mod shard_count.  Host-only (no
+ * device work).  tri = NULL returns the count in *n; otherwise tri[3 * *n] receives them.
+ * Replaces the reference's dynamic task split over ranks (a global atomic counter,
+ * ac->fetch_add at ccsd_t_fused_driver.hpp:172,456): every triplet of a closed-shell run costs
+ * the same 12 v^3 (o + v) flops, so a static split is balanced and needs no counter. */
+ccsdt_status ccsdt_shard_triplets(int o, int shard_index, int shard_count, long* n, int* tri);
+
+/* Full (T): E[T] and E(T) over every occupied triplet of the shard in opts.  Blocking. */
 ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, ccsdt_result* out);
 
 /* Per-triplet contributions for an explicit list tri[3n] (each i <= j <= k < o):
@@ -110,6 +119,15 @@ ccsdt_status ccsdt_triplet_energies(ccsdt_handle* h, const ccsdt_opts* opts, lon
  * CUDA events on its own stream.  No counterpart in the reference (it used one pooled
  * stream per rank, ccsd_t_all_fused.hpp:108). */
 ccsdt_status ccsdt_set_stream(ccsdt_handle* h, void* stream);
+
+/* Live per-phase device timing of the batched split-precision path (the persistent tcgen05
+ * kernels).  on != 0 starts the accumulation (and zeroes it): CUDA events on the handle's
+ * stream around the l-sum contraction, the d-sum contraction and the energy of every batch,
+ * read when the call returns.  ccsdt_phase_times gives the accumulated milliseconds ms3[3]
+ * and the numbers of batches and triplets they cover.  Batches replayed from a CUDA graph
+ * are not timed.  No counterpart in the reference (its timers are host-side, ccsd_t.cpp). */
+ccsdt_status ccsdt_set_phase_timing(ccsdt_handle* h, int on);
+ccsdt_status ccsdt_phase_times(const ccsdt_handle* h, double* ms3, long* batches, long* triplets);
 
 /* Device milliseconds of each phase of one triplet (i <= j <= k), measured with CUDA
  * events on the handle's stream: out_ms[0] l-sum contractions, [1] d-sum contractions,
@@ -178,7 +196,7 @@ ccsdt_status ccsdt_mlp_predict(const float* params, const float* X, int n, int* 
 ccsdt_status ccsdt_triplet_features(ccsdt_handle* h, long n, const int* tri, float* feats);
 
 /* Install (params != NULL, CCSDT_MLP_NPARAM floats) or clear the model CCSDT_MODE_LEARNED uses.
- * In that mode opts->slices is the full count used for the fallback (default 6) and
+ * In that mode opts->slices is the full count used for the fallback (default 5) and
  * opts->energy_budget the relative per-triplet budget of the a-posteriori check. */
 ccsdt_status ccsdt_set_slice_model(ccsdt_handle* h, const float* params);
 

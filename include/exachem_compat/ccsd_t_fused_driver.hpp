@@ -24,6 +24,7 @@
 
 #include <chrono>
 #include <cstddef>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -133,7 +134,23 @@ SpatialInputs gather_closed_shell(const std::vector<size_t>& mo_tiles, size_t no
   return S;
 }
 
+// Mode from the environment: EXACHEM_GB300_MODE = fp64 (default) | ozaki | learned,
+// EXACHEM_GB300_SLICES = digit planes for ozaki (default 3).
+inline ccsdt_opts opts_from_env() {
+  ccsdt_opts  op{};
+  const char* m = std::getenv("EXACHEM_GB300_MODE");
+  std::string mode = m ? m : "fp64";
+  if(mode == "fp64") op.mode = CCSDT_MODE_FP64;
+  else if(mode == "ozaki") op.mode = CCSDT_MODE_OZAKI;
+  else if(mode == "learned") op.mode = CCSDT_MODE_LEARNED;
+  else throw std::invalid_argument("EXACHEM_GB300_MODE must be fp64, ozaki or learned: " + mode);
+  const char* sl = std::getenv("EXACHEM_GB300_SLICES");
+  op.slices      = sl ? std::atoi(sl) : 3;
+  return op;
+}
+
 // Runs (T) on the spatial inputs through the C ABI: returns (E[T], E(T), device seconds).
+// device -1 = the calling thread's current CUDA device.
 inline std::tuple<double, double, double> run_closed_shell(const SpatialInputs& S, int device,
                                                            const ccsdt_opts& opts) {
   ccsdt_layout  L{S.o, S.v, (int) S.occ_tiles.size(), S.occ_tiles.data(), (int) S.vir_tiles.size(),
@@ -178,12 +195,10 @@ public:
     for(auto x: MO.input_tile_sizes()) mo.push_back((size_t) x);
     const size_t noa = MO("occ_alpha").num_tiles(), nva = MO("virt_alpha").num_tiles();
     auto         S   = exachem_gb300::gather_closed_shell<T>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl_sorted);
-    ccsdt_opts   op{};
-    op.mode        = CCSDT_MODE_FP64;
-    op.shard_index = (int) ec.pg().rank().value();
-    op.shard_count = (int) ec.pg().size().value();
-    int dev        = 0;
-    auto [e4, e5, work] = exachem_gb300::run_closed_shell(S, dev, op);
+    ccsdt_opts   op = exachem_gb300::opts_from_env();
+    op.shard_index  = (int) ec.pg().rank().value();
+    op.shard_count  = (int) ec.pg().size().value();
+    auto [e4, e5, work] = exachem_gb300::run_closed_shell(S, /*current device*/ -1, op);
     double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return {(T) e4, (T) e5, work, total};
   }

@@ -53,11 +53,12 @@ def test_split_error_shrinks_with_slices(built):
     assert errs[3] < errs[2] and errs[4] < errs[3]
 
 
-def test_split_triplet_w_close_to_fp64(built):
+@pytest.mark.parametrize("kernel", [0, 2])   # 0 persistent queue, 2 one CTA per tile
+def test_split_triplet_w_close_to_fp64(built, kernel):
     ft = _ft(6, 40, 0)
     for (i, j, k) in [(0, 1, 2), (1, 3, 3), (0, 0, 5)]:
         wf = ft.triplet_w(i, j, k, "fp64")
-        ws = ft.triplet_w(i, j, k, "ozaki", slices=5)
+        ws = ft.triplet_w(i, j, k, "ozaki", slices=5, legacy_mma=kernel)
         assert np.abs(ws - wf).max() <= 1e-9 * np.abs(wf).max()
 
 
@@ -67,3 +68,24 @@ def test_split_per_triplet_sum_equals_total(built):
     tot = ft.energy("ozaki", slices=3)
     e4, e5 = ft.triplet_energies(all_triplets(7), "ozaki", slices=3)
     assert e5.sum() == pytest.approx(tot["e_paren_T"], rel=1e-13)
+
+
+@pytest.mark.parametrize("o,v,seed", [(6, 40, 0), (5, 130, 2), (9, 70, 5)])
+def test_persistent_queue_equals_per_triplet_tcgen05(built, o, v, seed):
+    ft = _ft(o, v, seed)
+    for S in (2, 3, 4):
+        per = ft.energy("ozaki", slices=S, legacy_mma=2)
+        pers = ft.energy("ozaki", slices=S)
+        graph = ft.energy("ozaki", slices=S, use_graph=1)
+        assert pers["e_paren_T"] == pytest.approx(per["e_paren_T"], rel=1e-13, abs=0)
+        assert graph["e_paren_T"] == pers["e_paren_T"]
+
+
+def test_persistent_batches_cover_every_triplet(built):
+    """more triplets than one batch, a ragged last batch, results in input order"""
+    from exachem_gb300.ccsd_t import all_triplets
+    ft = _ft(8, 33, 6)
+    tri = all_triplets(8)
+    e4, e5 = ft.triplet_energies(tri, "ozaki", slices=3)
+    r4, r5 = ft.triplet_energies(tri, "ozaki", slices=3, legacy_mma=2)
+    np.testing.assert_allclose(e5, r5, rtol=1e-12, atol=1e-12 * np.abs(r5).max())

@@ -70,7 +70,36 @@ def test_learned_mode_meets_budget_and_saves_products(built):
     lab, _, _ = learned.label_triplets(ft, tri, budget=1e-8, smax=6)
     fixed = int(lab.max())
     cost = lambda S: S * (S + 1) / 2
-    learned_cost = mean_s * (mean_s + 1) / 2
+    pred = learned.mlp_predict(params, learned.features(ft, tri))
+    n = len(tri)
+    learned_cost = (sum(cost(min(max(s, 2), 6)) for s in pred) + fallbacks * cost(6)) / n
     print(f"fixed S={fixed} ({cost(fixed)} products) vs learned mean S={mean_s:.2f} "
-          f"({learned_cost:.1f}), fallbacks={fallbacks}")
+          f"({learned_cost:.2f} products incl. {fallbacks} full-slice fallbacks)")
     assert learned_cost <= cost(fixed) + 1e-9
+    assert fallbacks <= 0.25 * n
+
+
+def test_learned_mode_groups_equal_fixed_count_runs(built):
+    """LEARNED runs each predicted count as one batched persistent pass with the results
+    scattered back to each triplet's own index: every triplet must equal the same triplet
+    run alone at its predicted count (no fallbacks with a budget of 1)."""
+    from exachem_gb300 import ccsd_t as ct, learned
+    from exachem_gb300.generator import generate
+    o, v = 9, 48
+    ft = ct.FusedTriples(o, v, ts=24)
+    ft.upload_dict(generate(o, v, 77))
+    tri = ct.all_triplets(o)
+    X = learned.features(ft, tri)
+    y = np.random.default_rng(3).integers(0, 4, len(tri)).astype(np.int32)   # counts 2..5
+    params, _ = learned.mlp_train(X, y, epochs=300, batch=32, lr=3e-3, seed=2)
+    pred = np.clip(learned.mlp_predict(params, X), 2, 5)
+    assert len(set(pred.tolist())) >= 2
+    learned.set_model(ft, params)
+    e4, e5 = ft.triplet_energies(tri, "learned", slices=5, energy_budget=1.0)
+    _, fallbacks = learned.learned_stats(ft)
+    assert fallbacks == 0
+    for S in sorted(set(pred.tolist())):
+        sel = pred == S
+        f4, f5 = ft.triplet_energies(tri[sel], "ozaki", slices=S)
+        np.testing.assert_allclose(e5[sel], f5, rtol=1e-13, atol=0)
+        np.testing.assert_allclose(e4[sel], f4, rtol=1e-13, atol=0)
