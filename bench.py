@@ -313,8 +313,9 @@ def main():
         pt = ft.phase_times()
         ft.set_phase_timing(False)
 
-    # roofline of the dominant kernel, the d-sum contraction (12 v^4 FP64-equivalent flops per
-    # triplet: 3 arrays x 2 terms x v^4 multiply-adds)
+    # roofline of the dominant kernel.  FP64 path: the d-sum contraction launch (12 v^4 flops per
+    # triplet: 3 arrays x 2 terms x v^4 multiply-adds).  Split path: the contraction launch with
+    # the l-sum and d-sum terms of a batch (12 v^3 (v + o) FP64-equivalent flops per triplet)
     fp64_eq = 12.0 * float(v) ** 4
     peaks = measured_peaks()
     if mode == "fp64":
@@ -330,14 +331,14 @@ def main():
     else:
         # live: CUDA events around every batch's launches inside the timed region
         nb, ntr = max(1, pt["batches"]), max(1, pt["triplets"])
-        gemm_ms = pt["d_sum_ms"] / nb                       # average d-sum launch (one batch)
+        gemm_ms = pt["contraction_ms"] / nb                 # average contraction launch (one batch)
+        fp64_eq = 12.0 * float(v) ** 3 * (v + o)           # l-sum and d-sum terms run in the same launch
         per_launch = fp64_eq * S * (S + 1) / 2 * ntr / nb  # BF16 digit-plane products of one launch
         peak, peak_src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (burst), of measured"
         kernel = "oz_persist_kernel"
-        phase = {"l_sum_per_triplet": pt["l_sum_ms"] / ntr, "d_sum_per_triplet": pt["d_sum_ms"] / ntr,
-                 "energy_per_triplet": pt["energy_ms"] / ntr, "batches": pt["batches"],
-                 "triplets_per_batch": ntr / nb}
-        timing = "live CUDA events on the launching stream around each batch's d-sum launch in the timed region"
+        phase = {"contraction_per_triplet": pt["contraction_ms"] / ntr, "energy_per_triplet": pt["energy_ms"] / ntr,
+                 "batches": pt["batches"], "triplets_per_batch": ntr / nb}
+        timing = "live CUDA events on the launching stream around each batch's contraction launch in the timed region"
     achieved = per_launch / (gemm_ms * 1e-3) / 1e12
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": profile_traffic(kernel), "kernel": kernel,

@@ -50,7 +50,7 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_last_launch_count", "ccsdt_reference_op_count", "ccsdt_destroy",
             "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet",
             "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc", "ccsdt_shard_triplets",
-            "ccsdt_set_phase_timing", "ccsdt_phase_times"]
+            "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates"]
 
 
 def load_library(path: str | os.PathLike | None = None):
@@ -71,6 +71,7 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_reference_op_count.argtypes = [ctypes.POINTER(Layout), dp, ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_set_stream.argtypes = [vp, vp]
     lib.ccsdt_set_phase_timing.argtypes = [vp, ctypes.c_int]
+    lib.ccsdt_triplet_error_estimates.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp, dp]
     lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
     lib.ccsdt_profile_triplet.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
@@ -84,7 +85,8 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_status_string.restype = ctypes.c_char_p
     for name in ("ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
                  "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet",
-                 "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times"):
+                 "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
+                 "ccsdt_triplet_error_estimates"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -206,16 +208,28 @@ class FusedTriples:
                                                    w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return w
 
+    def triplet_error_estimates(self, tri, slices: int):
+        """(E[T]_t, E(T)_t, estimated |E(T)_t - E(T)_t,fp64|) at `slices` BF16 digit planes."""
+        t = np.ascontiguousarray(np.asarray(tri, dtype=np.int32).reshape(-1, 3))
+        n = len(t)
+        e4, e5, est = np.zeros(n), np.zeros(n), np.zeros(n)
+        op = self.opts("ozaki", slices=slices)
+        dpp = ctypes.POINTER(ctypes.c_double)
+        self._check(self.lib.ccsdt_triplet_error_estimates(
+            self.h, ctypes.byref(op), n, t.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+            e4.ctypes.data_as(dpp), e5.ctypes.data_as(dpp), est.ctypes.data_as(dpp)))
+        return e4, e5, est
+
     def set_phase_timing(self, on: bool = True):
         """Start (and zero) or stop live per-phase timing of the batched split-precision path."""
         self._check(self.lib.ccsdt_set_phase_timing(self.h, int(on)))
 
     def phase_times(self) -> dict:
-        """Accumulated device ms of the l-sum, d-sum and energy phases since set_phase_timing."""
+        """Accumulated device ms of the contraction and energy launches since set_phase_timing."""
         ms = (ctypes.c_double * 3)()
         b, t = ctypes.c_long(), ctypes.c_long()
         self._check(self.lib.ccsdt_phase_times(self.h, ms, ctypes.byref(b), ctypes.byref(t)))
-        return {"l_sum_ms": ms[0], "d_sum_ms": ms[1], "energy_ms": ms[2], "batches": b.value, "triplets": t.value}
+        return {"contraction_ms": ms[0], "energy_ms": ms[1], "batches": b.value, "triplets": t.value}
 
     def launch_count(self) -> int:
         return int(self.lib.ccsdt_last_launch_count(self.h))

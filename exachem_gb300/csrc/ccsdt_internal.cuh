@@ -10,7 +10,7 @@
 #include "../../include/ccsdt.h"
 
 constexpr int kEnergyBlocks = 1216; // 8 x 152 SMs
-constexpr int kTiledBlocks  = 1216; // persistent grid of the tiled energy
+constexpr int kTiledBlocks  = 1216; // upper bound of the tiled energy's persistent grid
 
 struct ccsdt_handle {
   int              device = 0, o = 0, v = 0;
@@ -41,7 +41,7 @@ struct ccsdt_handle {
   float *            oovv_f = nullptr, *t1_f = nullptr;
   float2 *           F12 = nullptr, *F34 = nullptr, *F56 = nullptr;
   // tcgen05 path: TMA maps over the digit planes (built once per slicing) and an error flag
-  CUtensorMap        tmaps[6];
+  CUtensorMap        tmaps[9];
   bool               tmaps_ready = false;
   int                tmaps_S     = 0, tmaps_NT = 0;
   int*               d_err       = nullptr;
@@ -77,6 +77,7 @@ struct ccsdt_handle {
   ccsdt_status run_triplet_S(int i, int j, int k, int S, double* eout);
   // learned slice count
   ccsdt_status run_learned(const ccsdt_opts* opts, long n, const int* tri_host);
+  double       truncation_estimate(float tail_sq, double sens) const;
   ccsdt_status features(long n, const int* tri_dev, float* feats_dev);
   ccsdt_status ensure_stats();
   std::vector<float> model;          // MLP parameters (host copy); empty = no model
@@ -103,14 +104,17 @@ struct ccsdt_handle {
   // per-call statistics of the learned mode
   double             learned_mean_slices = 0.0;
   long               learned_fallbacks   = 0;
+  double             learned_cost_products = 0.0; // digit-plane products run, incl. escalations
   ccsdt_status check_device_error();
   bool         force_mma_sync = false; // use the mma.sync slice kernel even where tcgen05 applies
-  // live per-phase timing of the batched path: 4 events per batch, read after the call
+  // live per-phase timing of the batched path: 3 events per batch, read after the call
   bool                     phase_timing = false, capturing = false;
   std::vector<cudaEvent_t> tev;
   size_t                   tev_used = 0;
   std::vector<int>         tev_slots;
-  double                   phase_ms[3]   = {0, 0, 0}; // l-sum, d-sum, energy + reduction
+  double                   phase_ms[3]   = {0, 0, 0}; // contraction, energy + reduction, unused
   long                     phase_batches = 0, phase_triplets = 0;
   ccsdt_status collect_phase_times();
+  int          energy_grid_ = 0; // resident CTAs of the tiled energy kernels (one full wave)
+  int          energy_grid();
 };

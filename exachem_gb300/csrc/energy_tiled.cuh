@@ -26,7 +26,7 @@ struct TiledEnergyArgs {
   const int3*   tiles;     // sorted block triples
   int           ntiles;
   int           o, v, i, j, k;
-  double*       part;      // 6 doubles per CTA: E[T] (s, c), E(T) (s, c), sum ((|Z| + |Y|) / |D|)^2, 0
+  double*       part;      // 6 doubles per CTA: E[T] (s, c), E(T) (s, c), sum (18 Y^2 + 12 Z^2) / D^2, 0
 };
 
 // slot s <-> permutation (p0, p1, p2) of the block positions
@@ -45,6 +45,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   __shared__ float  Ojk[3][3][B * B], Oik[3][3][B * B], Oij[3][3][B * B];
   __shared__ float  ti[3][B], tj[3][B], tk[3][B];
   __shared__ float2 evs[3][B];
+  __shared__ float2 dab[3][3][B * B];    // e_i + e_j + e_k - e_a - e_b (float-float), per block pair
   __shared__ int    blk0[3], blkn[3];
   __shared__ int    slot_on[6];
 
@@ -92,6 +93,13 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       tk[u][x] = ok ? A.t1[(long long) k * v + a] : 0.f;
       const ff e = ok ? ff_from_double(A.ev[a]) : ff{0.f, 0.f};
       evs[u][x] = make_float2(e.hi, e.lo);
+    }
+    __syncthreads();
+    for(int e = tid; e < 9 * B * B; e += ET_THREADS) {
+      const int    u = e / (3 * B * B), w = (e / (B * B)) % 3, x = (e / B) % B, y = e % B;
+      const float2 ea = evs[u][x], eb = evs[w][y];
+      const ff     d  = ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y});
+      dab[u][w][x * B + y] = make_float2(d.hi, d.lo);
     }
     // W of the six slots: three passes, each reading one array along its contiguous index
 #pragma unroll 1
@@ -150,15 +158,19 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       const float sgl = 3.f * SG(p0, p1, p2, a, b, c) - SG(p0, p2, p1, a, c, b) - SG(p1, p0, p2, b, a, c) -
                         SG(p2, p1, p0, c, b, a);
       const ff z  = ff_add(ff_add(ff_scale(wabc, 4.f), wbca), wcab);
-      const ff y4 = ff_add(ff_add(ff_scale(wabc, 3.f), ff_scale(wacb, -1.f)),
-                           ff_add(ff_scale(wbac, -1.f), ff_scale(wcba, -1.f)));
+      const ff y4 = ff_add(ff_mul_f(wabc, 3.f), ff_neg(ff_add(ff_add(wacb, wbac), wcba)));
       const ff y5 = ff_add_f(y4, sgl);
-      const float2 ea = evs[p0][a], eb = evs[p1][b], ec = evs[p2][c];
-      const ff d = ff_add(ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y}), ff{-ec.x, -ec.y});
-      s4 = ff_add(s4, ff_div(ff_mul(z, y4), d));
-      s5 = ff_add(s5, ff_div(ff_mul(z, y5), d));
-      const float g = (fabsf(z.hi) + fabsf(y5.hi)) / fabsf(d.hi); // |de / dW| up to a constant
-      sens += g * g;
+      const float2 dd = dab[p0][p1][a * B + b], ec = evs[p2][c];
+      const ff d  = ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y});
+      const ff id = ff_div(ff{1.f, 0.f}, d);              // 1 / D
+      const ff zi = ff_mul(z, id);                        // Z / D
+      s4 = ff_add(s4, ff_mul(zi, y4));
+      s5 = ff_add(s5, ff_mul(zi, y5));
+      // first-order sensitivity to errors in W: W_abc enters Z_abc (x4), Z_bca, Z_cab and, through
+      // V, Y_abc (x3), Y_acb, Y_bac, Y_cba; with uncorrelated signs
+      //   |dE/dW|^2 ~ (16 + 1 + 1) Y^2 / D^2 + (9 + 1 + 1 + 1) Z^2 / D^2
+      const float yr = y5.hi * id.hi, zr = zi.hi;
+      sens = fmaf(18.f * yr, yr, fmaf(12.f * zr, zr, sens));
     }
   }
   CSum c4, c5;

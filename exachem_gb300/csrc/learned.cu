@@ -183,10 +183,68 @@ extern "C" ccsdt_status ccsdt_set_slice_model(ccsdt_handle* h, const float* para
   return CCSDT_OK;
 }
 
-extern "C" ccsdt_status ccsdt_learned_stats(const ccsdt_handle* h, double* mean_slices, long* fallbacks) {
+extern "C" ccsdt_status ccsdt_learned_stats(const ccsdt_handle* h, double* mean_slices, long* fallbacks,
+                                            double* products) {
   if(!h) return CCSDT_E_INVALID;
   if(mean_slices) *mean_slices = h->learned_mean_slices;
   if(fallbacks) *fallbacks = h->learned_fallbacks;
+  if(products) *products = h->learned_cost_products;
+  return CCSDT_OK;
+}
+
+// A-posteriori estimate of the standard deviation of a triplet's truncation error E_S - E_exact
+// from the sum of squares of its last kept level's terms (tail_sq, over the 12 v^3 term values of
+// the twelve contraction terms) and its sensitivity sens = (m/9)^2 sum_abc (18 Y^2 + 12 Z^2) / D^2
+// (|dE/dW_abc|^2 with uncorrelated signs).  The dropped levels are ~2^-7 of the last kept one,
+// with signs that do not correlate across the v^3 elements, so
+//   sigma ~ kEstScale 2^-7 sqrt(sens tail_sq / v^3).
+// A statistical estimate (random-walk model), not a rigorous bound; kEstScale is fitted to
+// errors measured against the FP64 path (tests/test_learned.py checks that 3 sigma covers them).
+double ccsdt_handle::truncation_estimate(float tail_sq, double sens) const {
+  constexpr double kEstScale = 5.0;
+  const double     v3         = (double) v * v * v;
+  return kEstScale * std::ldexp(1.0, -7) * std::sqrt(sens * (double) tail_sq / v3);
+}
+
+extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccsdt_opts* opts, long n, const int* tri,
+                                                      double* e_bracket, double* e_paren, double* est) {
+  if(!h) return CCSDT_E_INVALID;
+  if(!opts || opts->mode != CCSDT_MODE_OZAKI || n < 0 || (n && (!tri || !e_paren || !est)))
+    return h->fail(CCSDT_E_INVALID, "ccsdt_triplet_error_estimates: needs CCSDT_MODE_OZAKI and output arrays");
+  if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_triplet_error_estimates before ccsdt_upload");
+  if(!h->tc_eligible(opts->slices, opts->slice_kind))
+    return h->fail(CCSDT_E_INVALID, "error estimates need the tcgen05 path (BF16 digits, 1..5 planes)");
+  for(long t = 0; t < n; t++) {
+    const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
+    if(!(0 <= i && i <= j && j <= k && k < h->o)) return h->fail(CCSDT_E_INVALID, "triplet outside 0 <= i <= j <= k < o");
+  }
+  if(cudaSetDevice(h->device) != cudaSuccess) return h->fail(CCSDT_E_CUDA, "cudaSetDevice");
+  if(n == 0) return CCSDT_OK;
+  ccsdt_status s;
+  if((s = h->ensure_triplet_slots(n)) || (s = h->ensure_slices(opts->slices, 0))) return s;
+  Scratch sc;
+  float*  dtail = sc.get<float>((size_t) n);
+  double* dsens = sc.get<double>((size_t) n);
+  if(!dtail || !dsens) return h->fail(CCSDT_E_OOM, "estimate scratch");
+  if(cudaMemsetAsync(dtail, 0, sizeof(float) * n, h->stream) != cudaSuccess ||
+     cudaMemsetAsync(dsens, 0, sizeof(double) * n, h->stream) != cudaSuccess ||
+     cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream) != cudaSuccess)
+    return h->fail(CCSDT_E_CUDA, "estimate scratch init");
+  h->force_mma_sync = false;
+  if((s = h->run_batched(opts->slices, n, tri, false, dtail, dsens))) return s;
+  std::vector<double> E(2 * n), sens(n);
+  std::vector<float>  tail(n);
+  if(cudaMemcpyAsync(E.data(), h->etrip, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+     cudaMemcpyAsync(tail.data(), dtail, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+     cudaMemcpyAsync(sens.data(), dsens, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+     cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return h->fail(CCSDT_E_CUDA, "estimate readback");
+  if((s = h->check_device_error())) return s;
+  for(long t = 0; t < n; t++) {
+    if(e_bracket) e_bracket[t] = E[2 * t];
+    e_paren[t] = E[2 * t + 1];
+    est[t]     = tri[3 * t] == tri[3 * t + 2] ? 0.0 : h->truncation_estimate(tail[t], sens[t]);
+  }
   return CCSDT_OK;
 }
 
@@ -257,36 +315,85 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
     }
     return CCSDT_OK;
   };
+  // effective count: predictions the estimate cannot check (above the tcgen05 range, which
+  // collects it) run at the full count directly
+  for(long t = 0; t < n; t++) {
+    S[t] = std::min(std::max(S[t], 2), Sfull);
+    if(!tc_eligible(S[t], 0)) S[t] = Sfull;
+  }
   for(int cnt = 2; cnt <= Sfull; cnt++) {
     std::vector<long> ids;
     for(long t = 0; t < n; t++)
-      if(std::min(std::max(S[t], 2), Sfull) == cnt) ids.push_back(t);
-    ssum += (double) cnt * (double) ids.size();
-    if((s = group(cnt, ids, cnt < Sfull))) return s;
+      if(S[t] == cnt) ids.push_back(t);
+    if((s = group(cnt, ids, true))) return s;
   }
-  learned_mean_slices = n ? ssum / n : 0.0;
-  // a-posteriori check and full-slice fallback
-  std::vector<double> E(2 * n), sens(n);
+  learned_mean_slices = 0;
+  ssum                = 0; // digit-plane products actually run (S (S + 1) / 2 per run)
+  long nz             = 0;
+  for(long t = 0; t < n; t++)
+    if(tri[3 * t] != tri[3 * t + 2]) {
+      learned_mean_slices += S[t];
+      ssum += S[t] * (S[t] + 1) / 2.0;
+      nz++;
+    }
+  learned_mean_slices = nz ? learned_mean_slices / nz : 0.0;
+  // Acceptance on the total: the triplets' truncation errors are independent with estimated
+  // standard deviations est_t, so the call is accepted when 3 sqrt(sum_t est_t^2) <= budget x
+  // sum_t |E(T)_t|.  Otherwise the triplets with the largest estimates are rerun one count
+  // higher (each step divides a triplet's error by ~2^7) until the prediction passes.
+  std::vector<double> E(2 * n), sens(n), est(n, 0.0);
   std::vector<float>  tail(n);
-  if(cudaMemcpyAsync(E.data(), etrip, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-     cudaMemcpyAsync(tail.data(), dtail, sizeof(float) * n, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-     cudaMemcpyAsync(sens.data(), dsens, sizeof(double) * n, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-     cudaStreamSynchronize(stream) != cudaSuccess)
-    return fail(CCSDT_E_CUDA, "learned-mode readback");
-  const double budget = opts->energy_budget > 0 ? opts->energy_budget : 1e-8;
+  auto readback = [&]() -> ccsdt_status {
+    if(cudaMemcpyAsync(E.data(), etrip, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+       cudaMemcpyAsync(tail.data(), dtail, sizeof(float) * n, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+       cudaMemcpyAsync(sens.data(), dsens, sizeof(double) * n, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+       cudaStreamSynchronize(stream) != cudaSuccess)
+      return fail(CCSDT_E_CUDA, "learned-mode readback");
+    for(long t = 0; t < n; t++)
+      est[t] = (tri[3 * t] == tri[3 * t + 2] || !tc_eligible(S[t], 0)) ? 0.0 : truncation_estimate(tail[t], sens[t]);
+    return CCSDT_OK;
+  };
+  if((s = readback())) return s;
+  double abs_sum = 0;
+  for(long t = 0; t < n; t++) abs_sum += std::fabs(E[2 * t + 1]);
+  const double target = (opts->energy_budget > 0 ? opts->energy_budget : 1e-8) * abs_sum / 3.0; // on sqrt(sum est^2)
   learned_fallbacks   = 0;
-  double            bound = 0;
-  std::vector<long> redo;
-  for(long t = 0; t < n; t++) {
-    const int i = tri[3 * t], k = tri[3 * t + 2];
-    const int st = std::min(std::max(S[t], 2), Sfull);
-    if(i == k || st >= Sfull) continue;
-    const double est = 6.0 * std::ldexp((double) tail[t], -6) * std::sqrt(sens[t]);
-    if(!(est <= budget * std::fabs(E[2 * t + 1]))) redo.push_back(t);
-    else bound += est;
+  for(int round = 0; round < 16; round++) {
+    double var = 0;
+    for(long t = 0; t < n; t++) var += est[t] * est[t];
+    if(var <= target * target) break;
+    // greedy: largest estimates first, assuming a rerun one count higher leaves 2^-7 of the error
+    std::vector<long> order;
+    for(long t = 0; t < n; t++)
+      if(est[t] > 0 && S[t] < Sfull) order.push_back(t);
+    if(order.empty()) break;
+    std::sort(order.begin(), order.end(), [&](long a, long b) { return est[a] > est[b]; });
+    std::vector<long> redo;
+    for(long t: order) {
+      if(var <= target * target) break;
+      var -= est[t] * est[t] * (1.0 - std::ldexp(1.0, -14));
+      redo.push_back(t);
+    }
+    learned_fallbacks += (long) redo.size();
+    for(int cnt = 3; cnt <= Sfull; cnt++) {
+      std::vector<long> ids;
+      for(long t: redo)
+        if(S[t] + 1 == cnt) ids.push_back(t);
+      if(ids.empty()) continue;
+      for(long t: ids) { // fresh estimate slots for the rerun
+        ssum += cnt * (cnt + 1) / 2.0;
+        if(cudaMemsetAsync(dtail + t, 0, sizeof(float), stream) != cudaSuccess ||
+           cudaMemsetAsync(dsens + t, 0, sizeof(double), stream) != cudaSuccess)
+          return fail(CCSDT_E_CUDA, "estimate reset");
+      }
+      if((s = group(cnt, ids, true))) return s;
+    }
+    for(long t: redo) S[t] += 1;
+    if((s = readback())) return s;
   }
-  learned_fallbacks = (long) redo.size();
-  if((s = group(Sfull, redo, false))) return s;
-  last_err_bound = bound;
+  double var = 0;
+  for(long t = 0; t < n; t++) var += est[t] * est[t];
+  last_err_bound = 3.0 * std::sqrt(var);
+  learned_cost_products = ssum;
   return CCSDT_OK;
 }

@@ -1,11 +1,13 @@
 // Persistent split-precision contraction: one CTA per SM pulls tiles from a device work queue.
 //
-// Work item = (triplet slot, job, x, y-block, n-block) of one contraction family (phase 0: the
-// l-sum / hole terms, phase 1: the d-sum / particle terms) for a batch of occupied triplets.  The
-// host orders the items by estimated cost (tile rows x columns, largest first; ties keep the
-// natural order, n-block fastest, so concurrently running CTAs share the A tile in L2) and the
-// CTAs take them with atomicAdd on a device counter.  The triplets come from a device table, so
-// the launch sequence of a batch is the same for every batch and is replayed from a CUDA graph.
+// Work item = (triplet slot, job, x, y-block, n-block): one 128 x NT tile of one of the three
+// partial arrays (job 0/1/2 = P12/P34/P56) of one occupied triplet, with all four of its terms
+// (two d-sum terms, K = v, and two l-sum terms, K = o) accumulated into the same tile, so each
+// element of P is written exactly once.  The host orders the items by estimated cost (largest
+// first; ties keep the natural order, n-block fastest, so concurrently running CTAs share the A
+// tile in L2) and the CTAs take them with atomicAdd on a device counter.  The triplets come from
+// a device table, so the launch sequence of a batch is the same for every batch and can be
+// replayed from a CUDA graph.
 //
 // Roles (320 threads): warp 0 lane 0 fetches items and issues TMA loads (running ahead across
 // items), warp 1 lane 0 issues the MMAs, warps 2-9 fold the digit levels into float-float.  The
@@ -21,17 +23,17 @@
 
 namespace ccsdt {
 
-constexpr int PZ_BM = 128, PZ_KC = 64, PZ_THREADS = 320, PZ_IR = 4;
+constexpr int PZ_BM = 128, PZ_KC = 64, PZ_THREADS = 320, PZ_IR = 4, PZ_TERMS = 4;
 constexpr unsigned PZ_END = 0xffffffffu;
 
-enum { PZ_OVVV_NAT = 0, PZ_OVVV_SWP = 1, PZ_T2 = 2, PZ_T2H_NAT = 3, PZ_T2H_SWP = 4, PZ_OOOVH = 5 };
+// map indices (the handle's map table): the d-sum uses 0-2, the l-sum 6-8
+enum { PZ_OVVV_NAT = 0, PZ_OVVV_SWP = 1, PZ_T2 = 2, PZ_T2H_NAT_B = 6, PZ_T2H_SWP_B = 7, PZ_OOOVH_A = 8, PZ_NMAPS = 9 };
 
 struct PzParams {
-  CUtensorMap     maps[6];
+  CUtensorMap     maps[PZ_NMAPS];
   const int*      tri;        // triplet table (4 ints per triplet: i, j, k, output index)
   const int*      base;       // device batch base index into tri (nullable -> 0)
   int             nslots;     // triplets per launch
-  int             phase;      // 0: l-sum, 1: d-sum
   int             o, v, kp_v, kp_o;
   float2*         F;          // P arrays of slot s: F + s * 3 v^3 (P12, P34, P56 consecutive)
   const int *     ex_t2, *ex_t2h, *ex_ovvv, *ex_ooovh;
@@ -39,37 +41,31 @@ struct PzParams {
   unsigned        nitems;
   unsigned*       queue;      // work counter, 0 at launch
   int*            err;        // set on a bounded-wait timeout
-  float*          tail;       // optional: tail[output index] = max |last kept level term|
+  float*          tail;       // optional: tail[output index] += sum of squares of the last
+                              // kept level's terms (a-posteriori truncation estimate)
 };
 
 struct PzTerm {
-  int       mapA, mapB, az, by, bx, Kp;
-  const int *eA, *eB;
-  long long eA_base, eA_x, eA_y;
-  float     sign;
+  int        mapA, mapB, a2, a3, b2, b3, Kp; // maps and their tile coordinates along dims 2, 3
+  const int *eA, *eB;                         // row exponents eA[eA_base + y eA_y], column eB[eB_base + n eB_n]
+  long long  eA_base, eA_y, eB_base, eB_n;
+  float      sign;
 };
 
-// The two terms of a job, from (phase, job, i, j, k) - the same plan as the host-side batches:
-// l-sum  P12[(a,c)][b]: t2h(i) nat x ooovh(k,j), t2h(k) swp x ooovh(i,j)   (P34, P56 likewise)
-// d-sum  P12[a][(c,b)]: ovvv(k) nat x t2(i,j),  ovvv(j) swp x t2(i,k)     (P34, P56 likewise)
-__device__ __forceinline__ PzTerm pz_term(const PzParams& P, int job, int t, int i, int j, int k) {
+// The four terms of a job's tile, from (job, t, i, j, k) and the item's x.  The tile holds
+// P[n][x][y] for 128 rows y and NT columns n (P12[a][c][b]: n = a, x = c, y = b; P34[b][a][c];
+// P56[c][b][a]):
+//   t = 0, 1  d-sum  P[n][x][y] += sum_d ovvv(z)[(x,y) or (y,x)][d] t2(xx,yy)[n][d]
+//   t = 2, 3  l-sum  P[n][x][y] -= sum_l t2h(xx)[(n,x) or (x,n)][l] ooovh(yy,zz)[y][l]
+// with, per job, (first index, natural pair order?, second, third):
+//   d-sum  job 0: (k,1,i,j) (j,0,i,k)   job 1: (k,0,j,i) (i,1,j,k)   job 2: (j,1,k,i) (i,0,k,j)
+//   l-sum  job 0: (i,1,k,j) (k,0,i,j)   job 1: (i,0,j,k) (j,1,i,k)   job 2: (j,0,k,i) (k,1,j,i)
+// The l-sum's "natural" pair (first, second) = (n, x) is read through the swapped-stride map.
+__device__ __forceinline__ PzTerm pz_term(const PzParams& P, int job, int t, int i, int j, int k, int x) {
   const long long v = P.v, o = P.o, v2 = v * v;
-  // l-sum jobs: (first, natural?, second, third) of term 0 / term 1
-  //   job 0: (i,1,k,j) (k,0,i,j)   job 1: (i,0,j,k) (j,1,i,k)   job 2: (j,0,k,i) (k,1,j,i)
-  // d-sum jobs:
-  //   job 0: (k,1,i,j) (j,0,i,k)   job 1: (k,0,j,i) (i,1,j,k)   job 2: (j,1,k,i) (i,0,k,j)
-  const int sel = job * 2 + t;
-  int       e0, nat, e2, e3;
-  if(P.phase == 0) {
-    switch(sel) {
-      case 0: e0 = i, nat = 1, e2 = k, e3 = j; break;
-      case 1: e0 = k, nat = 0, e2 = i, e3 = j; break;
-      case 2: e0 = i, nat = 0, e2 = j, e3 = k; break;
-      case 3: e0 = j, nat = 1, e2 = i, e3 = k; break;
-      case 4: e0 = j, nat = 0, e2 = k, e3 = i; break;
-      default: e0 = k, nat = 1, e2 = j, e3 = i; break;
-    }
-  } else {
+  const int       sel = job * 2 + (t & 1);
+  int             e0, nat, e2, e3;
+  if(t < 2) {
     switch(sel) {
       case 0: e0 = k, nat = 1, e2 = i, e3 = j; break;
       case 1: e0 = j, nat = 0, e2 = i, e3 = k; break;
@@ -78,24 +74,33 @@ __device__ __forceinline__ PzTerm pz_term(const PzParams& P, int job, int t, int
       case 4: e0 = j, nat = 1, e2 = k, e3 = i; break;
       default: e0 = i, nat = 0, e2 = k, e3 = j; break;
     }
+  } else {
+    switch(sel) {
+      case 0: e0 = i, nat = 1, e2 = k, e3 = j; break;
+      case 1: e0 = k, nat = 0, e2 = i, e3 = j; break;
+      case 2: e0 = i, nat = 0, e2 = j, e3 = k; break;
+      case 3: e0 = j, nat = 1, e2 = i, e3 = k; break;
+      case 4: e0 = j, nat = 0, e2 = k, e3 = i; break;
+      default: e0 = k, nat = 1, e2 = j, e3 = i; break;
+    }
   }
   PzTerm T;
-  if(P.phase == 0) {
-    const int xx = e0, yy = e2, zz = e3;
-    T.mapA = nat ? PZ_T2H_NAT : PZ_T2H_SWP;
-    T.mapB = PZ_OOOVH;
-    T.az = xx, T.by = zz, T.bx = yy, T.Kp = P.kp_o;
-    T.eA = P.ex_t2h, T.eA_base = xx * v2, T.eA_x = nat ? v : 1, T.eA_y = nat ? 1 : v;
-    T.eB   = P.ex_ooovh + (yy * o + zz) * v;
-    T.sign = -1.f;
-  } else {
+  if(t < 2) {
     const int z = e0, xx = e2, yy = e3;
-    T.mapA = nat ? PZ_OVVV_NAT : PZ_OVVV_SWP;
-    T.mapB = PZ_T2;
-    T.az = z, T.by = yy, T.bx = xx, T.Kp = P.kp_v;
-    T.eA = P.ex_ovvv, T.eA_base = z * v2, T.eA_x = nat ? v : 1, T.eA_y = nat ? 1 : v;
-    T.eB   = P.ex_t2 + (xx * o + yy) * v;
+    T.mapA = nat ? PZ_OVVV_NAT : PZ_OVVV_SWP, T.a2 = x, T.a3 = z;     // rows (z, x, y) or (z, y, x)
+    T.mapB = PZ_T2, T.b2 = yy, T.b3 = xx;                            // rows (xx, yy, n)
+    T.Kp = P.kp_v;
+    T.eA = P.ex_ovvv, T.eA_base = z * v2 + (nat ? x * v : x), T.eA_y = nat ? 1 : v;
+    T.eB = P.ex_t2, T.eB_base = (xx * o + yy) * v, T.eB_n = 1;
     T.sign = 1.f;
+  } else {
+    const int xx = e0, yy = e2, zz = e3;
+    T.mapA = PZ_OOOVH_A, T.a2 = zz, T.a3 = yy;                        // rows (yy, zz, y)
+    T.mapB = nat ? PZ_T2H_SWP_B : PZ_T2H_NAT_B, T.b2 = x, T.b3 = xx;   // pair rows (n, x) or (x, n)
+    T.Kp = P.kp_o;
+    T.eA = P.ex_ooovh, T.eA_base = (yy * o + zz) * v, T.eA_y = 1;
+    T.eB = P.ex_t2h, T.eB_base = xx * v2 + (nat ? x : x * v), T.eB_n = nat ? v : 1;
+    T.sign = -1.f;
   }
   return T;
 }
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
   if(warp == 0) {
     // ------------------------------------------------------------ work fetch + TMA producer
     if(lane == 0) {
-      for(int m = 0; m < 6; m++) sm100::prefetch_tmap(&P.maps[m]);
+      for(int m: {PZ_OVVV_NAT, PZ_OVVV_SWP, PZ_T2, PZ_T2H_NAT_B, PZ_T2H_SWP_B, PZ_OOOVH_A}) sm100::prefetch_tmap(&P.maps[m]);
       int stage_it = 0;
       for(int it = 0;; it++) {
         const unsigned q  = atomicAdd(P.queue, 1u);
@@ -198,8 +203,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         const PzItem w = pz_decode(id, v, yblocks, nblocks);
         const int*   tp = P.tri + 4 * (base + w.slot);
         const int    i = tp[0], j = tp[1], k = tp[2];
-        for(int t = 0; t < 2; t++) {
-          const PzTerm T = pz_term(P, w.job, t, i, j, k);
+        for(int t = 0; t < PZ_TERMS; t++) {
+          const PzTerm T = pz_term(P, w.job, t, i, j, k, w.x);
           for(int k0 = 0; k0 < T.Kp; k0 += PZ_KC, stage_it++) {
             const int s = stage_it % STAGES, use = stage_it / STAGES;
             if(use > 0 && !sm100::mbar_wait(&empty[s], (use - 1) & 1)) {
@@ -208,8 +213,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
             }
             unsigned char* a = smem + s * C::STAGE_BYTES;
             sm100::mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
-            sm100::tma_load_5d(a, &P.maps[T.mapA], &full[s], k0, w.yb * PZ_BM, w.x, T.az, 0);
-            sm100::tma_load_5d(a + C::A_BYTES, &P.maps[T.mapB], &full[s], k0, w.nb * NT, T.by, T.bx, 0);
+            sm100::tma_load_5d(a, &P.maps[T.mapA], &full[s], k0, w.yb * PZ_BM, T.a2, T.a3, 0);
+            sm100::tma_load_5d(a + C::A_BYTES, &P.maps[T.mapB], &full[s], k0, w.nb * NT, T.b2, T.b3, 0);
           }
         }
       }
@@ -229,8 +234,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         const unsigned id = item_id[r];
         sm100::mbar_arrive(&item_empty[r]);
         if(id == PZ_END) break;
-        const int Kp = P.phase == 0 ? P.kp_o : P.kp_v;
-        for(int t = 0; t < 2; t++, term_it++) {
+        for(int t = 0; t < PZ_TERMS; t++, term_it++) {
+          const int Kp  = t < 2 ? P.kp_v : P.kp_o;
           const int buf = term_it & 1;
           if(term_it >= 2 && !sm100::mbar_wait(&lvl_empty[buf], ((term_it >> 1) - 1) & 1)) {
             fail();
@@ -264,12 +269,17 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     }
   } else {
     // ------------------------------------------------------------ epilogue: 8 warps
+    // Thread = one tile row (TMEM lane) x half of the tile's columns.  Per item it first issues
+    // the global loads the item needs (the four terms' row exponents and one column exponent per
+    // lane), then per term waits for the MMAs, folds the S exact levels with oz_horner, scales by
+    // 2^(e_row + e_col - 7 (S + 1)) and adds in float-float; the finished tile is stored once.
     const int      q = warp & 3, half = (warp - 2) >> 2;   // lane quarter, column half
     const int      row = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
     const int      c_lo = half * C::HALF;
+    const long long v2 = (long long) v * v;
     int            term_it = 0;
-    float          tmax = 0.f;
+    float          tsq = 0.f;                                // sum of squares of last-level terms
     int            tail_slot = -1;
     for(int it = 0;; it++) {
       const int  r  = it % PZ_IR;
@@ -284,50 +294,66 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
       if(id == PZ_END) break;
       const PzItem w = pz_decode(id, v, yblocks, nblocks);
       const int* tp = P.tri + 4 * (base + w.slot);
-      if(P.tail && tp[3] != tail_slot) { // flush the per-triplet maximum when the triplet changes
+      if(P.tail && tp[3] != tail_slot) { // flush the per-triplet sum when the triplet changes
         if(tail_slot >= 0) {
 #pragma unroll
-          for(int off = 16; off > 0; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
-          if(lane == 0 && tmax > 0.f) atomicMax(reinterpret_cast<int*>(P.tail + tail_slot), __float_as_int(tmax));
+          for(int off = 16; off > 0; off >>= 1) tsq += __shfl_xor_sync(0xffffffffu, tsq, off);
+          if(lane == 0 && tsq > 0.f) atomicAdd(P.tail + tail_slot, tsq);
         }
-        tmax      = 0.f;
+        tsq       = 0.f;
         tail_slot = tp[3];
       }
       const int  i = tp[0], j = tp[1], k = tp[2];
       const int  y = w.yb * PZ_BM + row, n0 = w.nb * NT + c_lo;
       const bool vrow = y < v;
+      const bool vcol = lane < C::HALF && n0 + lane < v;
+      const long long nl = n0 + lane;
+      int   ea[PZ_TERMS], eb[PZ_TERMS];
+      float sgn[PZ_TERMS];
+#pragma unroll
+      for(int t = 0; t < PZ_TERMS; t++) {
+        const PzTerm T = pz_term(P, w.job, t, i, j, k, w.x);
+        ea[t]  = vrow ? T.eA[T.eA_base + y * T.eA_y] : 0;
+        eb[t]  = vcol ? T.eB[T.eB_base + nl * T.eB_n] : 0;
+        sgn[t] = T.sign;
+      }
+      // element (y, n) of the tile: P[n][x][y] (consecutive rows -> consecutive addresses)
+      float2* Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
       float hi[C::HALF], lo[C::HALF];
 #pragma unroll
       for(int e = 0; e < C::HALF; e++) hi[e] = lo[e] = 0.f;
       bool aborted = false;
-      for(int t = 0; t < 2; t++, term_it++) {
-        const PzTerm T   = pz_term(P, w.job, t, i, j, k);
-        const int    buf = term_it & 1;
-        const bool   okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it >> 1) & 1) && !*abort_flag);
+#pragma unroll 1
+      for(int t = 0; t < PZ_TERMS; t++, term_it++) {
+        const int   buf = term_it & 1;
+        const int   ea_t = t == 0 ? ea[0] : t == 1 ? ea[1] : t == 2 ? ea[2] : ea[3];
+        const int   eb_t = t == 0 ? eb[0] : t == 1 ? eb[1] : t == 2 ? eb[2] : eb[3];
+        const float sg_t = t == 0 ? sgn[0] : t == 1 ? sgn[1] : t == 2 ? sgn[2] : sgn[3];
+        const float sa  = ldexpf(sg_t, ea_t - OZ_BITS * (S + 1));
+        const float sbl = ldexpf(1.f, eb_t);
+        const bool  okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it >> 1) & 1) && !*abort_flag);
         if(!okw) {
           fail();
           aborted = true;
           break;
         }
         sm100::tc_fence_after();
-        const int ea = vrow ? T.eA[T.eA_base + (long long) w.x * T.eA_x + (long long) y * T.eA_y] : 0;
 #pragma unroll
         for(int c0 = 0; c0 < C::HALF; c0 += 16) {
-          int eb[16];
+          uint32_t rv[S][16];
 #pragma unroll
-          for(int e = 0; e < 16; e++) eb[e] = (n0 + c0 + e < v) ? T.eB[n0 + c0 + e] : 0;
-#pragma unroll 1
-          for(int l = 0; l < S; l++) {
-            uint32_t rv[16];
-            sm100::tmem_ld16(lane_base + buf * S * NT + l * NT + c_lo + c0, rv);
-            sm100::tmem_wait_ld();
+          for(int l = 0; l < S; l++) sm100::tmem_ld16(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
+          sm100::tmem_wait_ld();
 #pragma unroll
-            for(int e = 0; e < 16; e++) {
-              const float term = __uint_as_float(rv[e]) * ldexpf(T.sign, ea + eb[e] - OZ_BITS * (l + 2));
-              const ff    a    = ff_add_f(ff{hi[c0 + e], lo[c0 + e]}, term);
-              hi[c0 + e]       = a.hi;
-              lo[c0 + e]       = a.lo;
-              if(l == S - 1 && vrow) tmax = fmaxf(tmax, fabsf(term));
+          for(int e = 0; e < 16; e++) {
+            const float sb = __shfl_sync(0xffffffffu, sbl, c0 + e);
+            const ff    x  = oz_horner<S>(rv, e);
+            const ff    a  = ff_add(ff{hi[c0 + e], lo[c0 + e]}, ff{(x.hi * sa) * sb, (x.lo * sa) * sb});
+            hi[c0 + e]     = a.hi;
+            lo[c0 + e]     = a.lo;
+            if(P.tail) {
+              const float tl = (__uint_as_float(rv[S - 1][e]) * sa) * sb;
+              tsq            = fmaf(tl, tl, tsq);
             }
           }
         }
@@ -337,27 +363,17 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
       }
       if(aborted) break;
       if(vrow) {
-        const long long v2 = (long long) v * v, m = (long long) w.x * v + y;
-        float2*         Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v;
-        const long long csm = P.phase == 0 ? v : 1, csn = P.phase == 0 ? 1 : v2;
 #pragma unroll
         for(int e = 0; e < C::HALF; e++) {
           const int n = n0 + e;
-          if(n >= v) continue;
-          float2* cp = Cb + m * csm + (long long) n * csn;
-          ff      rr{hi[e], lo[e]};
-          if(P.phase == 1) {
-            const float2 old = *cp;
-            rr = ff_add(rr, ff{old.x, old.y});
-          }
-          *cp = make_float2(rr.hi, rr.lo);
+          if(n < v) Cb[(long long) n * v2] = make_float2(hi[e], lo[e]);
         }
       }
     }
     if(P.tail && tail_slot >= 0) {
 #pragma unroll
-      for(int off = 16; off > 0; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
-      if(lane == 0 && tmax > 0.f) atomicMax(reinterpret_cast<int*>(P.tail + tail_slot), __float_as_int(tmax));
+      for(int off = 16; off > 0; off >>= 1) tsq += __shfl_xor_sync(0xffffffffu, tsq, off);
+      if(lane == 0 && tsq > 0.f) atomicAdd(P.tail + tail_slot, tsq);
     }
   }
   sm100::tc_fence_before();

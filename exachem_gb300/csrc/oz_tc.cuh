@@ -51,7 +51,7 @@ struct TcBatch {
   int         v;        // pair rows per x and single rows
   int         xblocks;  // x values (= v)
   int*        err;      // device error flag (set on a wait timeout)
-  float*      tail;     // optional: max |contribution of the last kept level| (a-posteriori estimate)
+  float*      tail;     // optional: += sum of squares of the last kept level's terms (a-posteriori estimate)
 };
 
 template<int S, int NT, int STAGES>
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
     const bool vrow = y < v;
     const long long m = (long long) x * v + y;
     const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-    float          tmax      = 0.f; // largest |last-level term| seen by this thread
+    float          tsq       = 0.f; // sum of squares of this thread's last-level terms
     for(int t = 0; t < J.nterms; t++) {
       const TcTerm& T = J.t[t];
       // warp-uniform decision: the tcgen05.ld / st below are .sync.aligned
@@ -217,19 +217,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
             lo[e] = __uint_as_float(rl[e]);
           }
         }
-#pragma unroll 1
-        for(int l = 0; l < S; l++) {
-          uint32_t rv[16];
-          sm100::tmem_ld16(lane_base + l * NT + c0, rv);
-          sm100::tmem_wait_ld();
+        // S exact levels -> float-float (oz_horner), scaled by 2^(e_row + e_col - 7 (S + 1))
+        uint32_t rv[S][16];
 #pragma unroll
-          for(int e = 0; e < 16; e++) {
-            const float sc   = ldexpf(T.sign, ea + eb[e] - OZ_BITS * (l + 2));
-            const float term = __uint_as_float(rv[e]) * sc;
-            ff a = ff_add_f(ff{hi[e], lo[e]}, term);
-            hi[e] = a.hi;
-            lo[e] = a.lo;
-            if(l == S - 1 && vrow) tmax = fmaxf(tmax, fabsf(term));
+        for(int l = 0; l < S; l++) sm100::tmem_ld16(lane_base + l * NT + c0, rv[l]);
+        sm100::tmem_wait_ld();
+        const float sa = ldexpf(T.sign, ea - OZ_BITS * (S + 1));
+#pragma unroll
+        for(int e = 0; e < 16; e++) {
+          const float sb = ldexpf(1.f, eb[e]);
+          const ff    xx = oz_horner<S>(rv, e);
+          const ff    a  = ff_add(ff{hi[e], lo[e]}, ff{(xx.hi * sa) * sb, (xx.lo * sa) * sb});
+          hi[e]          = a.hi;
+          lo[e]          = a.lo;
+          if(P.tail) {
+            const float tl = (__uint_as_float(rv[S - 1][e]) * sa) * sb;
+            tsq            = fmaf(tl, tl, tsq);
           }
         }
         if(!last) {
@@ -262,8 +265,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
     }
     if(P.tail) {
 #pragma unroll
-      for(int off = 16; off > 0; off >>= 1) tmax = fmaxf(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
-      if(lane == 0 && tmax > 0.f) atomicMax(reinterpret_cast<int*>(P.tail), __float_as_int(tmax));
+      for(int off = 16; off > 0; off >>= 1) tsq += __shfl_xor_sync(0xffffffffu, tsq, off);
+      if(lane == 0 && tsq > 0.f) atomicAdd(P.tail, tsq);
     }
   }
   sm100::tc_fence_before();

@@ -43,7 +43,17 @@ __device__ __forceinline__ ff ff_add_f(ff a, float b) {
   float hi = s.hi + lo;
   return ff{hi, lo - (hi - s.hi)};
 }
-__device__ __forceinline__ ff ff_scale(ff a, float s) { return ff{a.hi * s, a.lo * s}; } // s = small integer or 2^k
+// a * s, exact only for s = +-2^k (both words scale without rounding)
+__device__ __forceinline__ ff ff_scale(ff a, float s) { return ff{a.hi * s, a.lo * s}; }
+// a * s for any float s: error-free product of the high word (fma), so the result keeps
+// float-float precision (for s = 3, say, a.hi * s alone would round at 2^-25)
+__device__ __forceinline__ ff ff_mul_f(ff a, float s) {
+  const float p = a.hi * s, e = fmaf(a.hi, s, -p);
+  const float lo = fmaf(a.lo, s, e);
+  const float hi = p + lo;
+  return ff{hi, lo - (hi - p)};
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   float p = a.hi * b.hi;
   float e = fmaf(a.hi, b.hi, -p);
@@ -62,6 +72,24 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
 __device__ __forceinline__ ff ff_from_double(double x) {
   float hi = (float) x;
   return ff{hi, (float) (x - (double) hi)};
+}
+
+// Horner fold of S exact level sums (integers held in FP32, most significant first) into
+// float-float: returns X = sum_l L[l] 2^{7 (S - 1 - l)}.  Each step multiplies by 2^7 (exact)
+// and adds the next level with an error-free two-sum, so the only rounding is in the low word
+// (relative 2^-48); X < 2^{24 + 7 (S - 1)} stays far inside the FP32 range.
+template<int S>
+__device__ __forceinline__ ff oz_horner(const uint32_t (&L)[S][16], int e) {
+  float hi = __uint_as_float(L[0][e]), lo = 0.f;
+#pragma unroll
+  for(int l = 1; l < S; l++) {
+    const float a = hi * 128.f, b = __uint_as_float(L[l][e]);
+    const float s = a + b, z = s - a;
+    lo = fmaf(lo, 128.f, (a - (s - z)) + (b - z));
+    hi = s;
+  }
+  const float h = hi + lo;
+  return ff{h, lo - (h - hi)};
 }
 
 // ---------------------------------------------------------------------------------- slicing

@@ -139,6 +139,20 @@ ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
   return CCSDT_OK;
 }
 
+// One full wave of the tiled energy kernels (resident CTAs per SM x SMs), capped at
+// kTiledBlocks: a grid-stride loop over more CTAs than fit at once would leave a partial wave.
+int ccsdt_handle::energy_grid() {
+  if(energy_grid_ > 0) return energy_grid_;
+  int sm = 0, per = 0, per1 = 0;
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tiled_batch_kernel, ET_THREADS, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, energy_tiled_kernel, ET_THREADS, 0);
+  per          = std::min(per, per1);
+  energy_grid_ = std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
+  cudaGetLastError();
+  return energy_grid_;
+}
+
 // Launch the sequence of one batch of `nslots` triplets starting at the device base counter.
 ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails,
                                         double* sens) {
@@ -148,7 +162,8 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   int sm = 0;
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
   PzParams p;
-  std::memcpy(p.maps, tmaps, sizeof(tmaps));
+  static_assert(sizeof(p.maps) == sizeof(tmaps), "the persistent kernel takes every map");
+  std::memcpy(p.maps, tmaps, sizeof(p.maps));
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F, p.ex_t2 = ex_t2, p.ex_t2h = ex_t2h, p.ex_ovvv = ex_ovvv, p.ex_ooovh = ex_ooovh;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
@@ -159,40 +174,41 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   const bool partial = nslots != bt_B;
   cudaError_t e = cudaSuccess;
   if(partial) p.order = bt_order_partial;
-  cudaEvent_t tv[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t tv[3] = {nullptr, nullptr, nullptr};
   if(phase_timing && !capturing && !profiling) {
-    while(tev.size() < tev_used + 4) {
+    while(tev.size() < tev_used + 3) {
       cudaEvent_t ev = nullptr;
       if(cudaEventCreate(&ev) != cudaSuccess) return fail(CCSDT_E_CUDA, "phase-timing event");
       tev.push_back(ev);
     }
-    for(int q = 0; q < 4; q++) tv[q] = tev[tev_used + q];
-    tev_used += 4;
+    for(int q = 0; q < 3; q++) tv[q] = tev[tev_used + q];
+    tev_used += 3;
     tev_slots.push_back(nslots);
   }
-  for(int phase = 0; phase < 2 && e == cudaSuccess; phase++) {
-    p.phase = phase;
-    p.queue = reinterpret_cast<unsigned*>(bt_ctrl + phase);
-    if(tv[phase]) cudaEventRecord(tv[phase], stream);
-    e       = cudaMemsetAsync(p.queue, 0, sizeof(unsigned), stream);
-    if(profiling) cudaEventRecord(prof_ev[phase], stream);
-    if(e == cudaSuccess) e = launch_pz_any(S, p, sm, stream);
-    launches++;
+  // one launch: every tile of the three partial arrays with its l-sum and d-sum terms
+  p.queue = reinterpret_cast<unsigned*>(bt_ctrl);
+  if(tv[0]) cudaEventRecord(tv[0], stream);
+  e = cudaMemsetAsync(p.queue, 0, sizeof(unsigned), stream);
+  if(profiling) {
+    cudaEventRecord(prof_ev[0], stream);
+    cudaEventRecord(prof_ev[1], stream); // no separate l-sum phase
   }
+  if(e == cudaSuccess) e = launch_pz_any(S, p, sm, stream);
+  launches++;
   if(profiling) cudaEventRecord(prof_ev[2], stream);
-  if(tv[2]) cudaEventRecord(tv[2], stream);
+  if(tv[1]) cudaEventRecord(tv[1], stream);
   if(e == cudaSuccess) {
     BatchEnergyArgs ea;
     ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
                                    o, v, 0, 0, 0, nullptr};
     ea.tri = bt_tri, ea.base = bt_ctrl + 2, ea.F = bt_F, ea.part = bt_part;
-    const int G = std::min(e_ntiles, kTiledBlocks);
+    const int G = std::min(e_ntiles, energy_grid());
     energy_tiled_batch_kernel<<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
     if(profiling) cudaEventRecord(prof_ev[3], stream);
     reduce_parts_batch_kernel<<<nslots, 256, 0, stream>>>(bt_part, G, bt_tri, bt_ctrl + 2, etrip, sens);
     if(advance) advance_base_kernel<<<1, 32, 0, stream>>>(bt_ctrl + 2, nslots);
     if(profiling) cudaEventRecord(prof_ev[4], stream);
-    if(tv[3]) cudaEventRecord(tv[3], stream);
+    if(tv[2]) cudaEventRecord(tv[2], stream);
     launches += 2 + (advance ? 1 : 0);
     e = cudaGetLastError();
   }
@@ -280,7 +296,7 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
           cudaGraphDestroy(g);
           return fail(CCSDT_E_CUDA, "graph launch");
         }
-      launches += (full - 1) * 5;
+      launches += (full - 1) * 4; // contraction, energy, reduction, base advance per replay
       graph_replays += full;
       cudaGraphExecDestroy(ge);
       cudaGraphDestroy(g);
@@ -300,9 +316,9 @@ ccsdt_status ccsdt_handle::collect_phase_times() {
   if(tev_used == 0) return CCSDT_OK;
   if(cudaStreamSynchronize(stream) != cudaSuccess) return fail(CCSDT_E_CUDA, "phase-timing sync");
   for(size_t b = 0; b < tev_slots.size(); b++)
-    for(int q = 0; q < 3; q++) {
+    for(int q = 0; q < 2; q++) {
       float ms = 0;
-      if(cudaEventElapsedTime(&ms, tev[4 * b + q], tev[4 * b + q + 1]) != cudaSuccess)
+      if(cudaEventElapsedTime(&ms, tev[3 * b + q], tev[3 * b + q + 1]) != cudaSuccess)
         return fail(CCSDT_E_CUDA, "phase-timing elapsed time");
       phase_ms[q] += ms;
     }

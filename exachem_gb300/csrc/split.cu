@@ -241,8 +241,7 @@ __global__ void __launch_bounds__(E_THREADS) energy_split_kernel(const __grid_co
     const ff wabc = W(a, b, c), wbca = W(b, c, a), wcab = W(c, a, b);
     const ff wacb = W(a, c, b), wbac = W(b, a, c), wcba = W(c, b, a);
     const ff z    = ff_add(ff_add(ff_scale(wabc, 4.f), wbca), wcab);
-    const ff y4   = ff_add(ff_add(ff_scale(wabc, 3.f), ff_scale(wacb, -1.f)),
-                           ff_add(ff_scale(wbac, -1.f), ff_scale(wcba, -1.f)));
+    const ff y4   = ff_add(ff_mul_f(wabc, 3.f), ff_neg(ff_add(ff_add(wacb, wbac), wcba)));
     const float sgl = 3.f * SG(a, b, c) - SG(a, c, b) - SG(b, a, c) - SG(c, b, a);
     const ff    y5  = ff_add_f(y4, sgl);
     const ff    d   = ff_add(ff_add(ff_add(eijk, ff_from_double(-A.ev[a])), ff_from_double(-A.ev[b])),
@@ -385,7 +384,12 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
 
 namespace {
 
-enum { MAP_OVVV_NAT = 0, MAP_OVVV_SWP = 1, MAP_T2 = 2, MAP_T2H_NAT = 3, MAP_T2H_SWP = 4, MAP_OOOVH = 5 };
+enum {
+  MAP_OVVV_NAT = 0, MAP_OVVV_SWP = 1, MAP_T2 = 2, MAP_T2H_NAT = 3, MAP_T2H_SWP = 4, MAP_OOOVH = 5,
+  // the persistent kernel's l-sum runs with the single index on the tile rows: ooovh as the
+  // 128-row A operand, t2h pair rows as the NT-row B operand
+  MAP_T2H_NAT_B = 6, MAP_T2H_SWP_B = 7, MAP_OOOVH_A = 8
+};
 
 // tcgen05 configurations: digit planes S -> columns per level NT (S NT <= 256, (S + 2) NT <= 512)
 template<int S>
@@ -473,6 +477,9 @@ ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT) {
   // B side (single rows, NT-row boxes): t2 rows (xx, yy, a); ooovh rows (yy, zz, c)
   ok &= encode_map(&tmaps[MAP_T2], sl_t2, (int) Kv, v, o, o, P, Kv, v * Kv, o * v * Kv, pl_t2, NT, (int) S_);
   ok &= encode_map(&tmaps[MAP_OOOVH], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, NT, (int) S_);
+  ok &= encode_map(&tmaps[MAP_T2H_NAT_B], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, NT, (int) S_);
+  ok &= encode_map(&tmaps[MAP_T2H_SWP_B], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, NT, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OOOVH_A], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, (int) S_);
   if(!ok) return fail(CCSDT_E_CUDA, "cuTensorMapEncodeTiled failed for the digit planes");
   tmaps_ready = true;
   tmaps_S     = S;
@@ -525,7 +532,7 @@ ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eo
                   z * v2, ex_t2 + ((long long) xx * o + yy) * v, kp_v, 1.f};
   };
   TcBatch b;
-  std::memcpy(b.maps, tmaps, sizeof(tmaps));
+  std::memcpy(b.maps, tmaps, sizeof(b.maps)); // the first six maps
   b.v       = (int) v;
   b.xblocks = (int) v;
   b.err     = d_err;
@@ -611,7 +618,8 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 }
 
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
-  last_batched = false;
+  last_batched   = false;
+  last_err_bound = 0.0; // only the LEARNED mode estimates its error
   if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
   const int S       = opts->slices;
   const int variant = opts->slice_kind;
@@ -655,7 +663,7 @@ ccsdt_status ccsdt_handle::check_device_error() {
 }
 
 ccsdt_status ccsdt_handle::launch_energy_tiled(int i, int j, int k, double* eout) {
-  const int       G = e_ntiles < kTiledBlocks ? e_ntiles : kTiledBlocks;
+  const int       G = std::min(e_ntiles, energy_grid());
   TiledEnergyArgs ea{F12, F34, F56, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles, o, v, i, j, k, e_part};
   energy_tiled_kernel<<<G, ET_THREADS, 0, stream>>>(ea);
   if(profiling) cudaEventRecord(prof_ev[3], stream);

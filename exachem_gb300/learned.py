@@ -1,13 +1,17 @@
 """Training data, training and use of the per-triplet slice-count model.
 
-Labels: for an occupied triplet, the smallest digit-plane count S in 2..smax whose
-triplet energy E_t(S) satisfies |E_t(S) - E_t(FP64)| <= budget * |E_t(FP64)|, measured
-against the library's own FP64 path (the plain kernel judges the error).  Features come
-from the library (ccsdt_triplet_features, 12 per triplet).  Training runs on the GPU
-through ccsdt_mlp_train (hand-written FP32 forward / backward / Adam kernels).
+Labels: for an occupied triplet, the smallest digit-plane count S in 2..smax whose triplet
+energy E_t(S) satisfies |E_t(S) - E_t(FP64)| <= budget * mean_t |E_t(FP64)| * sqrt(N) / 3,
+measured against the library's own FP64 path (the plain kernel judges the error); N is the
+system's number of occupied triplets and the mean is over its sampled triplets.  That is the
+equal share of the LEARNED mode's acceptance test 3 sqrt(sum_t sigma_t^2) <= budget sum_t |E_t|
+(independent per-triplet errors add like a random walk).  Features come from the library
+(ccsdt_triplet_features, 12 per triplet).  Training runs on the GPU through ccsdt_mlp_train
+(hand-written FP32 forward / backward / Adam kernels).
 
-The budget is relative: with the synthetic generator triplet energies range over many
-decades (1e-6 .. 1e7 Eh), so a fixed absolute budget would be either unreachable or void.
+The allowance scales with the system's own energies: with the synthetic generator triplet
+energies range over many decades (1e-6 .. 1e7 Eh), so a fixed absolute budget would be either
+unreachable or void.
 """
 from __future__ import annotations
 
@@ -34,7 +38,7 @@ def _lib():
     lib.ccsdt_triplet_features.argtypes = [ctypes.c_void_p, ctypes.c_long, _I, _F]
     lib.ccsdt_set_slice_model.argtypes = [ctypes.c_void_p, _F]
     lib.ccsdt_learned_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
-                                        ctypes.POINTER(ctypes.c_long)]
+                                        ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_double)]
     for n in ("ccsdt_mlp_grad", "ccsdt_mlp_train", "ccsdt_mlp_predict", "ccsdt_triplet_features",
               "ccsdt_set_slice_model", "ccsdt_learned_stats"):
         getattr(lib, n).restype = ctypes.c_int
@@ -89,21 +93,30 @@ def set_model(ft: "ct.FusedTriples", params):
     ft._check(_lib().ccsdt_set_slice_model(ft.h, p.ctypes.data_as(_F)))
 
 
-def learned_stats(ft: "ct.FusedTriples"):
-    m, f = ctypes.c_double(), ctypes.c_long()
-    _lib().ccsdt_learned_stats(ft.h, ctypes.byref(m), ctypes.byref(f))
-    return m.value, f.value
+def learned_stats(ft: "ct.FusedTriples", with_products=False):
+    """(mean predicted slice count, escalations[, digit-plane products run]) of the last call."""
+    m, f, p = ctypes.c_double(), ctypes.c_long(), ctypes.c_double()
+    _lib().ccsdt_learned_stats(ft.h, ctypes.byref(m), ctypes.byref(f), ctypes.byref(p))
+    return (m.value, f.value, p.value) if with_products else (m.value, f.value)
+
+
+def share(ft, ref, budget):
+    """Equal per-triplet share of the acceptance test: budget * mean|E_t| * sqrt(N) / 3."""
+    n_all = ft.o * (ft.o + 1) * (ft.o + 2) // 6
+    return budget * max(float(np.mean(np.abs(ref))), 1e-300) * np.sqrt(n_all) / 3.0
 
 
 def label_triplets(ft, tri, budget=1e-8, smax=7):
-    """Minimal S in 2..smax meeting the relative budget per triplet (smax if none does)."""
+    """Minimal S in 2..smax with |E_t(S) - E_t(fp64)| <= the equal share (smax if none).
+    Returns the labels, the errors [S-2][t] in units of that share, and the FP64 energies."""
     _, ref = ft.triplet_energies(tri, "fp64")
+    allow = share(ft, ref, budget)
     errs = []
     for S in range(2, smax + 1):
         _, e = ft.triplet_energies(tri, "ozaki", slices=S)
-        errs.append(np.abs(e - ref) / np.maximum(np.abs(ref), 1e-300))
+        errs.append(np.abs(e - ref) / allow)
     errs = np.array(errs)                                   # [S-2][t]
-    ok = errs <= budget
+    ok = errs <= 1.0
     lab = np.where(ok.any(0), ok.argmax(0) + 2, smax)
     return lab, errs, ref
 

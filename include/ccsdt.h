@@ -71,14 +71,15 @@ typedef struct {
   int    use_graph;     /* capture the per-call launch sequence in a CUDA graph               */
   int    shard_index;   /* process triplets t with t % shard_count == shard_index; the        */
   int    shard_count;   /* caller sums the partial energies (0 or 1 = every triplet)          */
-  double energy_budget; /* LEARNED: per-triplet |dE| budget relative to |E_triplet|           */
+  double energy_budget; /* LEARNED: accept when 3 sqrt(sum_t sigma_t^2) <= budget x          */
+                        /* sum_t |E(T)_t| (sigma_t: estimated error of triplet t; default 1e-8) */
   int    reserved[6];
 } ccsdt_opts;
 
 typedef struct {
   double e_bracket_T;      /* E[T]                                                            */
   double e_paren_T;        /* E(T)                                                            */
-  double abs_err_bound;    /* a-posteriori bound on |E(T) - E(T)_fp64| (0 in FP64 mode)        */
+  double abs_err_bound;    /* LEARNED: 3-sigma a-posteriori estimate of |E(T) - E(T)_fp64|     */
   double seconds;          /* device time of the call                                         */
   double flops_executed;   /* 2 x multiply-adds of the contractions (FP64-equivalent)         */
   double flops_ref_equiv;  /* the reference's own spin-orbital op count for this layout       */
@@ -121,11 +122,12 @@ ccsdt_status ccsdt_triplet_energies(ccsdt_handle* h, const ccsdt_opts* opts, lon
 ccsdt_status ccsdt_set_stream(ccsdt_handle* h, void* stream);
 
 /* Live per-phase device timing of the batched split-precision path (the persistent tcgen05
- * kernels).  on != 0 starts the accumulation (and zeroes it): CUDA events on the handle's
- * stream around the l-sum contraction, the d-sum contraction and the energy of every batch,
- * read when the call returns.  ccsdt_phase_times gives the accumulated milliseconds ms3[3]
- * and the numbers of batches and triplets they cover.  Batches replayed from a CUDA graph
- * are not timed.  No counterpart in the reference (its timers are host-side, ccsd_t.cpp). */
+ * kernel).  on != 0 starts the accumulation (and zeroes it): CUDA events on the handle's
+ * stream around the contraction launch (l-sum and d-sum terms) and around the energy launches
+ * of every batch, read when the call returns.  ccsdt_phase_times gives the accumulated
+ * milliseconds ms3 = {contraction, energy, 0} and the numbers of batches and triplets they
+ * cover.  Batches replayed from a CUDA graph are not timed.  No counterpart in the reference
+ * (its timers are host-side, ccsd_t.cpp). */
 ccsdt_status ccsdt_set_phase_timing(ccsdt_handle* h, int on);
 ccsdt_status ccsdt_phase_times(const ccsdt_handle* h, double* ms3, long* batches, long* triplets);
 
@@ -200,8 +202,19 @@ ccsdt_status ccsdt_triplet_features(ccsdt_handle* h, long n, const int* tri, flo
  * opts->energy_budget the relative per-triplet budget of the a-posteriori check. */
 ccsdt_status ccsdt_set_slice_model(ccsdt_handle* h, const float* params);
 
-/* Mean predicted slice count and number of full-slice fallbacks of the last LEARNED call. */
-ccsdt_status ccsdt_learned_stats(const ccsdt_handle* h, double* mean_slices, long* fallbacks);
+/* Per-triplet energies at opts->slices digit planes (CCSDT_MODE_OZAKI, BF16 digits, 1..5
+ * planes) together with the a-posteriori estimate est[t] of |E(T)_t - E(T)_t,fp64| that the
+ * LEARNED mode checks against its budget: the estimated standard deviation of the triplet's
+ * truncation error, from the last kept level's terms and the energy's sensitivity (a statistical
+ * estimate, not a rigorous bound).  e_bracket may be NULL. */
+ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccsdt_opts* opts, long n, const int* tri,
+                                           double* e_bracket, double* e_paren, double* est);
+
+/* Statistics of the last LEARNED call: mean predicted slice count, number of escalations (when
+ * the total misses the budget, the triplets with the largest estimates are rerun one count
+ * higher, up to opts->slices), and the digit-plane products actually run, sum over triplets of
+ * S (S + 1) / 2 per run (any may be NULL). */
+ccsdt_status ccsdt_learned_stats(const ccsdt_handle* h, double* mean_slices, long* fallbacks, double* products);
 
 void        ccsdt_destroy(ccsdt_handle* h);
 const char* ccsdt_last_error(const ccsdt_handle* h);

@@ -50,39 +50,46 @@ def test_mlp_training_reduces_loss_and_bf16_inference(built):
 
 
 def test_learned_mode_meets_budget_and_saves_products(built):
+    """LEARNED accepts when 3 sqrt(sum sigma_t^2) <= budget sum |E_t|: the measured error must
+    meet the budget, and the digit-plane products it runs (escalations included) must not exceed
+    those of the smallest fixed count that passes the same test."""
     from exachem_gb300 import ccsd_t as ct, learned
     from exachem_gb300.generator import generate
-    # train on three small systems, evaluate on a held-out one
+    budget = 1e-8
     systems = [(10, 60, 100, 1.0), (12, 70, 101, 2.0), (14, 64, 102, 0.7)]
-    X, y, _ = learned.build_training_set(systems, per_system=30, budget=1e-8, smax=6, log=lambda *a: None)
+    X, y, _ = learned.build_training_set(systems, per_system=30, budget=budget, smax=6, log=lambda *a: None)
     params, _ = learned.mlp_train(X, y, epochs=300, batch=32, lr=3e-3, seed=5)
     d = generate(11, 66, 103, t2_scale=1.5)
     ft = ct.FusedTriples(11, 66, ts=40)
     ft.upload_dict(d)
     ref = ft.energy("fp64")["e_paren_T"]
-    learned.set_model(ft, params)
-    r = ft.energy("learned", slices=6, energy_budget=1e-8)
-    mean_s, fallbacks = learned.learned_stats(ft)
-    assert abs(r["e_paren_T"] - ref) <= 2e-8 * abs(ref)
-    # the fixed count that meets the same per-triplet budget everywhere
     tri = ct.all_triplets(11)
     tri = tri[tri[:, 0] != tri[:, 2]]
-    lab, _, _ = learned.label_triplets(ft, tri, budget=1e-8, smax=6)
-    fixed = int(lab.max())
+    _, ref_t = ft.triplet_energies(tri, "fp64")
+    allow = budget * np.abs(ref_t).sum()
+    learned.set_model(ft, params)
+    r = ft.energy("learned", slices=5, energy_budget=budget)
+    mean_s, escalations, products = learned.learned_stats(ft, with_products=True)
+    assert abs(r["e_paren_T"] - ref) <= allow
+    assert r["abs_err_bound"] <= allow * (1 + 1e-12)
     cost = lambda S: S * (S + 1) / 2
-    pred = learned.mlp_predict(params, learned.features(ft, tri))
+    fixed = 5
+    for S in (2, 3, 4):
+        _, _, est = ft.triplet_error_estimates(tri, S)
+        if 3 * np.sqrt(np.sum(est ** 2)) <= allow:
+            fixed = S
+            break
     n = len(tri)
-    learned_cost = (sum(cost(min(max(s, 2), 6)) for s in pred) + fallbacks * cost(6)) / n
     print(f"fixed S={fixed} ({cost(fixed)} products) vs learned mean S={mean_s:.2f} "
-          f"({learned_cost:.2f} products incl. {fallbacks} full-slice fallbacks)")
-    assert learned_cost <= cost(fixed) + 1e-9
-    assert fallbacks <= 0.25 * n
+          f"({products / n:.2f} products incl. {escalations} escalations)")
+    assert products / n <= 1.05 * cost(fixed)
 
 
 def test_learned_mode_groups_equal_fixed_count_runs(built):
     """LEARNED runs each predicted count as one batched persistent pass with the results
     scattered back to each triplet's own index: every triplet must equal the same triplet
-    run alone at its predicted count (no fallbacks with a budget of 1)."""
+    run alone at its predicted count (no escalations with a budget of 1, i.e. an allowance of
+    the mean |E(T)_t| per triplet)."""
     from exachem_gb300 import ccsd_t as ct, learned
     from exachem_gb300.generator import generate
     o, v = 9, 48
@@ -103,3 +110,29 @@ def test_learned_mode_groups_equal_fixed_count_runs(built):
         f4, f5 = ft.triplet_energies(tri[sel], "ozaki", slices=S)
         np.testing.assert_allclose(e5[sel], f5, rtol=1e-13, atol=0)
         np.testing.assert_allclose(e4[sel], f4, rtol=1e-13, atol=0)
+
+
+def test_error_estimate_covers_measured_error(built):
+    """The per-triplet estimate sigma_t (ccsdt_triplet_error_estimates) is a standard deviation:
+    3 sigma must cover the error measured against the FP64 path for nearly every triplet, and
+    sigma must not be uselessly pessimistic."""
+    from exachem_gb300 import ccsd_t as ct
+    from exachem_gb300.generator import generate
+    ratios = []
+    for (o, v, seed, sc) in [(10, 64, 301, 1.0), (12, 90, 302, 2.5), (9, 120, 303, 0.6)]:
+        ft = ct.FusedTriples(o, v, ts=32)
+        ft.upload_dict(generate(o, v, seed, t2_scale=sc))
+        tri = ct.all_triplets(o)
+        tri = tri[tri[:, 0] != tri[:, 2]]
+        _, ref = ft.triplet_energies(tri, "fp64")
+        for S in (2, 3, 4):
+            _, e5, est = ft.triplet_error_estimates(tri, S)
+            err = np.abs(e5 - ref)
+            keep = err > 1e-13 * np.abs(ref)          # below that the float-float floor dominates
+            ratios.append(est[keep] / err[keep])
+        ft.close()
+    r = np.concatenate(ratios)
+    q = np.quantile(r, [0.01, 0.05, 0.5])
+    print(f"sigma / measured error: 1% {q[0]:.2f}, 5% {q[1]:.2f}, median {q[2]:.2f} over {len(r)} cases")
+    assert (3 * r >= 1).mean() >= 0.98
+    assert q[2] <= 10
