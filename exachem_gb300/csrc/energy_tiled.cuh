@@ -29,7 +29,23 @@ struct TiledEnergyArgs {
   double*       part;      // 6 doubles per CTA: E[T] (s, c), E(T) (s, c), sum (18 Y^2 + 12 Z^2) / D^2, 0
 };
 
-// slot s <-> permutation (p0, p1, p2) of the block positions
+// slot s <-> permutation (p0, p1, p2) of the block positions; for the ordering xyz of slot s,
+// the slots of the orderings yzx, zxy (cyclic) and xzy, yxz, zyx (one transposition)
+// (constexpr functions, folded at compile time inside the unrolled loops)
+__host__ __device__ constexpr int kPerm(int s, int pos) {
+  return pos == 0 ? s >> 1 : pos == 1 ? (s == 0 || s == 5 ? 1 : s == 1 || s == 3 ? 2 : 0) : (s == 1 || s == 4 ? 1 : s == 0 || s == 2 ? 2 : 0);
+}
+__host__ __device__ constexpr int kSlot(int p0, int p1, int p2) { return p0 * 2 + (p1 > p2 ? 1 : 0); }
+__host__ __device__ constexpr int kCyc1(int s) { return kSlot(kPerm(s, 1), kPerm(s, 2), kPerm(s, 0)); }
+__host__ __device__ constexpr int kCyc2(int s) { return kSlot(kPerm(s, 2), kPerm(s, 0), kPerm(s, 1)); }
+__host__ __device__ constexpr int kXzy(int s) { return kSlot(kPerm(s, 0), kPerm(s, 2), kPerm(s, 1)); }
+__host__ __device__ constexpr int kYxz(int s) { return kSlot(kPerm(s, 1), kPerm(s, 0), kPerm(s, 2)); }
+__host__ __device__ constexpr int kZyx(int s) { return kSlot(kPerm(s, 2), kPerm(s, 1), kPerm(s, 0)); }
+static_assert(kCyc1(0) == 3 && kCyc1(1) == 5 && kCyc1(2) == 1 && kCyc1(3) == 4 && kCyc1(4) == 0 && kCyc1(5) == 2, "");
+static_assert(kCyc2(0) == 4 && kCyc2(1) == 2 && kCyc2(2) == 5 && kCyc2(3) == 0 && kCyc2(4) == 3 && kCyc2(5) == 1, "");
+static_assert(kXzy(0) == 1 && kXzy(1) == 0 && kXzy(2) == 3 && kXzy(3) == 2 && kXzy(4) == 5 && kXzy(5) == 4, "");
+static_assert(kYxz(0) == 2 && kYxz(1) == 4 && kYxz(2) == 0 && kYxz(3) == 5 && kYxz(4) == 1 && kYxz(5) == 3, "");
+static_assert(kZyx(0) == 5 && kZyx(1) == 3 && kZyx(2) == 4 && kZyx(3) == 1 && kZyx(4) == 2 && kZyx(5) == 0, "");
 static __device__ __constant__ int c_perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 
 __device__ __forceinline__ int perm_slot(int p0, int p1, int p2) {
@@ -101,11 +117,19 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       const ff     d  = ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y});
       dab[u][w][x * B + y] = make_float2(d.hi, d.lo);
     }
-    // W of the six slots: three passes, each reading one array along its contiguous index
+    // W of the six slots: three passes, each reading one array along its contiguous index.
+    // A thread issues all of its loads of a pass before touching shared memory (12 in flight).
+    constexpr int kPerThread = 6 * B3 / ET_THREADS;
+    static_assert(kPerThread * ET_THREADS == 6 * B3, "the six cubes split evenly over the block");
+    float2* Wf = &W[0][0];
 #pragma unroll 1
     for(int pass = 0; pass < 3; pass++) {
       __syncthreads();
-      for(int e = tid; e < 6 * B3; e += ET_THREADS) {
+      float2 x[kPerThread];
+      int    widx[kPerThread];
+#pragma unroll
+      for(int it = 0; it < kPerThread; it++) {
+        const int  e = tid + it * ET_THREADS;
         const int  s = e / B3, r = e % B3;
         const int  f = r % B, m = (r / B) % B, sl = r / (B * B); // fastest, middle, slowest local index
         const int* P = c_perm[s];
@@ -127,50 +151,61 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
           off = ((long long) (blk0[P[2]] + lc) * v + blk0[P[1]] + lb) * v + blk0[P[0]] + la;
         }
         const bool ok = la < blkn[P[0]] && lb < blkn[P[1]] && lc < blkn[P[2]];
-        const float2 x = ok ? src[off] : make_float2(0.f, 0.f);
-        const int    w = (la * B + lb) * B + lc;
-        if(pass == 0) W[s][w] = x;
+        x[it]         = ok ? src[off] : make_float2(0.f, 0.f);
+        widx[it]      = s * B3 + (la * B + lb) * B + lc;
+      }
+#pragma unroll
+      for(int it = 0; it < kPerThread; it++) {
+        if(pass == 0) Wf[widx[it]] = x[it];
         else {
-          const ff r = ff_add(ff{W[s][w].x, W[s][w].y}, ff{x.x, x.y});
-          W[s][w]    = make_float2(r.hi, r.lo);
+          const float2 o = Wf[widx[it]];
+          const ff     r = ff_add(ff{o.x, o.y}, ff{x[it].x, x[it].y});
+          Wf[widx[it]]   = make_float2(r.hi, r.lo);
         }
       }
     }
     __syncthreads();
-    // energies of the distinct ordered cubes
-    for(int e = tid; e < 6 * B3; e += ET_THREADS) {
-      const int s = e / B3, r = e % B3;
-      if(!slot_on[s]) continue;
-      const int* P = c_perm[s];
-      const int  p0 = P[0], p1 = P[1], p2 = P[2];
-      const int  a = r / (B * B), b = (r / B) % B, c = r % B;
-      if(a >= blkn[p0] || b >= blkn[p1] || c >= blkn[p2]) continue;
-      auto Wat = [&](int q0, int q1, int q2, int x, int y, int z) {
-        const float2 t = W[perm_slot(q0, q1, q2)][(x * B + y) * B + z];
-        return ff{t.x, t.y};
-      };
-      const ff wabc = Wat(p0, p1, p2, a, b, c), wbca = Wat(p1, p2, p0, b, c, a), wcab = Wat(p2, p0, p1, c, a, b);
-      const ff wacb = Wat(p0, p2, p1, a, c, b), wbac = Wat(p1, p0, p2, b, a, c), wcba = Wat(p2, p1, p0, c, b, a);
-      // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z, x in block qx ...
-      auto SG = [&](int qx, int qy, int qz, int x, int y, int z) {
-        return Ojk[qy][qz][y * B + z] * ti[qx][x] + Oik[qx][qz][x * B + z] * tj[qy][y] + Oij[qx][qy][x * B + y] * tk[qz][z];
-      };
-      const float sgl = 3.f * SG(p0, p1, p2, a, b, c) - SG(p0, p2, p1, a, c, b) - SG(p1, p0, p2, b, a, c) -
-                        SG(p2, p1, p0, c, b, a);
-      const ff z  = ff_add(ff_add(ff_scale(wabc, 4.f), wbca), wcab);
-      const ff y4 = ff_add(ff_mul_f(wabc, 3.f), ff_neg(ff_add(ff_add(wacb, wbac), wcba)));
-      const ff y5 = ff_add_f(y4, sgl);
-      const float2 dd = dab[p0][p1][a * B + b], ec = evs[p2][c];
-      const ff d  = ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y});
-      const ff id = ff_div(ff{1.f, 0.f}, d);              // 1 / D
-      const ff zi = ff_mul(z, id);                        // Z / D
-      s4 = ff_add(s4, ff_mul(zi, y4));
-      s5 = ff_add(s5, ff_mul(zi, y5));
-      // first-order sensitivity to errors in W: W_abc enters Z_abc (x4), Z_bca, Z_cab and, through
-      // V, Y_abc (x3), Y_acb, Y_bac, Y_cba; with uncorrelated signs
-      //   |dE/dW|^2 ~ (16 + 1 + 1) Y^2 / D^2 + (9 + 1 + 1 + 1) Z^2 / D^2
-      const float yr = y5.hi * id.hi, zr = zi.hi;
-      sens = fmaf(18.f * yr, yr, fmaf(12.f * zr, zr, sens));
+    // energies by orbit: a thread takes one index triple (a' in block 0, b' in block 1, c' in
+    // block 2 of the sorted triple) and all six of its orderings, which live in the six slots.
+    // The six W values are read once, D is common to the orbit, and an ordering counts only if
+    // its slot is a distinct ordered block triple (so every ordered (a, b, c) counts once).
+    for(int r = tid; r < B3; r += ET_THREADS) {
+      const int la = r / (B * B), lb = (r / B) % B, lc = r % B;
+      if(la >= blkn[0] || lb >= blkn[1] || lc >= blkn[2]) continue;
+      const int loc[3] = {la, lb, lc};
+      ff        w[6];
+      float     sg[6];
+#pragma unroll
+      for(int q = 0; q < 6; q++) {
+        const int    p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
+        const int    x = loc[p0], y = loc[p1], z = loc[p2];
+        const float2 t = W[q][(x * B + y) * B + z];
+        w[q]           = ff{t.x, t.y};
+        // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z
+        sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
+      }
+      ff    zy4{0.f, 0.f}, zy5{0.f, 0.f};
+      float sn = 0.f;
+#pragma unroll
+      for(int q = 0; q < 6; q++) {
+        if(!slot_on[q]) continue;
+        // ordering xyz of slot q: Z = 4 W_xyz + W_yzx + W_zxy, Y = 3 V_xyz - V_xzy - V_yxz - V_zyx
+        const ff    z  = ff_add(ff_add(ff_scale(w[q], 4.f), w[kCyc1(q)]), w[kCyc2(q)]);
+        const ff    y4 = ff_add(ff_mul_f(w[q], 3.f), ff_neg(ff_add(ff_add(w[kXzy(q)], w[kYxz(q)]), w[kZyx(q)])));
+        const float ys = 3.f * sg[q] - sg[kXzy(q)] - sg[kYxz(q)] - sg[kZyx(q)];
+        const ff    y5 = ff_add_f(y4, ys);
+        zy4 = ff_add(zy4, ff_mul(z, y4));
+        zy5 = ff_add(zy5, ff_mul(z, y5));
+        // first-order sensitivity to errors in W: W_abc enters Z_abc (x4), Z_bca, Z_cab and,
+        // through V, Y_abc (x3), Y_acb, Y_bac, Y_cba; with uncorrelated signs
+        //   |dE/dW|^2 ~ (16 + 1 + 1) Y^2 / D^2 + (9 + 1 + 1 + 1) Z^2 / D^2
+        sn = fmaf(18.f * y5.hi, y5.hi, fmaf(12.f * z.hi, z.hi, sn));
+      }
+      const float2 dd = dab[0][1][la * B + lb], ec = evs[2][lc];
+      const ff     id = ff_div(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
+      s4   = ff_add(s4, ff_mul(zy4, id));
+      s5   = ff_add(s5, ff_mul(zy5, id));
+      sens = fmaf(sn * id.hi, id.hi, sens);
     }
   }
   CSum c4, c5;
@@ -193,7 +228,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   }
 }
 
-static __global__ void __launch_bounds__(ET_THREADS) energy_tiled_kernel(const __grid_constant__ TiledEnergyArgs A) {
+static __global__ void __launch_bounds__(ET_THREADS, 4) energy_tiled_kernel(const __grid_constant__ TiledEnergyArgs A) {
   energy_tiled_body(A, A.P12, A.P34, A.P56, A.i, A.j, A.k, A.part + 6 * (long long) blockIdx.x, blockIdx.x, gridDim.x);
 }
 
@@ -207,7 +242,7 @@ struct BatchEnergyArgs {
   double*         part;      // [slot][gridDim.x][6]
 };
 
-static __global__ void __launch_bounds__(ET_THREADS) energy_tiled_batch_kernel(const __grid_constant__ BatchEnergyArgs A) {
+static __global__ void __launch_bounds__(ET_THREADS, 4) energy_tiled_batch_kernel(const __grid_constant__ BatchEnergyArgs A) {
   const int       slot = blockIdx.y, b0 = A.base ? *A.base : 0;
   const int*      tp   = A.tri + 4 * (b0 + slot);
   const long long v3   = (long long) A.base_args.v * A.base_args.v * A.base_args.v;
