@@ -36,6 +36,13 @@ __host__ __device__ constexpr int kPerm(int s, int pos) {
   return pos == 0 ? s >> 1 : pos == 1 ? (s == 0 || s == 5 ? 1 : s == 1 || s == 3 ? 2 : 0) : (s == 1 || s == 4 ? 1 : s == 0 || s == 2 ? 2 : 0);
 }
 __host__ __device__ constexpr int kSlot(int p0, int p1, int p2) { return p0 * 2 + (p1 > p2 ? 1 : 0); }
+// Shared-memory position of orbit coordinates (la, lb, lc) in a W cube: an XOR swizzle (linear over
+// GF(2), a bijection on 0..511) under which every half-warp access the kernel makes - any two of
+// the three coordinates varying, one over 0..7 and one over an aligned pair - touches 16 distinct
+// bank pairs: bank bits = (lc ^ la ^ (lb & 6), (lb ^ la) & 1).
+__host__ __device__ constexpr int kSwz(int la, int lb, int lc) {
+  return (la << 6) | ((lb & 6) << 3) | (((lb ^ la) & 1) << 3) | ((lc ^ la ^ (lb & 6)) & 7);
+}
 __host__ __device__ constexpr int kCyc1(int s) { return kSlot(kPerm(s, 1), kPerm(s, 2), kPerm(s, 0)); }
 __host__ __device__ constexpr int kCyc2(int s) { return kSlot(kPerm(s, 2), kPerm(s, 0), kPerm(s, 1)); }
 __host__ __device__ constexpr int kXzy(int s) { return kSlot(kPerm(s, 0), kPerm(s, 2), kPerm(s, 1)); }
@@ -117,45 +124,47 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       const ff     d  = ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y});
       dab[u][w][x * B + y] = make_float2(d.hi, d.lo);
     }
-    // W of the six slots: three passes, each reading one array along its contiguous index.
-    // A thread issues all of its loads of a pass before touching shared memory (12 in flight).
-    constexpr int kPerThread = 6 * B3 / ET_THREADS;
-    static_assert(kPerThread * ET_THREADS == 6 * B3, "the six cubes split evenly over the block");
+    // W of the six slots, stored by orbit coordinates (loc[P[0]], loc[P[1]], loc[P[2]]) = the
+    // slot's local (a', b', c'): three passes, each reading one array along its contiguous index
+    // (a thread's 12 loads of a pass are issued before its shared-memory updates).  Thread tid
+    // handles local positions r = tid and tid + 256 of every slot: (slowest, middle, fastest)
+    // local index of the pass's array = (r / 64, r / 8 % 8, r % 8).
+    static_assert(6 * B3 == 12 * ET_THREADS, "two positions of each of the six cubes per thread");
     float2* Wf = &W[0][0];
-#pragma unroll 1
+#pragma unroll
     for(int pass = 0; pass < 3; pass++) {
       __syncthreads();
-      float2 x[kPerThread];
-      int    widx[kPerThread];
+      float2 x[12];
+      int    widx[12];
 #pragma unroll
-      for(int it = 0; it < kPerThread; it++) {
-        const int  e = tid + it * ET_THREADS;
-        const int  s = e / B3, r = e % B3;
-        const int  f = r % B, m = (r / B) % B, sl = r / (B * B); // fastest, middle, slowest local index
-        const int* P = c_perm[s];
-        int        la, lb, lc; // local (a', b', c') of this element within the slot
+      for(int it = 0; it < 12; it++) {
+        const int s = it >> 1, r = tid + (it & 1) * ET_THREADS;
+        const int P0 = kPerm(s, 0), P1 = kPerm(s, 1), P2 = kPerm(s, 2);
+        const int f = r & 7, m = (r >> 3) & 7, sl = r >> 6;
+        int       la, lb, lc; // slot-local (a', b', c'): a in block P0, b in P1, c in P2
         const float2* src;
         long long     off;
-        // slot blocks: a in block P[0], b in P[1], c in P[2]
         if(pass == 0) { // P12[a][c][b]: b fastest
           la = sl, lc = m, lb = f;
           src = P12;
-          off = ((long long) (blk0[P[0]] + la) * v + blk0[P[2]] + lc) * v + blk0[P[1]] + lb;
+          off = ((long long) (blk0[P0] + la) * v + blk0[P2] + lc) * v + blk0[P1] + lb;
         } else if(pass == 1) { // P34[b][a][c]: c fastest
           lb = sl, la = m, lc = f;
           src = P34;
-          off = ((long long) (blk0[P[1]] + lb) * v + blk0[P[0]] + la) * v + blk0[P[2]] + lc;
+          off = ((long long) (blk0[P1] + lb) * v + blk0[P0] + la) * v + blk0[P2] + lc;
         } else { // P56[c][b][a]: a fastest
           lc = sl, lb = m, la = f;
           src = P56;
-          off = ((long long) (blk0[P[2]] + lc) * v + blk0[P[1]] + lb) * v + blk0[P[0]] + la;
+          off = ((long long) (blk0[P2] + lc) * v + blk0[P1] + lb) * v + blk0[P0] + la;
         }
-        const bool ok = la < blkn[P[0]] && lb < blkn[P[1]] && lc < blkn[P[2]];
+        const bool ok = la < blkn[P0] && lb < blkn[P1] && lc < blkn[P2];
         x[it]         = ok ? src[off] : make_float2(0.f, 0.f);
-        widx[it]      = s * B3 + (la * B + lb) * B + lc;
+        int loc[3]    = {0, 0, 0};
+        loc[P0] = la, loc[P1] = lb, loc[P2] = lc;
+        widx[it] = s * B3 + kSwz(loc[0], loc[1], loc[2]);
       }
 #pragma unroll
-      for(int it = 0; it < kPerThread; it++) {
+      for(int it = 0; it < 12; it++) {
         if(pass == 0) Wf[widx[it]] = x[it];
         else {
           const float2 o = Wf[widx[it]];
@@ -179,7 +188,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       for(int q = 0; q < 6; q++) {
         const int    p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
         const int    x = loc[p0], y = loc[p1], z = loc[p2];
-        const float2 t = W[q][(x * B + y) * B + z];
+        const float2 t = W[q][kSwz(la, lb, lc)]; // = W at (x, y, z) of slot q
         w[q]           = ff{t.x, t.y};
         // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z
         sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
