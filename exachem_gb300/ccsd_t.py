@@ -161,7 +161,7 @@ class FusedTriples:
 
     @staticmethod
     def opts(mode="fp64", slices=4, slice_kind="bf16", energy_budget=1e-9, use_graph=0,
-             shard_index=0, shard_count=1, legacy_mma=0) -> Opts:
+             shard_index=0, shard_count=1, legacy_mma=0, single_cta=0) -> Opts:
         o = Opts()
         o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
         o.slices = slices
@@ -170,6 +170,7 @@ class FusedTriples:
         o.use_graph = use_graph
         o.shard_index, o.shard_count = shard_index, shard_count
         o.reserved[0] = legacy_mma   # 1: mma.sync slice kernel instead of tcgen05 (testing)
+        o.reserved[1] = single_cta   # 1: single-CTA persistent kernel, not the 2-CTA cluster one (testing)
         return o
 
     def energy(self, mode="fp64", **kw) -> dict:

@@ -41,7 +41,7 @@ struct ccsdt_handle {
   float *            oovv_f = nullptr, *t1_f = nullptr;
   float2 *           F12 = nullptr, *F34 = nullptr, *F56 = nullptr;
   // tcgen05 path: TMA maps over the digit planes (built once per slicing) and an error flag
-  CUtensorMap        tmaps[9];
+  CUtensorMap        tmaps[12];
   bool               tmaps_ready = false;
   int                tmaps_S     = 0, tmaps_NT = 0;
   int*               d_err       = nullptr;
@@ -96,6 +96,10 @@ struct ccsdt_handle {
   int*      bt_tri = nullptr;        // triplet table (i, j, k, output index)
   long      bt_tri_cap = 0;
   int       batch_slots = 4;         // triplets per batch
+  bool      pz_pair = false;         // this call runs the two-CTA cluster kernel
+  bool      force_single_cta = false; // test knob: the single-CTA persistent kernel instead
+  int       pz_pair_clusters = 0;    // co-resident clusters of the cluster kernel (this S)
+  int       pair_clusters_by_S[6] = {-1, -1, -1, -1, -1, -1};
   long      graph_replays = 0;
   ccsdt_status ensure_batch(int S, int B);
   ccsdt_status launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails, double* sens);

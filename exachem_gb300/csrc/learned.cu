@@ -230,7 +230,8 @@ extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccs
      cudaMemsetAsync(dsens, 0, sizeof(double) * n, h->stream) != cudaSuccess ||
      cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream) != cudaSuccess)
     return h->fail(CCSDT_E_CUDA, "estimate scratch init");
-  h->force_mma_sync = false;
+  h->force_mma_sync   = false;
+  h->force_single_cta = opts->reserved[1] == 1;
   if((s = h->run_batched(opts->slices, n, tri, false, dtail, dsens))) return s;
   std::vector<double> E(2 * n), sens(n);
   std::vector<float>  tail(n);

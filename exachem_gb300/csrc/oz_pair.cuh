@@ -1,0 +1,215 @@
+// Two-CTA cluster form of the persistent split-precision contraction.
+//
+// The two CTAs of a cluster work on the same A tile (same triplet slot, job, x, y-block and term)
+// and on adjacent N blocks (nb = 2 nbp + cluster rank), so the A tile - the large operand, re-read
+// by every N block - crosses L2 once for both: each CTA loads the digit planes of its parity
+// (p % 2 == rank) with a cluster multicast into both CTAs' shared memory, and its own B tile
+// without multicast.  This cuts the L2 -> SM bytes per digit-plane product by ~1.5x, the bound of
+// the single-CTA kernel once its epilogue keeps up.
+//
+// Scheduling is static: cluster c takes the pair items c, c + nclusters, ... of the host's
+// cost-ordered table, so both CTAs walk the same sequence without exchanging item ids.
+// Synchronisation across the pair:
+//   full[s]  (count 1, local): the local producer's arrive.expect_tx for the whole stage; the A
+//            planes arrive from both CTAs' multicasts, B from the local load;
+//   empty[s] (count 2): both CTAs' MMA issuers commit with a cluster multicast, so a producer that
+//            sees empty[s] knows stage s is free in both CTAs before it multicasts into it.
+// A cluster barrier follows the mbarrier initialisation (no remote arrival or multicast reaches
+// an uninitialised barrier) and precedes exit (after each producer has seen the last use of every
+// stage consumed by both MMAs, so nothing is still in flight towards this CTA's shared memory).
+// Every mbarrier wait is bounded (sm100::kSpinLimit); a CTA that gives up sets the error flag,
+// and its peer's waits then give up too, so both reach the final cluster barrier.
+#pragma once
+
+#include "oz_persist.cuh"
+
+namespace ccsdt {
+
+struct PzPairItem {
+  int slot, job, x, yb, nbp;
+};
+// pair item id -> fields; ids are dense in (slot, job, x, yb, nbp), nbp fastest
+__device__ __forceinline__ PzPairItem pz_decode_pair(unsigned id, int v, int yblocks, int npairs) {
+  PzPairItem it;
+  it.nbp = id % npairs;
+  id /= npairs;
+  it.yb = id % yblocks;
+  id /= yblocks;
+  it.x = id % v;
+  id /= v;
+  it.job  = id % 3;
+  it.slot = id / 3;
+  return it;
+}
+
+__device__ __forceinline__ int pz_plane_map(int mapA) {
+  return mapA == PZ_OVVV_NAT ? PZ_OVVV_NAT_P1 : mapA == PZ_OVVV_SWP ? PZ_OVVV_SWP_P1 : PZ_OOOVH_A_P1;
+}
+
+template<int S, int NT, int STAGES>
+__global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_constant__ PzParams P) {
+  using C = PzCfg<S, NT, STAGES>;
+  constexpr uint16_t kBoth = 0x3;
+  const int      v = P.v, yblocks = (v + PZ_BM - 1) / PZ_BM, nblocks = (v + NT - 1) / NT, npairs = (nblocks + 1) / 2;
+  const int      base = P.base ? *P.base : 0;
+  const int      rank = (int) sm100::cluster_ctarank();
+  const unsigned cid = sm100::cluster_id_x(), ncl = sm100::cluster_count_x();
+
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full      = reinterpret_cast<uint64_t*>(smem + STAGES * C::STAGE_BYTES);
+  uint64_t* empty     = full + STAGES;
+  uint64_t* lvl_full  = empty + STAGES; // [2] MMAs of a term done
+  uint64_t* lvl_empty = lvl_full + 2;   // [2] epilogue drained the buffer
+  uint64_t* drain     = lvl_empty + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if(threadIdx.x == 0) {
+    for(int s = 0; s < STAGES; s++) {
+      sm100::mbar_init(&full[s], 1);
+      sm100::mbar_init(&empty[s], 2); // one commit from each CTA's MMA issuer
+    }
+    for(int b = 0; b < 2; b++) {
+      sm100::mbar_init(&lvl_full[b], 1);
+      sm100::mbar_init(&lvl_empty[b], PZ_EPI);
+    }
+    sm100::mbar_init(drain, 1);
+    *abort_flag = 0;
+    sm100::mbar_fence_init();
+  }
+  if(warp == 1) {
+    sm100::tmem_alloc(tmem_slot, C::TMEM_COLS);
+    sm100::tmem_relinquish();
+  }
+  sm100::tc_fence_before();
+  __syncthreads();
+  sm100::cluster_sync(); // both CTAs' barriers are initialised before any multicast or remote arrival
+  sm100::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  auto fail = [&]() {
+    *abort_flag = 1;
+    if(P.err) atomicExch(P.err, 1);
+  };
+  // the k-th item of this cluster, or false past the end
+  auto item = [&](unsigned kk, PzItem& w) {
+    const unsigned q = cid + kk * ncl;
+    if(q >= P.nitems) return false;
+    const PzPairItem pi = pz_decode_pair(P.order[q], v, yblocks, npairs);
+    w = PzItem{pi.slot, pi.job, pi.x, pi.yb, 2 * pi.nbp + rank};
+    return true;
+  };
+
+  if(warp == 0) {
+    // ------------------------------------------------------------ TMA producer
+    if(lane == 0) {
+      for(int m: {PZ_OVVV_NAT_P1, PZ_OVVV_SWP_P1, PZ_T2, PZ_T2H_NAT_B, PZ_T2H_SWP_B, PZ_OOOVH_A_P1})
+        sm100::prefetch_tmap(&P.maps[m]);
+      int  stage_it = 0;
+      bool ok       = true;
+      PzItem w;
+      for(unsigned kk = 0; ok && !*abort_flag && item(kk, w); kk++) {
+        const int* tp = P.tri + 4 * (base + w.slot);
+        const int  i = tp[0], j = tp[1], k = tp[2];
+        for(int t = 0; t < PZ_TERMS && ok; t++) {
+          const PzTerm T  = pz_term(P, w.job, t, i, j, k, w.x);
+          const int    mA = pz_plane_map(T.mapA);
+          for(int k0 = 0; k0 < T.Kp; k0 += PZ_KC, stage_it++) {
+            const int s = stage_it % STAGES, use = stage_it / STAGES;
+            if(use > 0 && !sm100::mbar_wait(&empty[s], (use - 1) & 1)) {
+              fail();
+              ok = false;
+              break;
+            }
+            unsigned char* a = smem + s * C::STAGE_BYTES;
+            sm100::mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
+#pragma unroll
+            for(int p = 0; p < S; p++)
+              if((p & 1) == rank)
+                sm100::tma_load_5d_mc(a + p * PZ_BM * 128, &P.maps[mA], &full[s], k0, w.yb * PZ_BM, T.a2, T.a3, p, kBoth);
+            sm100::tma_load_5d(a + C::A_BYTES, &P.maps[T.mapB], &full[s], k0, w.nb * NT, T.b2, T.b3, 0);
+          }
+        }
+      }
+      // the last use of every stage consumed by both MMA issuers: their commits have landed
+      // here and no load towards this CTA's shared memory is still in flight
+      for(int u = (stage_it > STAGES ? stage_it - STAGES : 0); u < stage_it; u++)
+        if(!sm100::mbar_wait(&empty[u % STAGES], (u / STAGES) & 1)) fail();
+    }
+  } else if(warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if(lane == 0) {
+      int    stage_it = 0, term_it = 0;
+      bool   ok       = true;
+      PzItem w;
+      for(unsigned kk = 0; ok && !*abort_flag && item(kk, w); kk++) {
+        for(int t = 0; t < PZ_TERMS && ok; t++, term_it++) {
+          const int Kp  = t < 2 ? P.kp_v : P.kp_o;
+          const int buf = term_it & 1;
+          if(term_it >= 2 && !sm100::mbar_wait(&lvl_empty[buf], ((term_it >> 1) - 1) & 1)) {
+            fail();
+            ok = false;
+            break;
+          }
+          sm100::tc_fence_after();
+          const uint32_t dbase = tmem + buf * S * NT;
+          for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
+            const int s = stage_it % STAGES, use = stage_it / STAGES;
+            if(!sm100::mbar_wait(&full[s], use & 1)) {
+              fail();
+              ok = false;
+              break;
+            }
+            sm100::tc_fence_after();
+            const uint32_t a = sm100::smem_u32(smem + s * C::STAGE_BYTES), b = a + C::A_BYTES;
+#pragma unroll
+            for(int ks = 0; ks < PZ_KC / 16; ks++)
+#pragma unroll
+              for(int p = 1; p <= S; p++)
+                sm100::mma_bf16(dbase + (p - 1) * NT, sm100::desc_kmajor_sw128(a + (p - 1) * PZ_BM * 128 + ks * 32),
+                                sm100::desc_kmajor_sw128(b + ks * 32), sm100::idesc_bf16_f32(PZ_BM, (S + 1 - p) * NT),
+                                (k0 == 0 && ks == 0 && p == 1) ? 0u : 1u);
+            sm100::mma_commit_mc(&empty[s], kBoth); // stage free in this CTA, as seen by both producers
+          }
+          if(ok) sm100::mma_commit(&lvl_full[buf]);
+        }
+      }
+      sm100::mma_commit(drain);
+      if(!sm100::mbar_wait(drain, 0)) fail();
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue: PZ_EPI warps
+    const int      q = warp & 3, cq = (warp - 2) >> 2; // TMEM lane quarter, column quarter
+    const int      row = q * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
+    const int      c_lo = cq * C::COLS;
+    int            term_it = 0;
+    float          tsq = 0.f;
+    int            tail_slot = -1;
+    PzItem         w;
+    for(unsigned kk = 0; item(kk, w); kk++) {
+      const int* tp = P.tri + 4 * (base + w.slot);
+      if(P.tail && tp[3] != tail_slot) {
+        if(tail_slot >= 0) pz_flush_tail(P.tail, tail_slot, tsq, lane);
+        tsq       = 0.f;
+        tail_slot = tp[3];
+      }
+      if(!pz_epilogue_item<S, NT>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
+                                  abort_flag)) {
+        fail();
+        break;
+      }
+    }
+    if(P.tail && tail_slot >= 0) pz_flush_tail(P.tail, tail_slot, tsq, lane);
+  }
+  sm100::tc_fence_before();
+  __syncthreads();
+  sm100::cluster_sync(); // the peer is done with this CTA's barriers and shared memory
+  if(warp == 1) {
+    sm100::tc_fence_after();
+    sm100::tmem_dealloc(tmem, C::TMEM_COLS);
+  }
+}
+
+} // namespace ccsdt

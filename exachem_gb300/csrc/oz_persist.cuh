@@ -9,11 +9,11 @@
 // a device table, so the launch sequence of a batch is the same for every batch and can be
 // replayed from a CUDA graph.
 //
-// Roles (320 threads): warp 0 lane 0 fetches items and issues TMA loads (running ahead across
-// items), warp 1 lane 0 issues the MMAs, warps 2-9 fold the digit levels into float-float.  The
+// Roles (576 threads): warp 0 lane 0 fetches items and issues TMA loads (running ahead across
+// items), warp 1 lane 0 issues the MMAs, warps 2-17 fold the digit levels into float-float.  The
 // TMEM level accumulators are double buffered by term, so the fold of one term overlaps the MMAs
 // of the next; the float-float accumulator of a tile lives in registers (each epilogue thread owns
-// one row and half of the tile's columns).  All waits are bounded (sm100::kSpinLimit).
+// one row and a quarter of the tile's columns).  All waits are bounded (sm100::kSpinLimit).
 #pragma once
 
 #include <cuda.h>
@@ -23,11 +23,16 @@
 
 namespace ccsdt {
 
-constexpr int PZ_BM = 128, PZ_KC = 64, PZ_THREADS = 320, PZ_IR = 4, PZ_TERMS = 4;
+// 2 role warps (TMA producer, MMA issuer) + PZ_EPI epilogue warps (4 per TMEM lane quarter)
+constexpr int PZ_BM = 128, PZ_KC = 64, PZ_EPI = 16, PZ_THREADS = 64 + 32 * PZ_EPI, PZ_IR = 4, PZ_TERMS = 4;
 constexpr unsigned PZ_END = 0xffffffffu;
 
 // map indices (the handle's map table): the d-sum uses 0-2, the l-sum 6-8
-enum { PZ_OVVV_NAT = 0, PZ_OVVV_SWP = 1, PZ_T2 = 2, PZ_T2H_NAT_B = 6, PZ_T2H_SWP_B = 7, PZ_OOOVH_A = 8, PZ_NMAPS = 9 };
+enum {
+  PZ_OVVV_NAT = 0, PZ_OVVV_SWP = 1, PZ_T2 = 2, PZ_T2H_NAT_B = 6, PZ_T2H_SWP_B = 7, PZ_OOOVH_A = 8,
+  // the A maps again with a one-plane box (the cluster kernel loads A plane by plane)
+  PZ_OVVV_NAT_P1 = 9, PZ_OVVV_SWP_P1 = 10, PZ_OOOVH_A_P1 = 11, PZ_NMAPS = 12
+};
 
 struct PzParams {
   CUtensorMap     maps[PZ_NMAPS];
@@ -122,14 +127,99 @@ __device__ __forceinline__ PzItem pz_decode(unsigned id, int v, int yblocks, int
   return it;
 }
 
+// Epilogue of one item (shared by the persistent kernels): thread = one tile row (TMEM lane
+// quarter q, row = 32 q + lane) x COLS = NT / 4 columns from c_lo.  Issues the item's exponent
+// loads, then per term waits for the MMAs (lvl_full of the term's buffer), folds the S exact levels
+// with oz_horner in chunks of 8 columns, scales by 2^(e_row + e_col - 7 (S + 1)) and adds in
+// float-float, releases the buffer (lvl_empty); finally stores the tile once.  Returns false when
+// a bounded wait gave up.
+template<int S, int NT>
+__device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem& w, int nb, const int* tp,
+                                                 uint32_t lane_base, int c_lo, int row, int lane, int& term_it,
+                                                 float& tsq, uint64_t* lvl_full, uint64_t* lvl_empty,
+                                                 volatile int* abort_flag) {
+  constexpr int COLS = NT / 4;
+  static_assert(COLS % 8 == 0 && COLS <= 32, "epilogue column chunks of 8");
+  const int     v = P.v;
+  const long long v2 = (long long) v * v;
+  const int  i = tp[0], j = tp[1], k = tp[2];
+  const int  y = w.yb * PZ_BM + row, n0 = nb * NT + c_lo;
+  const bool vrow = y < v;
+  const bool vcol = lane < COLS && n0 + lane < v;
+  const long long nl = n0 + lane;
+  int   ea[PZ_TERMS], eb[PZ_TERMS];
+  float sgn[PZ_TERMS];
+#pragma unroll
+  for(int t = 0; t < PZ_TERMS; t++) {
+    const PzTerm T = pz_term(P, w.job, t, i, j, k, w.x);
+    ea[t]  = vrow ? T.eA[T.eA_base + y * T.eA_y] : 0;
+    eb[t]  = vcol ? T.eB[T.eB_base + nl * T.eB_n] : 0;
+    sgn[t] = T.sign;
+  }
+  // element (y, n) of the tile: P[n][x][y] (consecutive rows -> consecutive addresses)
+  float2* Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
+  float hi[COLS], lo[COLS];
+#pragma unroll
+  for(int e = 0; e < COLS; e++) hi[e] = lo[e] = 0.f;
+#pragma unroll 1
+  for(int t = 0; t < PZ_TERMS; t++, term_it++) {
+    const int   buf  = term_it & 1;
+    const int   ea_t = t == 0 ? ea[0] : t == 1 ? ea[1] : t == 2 ? ea[2] : ea[3];
+    const int   eb_t = t == 0 ? eb[0] : t == 1 ? eb[1] : t == 2 ? eb[2] : eb[3];
+    const float sg_t = t == 0 ? sgn[0] : t == 1 ? sgn[1] : t == 2 ? sgn[2] : sgn[3];
+    const float sa   = ldexpf(sg_t, ea_t - OZ_BITS * (S + 1));
+    const float sbl  = ldexpf(1.f, eb_t);
+    const bool  okw  = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it >> 1) & 1) && !*abort_flag);
+    if(!okw) return false;
+    sm100::tc_fence_after();
+#pragma unroll
+    for(int c0 = 0; c0 < COLS; c0 += 8) {
+      uint32_t rv[S][8];
+#pragma unroll
+      for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
+      sm100::tmem_wait_ld();
+#pragma unroll
+      for(int e = 0; e < 8; e++) {
+        const float sb = __shfl_sync(0xffffffffu, sbl, c0 + e);
+        const ff    x  = oz_horner<S, 8>(rv, e);
+        const ff    a  = ff_add(ff{hi[c0 + e], lo[c0 + e]}, ff{(x.hi * sa) * sb, (x.lo * sa) * sb});
+        hi[c0 + e]     = a.hi;
+        lo[c0 + e]     = a.lo;
+        if(P.tail) {
+          const float tl = (__uint_as_float(rv[S - 1][e]) * sa) * sb;
+          tsq            = fmaf(tl, tl, tsq);
+        }
+      }
+    }
+    sm100::tc_fence_before();
+    __syncwarp();
+    if(lane == 0) sm100::mbar_arrive(&lvl_empty[buf]);
+  }
+  if(vrow) {
+#pragma unroll
+    for(int e = 0; e < COLS; e++) {
+      const int n = n0 + e;
+      if(n < v) Cb[(long long) n * v2] = make_float2(hi[e], lo[e]);
+    }
+  }
+  return true;
+}
+
+// Adds a warp's per-thread sums of squares to tail[slot] (one atomic per warp).
+__device__ __forceinline__ void pz_flush_tail(float* tail, int slot, float tsq, int lane) {
+#pragma unroll
+  for(int off = 16; off > 0; off >>= 1) tsq += __shfl_xor_sync(0xffffffffu, tsq, off);
+  if(lane == 0 && tsq > 0.f) atomicAdd(tail + slot, tsq);
+}
+
 template<int S, int NT, int STAGES>
 struct PzCfg {
   static constexpr int A_BYTES = S * PZ_BM * 128, B_BYTES = S * NT * 128, STAGE_BYTES = A_BYTES + B_BYTES;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 512;
-  static constexpr int HALF = NT / 2;   // columns per epilogue thread
+  static constexpr int COLS = NT / 4;   // columns per epilogue thread
   static constexpr uint32_t TMEM_COLS = 512;
   static_assert(2 * S * NT <= 512, "two level buffers must fit in TMEM");
-  static_assert(S * NT <= 256 && NT % 32 == 0, "MMA N limit / epilogue halves of 16");
+  static_assert(S * NT <= 256 && NT % 32 == 0, "MMA N limit / epilogue quarters of 8");
 };
 
 template<int S, int NT, int STAGES>
@@ -159,11 +249,11 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     }
     for(int r = 0; r < PZ_IR; r++) {
       sm100::mbar_init(&item_full[r], 1);
-      sm100::mbar_init(&item_empty[r], 1 + 8); // MMA thread + one arrival per epilogue warp
+      sm100::mbar_init(&item_empty[r], 1 + PZ_EPI); // MMA thread + one arrival per epilogue warp
     }
     for(int b = 0; b < 2; b++) {
       sm100::mbar_init(&lvl_full[b], 1);
-      sm100::mbar_init(&lvl_empty[b], 8);
+      sm100::mbar_init(&lvl_empty[b], PZ_EPI);
     }
     sm100::mbar_init(drain, 1);
     *abort_flag = 0;
@@ -268,16 +358,12 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
       if(!sm100::mbar_wait(drain, 0)) fail();
     }
   } else {
-    // ------------------------------------------------------------ epilogue: 8 warps
-    // Thread = one tile row (TMEM lane) x half of the tile's columns.  Per item it first issues
-    // the global loads the item needs (the four terms' row exponents and one column exponent per
-    // lane), then per term waits for the MMAs, folds the S exact levels with oz_horner, scales by
-    // 2^(e_row + e_col - 7 (S + 1)) and adds in float-float; the finished tile is stored once.
-    const int      q = warp & 3, half = (warp - 2) >> 2;   // lane quarter, column half
+    // ------------------------------------------------------------ epilogue: PZ_EPI warps
+    // Thread = one tile row (TMEM lane) x a quarter of the tile's columns (pz_epilogue_item).
+    const int      q = warp & 3, cq = (warp - 2) >> 2;     // TMEM lane quarter, column quarter
     const int      row = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
-    const int      c_lo = half * C::HALF;
-    const long long v2 = (long long) v * v;
+    const int      c_lo = cq * C::COLS;
     int            term_it = 0;
     float          tsq = 0.f;                                // sum of squares of last-level terms
     int            tail_slot = -1;
@@ -295,86 +381,17 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
       const PzItem w = pz_decode(id, v, yblocks, nblocks);
       const int* tp = P.tri + 4 * (base + w.slot);
       if(P.tail && tp[3] != tail_slot) { // flush the per-triplet sum when the triplet changes
-        if(tail_slot >= 0) {
-#pragma unroll
-          for(int off = 16; off > 0; off >>= 1) tsq += __shfl_xor_sync(0xffffffffu, tsq, off);
-          if(lane == 0 && tsq > 0.f) atomicAdd(P.tail + tail_slot, tsq);
-        }
+        if(tail_slot >= 0) pz_flush_tail(P.tail, tail_slot, tsq, lane);
         tsq       = 0.f;
         tail_slot = tp[3];
       }
-      const int  i = tp[0], j = tp[1], k = tp[2];
-      const int  y = w.yb * PZ_BM + row, n0 = w.nb * NT + c_lo;
-      const bool vrow = y < v;
-      const bool vcol = lane < C::HALF && n0 + lane < v;
-      const long long nl = n0 + lane;
-      int   ea[PZ_TERMS], eb[PZ_TERMS];
-      float sgn[PZ_TERMS];
-#pragma unroll
-      for(int t = 0; t < PZ_TERMS; t++) {
-        const PzTerm T = pz_term(P, w.job, t, i, j, k, w.x);
-        ea[t]  = vrow ? T.eA[T.eA_base + y * T.eA_y] : 0;
-        eb[t]  = vcol ? T.eB[T.eB_base + nl * T.eB_n] : 0;
-        sgn[t] = T.sign;
-      }
-      // element (y, n) of the tile: P[n][x][y] (consecutive rows -> consecutive addresses)
-      float2* Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
-      float hi[C::HALF], lo[C::HALF];
-#pragma unroll
-      for(int e = 0; e < C::HALF; e++) hi[e] = lo[e] = 0.f;
-      bool aborted = false;
-#pragma unroll 1
-      for(int t = 0; t < PZ_TERMS; t++, term_it++) {
-        const int   buf = term_it & 1;
-        const int   ea_t = t == 0 ? ea[0] : t == 1 ? ea[1] : t == 2 ? ea[2] : ea[3];
-        const int   eb_t = t == 0 ? eb[0] : t == 1 ? eb[1] : t == 2 ? eb[2] : eb[3];
-        const float sg_t = t == 0 ? sgn[0] : t == 1 ? sgn[1] : t == 2 ? sgn[2] : sgn[3];
-        const float sa  = ldexpf(sg_t, ea_t - OZ_BITS * (S + 1));
-        const float sbl = ldexpf(1.f, eb_t);
-        const bool  okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it >> 1) & 1) && !*abort_flag);
-        if(!okw) {
-          fail();
-          aborted = true;
-          break;
-        }
-        sm100::tc_fence_after();
-#pragma unroll
-        for(int c0 = 0; c0 < C::HALF; c0 += 16) {
-          uint32_t rv[S][16];
-#pragma unroll
-          for(int l = 0; l < S; l++) sm100::tmem_ld16(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
-          sm100::tmem_wait_ld();
-#pragma unroll
-          for(int e = 0; e < 16; e++) {
-            const float sb = __shfl_sync(0xffffffffu, sbl, c0 + e);
-            const ff    x  = oz_horner<S>(rv, e);
-            const ff    a  = ff_add(ff{hi[c0 + e], lo[c0 + e]}, ff{(x.hi * sa) * sb, (x.lo * sa) * sb});
-            hi[c0 + e]     = a.hi;
-            lo[c0 + e]     = a.lo;
-            if(P.tail) {
-              const float tl = (__uint_as_float(rv[S - 1][e]) * sa) * sb;
-              tsq            = fmaf(tl, tl, tsq);
-            }
-          }
-        }
-        sm100::tc_fence_before();
-        __syncwarp();
-        if(lane == 0) sm100::mbar_arrive(&lvl_empty[buf]);
-      }
-      if(aborted) break;
-      if(vrow) {
-#pragma unroll
-        for(int e = 0; e < C::HALF; e++) {
-          const int n = n0 + e;
-          if(n < v) Cb[(long long) n * v2] = make_float2(hi[e], lo[e]);
-        }
+      if(!pz_epilogue_item<S, NT>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
+                                  abort_flag)) {
+        fail();
+        break;
       }
     }
-    if(P.tail && tail_slot >= 0) {
-#pragma unroll
-      for(int off = 16; off > 0; off >>= 1) tsq += __shfl_xor_sync(0xffffffffu, tsq, off);
-      if(lane == 0 && tsq > 0.f) atomicAdd(P.tail + tail_slot, tsq);
-    }
+    if(P.tail && tail_slot >= 0) pz_flush_tail(P.tail, tail_slot, tsq, lane);
   }
   sm100::tc_fence_before();
   __syncthreads();

@@ -78,8 +78,8 @@ __device__ __forceinline__ ff ff_from_double(double x) {
 // float-float: returns X = sum_l L[l] 2^{7 (S - 1 - l)}.  Each step multiplies by 2^7 (exact)
 // and adds the next level with an error-free two-sum, so the only rounding is in the low word
 // (relative 2^-48); X < 2^{24 + 7 (S - 1)} stays far inside the FP32 range.
-template<int S>
-__device__ __forceinline__ ff oz_horner(const uint32_t (&L)[S][16], int e) {
+template<int S, int W = 16>
+__device__ __forceinline__ ff oz_horner(const uint32_t (&L)[S][W], int e) {
   float hi = __uint_as_float(L[0][e]), lo = 0.f;
 #pragma unroll
   for(int l = 1; l < S; l++) {

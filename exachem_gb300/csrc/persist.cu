@@ -17,6 +17,7 @@
 #include "ccsdt_internal.cuh"
 #include "energy_tiled.cuh"
 #include "fp64_kernels.cuh"
+#include "oz_pair.cuh"
 #include "oz_persist.cuh"
 
 using namespace ccsdt;
@@ -80,18 +81,103 @@ cudaError_t launch_pz_any(int S, const PzParams& p, int grid, cudaStream_t st) {
 
 // Item ids of B slots sorted by estimated cost (rows x columns of the tile), largest first; ties
 // keep the natural order (n-block fastest) so concurrently running CTAs share A tiles in L2.
-std::vector<unsigned> cost_order(int B, int v, int NT) {
-  const int  yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT;
-  const long n  = (long) B * 3 * v * yb * nb;
+// pair = true: items of the cluster kernel, one per pair of adjacent n-blocks.
+std::vector<unsigned> cost_order(int B, int v, int NT, bool pair) {
+  const int  yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT, nn = pair ? (nb + 1) / 2 : nb;
+  const long n  = (long) B * 3 * v * yb * nn;
   std::vector<unsigned> ids(n);
   std::iota(ids.begin(), ids.end(), 0u);
+  auto cols = [&](int b) { return b < nb ? std::min(NT, v - b * NT) : 0; };
   auto cost = [&](unsigned id) {
-    const int n_b = id % nb, y_b = (id / nb) % yb;
-    const int rows = std::min(PZ_BM, v - y_b * PZ_BM), cols = std::min(NT, v - n_b * NT);
-    return rows * cols;
+    const int n_b = id % nn, y_b = (id / nn) % yb;
+    const int rows = std::min(PZ_BM, v - y_b * PZ_BM);
+    return rows * (pair ? cols(2 * n_b) + cols(2 * n_b + 1) : cols(n_b));
   };
   std::stable_sort(ids.begin(), ids.end(), [&](unsigned a, unsigned b) { return cost(a) > cost(b); });
   return ids;
+}
+
+// Items per triplet slot of one launch.
+long items_per_slot(int v, int NT, bool pair) {
+  const int yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT;
+  return 3L * v * yb * (pair ? (nb + 1) / 2 : nb);
+}
+
+template<int S>
+cudaError_t launch_pair(const PzParams& p, int ncl, cudaStream_t st) {
+  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST;
+  using Cfg        = PzCfg<S, NT, ST>;
+  cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
+  if(e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id               = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim              = dim3(2 * ncl, 1, 1);
+  cfg.blockDim             = dim3(PZ_THREADS, 1, 1);
+  cfg.dynamicSmemBytes     = Cfg::SMEM;
+  cfg.stream               = st;
+  cfg.attrs                = attr;
+  cfg.numAttrs             = 1;
+  e = cudaLaunchKernelEx(&cfg, oz_pair_kernel<S, NT, ST>, p);
+  if(e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_any(int S, const PzParams& p, int ncl, cudaStream_t st) {
+  switch(S) {
+    case 1: return launch_pair<1>(p, ncl, st);
+    case 2: return launch_pair<2>(p, ncl, st);
+    case 3: return launch_pair<3>(p, ncl, st);
+    case 4: return launch_pair<4>(p, ncl, st);
+    case 5: return launch_pair<5>(p, ncl, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+// Co-resident two-CTA clusters of the cluster kernel for S planes (0: cannot run).
+template<int S>
+int pair_clusters() {
+  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST;
+  using Cfg        = PzCfg<S, NT, ST>;
+  if(cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM) !=
+     cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  int sm = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id               = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim              = dim3(2 * (sm / 2), 1, 1);
+  cfg.blockDim             = dim3(PZ_THREADS, 1, 1);
+  cfg.dynamicSmemBytes     = Cfg::SMEM;
+  cfg.attrs                = attr;
+  cfg.numAttrs             = 1;
+  int n = 0;
+  if(cudaOccupancyMaxActiveClusters(&n, oz_pair_kernel<S, NT, ST>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int pair_clusters_any(int S) {
+  switch(S) {
+    case 1: return pair_clusters<1>();
+    case 2: return pair_clusters<2>();
+    case 3: return pair_clusters<3>();
+    case 4: return pair_clusters<4>();
+    case 5: return pair_clusters<5>();
+  }
+  return 0;
 }
 
 } // namespace
@@ -115,9 +201,9 @@ ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
     bt_B = B;
     bt_order_key = -1;
   }
-  const int key = S * 100000 + B;
+  const int key = (S * 100000 + B) * 2 + (pz_pair ? 1 : 0);
   if(bt_order_key != key) {
-    auto ids = cost_order(B, v, NT);
+    auto ids = cost_order(B, v, NT, pz_pair);
     if(bt_order) cudaFree(bt_order);
     bt_order = nullptr;
     if(cudaMalloc((void**) &bt_order, ids.size() * sizeof(unsigned)) != cudaSuccess) {
@@ -167,8 +253,8 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F, p.ex_t2 = ex_t2, p.ex_t2h = ex_t2h, p.ex_ovvv = ex_ovvv, p.ex_ooovh = ex_ooovh;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
-  const int NT  = pz_nt(S);
-  const int per = 3 * v * ((v + PZ_BM - 1) / PZ_BM) * ((v + NT - 1) / NT);
+  const int  NT  = pz_nt(S);
+  const long per = items_per_slot(v, NT, pz_pair);
   if(nitems_override <= 0) p.nitems = (unsigned) (per * nslots);
   // the cost-ordered table was built for bt_B slots; a smaller last batch has its own table
   const bool partial = nslots != bt_B;
@@ -193,7 +279,9 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
     cudaEventRecord(prof_ev[0], stream);
     cudaEventRecord(prof_ev[1], stream); // no separate l-sum phase
   }
-  if(e == cudaSuccess) e = launch_pz_any(S, p, sm, stream);
+  if(e == cudaSuccess)
+    e = pz_pair ? launch_pair_any(S, p, (int) std::min<long>(pz_pair_clusters, (long) p.nitems), stream)
+                : launch_pz_any(S, p, sm, stream);
   launches++;
   if(profiling) cudaEventRecord(prof_ev[2], stream);
   if(tv[1]) cudaEventRecord(tv[1], stream);
@@ -223,6 +311,10 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
   ccsdt_status s;
   tev_used = 0; // events of a batch that failed earlier are not read
   tev_slots.clear();
+  // the two-CTA cluster kernel when its clusters can be resident (and not switched off for a test)
+  if(S >= 1 && S <= 5 && pair_clusters_by_S[S] < 0) pair_clusters_by_S[S] = pair_clusters_any(S);
+  pz_pair_clusters = (S >= 1 && S <= 5) ? pair_clusters_by_S[S] : 0;
+  pz_pair          = !force_single_cta && pz_pair_clusters > 0;
   if((s = ensure_slices(std::max(S, slices_ready), 0)) || (s = ensure_tmaps(S, pz_nt(S)))) return s;
   // table of non-zero triplets (i < k); i = j = k contributes exactly zero
   std::vector<int> tab;
@@ -251,10 +343,10 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
   }
   // natural-order table for a partial last batch
   const int  NT  = pz_nt(S);
-  const long per = 3L * v * ((v + PZ_BM - 1) / PZ_BM) * ((v + NT - 1) / NT);
+  const long per = items_per_slot(v, NT, pz_pair);
   const long rem = m % B;
   if(rem) {
-    auto ids = cost_order((int) rem, v, NT);
+    auto ids = cost_order((int) rem, v, NT, pz_pair);
     if(bt_order_partial) cudaFree(bt_order_partial);
     bt_order_partial = nullptr;
     if(cudaMalloc((void**) &bt_order_partial, ids.size() * sizeof(unsigned)) != cudaSuccess) {

@@ -388,7 +388,9 @@ enum {
   MAP_OVVV_NAT = 0, MAP_OVVV_SWP = 1, MAP_T2 = 2, MAP_T2H_NAT = 3, MAP_T2H_SWP = 4, MAP_OOOVH = 5,
   // the persistent kernel's l-sum runs with the single index on the tile rows: ooovh as the
   // 128-row A operand, t2h pair rows as the NT-row B operand
-  MAP_T2H_NAT_B = 6, MAP_T2H_SWP_B = 7, MAP_OOOVH_A = 8
+  MAP_T2H_NAT_B = 6, MAP_T2H_SWP_B = 7, MAP_OOOVH_A = 8,
+  // A maps with a one-plane box: the cluster kernel multicasts A plane by plane
+  MAP_OVVV_NAT_P1 = 9, MAP_OVVV_SWP_P1 = 10, MAP_OOOVH_A_P1 = 11
 };
 
 // tcgen05 configurations: digit planes S -> columns per level NT (S NT <= 256, (S + 2) NT <= 512)
@@ -480,6 +482,9 @@ ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT) {
   ok &= encode_map(&tmaps[MAP_T2H_NAT_B], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, NT, (int) S_);
   ok &= encode_map(&tmaps[MAP_T2H_SWP_B], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, NT, (int) S_);
   ok &= encode_map(&tmaps[MAP_OOOVH_A], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OVVV_NAT_P1], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, 1);
+  ok &= encode_map(&tmaps[MAP_OVVV_SWP_P1], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, 1);
+  ok &= encode_map(&tmaps[MAP_OOOVH_A_P1], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, 1);
   if(!ok) return fail(CCSDT_E_CUDA, "cuTensorMapEncodeTiled failed for the digit planes");
   tmaps_ready = true;
   tmaps_S     = S;
@@ -618,8 +623,9 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 }
 
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
-  last_batched   = false;
-  last_err_bound = 0.0; // only the LEARNED mode estimates its error
+  last_batched     = false;
+  last_err_bound   = 0.0; // only the LEARNED mode estimates its error
+  force_single_cta = opts->reserved[1] == 1; // test knob: the single-CTA persistent kernel
   if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
   const int S       = opts->slices;
   const int variant = opts->slice_kind;

@@ -89,3 +89,16 @@ def test_persistent_batches_cover_every_triplet(built):
     e4, e5 = ft.triplet_energies(tri, "ozaki", slices=3)
     r4, r5 = ft.triplet_energies(tri, "ozaki", slices=3, legacy_mma=2)
     np.testing.assert_allclose(e5, r5, rtol=1e-12, atol=1e-12 * np.abs(r5).max())
+
+
+@pytest.mark.parametrize("o,v,seed", [(6, 40, 0), (5, 130, 2), (9, 70, 5), (4, 200, 7)])
+def test_cluster_kernel_equals_single_cta(built, o, v, seed):
+    """The two-CTA cluster kernel (A planes multicast to both CTAs of a cluster) computes every
+    tile with the same operations as the single-CTA kernel: energies are bit-identical.  The
+    shapes give odd and even numbers of N blocks (an odd count leaves the second CTA of the last
+    pair without columns)."""
+    ft = _ft(o, v, seed)
+    for S in (1, 2, 3, 4, 5):
+        a = ft.energy("ozaki", slices=S)
+        b = ft.energy("ozaki", slices=S, single_cta=1)
+        assert a["e_paren_T"] == b["e_paren_T"] and a["e_bracket_T"] == b["e_bracket_T"], (S, a, b)
