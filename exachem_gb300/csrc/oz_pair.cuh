@@ -162,14 +162,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
               break;
             }
             sm100::tc_fence_after();
-            const uint32_t a = sm100::smem_u32(smem + s * C::STAGE_BYTES), b = a + C::A_BYTES;
-#pragma unroll
-            for(int ks = 0; ks < PZ_KC / 16; ks++)
-#pragma unroll
-              for(int p = 1; p <= S; p++)
-                sm100::mma_bf16(dbase + (p - 1) * NT, sm100::desc_kmajor_sw128(a + (p - 1) * PZ_BM * 128 + ks * 32),
-                                sm100::desc_kmajor_sw128(b + ks * 32), sm100::idesc_bf16_f32(PZ_BM, (S + 1 - p) * NT),
-                                (k0 == 0 && ks == 0 && p == 1) ? 0u : 1u);
+            const uint32_t a = sm100::smem_u32(smem + s * C::STAGE_BYTES);
+            pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, k0 == 0);
             sm100::mma_commit_mc(&empty[s], kBoth); // stage free in this CTA, as seen by both producers
           }
           if(ok) sm100::mma_commit(&lvl_full[buf]);

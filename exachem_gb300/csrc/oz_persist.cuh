@@ -18,6 +18,8 @@
 
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "ozaki.cuh"
 #include "sm100_ptx.cuh"
 
@@ -167,21 +169,18 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
     const int   ea_t = t == 0 ? ea[0] : t == 1 ? ea[1] : t == 2 ? ea[2] : ea[3];
     const int   eb_t = t == 0 ? eb[0] : t == 1 ? eb[1] : t == 2 ? eb[2] : eb[3];
     const float sg_t = t == 0 ? sgn[0] : t == 1 ? sgn[1] : t == 2 ? sgn[2] : sgn[3];
-    const float sa   = ldexpf(sg_t, ea_t - OZ_BITS * (S + 1));
-    const float sbl  = ldexpf(1.f, eb_t);
+    const float sa   = copysignf(oz_pow2(ea_t - OZ_BITS * (S + 1)), sg_t);
+    const float sbl  = oz_pow2(eb_t);
     const bool  okw  = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it >> 1) & 1) && !*abort_flag);
     if(!okw) return false;
     sm100::tc_fence_after();
+    // fold `W` columns starting at c0 whose S levels are in rv
+    auto fold = [&](auto& rv, int c0, auto wtag) {
+      constexpr int W = decltype(wtag)::value;
 #pragma unroll
-    for(int c0 = 0; c0 < COLS; c0 += 8) {
-      uint32_t rv[S][8];
-#pragma unroll
-      for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
-      sm100::tmem_wait_ld();
-#pragma unroll
-      for(int e = 0; e < 8; e++) {
+      for(int e = 0; e < W; e++) {
         const float sb = __shfl_sync(0xffffffffu, sbl, c0 + e);
-        const ff    x  = oz_horner<S, 8>(rv, e);
+        const ff    x  = oz_horner<S, W>(rv, e);
         const ff    a  = ff_add(ff{hi[c0 + e], lo[c0 + e]}, ff{(x.hi * sa) * sb, (x.lo * sa) * sb});
         hi[c0 + e]     = a.hi;
         lo[c0 + e]     = a.lo;
@@ -189,6 +188,27 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
           const float tl = (__uint_as_float(rv[S - 1][e]) * sa) * sb;
           tsq            = fmaf(tl, tl, tsq);
         }
+      }
+    };
+    if constexpr(S * COLS <= 32) {
+      // every level of the thread's columns in one TMEM round trip (tcgen05.wait::ld waits for
+      // all of a thread's loads, so chunks could not overlap anyway)
+      uint32_t rv[S][COLS];
+#pragma unroll
+      for(int l = 0; l < S; l++) {
+        if constexpr(COLS == 16) sm100::tmem_ld16(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
+        else sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
+      }
+      sm100::tmem_wait_ld();
+      fold(rv, 0, std::integral_constant<int, COLS>{});
+    } else {
+#pragma unroll
+      for(int c0 = 0; c0 < COLS; c0 += 8) {
+        uint32_t rv[S][8];
+#pragma unroll
+        for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
+        sm100::tmem_wait_ld();
+        fold(rv, c0, std::integral_constant<int, 8>{});
       }
     }
     sm100::tc_fence_before();
@@ -210,6 +230,23 @@ __device__ __forceinline__ void pz_flush_tail(float* tail, int slot, float tsq, 
 #pragma unroll
   for(int off = 16; off > 0; off >>= 1) tsq += __shfl_xor_sync(0xffffffffu, tsq, off);
   if(lane == 0 && tsq > 0.f) atomicAdd(tail + slot, tsq);
+}
+
+// The MMAs of one pipeline stage (PZ_KC = 64 along K, 4 k-steps of 16): for every k-step, S
+// MMAs A_p x [B_1 .. B_{S+1-p}] into the level columns (p - 1) NT ...  The descriptors are built
+// once per stage: the start-address field (bits 0-13, address >> 4) is linear, so the plane and
+// k-step offsets (multiples of 16 B, all inside the 228 KB window) are added to it directly.
+// `first`: the stage opens the term (its first MMA overwrites the accumulators).
+template<int S, int NT>
+__device__ __forceinline__ void pz_issue_stage(uint32_t dbase, uint32_t a_smem, uint32_t b_smem, bool first) {
+  const uint64_t da = sm100::desc_kmajor_sw128(a_smem), db = sm100::desc_kmajor_sw128(b_smem);
+#pragma unroll
+  for(int ks = 0; ks < PZ_KC / 16; ks++)
+#pragma unroll
+    for(int p = 1; p <= S; p++)
+      sm100::mma_bf16(dbase + (p - 1) * NT, da + (uint64_t) (((p - 1) * PZ_BM * 128 + ks * 32) >> 4),
+                      db + (uint64_t) ((ks * 32) >> 4), sm100::idesc_bf16_f32(PZ_BM, (S + 1 - p) * NT),
+                      (first && ks == 0 && p == 1) ? 0u : 1u);
 }
 
 template<int S, int NT, int STAGES>
@@ -340,14 +377,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
               break;
             }
             sm100::tc_fence_after();
-            const uint32_t a = sm100::smem_u32(smem + s * C::STAGE_BYTES), b = a + C::A_BYTES;
-#pragma unroll
-            for(int ks = 0; ks < PZ_KC / 16; ks++)
-#pragma unroll
-              for(int p = 1; p <= S; p++)
-                sm100::mma_bf16(dbase + (p - 1) * NT, sm100::desc_kmajor_sw128(a + (p - 1) * PZ_BM * 128 + ks * 32),
-                                sm100::desc_kmajor_sw128(b + ks * 32), sm100::idesc_bf16_f32(PZ_BM, (S + 1 - p) * NT),
-                                (k0 == 0 && ks == 0 && p == 1) ? 0u : 1u);
+            const uint32_t a = sm100::smem_u32(smem + s * C::STAGE_BYTES);
+            pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, k0 == 0);
             sm100::mma_commit(&empty[s]);
           }
           sm100::mma_commit(&lvl_full[buf]);

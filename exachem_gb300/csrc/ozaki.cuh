@@ -74,6 +74,13 @@ __device__ __forceinline__ ff ff_from_double(double x) {
   return ff{hi, (float) (x - (double) hi)};
 }
 
+// 2^e as a float from its exponent bits (no libm call): exact for -126 <= e <= 127; below that
+// the scale (and the contribution it multiplies, under 2^-126 of the operands' units) flushes to
+// zero, above it the result is +inf.
+__device__ __forceinline__ float oz_pow2(int e) {
+  return e < -126 ? 0.f : __int_as_float((min(e, 128) + 127) << 23);
+}
+
 // Horner fold of S exact level sums (integers held in FP32, most significant first) into
 // float-float: returns X = sum_l L[l] 2^{7 (S - 1 - l)}.  Each step multiplies by 2^7 (exact)
 // and adds the next level with an error-free two-sum, so the only rounding is in the low word
