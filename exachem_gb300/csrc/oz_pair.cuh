@@ -92,26 +92,32 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
     *abort_flag = 1;
     if(P.err) atomicExch(P.err, 1);
   };
-  // the k-th item of this cluster, or false past the end
-  auto item = [&](unsigned kk, PzItem& w) {
-    const unsigned q = cid + kk * ncl;
-    if(q >= P.nitems) return false;
-    const PzPairItem pi = pz_decode_pair(P.order[q], v, yblocks, npairs);
-    w = PzItem{pi.slot, pi.job, pi.x, pi.yb, 2 * pi.nbp + rank};
-    return true;
+  // this cluster's items: table entries cid, cid + ncl, ...
+  const unsigned n_mine = P.nitems > cid ? (P.nitems - cid + ncl - 1) / ncl : 0;
+  auto decode = [&](unsigned id) {
+    const PzPairItem pi = pz_decode_pair(id, v, yblocks, npairs);
+    return PzItem{pi.slot, pi.job, pi.x, pi.yb, 2 * pi.nbp + rank};
   };
+  // item ids two ahead and triplet entries one ahead, so the loads of the next item overlap the
+  // current one: id(kk) -> entry(kk)
+  auto id_at = [&](unsigned kk) { return kk < n_mine ? P.order[cid + kk * ncl] : 0u; };
+  auto entry = [&](unsigned id) { return reinterpret_cast<const int4*>(P.tri)[base + decode(id).slot]; };
 
   if(warp == 0) {
     // ------------------------------------------------------------ TMA producer
     if(lane == 0) {
       for(int m: {PZ_OVVV_NAT_P1, PZ_OVVV_SWP_P1, PZ_T2, PZ_T2H_NAT_B, PZ_T2H_SWP_B, PZ_OOOVH_A_P1})
         sm100::prefetch_tmap(&P.maps[m]);
-      int  stage_it = 0;
-      bool ok       = true;
-      PzItem w;
-      for(unsigned kk = 0; ok && !*abort_flag && item(kk, w); kk++) {
-        const int* tp = P.tri + 4 * (base + w.slot);
-        const int  i = tp[0], j = tp[1], k = tp[2];
+      int      stage_it = 0;
+      bool     ok       = true;
+      unsigned id0 = id_at(0), id1 = id_at(1);
+      int4     e0  = n_mine ? entry(id0) : make_int4(0, 0, 0, 0);
+      for(unsigned kk = 0; ok && !*abort_flag && kk < n_mine; kk++) {
+        const PzItem w = decode(id0);
+        const int    i = e0.x, j = e0.y, k = e0.z;
+        const unsigned id2 = id_at(kk + 2);                        // prefetch
+        const int4     e1  = kk + 1 < n_mine ? entry(id1) : e0;
+        id0 = id1, id1 = id2;
         for(int t = 0; t < PZ_TERMS && ok; t++) {
           const PzTerm T  = pz_term(P, w.job, t, i, j, k, w.x);
           const int    mA = pz_plane_map(T.mapA);
@@ -131,6 +137,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
             sm100::tma_load_5d(a + C::A_BYTES, &P.maps[T.mapB], &full[s], k0, w.nb * NT, T.b2, T.b3, 0);
           }
         }
+        e0 = e1;
       }
       // the last use of every stage consumed by both MMA issuers: their commits have landed
       // here and no load towards this CTA's shared memory is still in flight
@@ -140,10 +147,9 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
   } else if(warp == 1) {
     // ------------------------------------------------------------ MMA issuer
     if(lane == 0) {
-      int    stage_it = 0, term_it = 0;
-      bool   ok       = true;
-      PzItem w;
-      for(unsigned kk = 0; ok && !*abort_flag && item(kk, w); kk++) {
+      int  stage_it = 0, term_it = 0;
+      bool ok       = true;
+      for(unsigned kk = 0; ok && !*abort_flag && kk < n_mine; kk++) { // the MMAs need no item data
         for(int t = 0; t < PZ_TERMS && ok; t++, term_it++) {
           const int Kp  = t < 2 ? P.kp_v : P.kp_o;
           const int buf = term_it & 1;
@@ -181,9 +187,14 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
     int            term_it = 0;
     float          tsq = 0.f;
     int            tail_slot = -1;
-    PzItem         w;
-    for(unsigned kk = 0; item(kk, w); kk++) {
-      const int* tp = P.tri + 4 * (base + w.slot);
+    unsigned id0 = id_at(0), id1 = id_at(1);
+    int4     e0  = n_mine ? entry(id0) : make_int4(0, 0, 0, 0);
+    for(unsigned kk = 0; kk < n_mine; kk++) {
+      const PzItem   w   = decode(id0);
+      const int      tp[4] = {e0.x, e0.y, e0.z, e0.w};
+      const unsigned id2 = id_at(kk + 2);                          // prefetch
+      const int4     e1  = kk + 1 < n_mine ? entry(id1) : e0;
+      id0 = id1, id1 = id2;
       if(P.tail && tp[3] != tail_slot) {
         if(tail_slot >= 0) pz_flush_tail(P.tail, tail_slot, tsq, lane);
         tsq       = 0.f;
@@ -194,6 +205,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
         fail();
         break;
       }
+      e0 = e1;
     }
     if(P.tail && tail_slot >= 0) pz_flush_tail(P.tail, tail_slot, tsq, lane);
   }

@@ -190,16 +190,22 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
         }
       }
     };
+    // the buffer is released as soon as its last levels are in registers, before the fold of
+    // those columns: the MMAs of the term after next need not wait for the arithmetic
+    auto release = [&]() {
+      sm100::tc_fence_before();
+      __syncwarp();
+      if(lane == 0) sm100::mbar_arrive(&lvl_empty[buf]);
+    };
     if constexpr(S * COLS <= 32) {
-      // every level of the thread's columns in one TMEM round trip (tcgen05.wait::ld waits for
-      // all of a thread's loads, so chunks could not overlap anyway)
-      uint32_t rv[S][COLS];
+      uint32_t rv[S][COLS]; // every level of the thread's columns in one TMEM round trip
 #pragma unroll
       for(int l = 0; l < S; l++) {
         if constexpr(COLS == 16) sm100::tmem_ld16(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
         else sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
       }
       sm100::tmem_wait_ld();
+      release();
       fold(rv, 0, std::integral_constant<int, COLS>{});
     } else {
 #pragma unroll
@@ -208,12 +214,10 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
 #pragma unroll
         for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
         sm100::tmem_wait_ld();
+        if(c0 + 8 == COLS) release();
         fold(rv, c0, std::integral_constant<int, 8>{});
       }
     }
-    sm100::tc_fence_before();
-    __syncwarp();
-    if(lane == 0) sm100::mbar_arrive(&lvl_empty[buf]);
   }
   if(vrow) {
 #pragma unroll
