@@ -59,9 +59,9 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
   unsigned char* smem = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full      = reinterpret_cast<uint64_t*>(smem + STAGES * C::STAGE_BYTES);
   uint64_t* empty     = full + STAGES;
-  uint64_t* lvl_full  = empty + STAGES; // [2] MMAs of a term done
-  uint64_t* lvl_empty = lvl_full + 2;   // [2] epilogue drained the buffer
-  uint64_t* drain     = lvl_empty + 2;
+  uint64_t* lvl_full  = empty + STAGES; // [NBUF] MMAs of a term done
+  uint64_t* lvl_empty = lvl_full + 3;   // [NBUF] epilogue drained the buffer
+  uint64_t* drain     = lvl_empty + 3;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
       sm100::mbar_init(&full[s], 1);
       sm100::mbar_init(&empty[s], 2); // one commit from each CTA's MMA issuer
     }
-    for(int b = 0; b < 2; b++) {
+    for(int b = 0; b < C::NBUF; b++) {
       sm100::mbar_init(&lvl_full[b], 1);
       sm100::mbar_init(&lvl_empty[b], PZ_EPI);
     }
@@ -152,8 +152,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
       for(unsigned kk = 0; ok && !*abort_flag && kk < n_mine; kk++) { // the MMAs need no item data
         for(int t = 0; t < PZ_TERMS && ok; t++, term_it++) {
           const int Kp  = t < 2 ? P.kp_v : P.kp_o;
-          const int buf = term_it & 1;
-          if(term_it >= 2 && !sm100::mbar_wait(&lvl_empty[buf], ((term_it >> 1) - 1) & 1)) {
+          const int buf = term_it % C::NBUF;
+          if(term_it >= C::NBUF && !sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1)) {
             fail();
             ok = false;
             break;
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
         tsq       = 0.f;
         tail_slot = tp[3];
       }
-      if(!pz_epilogue_item<S, NT>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
+      if(!pz_epilogue_item<S, NT, C::NBUF>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
                                   abort_flag)) {
         fail();
         break;

@@ -135,13 +135,13 @@ __device__ __forceinline__ PzItem pz_decode(unsigned id, int v, int yblocks, int
 // with oz_horner in chunks of 8 columns, scales by 2^(e_row + e_col - 7 (S + 1)) and adds in
 // float-float, releases the buffer (lvl_empty); finally stores the tile once.  Returns false when
 // a bounded wait gave up.
-template<int S, int NT>
+template<int S, int NT, int NBUF>
 __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem& w, int nb, const int* tp,
                                                  uint32_t lane_base, int c_lo, int row, int lane, int& term_it,
                                                  float& tsq, uint64_t* lvl_full, uint64_t* lvl_empty,
                                                  volatile int* abort_flag) {
   constexpr int COLS = NT / 4;
-  static_assert(COLS % 8 == 0 && COLS <= 32, "epilogue column chunks of 8");
+  static_assert(COLS % 4 == 0 && COLS <= 32, "epilogue column chunks of 8 (and a last one of 4)");
   const int     v = P.v;
   const long long v2 = (long long) v * v;
   const int  i = tp[0], j = tp[1], k = tp[2];
@@ -165,13 +165,13 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
   for(int e = 0; e < COLS; e++) hi[e] = lo[e] = 0.f;
 #pragma unroll 1
   for(int t = 0; t < PZ_TERMS; t++, term_it++) {
-    const int   buf  = term_it & 1;
+    const int   buf  = term_it % NBUF;
     const int   ea_t = t == 0 ? ea[0] : t == 1 ? ea[1] : t == 2 ? ea[2] : ea[3];
     const int   eb_t = t == 0 ? eb[0] : t == 1 ? eb[1] : t == 2 ? eb[2] : eb[3];
     const float sg_t = t == 0 ? sgn[0] : t == 1 ? sgn[1] : t == 2 ? sgn[2] : sgn[3];
     const float sa   = copysignf(oz_pow2(ea_t - OZ_BITS * (S + 1)), sg_t);
     const float sbl  = oz_pow2(eb_t);
-    const bool  okw  = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it >> 1) & 1) && !*abort_flag);
+    const bool  okw  = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it / NBUF) & 1) && !*abort_flag);
     if(!okw) return false;
     sm100::tc_fence_after();
     // fold `W` columns starting at c0 whose S levels are in rv
@@ -208,14 +208,35 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
       release();
       fold(rv, 0, std::integral_constant<int, COLS>{});
     } else {
-#pragma unroll
-      for(int c0 = 0; c0 < COLS; c0 += 8) {
+      // chunks of 8 columns and, when COLS % 8 == 4, one of 4; every TMEM access starts at a
+      // multiple of its own width (a thread whose first column is 4 mod 8 takes the 4 first)
+      auto chunk8 = [&](int c0, bool last) {
         uint32_t rv[S][8];
 #pragma unroll
         for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
         sm100::tmem_wait_ld();
-        if(c0 + 8 == COLS) release();
+        if(last) release();
         fold(rv, c0, std::integral_constant<int, 8>{});
+      };
+      auto chunk4 = [&](int c0, bool last) {
+        uint32_t rv[S][4];
+#pragma unroll
+        for(int l = 0; l < S; l++) sm100::tmem_ld4(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
+        sm100::tmem_wait_ld();
+        if(last) release();
+        fold(rv, c0, std::integral_constant<int, 4>{});
+      };
+      if constexpr(COLS % 8 == 0) {
+#pragma unroll
+        for(int c0 = 0; c0 < COLS; c0 += 8) chunk8(c0, c0 + 8 == COLS);
+      } else if((c_lo & 7) == 4) {
+        chunk4(0, false);
+#pragma unroll
+        for(int c0 = 4; c0 < COLS; c0 += 8) chunk8(c0, c0 + 8 == COLS);
+      } else {
+#pragma unroll
+        for(int c0 = 0; c0 + 8 <= COLS; c0 += 8) chunk8(c0, false);
+        chunk4(COLS - 4, true);
       }
     }
   }
@@ -259,8 +280,11 @@ struct PzCfg {
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 512;
   static constexpr int COLS = NT / 4;   // columns per epilogue thread
   static constexpr uint32_t TMEM_COLS = 512;
+  // level buffers in TMEM (S x NT columns each): three where they fit, so the MMA issuer can run
+  // two terms ahead of the epilogue (a short l-sum term then never leaves the tensor pipe idle)
+  static constexpr int NBUF = 3 * S * NT <= 512 ? 3 : 2;
   static_assert(2 * S * NT <= 512, "two level buffers must fit in TMEM");
-  static_assert(S * NT <= 256 && NT % 32 == 0, "MMA N limit / epilogue quarters of 8");
+  static_assert(S * NT <= 256 && NT % 16 == 0, "MMA N limit / epilogue quarters of 4k columns");
 };
 
 template<int S, int NT, int STAGES>
@@ -275,9 +299,9 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
   uint64_t* empty      = full + STAGES;
   uint64_t* item_full  = empty + STAGES;
   uint64_t* item_empty = item_full + PZ_IR;
-  uint64_t* lvl_full   = item_empty + PZ_IR;   // [2] MMAs of a term done
-  uint64_t* lvl_empty  = lvl_full + 2;         // [2] epilogue drained the buffer
-  uint64_t* drain      = lvl_empty + 2;
+  uint64_t* lvl_full   = item_empty + PZ_IR;   // [NBUF] MMAs of a term done
+  uint64_t* lvl_empty  = lvl_full + 3;         // [NBUF] epilogue drained the buffer
+  uint64_t* drain      = lvl_empty + 3;
   unsigned* item_id    = reinterpret_cast<unsigned*>(drain + 1);
   uint32_t* tmem_slot  = item_id + PZ_IR;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
@@ -292,7 +316,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
       sm100::mbar_init(&item_full[r], 1);
       sm100::mbar_init(&item_empty[r], 1 + PZ_EPI); // MMA thread + one arrival per epilogue warp
     }
-    for(int b = 0; b < 2; b++) {
+    for(int b = 0; b < C::NBUF; b++) {
       sm100::mbar_init(&lvl_full[b], 1);
       sm100::mbar_init(&lvl_empty[b], PZ_EPI);
     }
@@ -367,8 +391,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         if(id == PZ_END) break;
         for(int t = 0; t < PZ_TERMS; t++, term_it++) {
           const int Kp  = t < 2 ? P.kp_v : P.kp_o;
-          const int buf = term_it & 1;
-          if(term_it >= 2 && !sm100::mbar_wait(&lvl_empty[buf], ((term_it >> 1) - 1) & 1)) {
+          const int buf = term_it % C::NBUF;
+          if(term_it >= C::NBUF && !sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1)) {
             fail();
             break;
           }
@@ -420,7 +444,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         tsq       = 0.f;
         tail_slot = tp[3];
       }
-      if(!pz_epilogue_item<S, NT>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
+      if(!pz_epilogue_item<S, NT, C::NBUF>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
                                   abort_flag)) {
         fail();
         break;

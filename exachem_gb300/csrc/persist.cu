@@ -36,7 +36,7 @@ struct PzPick<2> {
 };
 template<>
 struct PzPick<3> {
-  static constexpr int NT = 64, ST = 3;
+  static constexpr int NT = 64, ST = 3; // (NT = 48 with three level buffers measured 1.5x slower)
 };
 template<>
 struct PzPick<4> {
