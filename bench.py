@@ -219,6 +219,9 @@ def main():
     ap.add_argument("--batch", type=int, default=48, help="triplets per step in split mode")
     ap.add_argument("--cpu-sample", type=int, default=1, help="triplets timed on the CPU baseline (0: skip)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--budget", type=float, default=1e-8,
+                    help="learned mode: 3 sqrt(sum sigma_t^2) <= budget x sum |E(T)_t|")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-mode side measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -272,6 +275,14 @@ def main():
     stream = torch.cuda.current_stream()
     ft.set_stream(stream.cuda_stream)
     kw = {"slices": S} if mode != "fp64" else {}
+    model = None
+    if mode == "learned" or (mode == "ozaki" and not args.no_learned):
+        from exachem_gb300 import learned
+        model, _ = learned.load_model()                  # the shipped slice-count model
+        learned.set_model(ft, model)
+    if mode == "learned":
+        # each timed call is a part of the whole (T) over all triplets: its acceptance share
+        kw = {"slices": 5, "energy_budget": args.budget, "budget_triplets": int(len(tri_all))}
 
     per_step = args.fp64_batch if mode == "fp64" else args.batch
     batches = [spread_sample(mine, per_step, offset=s) for s in range(args.steps)]
@@ -348,6 +359,32 @@ def main():
             "phase_ms": phase, "timing": timing}
 
     # plain FP64 on the same shape (projected from a few triplets) and |dE| on the CPU sample
+    # learned slice count on the same batches (side measurement; the headline is the fixed count)
+    learned_line = None
+    if mode == "ozaki" and model is not None:
+        from exachem_gb300 import learned
+        lkw = {"slices": 5, "energy_budget": args.budget, "budget_triplets": int(len(tri_all))}
+        ft.triplet_energies(warm[0], "learned", **lkw)
+        torch.cuda.synchronize()
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        mean_s, esc, prods = [], 0, 0.0
+        for b in batches:
+            ft.triplet_energies(b, "learned", **lkw)
+            m, e, pr = learned.learned_stats(ft, with_products=True)
+            mean_s.append(m)
+            esc += e
+            prods += pr
+        l1.record(stream)
+        torch.cuda.synchronize()
+        l_elapsed = l0.elapsed_time(l1) * 1e-3
+        learned_line = {"value": l_elapsed / frac, "unit": UNIT, "budget": args.budget,
+                        "acceptance": "3 sqrt(sum sigma_t^2) <= budget x sum |E(T)_t| over the whole call "
+                                      "(each batched call takes its sqrt(n_call / n_total) share)",
+                        "mean_predicted_slices": float(np.mean(mean_s)), "escalations": int(esc),
+                        "digit_plane_products_per_triplet": prods / max(1, timed_trip),
+                        "fixed_count_products_per_triplet": S * (S + 1) / 2}
+
     fp64_proj, dE = None, None
     if rank == 0 and mode != "fp64":
         fb = spread_sample(mine, args.fp64_batch, offset=7)
@@ -361,6 +398,15 @@ def main():
         s4, s5 = ft.triplet_energies(cpu_samp, mode, **kw)
         dE = {"triplets": cpu_samp.tolist(), "rel_E(T)_vs_fp64": (np.abs(s5 - f5) / np.abs(f5)).tolist(),
               "rel_E[T]_vs_fp64": (np.abs(s4 - f4) / np.abs(f4)).tolist()}
+        if learned_line is not None:
+            # one call of 4 triplets in learned mode against FP64 (the acceptance test is on a
+            # call's total; FP64 takes ~0.85 s per triplet at this size)
+            lb = batches[0][:4]
+            _, lf5 = ft.triplet_energies(lb, "fp64")
+            _, ll5 = ft.triplet_energies(lb, "learned", slices=5, energy_budget=args.budget,
+                                         budget_triplets=int(len(tri_all)))
+            learned_line["sample_rel_error_of_sum"] = float(abs(ll5.sum() - lf5.sum()) / np.abs(lf5).sum())
+            learned_line["sample"] = "4 triplets of the first batch, one call, against the FP64 path"
 
     # end to end through the C ABI with host (pinned) buffers: upload + one batch + readback
     e2e = None
@@ -410,6 +456,7 @@ def main():
                        "l2": "inputs (75 GB) and per-triplet scratch (3 GB) exceed L2; no flush"},
             "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
             "energy_sample": dE, "partial_energy_timed": {"e_bracket_T": esum4, "e_paren_T": esum5},
+            "learned": learned_line,
             "fp64_projected_s": fp64_proj, "speedup_vs_fp64": (fp64_proj / value) if fp64_proj else None,
             "setup": {"generate_s": t_gen, "fp64_dgemm_tflops": fp64_peak},
         }

@@ -36,7 +36,8 @@ class Layout(ctypes.Structure):
 class Opts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("slices", ctypes.c_int), ("slice_kind", ctypes.c_int),
                 ("use_graph", ctypes.c_int), ("shard_index", ctypes.c_int), ("shard_count", ctypes.c_int),
-                ("energy_budget", ctypes.c_double), ("reserved", ctypes.c_int * 6)]
+                ("energy_budget", ctypes.c_double), ("budget_triplets", ctypes.c_int),
+                ("test_kernel", ctypes.c_int), ("test_single_cta", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 class Result(ctypes.Structure):
@@ -161,7 +162,7 @@ class FusedTriples:
 
     @staticmethod
     def opts(mode="fp64", slices=4, slice_kind="bf16", energy_budget=1e-9, use_graph=0,
-             shard_index=0, shard_count=1, legacy_mma=0, single_cta=0) -> Opts:
+             shard_index=0, shard_count=1, legacy_mma=0, single_cta=0, budget_triplets=0) -> Opts:
         o = Opts()
         o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
         o.slices = slices
@@ -169,8 +170,9 @@ class FusedTriples:
         o.energy_budget = energy_budget
         o.use_graph = use_graph
         o.shard_index, o.shard_count = shard_index, shard_count
-        o.reserved[0] = legacy_mma   # 1: mma.sync slice kernel instead of tcgen05 (testing)
-        o.reserved[1] = single_cta   # 1: single-CTA persistent kernel, not the 2-CTA cluster one (testing)
+        o.budget_triplets = budget_triplets
+        o.test_kernel = legacy_mma       # 1: mma.sync slice kernel, 2: per-triplet tcgen05 kernel (testing)
+        o.test_single_cta = single_cta   # 1: single-CTA persistent kernel, not the 2-CTA cluster one (testing)
         return o
 
     def energy(self, mode="fp64", **kw) -> dict:

@@ -231,7 +231,7 @@ extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccs
      cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream) != cudaSuccess)
     return h->fail(CCSDT_E_CUDA, "estimate scratch init");
   h->force_mma_sync   = false;
-  h->force_single_cta = opts->reserved[1] == 1;
+  h->force_single_cta = opts->test_single_cta == 1;
   if((s = h->run_batched(opts->slices, n, tri, false, dtail, dsens))) return s;
   std::vector<double> E(2 * n), sens(n);
   std::vector<float>  tail(n);
@@ -357,7 +357,10 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
   if((s = readback())) return s;
   double abs_sum = 0;
   for(long t = 0; t < n; t++) abs_sum += std::fabs(E[2 * t + 1]);
-  const double target = (opts->energy_budget > 0 ? opts->energy_budget : 1e-8) * abs_sum / 3.0; // on sqrt(sum est^2)
+  // a call that is one part of a computation over budget_triplets triplets gets the share of the
+  // total allowance whose variances add up to the whole: x sqrt(budget_triplets / nz)
+  const double part   = (opts->budget_triplets > nz && nz > 0) ? std::sqrt((double) opts->budget_triplets / nz) : 1.0;
+  const double target = (opts->energy_budget > 0 ? opts->energy_budget : 1e-8) * abs_sum * part / 3.0; // on sqrt(sum est^2)
   learned_fallbacks   = 0;
   for(int round = 0; round < 16; round++) {
     double var = 0;

@@ -625,7 +625,7 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
   last_batched     = false;
   last_err_bound   = 0.0; // only the LEARNED mode estimates its error
-  force_single_cta = opts->reserved[1] == 1; // test knob: the single-CTA persistent kernel
+  force_single_cta = opts->test_single_cta == 1; // test knob: the single-CTA persistent kernel
   if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
   const int S       = opts->slices;
   const int variant = opts->slice_kind;
@@ -635,9 +635,9 @@ ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* 
   if((s = ensure_slices(S, variant))) return s;
   if(!d_err || !F12 || !F34 || !F56 || !e_tiles || !e_part || !oovv_f || !t1_f)
     return fail(CCSDT_E_STATE, "split-precision buffers missing after slicing");
-  // test knob opts->reserved[0]: 0 persistent tcgen05 (default), 1 mma.sync slice kernel,
+  // test knob opts->test_kernel: 0 persistent tcgen05 (default), 1 mma.sync slice kernel,
   // 2 per-triplet (non-persistent) tcgen05 kernel
-  const int kernel_kind = opts->reserved[0];
+  const int kernel_kind = opts->test_kernel;
   force_mma_sync        = kernel_kind == 1;
   cudaError_t e0 = cudaMemsetAsync(d_err, 0, sizeof(int), stream);
   if(e0 != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e0));

@@ -2,7 +2,7 @@
 
 Labels: for an occupied triplet, the smallest digit-plane count S in 2..smax whose triplet
 energy E_t(S) satisfies |E_t(S) - E_t(FP64)| <= budget * mean_t |E_t(FP64)| * sqrt(N) / 3,
-measured against the library's own FP64 path (the plain kernel judges the error); N is the
+measured against the library's own FP64 path (the plain kernel is the yardstick); N is the
 system's number of occupied triplets and the mean is over its sampled triplets.  That is the
 equal share of the LEARNED mode's acceptance test 3 sqrt(sum_t sigma_t^2) <= budget sum_t |E_t|
 (independent per-triplet errors add like a random walk).  Features come from the library

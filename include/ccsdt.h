@@ -73,7 +73,12 @@ typedef struct {
   int    shard_count;   /* caller sums the partial energies (0 or 1 = every triplet)          */
   double energy_budget; /* LEARNED: accept when 3 sqrt(sum_t sigma_t^2) <= budget x          */
                         /* sum_t |E(T)_t| (sigma_t: estimated error of triplet t; default 1e-8) */
-  int    reserved[6];
+  int    budget_triplets; /* LEARNED: the call is one part of a computation over this many    */
+                          /* triplets (batched calls): the acceptance allowance is scaled by    */
+                          /* sqrt(budget_triplets / triplets of the call); 0 = the whole call   */
+  int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05 */
+  int    test_single_cta; /* testing: 1 = single-CTA persistent kernel, not the 2-CTA cluster  */
+  int    reserved[3];
 } ccsdt_opts;
 
 typedef struct {

@@ -136,3 +136,21 @@ def test_error_estimate_covers_measured_error(built):
     print(f"sigma / measured error: 1% {q[0]:.2f}, 5% {q[1]:.2f}, median {q[2]:.2f} over {len(r)} cases")
     assert (3 * r >= 1).mean() >= 0.98
     assert q[2] <= 10
+
+
+def test_batched_call_takes_its_share_of_the_budget(built):
+    """A call that is one part of a larger computation (budget_triplets) is accepted against its
+    share of the whole allowance, sqrt(budget_triplets / n_call) times its own: never more
+    escalations than the same call judged as the whole computation."""
+    from exachem_gb300 import ccsd_t as ct, learned
+    from exachem_gb300.generator import generate
+    params, _ = learned.load_model()
+    ft = ct.FusedTriples(10, 64, ts=32)
+    ft.upload_dict(generate(10, 64, 404))
+    tri = ct.all_triplets(10)
+    learned.set_model(ft, params)
+    ft.triplet_energies(tri, "learned", slices=5, energy_budget=1e-10)
+    _, esc_whole, prod_whole = learned.learned_stats(ft, with_products=True)
+    ft.triplet_energies(tri, "learned", slices=5, energy_budget=1e-10, budget_triplets=100 * len(tri))
+    _, esc_part, prod_part = learned.learned_stats(ft, with_products=True)
+    assert esc_part <= esc_whole and prod_part <= prod_whole
