@@ -288,7 +288,7 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   if(e == cudaSuccess) {
     BatchEnergyArgs ea;
     ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
-                                   o, v, 0, 0, 0, nullptr};
+                                   o, v, 0, 0, 0, nullptr, sens != nullptr};
     ea.tri = bt_tri, ea.base = bt_ctrl + 2, ea.F = bt_F, ea.part = bt_part;
     const int G = std::min(e_ntiles, energy_grid());
     energy_tiled_batch_kernel<<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
