@@ -54,7 +54,12 @@ static_assert(kCyc2(0) == 4 && kCyc2(1) == 2 && kCyc2(2) == 5 && kCyc2(3) == 0 &
 static_assert(kXzy(0) == 1 && kXzy(1) == 0 && kXzy(2) == 3 && kXzy(3) == 2 && kXzy(4) == 5 && kXzy(5) == 4, "");
 static_assert(kYxz(0) == 2 && kYxz(1) == 4 && kYxz(2) == 0 && kYxz(3) == 5 && kYxz(4) == 1 && kYxz(5) == 3, "");
 static_assert(kZyx(0) == 5 && kZyx(1) == 3 && kZyx(2) == 4 && kZyx(3) == 1 && kZyx(4) == 2 && kZyx(5) == 0, "");
+static __device__ __constant__ int c_perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
 
+__device__ __forceinline__ int perm_slot(int p0, int p1, int p2) {
+  // (0,1,2)=0 (0,2,1)=1 (1,0,2)=2 (1,2,0)=3 (2,0,1)=4 (2,1,0)=5
+  return p0 * 2 + (p1 > p2 ? 1 : 0);
+}
 
 __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, const float2* P12, const float2* P34,
                                                   const float2* P56, int i, int j, int k, double* part, int gblock,
@@ -65,6 +70,8 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   __shared__ float  ti[3][B], tj[3][B], tk[3][B];
   __shared__ float2 evs[3][B];
   __shared__ float2 dab[3][3][B * B];    // e_i + e_j + e_k - e_a - e_b (float-float), per block pair
+  __shared__ int    blk0[3], blkn[3];
+  __shared__ int    slot_on[6];
 
   const int       v = A.v, o = A.o, tid = threadIdx.x;
   const long long v2 = (long long) v * v;
@@ -75,48 +82,48 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   float sens = 0.f; // first-order sensitivity of the energy to errors in W (a-posteriori estimate)
 
   for(int tile = gblock; tile < A.ntiles; tile += gsize) {
-    // the block triple, its extents and which of the six ordered slots are distinct, in every
-    // thread's registers (no barrier needed for them)
-    const int3 tb      = A.tiles[tile];
-    const int  b0[3]   = {tb.x * B, tb.y * B, tb.z * B};
-    const int  bn[3]   = {min(B, v - b0[0]), min(B, v - b0[1]), min(B, v - b0[2])};
-    unsigned   on_mask = 0;
-#pragma unroll
-    for(int q = 0; q < 6; q++) {
-      bool on = true;
-#pragma unroll
-      for(int r = 0; r < q; r++)
-        if(b0[kPerm(q, 0)] == b0[kPerm(r, 0)] && b0[kPerm(q, 1)] == b0[kPerm(r, 1)] && b0[kPerm(q, 2)] == b0[kPerm(r, 2)])
-          on = false;
-      on_mask |= on ? 1u << q : 0u;
+    __syncthreads();
+    if(tid < 3) {
+      const int3 t = A.tiles[tile];
+      const int  b = tid == 0 ? t.x : tid == 1 ? t.y : t.z;
+      blk0[tid]    = b * B;
+      blkn[tid]    = min(B, v - b * B);
     }
-    __syncthreads(); // the previous item's orbit phase is done with W and the staged singles
+    __syncthreads();
+    if(tid < 6) { // a slot counts once per distinct ordered block triple
+      const int* P  = c_perm[tid];
+      int        on = 1;
+      for(int q = 0; q < tid; q++) {
+        const int* Q = c_perm[q];
+        if(blk0[P[0]] == blk0[Q[0]] && blk0[P[1]] == blk0[Q[1]] && blk0[P[2]] == blk0[Q[2]]) on = 0;
+      }
+      slot_on[tid] = on;
+    }
     // singles data of the three blocks
     for(int e = tid; e < 9 * B * B; e += ET_THREADS) {
       const int u = e / (3 * B * B), w = (e / (B * B)) % 3, x = (e / B) % B, y = e % B;
-      const int bu = u == 0 ? b0[0] : u == 1 ? b0[1] : b0[2], nu = u == 0 ? bn[0] : u == 1 ? bn[1] : bn[2];
-      const int bw = w == 0 ? b0[0] : w == 1 ? b0[1] : b0[2], nw = w == 0 ? bn[0] : w == 1 ? bn[1] : bn[2];
-      const bool ok = x < nu && y < nw;
-      const long long off = (long long) (bu + x) * v + bw + y;
+      const bool ok = x < blkn[u] && y < blkn[w];
+      const long long off = (long long) (blk0[u] + x) * v + blk0[w] + y;
       Ojk[u][w][x * B + y] = ok ? gOjk[off] : 0.f;
       Oik[u][w][x * B + y] = ok ? gOik[off] : 0.f;
       Oij[u][w][x * B + y] = ok ? gOij[off] : 0.f;
-      // e_i + e_j + e_k - e_a - e_b for the block pair (u, w)
-      const ff ea = x < nu ? ff_from_double(A.ev[bu + x]) : ff{0.f, 0.f};
-      const ff eb = y < nw ? ff_from_double(A.ev[bw + y]) : ff{0.f, 0.f};
-      const ff d  = ff_add(ff_add(eijk, ff_neg(ea)), ff_neg(eb));
-      dab[u][w][x * B + y] = make_float2(d.hi, d.lo);
     }
     if(tid < 3 * B) {
       const int u = tid / B, x = tid % B;
-      const int bu = u == 0 ? b0[0] : u == 1 ? b0[1] : b0[2], nu = u == 0 ? bn[0] : u == 1 ? bn[1] : bn[2];
-      const bool ok = x < nu;
-      const int  a = bu + x;
+      const bool ok = x < blkn[u];
+      const int  a = blk0[u] + x;
       ti[u][x] = ok ? A.t1[(long long) i * v + a] : 0.f;
       tj[u][x] = ok ? A.t1[(long long) j * v + a] : 0.f;
       tk[u][x] = ok ? A.t1[(long long) k * v + a] : 0.f;
       const ff e = ok ? ff_from_double(A.ev[a]) : ff{0.f, 0.f};
       evs[u][x] = make_float2(e.hi, e.lo);
+    }
+    __syncthreads();
+    for(int e = tid; e < 9 * B * B; e += ET_THREADS) {
+      const int    u = e / (3 * B * B), w = (e / (B * B)) % 3, x = (e / B) % B, y = e % B;
+      const float2 ea = evs[u][x], eb = evs[w][y];
+      const ff     d  = ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y});
+      dab[u][w][x * B + y] = make_float2(d.hi, d.lo);
     }
     // W of the six slots, stored by orbit coordinates (loc[P[0]], loc[P[1]], loc[P[2]]) = the
     // slot's local (a', b', c'): three passes, each reading one array along its contiguous index
@@ -127,7 +134,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     float2* Wf = &W[0][0];
 #pragma unroll
     for(int pass = 0; pass < 3; pass++) {
-      if(pass > 0) __syncthreads(); // the previous pass's updates are in W
+      __syncthreads();
       float2 x[12];
       int    widx[12];
 #pragma unroll
@@ -141,17 +148,17 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         if(pass == 0) { // P12[a][c][b]: b fastest
           la = sl, lc = m, lb = f;
           src = P12;
-          off = ((long long) (b0[P0] + la) * v + b0[P2] + lc) * v + b0[P1] + lb;
+          off = ((long long) (blk0[P0] + la) * v + blk0[P2] + lc) * v + blk0[P1] + lb;
         } else if(pass == 1) { // P34[b][a][c]: c fastest
           lb = sl, la = m, lc = f;
           src = P34;
-          off = ((long long) (b0[P1] + lb) * v + b0[P0] + la) * v + b0[P2] + lc;
+          off = ((long long) (blk0[P1] + lb) * v + blk0[P0] + la) * v + blk0[P2] + lc;
         } else { // P56[c][b][a]: a fastest
           lc = sl, lb = m, la = f;
           src = P56;
-          off = ((long long) (b0[P2] + lc) * v + b0[P1] + lb) * v + b0[P0] + la;
+          off = ((long long) (blk0[P2] + lc) * v + blk0[P1] + lb) * v + blk0[P0] + la;
         }
-        const bool ok = la < bn[P0] && lb < bn[P1] && lc < bn[P2];
+        const bool ok = la < blkn[P0] && lb < blkn[P1] && lc < blkn[P2];
         x[it]         = ok ? src[off] : make_float2(0.f, 0.f);
         int loc[3]    = {0, 0, 0};
         loc[P0] = la, loc[P1] = lb, loc[P2] = lc;
@@ -174,7 +181,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     // its slot is a distinct ordered block triple (so every ordered (a, b, c) counts once).
     for(int r = tid; r < B3; r += ET_THREADS) {
       const int la = r / (B * B), lb = (r / B) % B, lc = r % B;
-      if(la >= bn[0] || lb >= bn[1] || lc >= bn[2]) continue;
+      if(la >= blkn[0] || lb >= blkn[1] || lc >= blkn[2]) continue;
       const int loc[3] = {la, lb, lc};
       ff        w[6];
       float     sg[6];
@@ -191,7 +198,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       float sn = 0.f;
 #pragma unroll
       for(int q = 0; q < 6; q++) {
-        if(!(on_mask >> q & 1u)) continue;
+        if(!slot_on[q]) continue;
         // ordering xyz of slot q: Z = 4 W_xyz + W_yzx + W_zxy, Y = 3 V_xyz - V_xzy - V_yxz - V_zyx
         const ff    z  = ff_add(ff_add(ff_scale(w[q], 4.f), w[kCyc1(q)]), w[kCyc2(q)]);
         const ff    y4 = ff_add(ff_mul_f(w[q], 3.f), ff_neg(ff_add(ff_add(w[kXzy(q)], w[kYxz(q)]), w[kZyx(q)])));
