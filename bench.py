@@ -346,7 +346,7 @@ def main():
         fp64_eq = 12.0 * float(v) ** 3 * (v + o)           # l-sum and d-sum terms run in the same launch
         per_launch = fp64_eq * S * (S + 1) / 2 * ntr / nb  # BF16 digit-plane products of one launch
         peak, peak_src = peaks.get("bf16_tflops", 1900.0), "MEASURED_PEAKS.json bf16_tflops (burst), of measured"
-        kernel = "oz_persist_kernel"
+        kernel = "oz_pair_kernel"                          # the two-CTA cluster contraction (default path)
         phase = {"contraction_per_triplet": pt["contraction_ms"] / ntr, "energy_per_triplet": pt["energy_ms"] / ntr,
                  "batches": pt["batches"], "triplets_per_batch": ntr / nb}
         timing = "live CUDA events on the launching stream around each batch's contraction launch in the timed region"

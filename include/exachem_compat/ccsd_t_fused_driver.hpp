@@ -24,6 +24,7 @@
 
 #include <chrono>
 #include <cstddef>
+#include <cstdio>
 #include <cstdlib>
 #include <stdexcept>
 #include <string>
@@ -134,8 +135,37 @@ SpatialInputs gather_closed_shell(const std::vector<size_t>& mo_tiles, size_t no
   return S;
 }
 
+// The slice-count model file written by exachem_gb300.learned (JSON: {"params": [floats], ...}):
+// the CCSDT_MLP_NPARAM numbers of the "params" array.
+inline std::vector<float> read_slice_model(const std::string& path) {
+  std::FILE* f = std::fopen(path.c_str(), "rb");
+  if(!f) throw std::runtime_error("cannot open the slice model " + path);
+  std::string text;
+  char        buf[1 << 16];
+  for(size_t k; (k = std::fread(buf, 1, sizeof(buf), f)) > 0;) text.append(buf, k);
+  std::fclose(f);
+  const size_t key = text.find("\"params\"");
+  const size_t lb  = key == std::string::npos ? key : text.find('[', key);
+  if(lb == std::string::npos) throw std::runtime_error("no params array in " + path);
+  std::vector<float> p;
+  const char*        c = text.c_str() + lb + 1;
+  while(*c && *c != ']') {
+    char*        end = nullptr;
+    const double x   = std::strtod(c, &end);
+    if(end == c) {
+      ++c; // separator
+      continue;
+    }
+    p.push_back((float) x);
+    c = end;
+  }
+  if((int) p.size() != CCSDT_MLP_NPARAM) throw std::runtime_error("slice model " + path + ": wrong parameter count");
+  return p;
+}
+
 // Mode from the environment: EXACHEM_GB300_MODE = fp64 (default) | ozaki | learned,
-// EXACHEM_GB300_SLICES = digit planes for ozaki (default 3).
+// EXACHEM_GB300_SLICES = digit planes (ozaki, default 3) or the largest count (learned, default 5),
+// EXACHEM_GB300_BUDGET = the learned mode's energy budget (default 1e-8).
 inline ccsdt_opts opts_from_env() {
   ccsdt_opts  op{};
   const char* m = std::getenv("EXACHEM_GB300_MODE");
@@ -145,14 +175,24 @@ inline ccsdt_opts opts_from_env() {
   else if(mode == "learned") op.mode = CCSDT_MODE_LEARNED;
   else throw std::invalid_argument("EXACHEM_GB300_MODE must be fp64, ozaki or learned: " + mode);
   const char* sl = std::getenv("EXACHEM_GB300_SLICES");
-  op.slices      = sl ? std::atoi(sl) : 3;
+  op.slices      = sl ? std::atoi(sl) : (op.mode == CCSDT_MODE_LEARNED ? 5 : 3);
+  const char* bu = std::getenv("EXACHEM_GB300_BUDGET");
+  op.energy_budget = bu ? std::atof(bu) : 1e-8;
   return op;
+}
+
+// The model the learned mode installs: EXACHEM_GB300_SLICE_MODEL (required for that mode).
+inline std::vector<float> slice_model_from_env() {
+  const char* p = std::getenv("EXACHEM_GB300_SLICE_MODEL");
+  if(!p) throw std::invalid_argument("the learned mode needs EXACHEM_GB300_SLICE_MODEL (a slice model file)");
+  return read_slice_model(p);
 }
 
 // Runs (T) on the spatial inputs through the C ABI: returns (E[T], E(T), device seconds).
 // device -1 = the calling thread's current CUDA device.
 inline std::tuple<double, double, double> run_closed_shell(const SpatialInputs& S, int device,
-                                                           const ccsdt_opts& opts) {
+                                                           const ccsdt_opts& opts,
+                                                           const std::vector<float>* slice_model = nullptr) {
   ccsdt_layout  L{S.o, S.v, (int) S.occ_tiles.size(), S.occ_tiles.data(), (int) S.vir_tiles.size(),
                  S.vir_tiles.data()};
   ccsdt_handle* h  = nullptr;
@@ -161,6 +201,7 @@ inline std::tuple<double, double, double> run_closed_shell(const SpatialInputs& 
   st = ccsdt_upload(h, S.eps_occ.data(), S.eps_vir.data(), S.t1.data(), S.t2.data(), S.oovv.data(),
                     S.ooov.data(), S.ovvv.data(), 0);
   ccsdt_result r{};
+  if(st == CCSDT_OK && slice_model) st = ccsdt_set_slice_model(h, slice_model->data());
   if(st == CCSDT_OK) st = ccsdt_energy(h, &opts, &r);
   if(st != CCSDT_OK) {
     std::string msg = ccsdt_last_error(h);
@@ -198,7 +239,14 @@ public:
     ccsdt_opts   op = exachem_gb300::opts_from_env();
     op.shard_index  = (int) ec.pg().rank().value();
     op.shard_count  = (int) ec.pg().size().value();
-    auto [e4, e5, work] = exachem_gb300::run_closed_shell(S, /*current device*/ -1, op);
+    std::vector<float> model;
+    if(op.mode == CCSDT_MODE_LEARNED) {
+      model = exachem_gb300::slice_model_from_env();
+      // every rank's call is one part of the whole: it is held to its share of the budget
+      op.budget_triplets = S.o * (S.o + 1) * (S.o + 2) / 6;
+    }
+    auto [e4, e5, work] =
+      exachem_gb300::run_closed_shell(S, /*current device*/ -1, op, model.empty() ? nullptr : &model);
     double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return {(T) e4, (T) e5, work, total};
   }
