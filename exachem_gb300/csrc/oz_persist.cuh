@@ -181,9 +181,11 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
       for(int e = 0; e < W; e++) {
         const float sb = __shfl_sync(0xffffffffu, sbl, c0 + e);
         const ff    x  = oz_horner<S, W>(rv, e);
-        const ff    a  = ff_add(ff{hi[c0 + e], lo[c0 + e]}, ff{(x.hi * sa) * sb, (x.lo * sa) * sb});
+        // accumulate without renormalising (exact two-sum of the high words, low words added);
+        // the tile is renormalised once before it is stored
+        const ff    a  = ff_two_sum(hi[c0 + e], (x.hi * sa) * sb);
         hi[c0 + e]     = a.hi;
-        lo[c0 + e]     = a.lo;
+        lo[c0 + e]     = lo[c0 + e] + (a.lo + (x.lo * sa) * sb);
         if(P.tail) {
           const float tl = (__uint_as_float(rv[S - 1][e]) * sa) * sb;
           tsq            = fmaf(tl, tl, tsq);
@@ -244,7 +246,8 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
 #pragma unroll
     for(int e = 0; e < COLS; e++) {
       const int n = n0 + e;
-      if(n < v) Cb[(long long) n * v2] = make_float2(hi[e], lo[e]);
+      const float h = hi[e] + lo[e];
+      if(n < v) Cb[(long long) n * v2] = make_float2(h, lo[e] - (h - hi[e]));
     }
   }
   return true;
