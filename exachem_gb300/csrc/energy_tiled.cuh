@@ -194,23 +194,33 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z
         sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
       }
-      ff    zy4{0.f, 0.f}, zy5{0.f, 0.f};
+      // The six orderings form two cyclic classes, {q, yzx(q), zxy(q)} and the three orderings
+      // one transposition away (xzy, yxz, zyx of q), which are the other class.  With the class
+      // sums C: Z_q = 4 W_q + W_yzx + W_zxy = 3 W_q + C_own, Y_q = 3 V_q - C_other(V).
+      const ff    ca  = ff_add(ff_add(w[0], w[3]), w[4]); // class of ordering 0: slots 0, 3, 4
+      const ff    cb  = ff_add(ff_add(w[1], w[2]), w[5]); // slots 1, 2, 5
+      const float sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
+      ff    zy4{0.f, 0.f}, zys{0.f, 0.f};
       float sn = 0.f;
 #pragma unroll
       for(int q = 0; q < 6; q++) {
         if(!slot_on[q]) continue;
-        // ordering xyz of slot q: Z = 4 W_xyz + W_yzx + W_zxy, Y = 3 V_xyz - V_xzy - V_yxz - V_zyx
-        const ff    z  = ff_add(ff_add(ff_scale(w[q], 4.f), w[kCyc1(q)]), w[kCyc2(q)]);
-        const ff    y4 = ff_add(ff_mul_f(w[q], 3.f), ff_neg(ff_add(ff_add(w[kXzy(q)], w[kYxz(q)]), w[kZyx(q)])));
-        const float ys = 3.f * sg[q] - sg[kXzy(q)] - sg[kYxz(q)] - sg[kZyx(q)];
-        const ff    y5 = ff_add_f(y4, ys);
+        const bool  in_a = q == 0 || q == 3 || q == 4;
+        const ff    t3 = ff_mul_f(w[q], 3.f);
+        const ff    z  = ff_add(t3, in_a ? ca : cb);
+        const ff    y4 = ff_add(t3, ff_neg(in_a ? cb : ca));
+        const float ys = 3.f * sg[q] - (in_a ? sgb : sga);   // singles part of Y
         zy4 = ff_add(zy4, ff_mul(z, y4));
-        zy5 = ff_add(zy5, ff_mul(z, y5));
+        zys = ff_add(zys, ff_mul_f(z, ys));
         // first-order sensitivity to errors in W: W_abc enters Z_abc (x4), Z_bca, Z_cab and,
         // through V, Y_abc (x3), Y_acb, Y_bac, Y_cba; with uncorrelated signs
         //   |dE/dW|^2 ~ (16 + 1 + 1) Y^2 / D^2 + (9 + 1 + 1 + 1) Z^2 / D^2
-        if(A.want_sens) sn = fmaf(18.f * y5.hi, y5.hi, fmaf(12.f * z.hi, z.hi, sn));
+        if(A.want_sens) {
+          const float y5 = y4.hi + ys;
+          sn = fmaf(18.f * y5, y5, fmaf(12.f * z.hi, z.hi, sn));
+        }
       }
+      const ff zy5 = ff_add(zy4, zys);
       const float2 dd = dab[0][1][la * B + lb], ec = evs[2][lc];
       const ff     id = ff_div(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
       s4   = ff_add(s4, ff_mul(zy4, id));

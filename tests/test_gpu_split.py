@@ -102,3 +102,20 @@ def test_cluster_kernel_equals_single_cta(built, o, v, seed):
         a = ft.energy("ozaki", slices=S)
         b = ft.energy("ozaki", slices=S, single_cta=1)
         assert a["e_paren_T"] == b["e_paren_T"] and a["e_bracket_T"] == b["e_bracket_T"], (S, a, b)
+
+
+@pytest.mark.parametrize("o,v,seed", [(3, 9, 31), (2, 17, 32), (4, 65, 33), (1, 30, 34), (5, 129, 35)])
+def test_split_edge_shapes(built, o, v, seed):
+    """Shapes at the edges of the tiling: v below one 8-wide energy block, below one N tile and
+    one 128-row tile, one past a multiple of 64 and of 128, and o = 1 (the only triplet is
+    i = j = k, which contributes exactly zero).  Split precision (S = 3 and 5) against the plain
+    FP64 path, both through the C ABI."""
+    ft = _ft(o, v, seed)
+    ref = ft.energy("fp64")
+    for S, tol in ((3, 1e-7), (5, 1e-10)):
+        r = ft.energy("ozaki", slices=S)
+        for key in ("e_bracket_T", "e_paren_T"):
+            if ref[key] == 0.0:
+                assert r[key] == 0.0
+            else:
+                assert abs(r[key] - ref[key]) <= tol * abs(ref[key]), (S, key, r[key], ref[key])
