@@ -109,10 +109,12 @@ def test_split_edge_shapes(built, o, v, seed):
     """Shapes at the edges of the tiling: v below one 8-wide energy block, below one N tile and
     one 128-row tile, one past a multiple of 64 and of 128, and o = 1 (the only triplet is
     i = j = k, which contributes exactly zero).  Split precision (S = 3 and 5) against the plain
-    FP64 path, both through the C ABI."""
+    FP64 path, both through the C ABI.  S = 5 is held to 1e-9: the singles part of V is formed
+    from FP32 copies of (ia|jb) and t1, a relative floor of ~6e-8 x the singles' share of E(T),
+    which averages out over large systems but not over the two triplets of o = 3."""
     ft = _ft(o, v, seed)
     ref = ft.energy("fp64")
-    for S, tol in ((3, 1e-7), (5, 1e-10)):
+    for S, tol in ((3, 1e-7), (5, 1e-9)):
         r = ft.energy("ozaki", slices=S)
         for key in ("e_bracket_T", "e_paren_T"):
             if ref[key] == 0.0:
