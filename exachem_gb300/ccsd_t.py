@@ -51,7 +51,9 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_last_launch_count", "ccsdt_reference_op_count", "ccsdt_destroy",
             "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet",
             "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc", "ccsdt_shard_triplets",
-            "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates"]
+            "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates",
+            "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end"]
+BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
 def load_library(path: str | os.PathLike | None = None):
@@ -72,6 +74,10 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_reference_op_count.argtypes = [ctypes.POINTER(Layout), dp, ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_set_stream.argtypes = [vp, vp]
     lib.ccsdt_set_phase_timing.argtypes = [vp, ctypes.c_int]
+    lib.ccsdt_upload_begin.argtypes = [vp, vp, vp, vp, ctypes.c_int]
+    lib.ccsdt_upload_blocks.argtypes = [vp, ctypes.c_int, ctypes.c_long, ip, ctypes.POINTER(ctypes.c_longlong), vp,
+                                        ctypes.c_longlong, ctypes.c_int]
+    lib.ccsdt_upload_end.argtypes = [vp]
     lib.ccsdt_triplet_error_estimates.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp, dp]
     lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
@@ -87,7 +93,7 @@ def load_library(path: str | os.PathLike | None = None):
     for name in ("ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
                  "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet",
                  "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
-                 "ccsdt_triplet_error_estimates"):
+                 "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -210,6 +216,27 @@ class FusedTriples:
         self._check(self.lib.ccsdt_debug_triplet_w(self.h, ctypes.byref(op), i, j, k,
                                                    w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return w
+
+    # ---- device-side retile of spin-orbital tile blocks (ccsdt_upload_begin / blocks / end)
+    def upload_begin(self, eps_occ, eps_vir, t1):
+        self._keep = [np.ascontiguousarray(x, dtype=np.float64) for x in (eps_occ, eps_vir, t1)]
+        self._check(self.lib.ccsdt_upload_begin(self.h, *[x.ctypes.data for x in self._keep], 0))
+
+    def upload_blocks(self, kind: str, tiles, offsets, data):
+        """tiles: (n, 4) tile positions; offsets: (n,) element offsets into data (numpy float64 on the
+        host, or a torch CUDA float64 tensor on the handle's device)."""
+        t = np.ascontiguousarray(np.asarray(tiles, dtype=np.int32).reshape(-1, 4))
+        off = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+        if hasattr(data, "data_ptr"):
+            ptr, n, dev = data.data_ptr(), data.numel(), 1
+        else:
+            arr = np.ascontiguousarray(data, dtype=np.float64)
+            ptr, n, dev = arr.ctypes.data, arr.size, 0
+        self._check(self.lib.ccsdt_upload_blocks(self.h, BLOCK_KINDS[kind], len(t), t.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                                 off.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), ptr, n, dev))
+
+    def upload_end(self):
+        self._check(self.lib.ccsdt_upload_end(self.h))
 
     def triplet_error_estimates(self, tri, slices: int):
         """(E[T]_t, E(T)_t, estimated |E(T)_t - E(T)_t,fp64|) at `slices` BF16 digit planes."""

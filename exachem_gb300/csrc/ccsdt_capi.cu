@@ -27,6 +27,13 @@ namespace {
     if(e__ != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
   } while(0)
 
+// the same inside ccsdt_handle methods
+#define CK_H(call)                                                                                 \
+  do {                                                                                             \
+    cudaError_t e__ = (call);                                                                      \
+    if(e__ != cudaSuccess) return fail(CCSDT_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e__)); \
+  } while(0)
+
 int multiplicity(int i, int j, int k) {
   if(i == j && j == k) return 1;
   if(i == j || j == k || i == k) return 3;
@@ -66,7 +73,56 @@ ccsdt_handle::~ccsdt_handle() {
     if(e) cudaEventDestroy(e);
   for(auto& e: tev)
     if(e) cudaEventDestroy(e);
+  if(blk_stage) cudaFree(blk_stage);
+  if(blk_meta) cudaFree(blk_meta);
   if(own_stream) cudaStreamDestroy(own_stream);
+}
+
+// Device arrays of the inputs (allocated once per handle).
+ccsdt_status ccsdt_handle::ensure_inputs() {
+  if(eo) return CCSDT_OK;
+  const size_t o = this->o, v = this->v;
+  const size_t n_t2 = o * o * v * v, n_ooov = o * o * o * v;
+  ccsdt_status s;
+  if((s = alloc(&eo, o)) || (s = alloc(&ev, v)) || (s = alloc(&t1, o * v)) || (s = alloc(&t2, n_t2)) ||
+     (s = alloc(&oovv, n_t2)) || (s = alloc(&ooov, n_ooov)) || (s = alloc(&ovvv, o * v * v * v)) ||
+     (s = alloc(&t2h, n_t2)) || (s = alloc(&ooovh, n_ooov)))
+    return s;
+  if(cudaMalloc((void**) &d_count, sizeof(unsigned long long)) != cudaSuccess) {
+    d_count = nullptr;
+    cudaGetLastError();
+    return fail(CCSDT_E_OOM, "cudaMalloc of the error counter failed");
+  }
+  owned_bytes.push_back(d_count);
+  return CCSDT_OK;
+}
+
+// After the inputs are in place: finiteness of every input, the kappa-contiguous copies for the
+// l-sum contractions, and the handle marked ready (digit planes of earlier inputs dropped).
+ccsdt_status ccsdt_handle::finish_inputs(const char* who) {
+  const size_t o = this->o, v = this->v;
+  struct {
+    const double* p;
+    size_t        n;
+  } in[] = {{eo, o}, {ev, v}, {t1, o * v}, {t2, o * o * v * v}, {oovv, o * o * v * v}, {ooov, o * o * o * v},
+            {ovvv, o * v * v * v}};
+  CK_H(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), stream));
+  for(auto& c: in) {
+    nonfinite_count_kernel<<<1024, 256, 0, stream>>>(c.p, (long long) c.n, d_count);
+    CK_H(cudaGetLastError());
+  }
+  transpose_mid_kernel<<<2048, 256, 0, stream>>>(t2, t2h, (int) o, (int) o, (long long) (v * v));
+  CK_H(cudaGetLastError());
+  transpose_mid_kernel<<<1024, 256, 0, stream>>>(ooov, ooovh, (int) o, (int) o, (long long) (o * v));
+  CK_H(cudaGetLastError());
+  unsigned long long bad = 0;
+  CK_H(cudaMemcpyAsync(&bad, d_count, sizeof(bad), cudaMemcpyDeviceToHost, stream));
+  CK_H(cudaStreamSynchronize(stream));
+  uploaded = false;
+  if(bad) return fail(CCSDT_E_NONFINITE, std::string(who) + ": " + std::to_string(bad) + " non-finite input values");
+  uploaded     = true;
+  slices_ready = 0;
+  return CCSDT_OK;
 }
 
 extern "C" {
@@ -166,50 +222,20 @@ ccsdt_status ccsdt_upload(ccsdt_handle* h, const double* eps_occ, const double* 
   if(!eps_occ || !eps_vir || !t1 || !t2 || !oovv || !ooov || !ovvv)
     return h->fail(CCSDT_E_INVALID, "ccsdt_upload: null input pointer");
   CK(cudaSetDevice(h->device));
+  ccsdt_status s;
+  if((s = h->ensure_inputs())) return s;
+  h->blocks_open = false;
   const size_t o = h->o, v = h->v;
-  const size_t n_eo = o, n_ev = v, n_t1 = o * v, n_t2 = o * o * v * v, n_oovv = n_t2,
-               n_ooov = o * o * o * v, n_ovvv = o * v * v * v;
-  if(!h->eo) {
-    ccsdt_status s;
-    if((s = h->alloc(&h->eo, n_eo)) || (s = h->alloc(&h->ev, n_ev)) || (s = h->alloc(&h->t1, n_t1)) ||
-       (s = h->alloc(&h->t2, n_t2)) || (s = h->alloc(&h->oovv, n_oovv)) ||
-       (s = h->alloc(&h->ooov, n_ooov)) || (s = h->alloc(&h->ovvv, n_ovvv)) ||
-       (s = h->alloc(&h->t2h, n_t2)) || (s = h->alloc(&h->ooovh, n_ooov)))
-      return s;
-    if(cudaMalloc((void**) &h->d_count, sizeof(unsigned long long)) != cudaSuccess) {
-      cudaGetLastError();
-      return h->fail(CCSDT_E_OOM, "cudaMalloc of the error counter failed");
-    }
-    h->owned_bytes.push_back(h->d_count);
-  }
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   struct {
     double*       dst;
     const double* src;
     size_t        n;
-  } cp[] = {{h->eo, eps_occ, n_eo},  {h->ev, eps_vir, n_ev},     {h->t1, t1, n_t1},
-            {h->t2, t2, n_t2},       {h->oovv, oovv, n_oovv},    {h->ooov, ooov, n_ooov},
-            {h->ovvv, ovvv, n_ovvv}};
+  } cp[] = {{h->eo, eps_occ, o},          {h->ev, eps_vir, v},          {h->t1, t1, o * v},
+            {h->t2, t2, o * o * v * v},   {h->oovv, oovv, o * o * v * v}, {h->ooov, ooov, o * o * o * v},
+            {h->ovvv, ovvv, o * v * v * v}};
   for(auto& c: cp) CK(cudaMemcpyAsync(c.dst, c.src, c.n * sizeof(double), kind, h->stream));
-  // finiteness of every input
-  CK(cudaMemsetAsync(h->d_count, 0, sizeof(unsigned long long), h->stream));
-  for(auto& c: cp) {
-    nonfinite_count_kernel<<<1024, 256, 0, h->stream>>>(c.dst, (long long) c.n, h->d_count);
-    CK(cudaGetLastError());
-  }
-  // kappa-contiguous copies for the l-sum contractions
-  transpose_mid_kernel<<<2048, 256, 0, h->stream>>>(h->t2, h->t2h, (int) o, (int) o, (long long) (v * v));
-  CK(cudaGetLastError());
-  transpose_mid_kernel<<<1024, 256, 0, h->stream>>>(h->ooov, h->ooovh, (int) o, (int) o, (long long) (o * v));
-  CK(cudaGetLastError());
-  unsigned long long bad = 0;
-  CK(cudaMemcpyAsync(&bad, h->d_count, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
-  CK(cudaStreamSynchronize(h->stream));
-  h->uploaded = false;
-  if(bad) return h->fail(CCSDT_E_NONFINITE, "ccsdt_upload: " + std::to_string(bad) + " non-finite input values");
-  h->uploaded = true;
-  h->slices_ready = 0;
-  return CCSDT_OK;
+  return h->finish_inputs("ccsdt_upload");
 }
 
 } // extern "C"

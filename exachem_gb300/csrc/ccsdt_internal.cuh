@@ -63,6 +63,15 @@ struct ccsdt_handle {
   ccsdt_status fail(ccsdt_status s, const std::string& msg);
   ccsdt_status alloc(double** p, size_t n);
   ccsdt_status ensure_scratch();
+  ccsdt_status ensure_inputs();
+  ccsdt_status finish_inputs(const char* who);
+  // device-side retile of spin-orbital tile blocks (ccsdt_upload_blocks)
+  double*      blk_stage = nullptr;    // device staging of a call's block data
+  long long    blk_stage_cap = 0;      // doubles
+  int*         blk_meta = nullptr;     // per block: 4 tile ids + 2 offset words
+  long         blk_meta_cap = 0;
+  int*         blk_tiles = nullptr;    // occupied / virtual tile offsets and extents
+  bool         blocks_open = false;    // between ccsdt_upload_begin and ccsdt_upload_end
   ccsdt_status ensure_triplet_slots(long n);
   ccsdt_status run_triplet_fp64(int i, int j, int k, double* eout);
   ccsdt_status run_list(const ccsdt_opts* opts, long n, const int* tri_host);

@@ -112,6 +112,30 @@ ccsdt_status ccsdt_upload(ccsdt_handle* h, const double* eps_occ, const double* 
  * the same 12 v^3 (o + v) flops, so a static split is balanced and needs no counter. */
 ccsdt_status ccsdt_shard_triplets(int o, int shard_index, int shard_count, long* n, int* tri);
 
+/* Device-side retile of ExaChem's spin-orbital tile blocks: instead of gathering the spatial
+ * arrays of ccsdt_upload on the host, hand over the blocks as Tensor::get returns them (row-major
+ * in the tensor's index order); the library copies them to the device and scatters them into its
+ * arrays with one kernel (the gathers at ccsd_t_all_fused_doubles1.hpp:216-246,
+ * ccsd_t_all_fused_doubles2.hpp:211-239,335-343 transpose each block on the host).
+ *   ccsdt_upload_begin(h, eps_occ, eps_vir, t1, on_device)   small inputs; the four-index arrays zeroed
+ *   ccsdt_upload_blocks(h, kind, n, tiles[4n], offsets[n], data, data_len, on_device)   any number
+ *   ccsdt_upload_end(h)                                      finiteness check, repacks; ready
+ * tiles: per block the positions of its four tiles in the layout's occupied / virtual tile lists
+ * (alpha tiles; beta blocks are not needed for the closed shell), in the block's index order;
+ * offsets: element offset of each block in data (data_len doubles).  Blocking (the caller may
+ * reuse its buffers when the call returns).  No counterpart as a call in the reference. */
+typedef enum {
+  CCSDT_BLOCKS_T2   = 0, /* t2(a_alpha, b_beta, i_alpha, j_beta) block (A, B, I, J), [a][b][i][j]      */
+  CCSDT_BLOCKS_OOVV = 1, /* v2ijab(i_a, j_b, a_a, b_b) = (ia|jb) block (I, J, A, B), [i][j][a][b]     */
+  CCSDT_BLOCKS_OOOV = 2, /* v2ijka(i_a, k_b, j_a, a_b) = (ij|ka) block (I, K, J, A), [i][k][j][a]     */
+  CCSDT_BLOCKS_OVVV = 3  /* v2iabc(i_a, b_b, a_a, c_b) = (ia|bc) block (I, B, A, C), [i][b][a][c]     */
+} ccsdt_block_kind;
+ccsdt_status ccsdt_upload_begin(ccsdt_handle* h, const double* eps_occ, const double* eps_vir, const double* t1,
+                                int on_device);
+ccsdt_status ccsdt_upload_blocks(ccsdt_handle* h, int kind, long n, const int* tiles, const long long* offsets,
+                                 const double* data, long long data_len, int on_device);
+ccsdt_status ccsdt_upload_end(ccsdt_handle* h);
+
 /* Full (T): E[T] and E(T) over every occupied triplet of the shard in opts.  Blocking. */
 ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, ccsdt_result* out);
 

@@ -188,6 +188,75 @@ inline std::vector<float> slice_model_from_env() {
   return read_slice_model(p);
 }
 
+// Uploads ExaChem's tiled inputs to a handle with the device-side retile (ccsdt_upload_begin /
+// blocks / end): each alpha / alpha-beta block is read with Tensor::get - the call the reference's
+// gathers make - into a host staging buffer of at most `stage_doubles` and handed over as is; the
+// scatter into the spatial arrays runs on the GPU.  Only t1 and the orbital energies are gathered
+// on the host (o v + o + v numbers).
+template<typename T, typename TensorT, typename V2T>
+void upload_tiled(ccsdt_handle* h, const std::vector<size_t>& mo_tiles, size_t noa, size_t nva, TensorT& d_t1,
+                  TensorT& d_t2, V2T& d_v2, const std::vector<T>& k_evl_sorted, size_t stage_doubles = 1u << 26) {
+  std::vector<size_t> ot(mo_tiles.begin(), mo_tiles.begin() + noa);
+  std::vector<size_t> vt(mo_tiles.begin() + 2 * noa, mo_tiles.begin() + 2 * noa + nva);
+  const auto   oo = detail::offsets(ot), vo = detail::offsets(vt);
+  const size_t o = oo.back() + ot.back(), v = vo.back() + vt.back();
+  auto check = [&](ccsdt_status st, const char* what) {
+    if(st != CCSDT_OK) throw std::runtime_error(std::string(what) + ": " + ccsdt_last_error(h));
+  };
+  std::vector<double> eo(k_evl_sorted.begin(), k_evl_sorted.begin() + o);
+  std::vector<double> ev(k_evl_sorted.begin() + 2 * o, k_evl_sorted.begin() + 2 * o + v);
+  std::vector<double> t1(o * v, 0.0);
+  std::vector<T>      buf;
+  for(size_t A = 0; A < nva; A++)
+    for(size_t I = 0; I < noa; I++) {
+      d_t1.get({A, I}, buf); // [a][i]
+      for(size_t a = 0; a < vt[A]; a++)
+        for(size_t i = 0; i < ot[I]; i++) t1[(oo[I] + i) * v + vo[A] + a] = buf[a * ot[I] + i];
+    }
+  check(ccsdt_upload_begin(h, eo.data(), ev.data(), t1.data(), 0), "ccsdt_upload_begin");
+  std::vector<double>    stage;
+  std::vector<int>       tiles;
+  std::vector<long long> offs;
+  stage.reserve(stage_doubles);
+  auto flush = [&](int kind) {
+    if(offs.empty()) return;
+    check(ccsdt_upload_blocks(h, kind, (long) offs.size(), tiles.data(), offs.data(), stage.data(),
+                              (long long) stage.size(), 0),
+          "ccsdt_upload_blocks");
+    stage.clear(), tiles.clear(), offs.clear();
+  };
+  // one block: Tensor::get (through `fetch`), appended to the staging buffer with its four tile
+  // positions
+  auto add = [&](int kind, auto&& fetch, std::initializer_list<size_t> pos) {
+    fetch(buf);
+    if(stage.size() + buf.size() > stage_doubles) flush(kind);
+    offs.push_back((long long) stage.size());
+    for(size_t p: pos) tiles.push_back((int) p);
+    stage.insert(stage.end(), buf.begin(), buf.end());
+  };
+  for(size_t A = 0; A < nva; A++)
+    for(size_t B = 0; B < nva; B++)
+      for(size_t I = 0; I < noa; I++)
+        for(size_t J = 0; J < noa; J++) add(CCSDT_BLOCKS_T2, [&](std::vector<T>& b) { d_t2.get({A, B + nva, I, J + noa}, b); }, {A, B, I, J});
+  flush(CCSDT_BLOCKS_T2);
+  for(size_t I = 0; I < noa; I++)
+    for(size_t J = 0; J < noa; J++)
+      for(size_t A = 0; A < nva; A++)
+        for(size_t B = 0; B < nva; B++) add(CCSDT_BLOCKS_OOVV, [&](std::vector<T>& b) { d_v2.v2ijab.get({I, J + noa, A, B + nva}, b); }, {I, J, A, B});
+  flush(CCSDT_BLOCKS_OOVV);
+  for(size_t I = 0; I < noa; I++)
+    for(size_t K = 0; K < noa; K++)
+      for(size_t J = 0; J < noa; J++)
+        for(size_t A = 0; A < nva; A++) add(CCSDT_BLOCKS_OOOV, [&](std::vector<T>& b) { d_v2.v2ijka.get({I, K + noa, J, A + nva}, b); }, {I, K, J, A});
+  flush(CCSDT_BLOCKS_OOOV);
+  for(size_t I = 0; I < noa; I++)
+    for(size_t B = 0; B < nva; B++)
+      for(size_t A = 0; A < nva; A++)
+        for(size_t C = 0; C < nva; C++) add(CCSDT_BLOCKS_OVVV, [&](std::vector<T>& b) { d_v2.v2iabc.get({I, B + nva, A, C + nva}, b); }, {I, B, A, C});
+  flush(CCSDT_BLOCKS_OVVV);
+  check(ccsdt_upload_end(h), "ccsdt_upload_end");
+}
+
 // Runs (T) on the spatial inputs through the C ABI: returns (E[T], E(T), device seconds).
 // device -1 = the calling thread's current CUDA device.
 inline std::tuple<double, double, double> run_closed_shell(const SpatialInputs& S, int device,
@@ -210,6 +279,45 @@ inline std::tuple<double, double, double> run_closed_shell(const SpatialInputs& 
   }
   ccsdt_destroy(h);
   return {r.e_bracket_T, r.e_paren_T, r.seconds};
+}
+
+// The whole drop-in call on ExaChem's tiled tensors: handle on the current CUDA device, inputs
+// through the device-side retile, (T) for this rank's shard; returns the reference driver's tuple
+// (E[T], E(T), device seconds, wall seconds since t0).
+template<typename T, typename TensorT, typename V2T>
+std::tuple<T, T, double, double> run_tiled(const std::vector<size_t>& mo, size_t noa, size_t nva, TensorT& d_t1,
+                                           TensorT& d_t2, V2T& d_v2, const std::vector<T>& k_evl_sorted,
+                                           ccsdt_opts op, std::chrono::steady_clock::time_point t0,
+                                           int device = -1) {
+  std::vector<int> ot, vt;
+  for(size_t t = 0; t < noa; t++) ot.push_back((int) mo[t]);
+  for(size_t t = 0; t < nva; t++) vt.push_back((int) mo[2 * noa + t]);
+  int o = 0, v = 0;
+  for(int x: ot) o += x;
+  for(int x: vt) v += x;
+  ccsdt_layout  L{o, v, (int) ot.size(), ot.data(), (int) vt.size(), vt.data()};
+  ccsdt_handle* h  = nullptr;
+  ccsdt_status  st = ccsdt_create(&h, &L, device);
+  if(st != CCSDT_OK) throw std::runtime_error(std::string("ccsdt_create: ") + ccsdt_status_string(st));
+  try {
+    upload_tiled<T>(h, mo, noa, nva, d_t1, d_t2, d_v2, k_evl_sorted);
+    std::vector<float> model;
+    if(op.mode == CCSDT_MODE_LEARNED) {
+      model = slice_model_from_env();
+      // every rank's call is one part of the whole: it is held to its share of the budget
+      op.budget_triplets = o * (o + 1) * (o + 2) / 6;
+      st                 = ccsdt_set_slice_model(h, model.data());
+    }
+    ccsdt_result r{};
+    if(st == CCSDT_OK) st = ccsdt_energy(h, &op, &r);
+    if(st != CCSDT_OK) throw std::runtime_error(std::string("ccsdt: ") + ccsdt_last_error(h));
+    ccsdt_destroy(h);
+    const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return {(T) r.e_bracket_T, (T) r.e_paren_T, r.seconds, total};
+  } catch(...) {
+    ccsdt_destroy(h);
+    throw;
+  }
 }
 
 } // namespace exachem_gb300
@@ -235,20 +343,10 @@ public:
     std::vector<size_t> mo;
     for(auto x: MO.input_tile_sizes()) mo.push_back((size_t) x);
     const size_t noa = MO("occ_alpha").num_tiles(), nva = MO("virt_alpha").num_tiles();
-    auto         S   = exachem_gb300::gather_closed_shell<T>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl_sorted);
     ccsdt_opts   op = exachem_gb300::opts_from_env();
     op.shard_index  = (int) ec.pg().rank().value();
     op.shard_count  = (int) ec.pg().size().value();
-    std::vector<float> model;
-    if(op.mode == CCSDT_MODE_LEARNED) {
-      model = exachem_gb300::slice_model_from_env();
-      // every rank's call is one part of the whole: it is held to its share of the budget
-      op.budget_triplets = S.o * (S.o + 1) * (S.o + 2) / 6;
-    }
-    auto [e4, e5, work] =
-      exachem_gb300::run_closed_shell(S, /*current device*/ -1, op, model.empty() ? nullptr : &model);
-    double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    return {(T) e4, (T) e5, work, total};
+    return exachem_gb300::run_tiled<T>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl_sorted, op, t0);
   }
 };
 #endif

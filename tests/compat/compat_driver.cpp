@@ -52,6 +52,16 @@ int main(int argc, char** argv) {
   std::ofstream g(argv[2], std::ios::binary);
   for(auto* a: {&S.eps_occ, &S.eps_vir, &S.t1, &S.t2, &S.oovv, &S.ooov, &S.ovvv})
     g.write(reinterpret_cast<const char*>(a->data()), sizeof(double) * a->size());
+  if(argc > 3 && std::string(argv[3]) == "--run-tiled") {
+    // the drop-in path: blocks through the device-side retile, then the (T) call
+    ccsdt_opts op{};
+    op.mode = CCSDT_MODE_FP64;
+    auto [e4, e5, secs, total] = exachem_gb300::run_tiled<double>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl, op,
+                                                                 std::chrono::steady_clock::now(), 0);
+    g.write(reinterpret_cast<const char*>(&e4), sizeof(double));
+    g.write(reinterpret_cast<const char*>(&e5), sizeof(double));
+    std::printf("E[T] %.17g E(T) %.17g (%.3f s device, %.3f s total)\n", e4, e5, secs, total);
+  }
   if(argc > 3 && std::string(argv[3]) == "--run") {
     ccsdt_opts op{};
     op.mode = CCSDT_MODE_FP64;
