@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
   uint64_t* drain     = lvl_empty + 3;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* gate_stop  = abort_flag + 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if(threadIdx.x == 0) {
@@ -77,6 +78,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
     }
     sm100::mbar_init(drain, 1);
     *abort_flag = 0;
+    *gate_stop  = 0;
     sm100::mbar_fence_init();
   }
   if(warp == 1) {
@@ -145,42 +147,63 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
         if(!sm100::mbar_wait(&empty[u % STAGES], (u / STAGES) & 1)) fail();
     }
   } else if(warp == 1) {
-    // ------------------------------------------------------------ MMA issuer
-    if(lane == 0) {
-      int  stage_it = 0, term_it = 0;
-      bool ok       = true;
-      for(unsigned kk = 0; ok && !*abort_flag && kk < n_mine; kk++) { // the MMAs need no item data
-        for(int t = 0; t < PZ_TERMS && ok; t++, term_it++) {
-          const int Kp  = t < 2 ? P.kp_v : P.kp_o;
-          const int buf = term_it % C::NBUF;
-          if(term_it >= C::NBUF && !sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1)) {
-            fail();
-            ok = false;
+    // ------------------------------------------------------------ MMA issuer (lane 0 issues; the
+    // gate warp does its waits, see pz_gate_sync)
+    int  stage_it = 0, term_it = 0;
+    bool go       = true;
+    for(unsigned kk = 0; go && kk < n_mine; kk++) { // the MMAs need no item data
+      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
+        const int      Kp    = t < 2 ? P.kp_v : P.kp_o;
+        const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
+        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
+          pz_gate_sync();
+          if(*gate_stop) {
+            go = false;
             break;
           }
-          sm100::tc_fence_after();
-          const uint32_t dbase = tmem + buf * S * NT;
-          for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
-            const int s = stage_it % STAGES, use = stage_it / STAGES;
-            if(!sm100::mbar_wait(&full[s], use & 1)) {
-              fail();
-              ok = false;
-              break;
-            }
+          if(lane == 0) {
             sm100::tc_fence_after();
-            const uint32_t a = sm100::smem_u32(smem + s * C::STAGE_BYTES);
+            const uint32_t a = sm100::smem_u32(smem + (stage_it % STAGES) * C::STAGE_BYTES);
             pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, k0 == 0);
-            sm100::mma_commit_mc(&empty[s], kBoth); // stage free in this CTA, as seen by both producers
+            sm100::mma_commit_mc(&empty[stage_it % STAGES], kBoth); // stage free here, as seen by both producers
           }
-          if(ok) sm100::mma_commit(&lvl_full[buf]);
+          __syncwarp();
         }
+        if(go && lane == 0) sm100::mma_commit(&lvl_full[term_it % C::NBUF]);
+        __syncwarp();
       }
+    }
+    if(lane == 0) {
       sm100::mma_commit(drain);
       if(!sm100::mbar_wait(drain, 0)) fail();
     }
+  } else if(warp == 2) {
+    // ------------------------------------------------------------ gate: the MMA issuer's waits
+    int  stage_it = 0, term_it = 0;
+    bool go       = true;
+    for(unsigned kk = 0; go && kk < n_mine; kk++) {
+      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
+        const int Kp  = t < 2 ? P.kp_v : P.kp_o;
+        const int buf = term_it % C::NBUF;
+        int       ok  = 1;
+        if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1);
+        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
+          if(lane == 0) {
+            if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1);
+            if(!ok) fail();
+            if(!ok || *abort_flag) *gate_stop = 1;
+          }
+          pz_gate_sync();
+          if(*gate_stop) {
+            go = false;
+            break;
+          }
+        }
+      }
+    }
   } else {
     // ------------------------------------------------------------ epilogue: PZ_EPI warps
-    const int      q = warp & 3, cq = (warp - 2) >> 2; // TMEM lane quarter, column quarter
+    const int      q = warp & 3, cq = (warp - PZ_EPI_W0) >> 2; // TMEM lane quarter, column quarter
     const int      row = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
     const int      c_lo = cq * C::COLS;

@@ -25,8 +25,20 @@
 
 namespace ccsdt {
 
-// 2 role warps (TMA producer, MMA issuer) + PZ_EPI epilogue warps (4 per TMEM lane quarter)
-constexpr int PZ_BM = 128, PZ_KC = 64, PZ_EPI = 16, PZ_THREADS = 64 + 32 * PZ_EPI, PZ_IR = 4, PZ_TERMS = 4;
+// 3 role warps (TMA producer, MMA issuer, gate) + PZ_EPI epilogue warps (4 per TMEM lane quarter)
+constexpr int PZ_BM = 128, PZ_KC = 64, PZ_EPI = 16, PZ_EPI_W0 = 3, PZ_THREADS = 32 * (PZ_EPI_W0 + PZ_EPI), PZ_IR = 4,
+              PZ_TERMS = 4;
+
+// The MMA warp and its gate warp meet at named barrier 1 (64 threads) once per pipeline stage.
+// tcgen05.mma issue proceeds at the tensor pipe's pace (the issuing thread holds only a few MMAs
+// ahead of the pipe), so anything else that thread does between stages idles the pipe for as
+// long: an mbarrier wait there, even on a completed phase, measured 170 - 550 cycles per stage on
+// GB300, against none for a named-barrier rendezvous with a warp that has already done the waits.
+// So the gate warp does every wait of the MMA loop (stage full, TMEM level buffer empty, work
+// items) and the MMA warp only rendezvouses.  Both walk the same stage sequence; a gate that must
+// stop (a bounded wait gave up, the abort flag, the end of the work) sets *stop before the
+// rendezvous and both leave at that same rendezvous, so neither is left waiting at the barrier.
+__device__ __forceinline__ void pz_gate_sync() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
 constexpr unsigned PZ_END = 0xffffffffu;
 
 // map indices (the handle's map table): the d-sum uses 0-2, the l-sum 6-8
@@ -43,7 +55,6 @@ struct PzParams {
   int             nslots;     // triplets per launch
   int             o, v, kp_v, kp_o;
   float2*         F;          // P arrays of slot s: F + s * 3 v^3 (P12, P34, P56 consecutive)
-  const int *     ex_t2, *ex_t2h, *ex_ovvv, *ex_ooovh;
   const unsigned* order;      // cost-ordered item ids, length nitems
   unsigned        nitems;
   unsigned*       queue;      // work counter, 0 at launch
@@ -53,10 +64,7 @@ struct PzParams {
 };
 
 struct PzTerm {
-  int        mapA, mapB, a2, a3, b2, b3, Kp; // maps and their tile coordinates along dims 2, 3
-  const int *eA, *eB;                         // row exponents eA[eA_base + y eA_y], column eB[eB_base + n eB_n]
-  long long  eA_base, eA_y, eB_base, eB_n;
-  float      sign;
+  int mapA, mapB, a2, a3, b2, b3, Kp; // maps and their tile coordinates along dims 2, 3
 };
 
 // The four terms of a job's tile, from (job, t, i, j, k) and the item's x.  The tile holds
@@ -69,9 +77,8 @@ struct PzTerm {
 //   l-sum  job 0: (i,1,k,j) (k,0,i,j)   job 1: (i,0,j,k) (j,1,i,k)   job 2: (j,0,k,i) (k,1,j,i)
 // The l-sum's "natural" pair (first, second) = (n, x) is read through the swapped-stride map.
 __device__ __forceinline__ PzTerm pz_term(const PzParams& P, int job, int t, int i, int j, int k, int x) {
-  const long long v = P.v, o = P.o, v2 = v * v;
-  const int       sel = job * 2 + (t & 1);
-  int             e0, nat, e2, e3;
+  const int sel = job * 2 + (t & 1);
+  int       e0, nat, e2, e3;
   if(t < 2) {
     switch(sel) {
       case 0: e0 = k, nat = 1, e2 = i, e3 = j; break;
@@ -97,17 +104,11 @@ __device__ __forceinline__ PzTerm pz_term(const PzParams& P, int job, int t, int
     T.mapA = nat ? PZ_OVVV_NAT : PZ_OVVV_SWP, T.a2 = x, T.a3 = z;     // rows (z, x, y) or (z, y, x)
     T.mapB = PZ_T2, T.b2 = yy, T.b3 = xx;                            // rows (xx, yy, n)
     T.Kp = P.kp_v;
-    T.eA = P.ex_ovvv, T.eA_base = z * v2 + (nat ? x * v : x), T.eA_y = nat ? 1 : v;
-    T.eB = P.ex_t2, T.eB_base = (xx * o + yy) * v, T.eB_n = 1;
-    T.sign = 1.f;
   } else {
     const int xx = e0, yy = e2, zz = e3;
     T.mapA = PZ_OOOVH_A, T.a2 = zz, T.a3 = yy;                        // rows (yy, zz, y)
     T.mapB = nat ? PZ_T2H_SWP_B : PZ_T2H_NAT_B, T.b2 = x, T.b3 = xx;   // pair rows (n, x) or (x, n)
     T.Kp = P.kp_o;
-    T.eA = P.ex_ooovh, T.eA_base = (yy * o + zz) * v, T.eA_y = 1;
-    T.eB = P.ex_t2h, T.eB_base = xx * v2 + (nat ? x : x * v), T.eB_n = nat ? v : 1;
-    T.sign = -1.f;
   }
   return T;
 }
@@ -130,11 +131,12 @@ __device__ __forceinline__ PzItem pz_decode(unsigned id, int v, int yblocks, int
 }
 
 // Epilogue of one item (shared by the persistent kernels): thread = one tile row (TMEM lane
-// quarter q, row = 32 q + lane) x COLS = NT / 4 columns from c_lo.  Issues the item's exponent
-// loads, then per term waits for the MMAs (lvl_full of the term's buffer), folds the S exact levels
-// with oz_horner in chunks of 8 columns, scales by 2^(e_row + e_col - 7 (S + 1)) and adds in
-// float-float, releases the buffer (lvl_empty); finally stores the tile once.  Returns false when
-// a bounded wait gave up.
+// quarter q, row = 32 q + lane) x COLS = NT / 4 columns from c_lo.  Per term it waits for the MMAs
+// (lvl_full of the term's buffer), folds the S exact levels with oz_horner in chunks of 8 columns
+// and adds (d-sum terms) or subtracts (l-sum terms) them in float-float, releases the buffer
+// (lvl_empty); finally it renormalises, scales by 2^(-7 (S + 1)) and stores the tile once.  The
+// BF16 digits carry the row scales, so the levels need no per-row or per-column factor.  Returns
+// false when a bounded wait gave up.
 template<int S, int NT, int NBUF>
 __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem& w, int nb, const int* tp,
                                                  uint32_t lane_base, int c_lo, int row, int lane, int& term_it,
@@ -142,22 +144,11 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
                                                  volatile int* abort_flag) {
   constexpr int COLS = NT / 4;
   static_assert(COLS % 4 == 0 && COLS <= 32, "epilogue column chunks of 8 (and a last one of 4)");
-  const int     v = P.v;
+  constexpr float kScale = 1.f / float(1ull << (OZ_BITS * (S + 1)));
+  const int       v  = P.v;
   const long long v2 = (long long) v * v;
-  const int  i = tp[0], j = tp[1], k = tp[2];
-  const int  y = w.yb * PZ_BM + row, n0 = nb * NT + c_lo;
-  const bool vrow = y < v;
-  const bool vcol = lane < COLS && n0 + lane < v;
-  const long long nl = n0 + lane;
-  int   ea[PZ_TERMS], eb[PZ_TERMS];
-  float sgn[PZ_TERMS];
-#pragma unroll
-  for(int t = 0; t < PZ_TERMS; t++) {
-    const PzTerm T = pz_term(P, w.job, t, i, j, k, w.x);
-    ea[t]  = vrow ? T.eA[T.eA_base + y * T.eA_y] : 0;
-    eb[t]  = vcol ? T.eB[T.eB_base + nl * T.eB_n] : 0;
-    sgn[t] = T.sign;
-  }
+  const int       y = w.yb * PZ_BM + row, n0 = nb * NT + c_lo;
+  (void) tp;
   // element (y, n) of the tile: P[n][x][y] (consecutive rows -> consecutive addresses)
   float2* Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
   float hi[COLS], lo[COLS];
@@ -165,29 +156,23 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
   for(int e = 0; e < COLS; e++) hi[e] = lo[e] = 0.f;
 #pragma unroll 1
   for(int t = 0; t < PZ_TERMS; t++, term_it++) {
-    const int   buf  = term_it % NBUF;
-    const int   ea_t = t == 0 ? ea[0] : t == 1 ? ea[1] : t == 2 ? ea[2] : ea[3];
-    const int   eb_t = t == 0 ? eb[0] : t == 1 ? eb[1] : t == 2 ? eb[2] : eb[3];
-    const float sg_t = t == 0 ? sgn[0] : t == 1 ? sgn[1] : t == 2 ? sgn[2] : sgn[3];
-    const float sa   = copysignf(oz_pow2(ea_t - OZ_BITS * (S + 1)), sg_t);
-    const float sbl  = oz_pow2(eb_t);
-    const bool  okw  = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it / NBUF) & 1) && !*abort_flag);
+    const int  buf = term_it % NBUF;
+    const bool okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it / NBUF) & 1) && !*abort_flag);
     if(!okw) return false;
     sm100::tc_fence_after();
-    // fold `W` columns starting at c0 whose S levels are in rv
-    auto fold = [&](auto& rv, int c0, auto wtag) {
+    // fold `W` columns starting at c0 whose S levels are in rv; `neg`: an l-sum term
+    auto fold = [&](auto& rv, int c0, auto wtag, bool neg) {
       constexpr int W = decltype(wtag)::value;
 #pragma unroll
       for(int e = 0; e < W; e++) {
-        const float sb = __shfl_sync(0xffffffffu, sbl, c0 + e);
         const ff    x  = oz_horner<S, W>(rv, e);
-        // accumulate without renormalising (exact two-sum of the high words, low words added);
-        // the tile is renormalised once before it is stored
-        const ff    a  = ff_two_sum(hi[c0 + e], (x.hi * sa) * sb);
-        hi[c0 + e]     = a.hi;
-        lo[c0 + e]     = lo[c0 + e] + (a.lo + (x.lo * sa) * sb);
+        const float xh = neg ? -x.hi : x.hi, xl = neg ? -x.lo : x.lo;
+        // two-sum of the high words, low words added; the tile is renormalised before the store
+        const float s = hi[c0 + e] + xh, z = s - hi[c0 + e];
+        lo[c0 + e]    = lo[c0 + e] + (((hi[c0 + e] - (s - z)) + (xh - z)) + xl);
+        hi[c0 + e]    = s;
         if(P.tail) {
-          const float tl = (__uint_as_float(rv[S - 1][e]) * sa) * sb;
+          const float tl = __uint_as_float(rv[S - 1][e]) * kScale;
           tsq            = fmaf(tl, tl, tsq);
         }
       }
@@ -199,55 +184,59 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
       __syncwarp();
       if(lane == 0) sm100::mbar_arrive(&lvl_empty[buf]);
     };
-    if constexpr(S * COLS <= 32) {
-      uint32_t rv[S][COLS]; // every level of the thread's columns in one TMEM round trip
+    auto run = [&](bool neg) {
+      if constexpr(S * COLS <= 32) {
+        uint32_t rv[S][COLS]; // every level of the thread's columns in one TMEM round trip
 #pragma unroll
-      for(int l = 0; l < S; l++) {
-        if constexpr(COLS == 16) sm100::tmem_ld16(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
-        else sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
-      }
-      sm100::tmem_wait_ld();
-      release();
-      fold(rv, 0, std::integral_constant<int, COLS>{});
-    } else {
-      // chunks of 8 columns and, when COLS % 8 == 4, one of 4; every TMEM access starts at a
-      // multiple of its own width (a thread whose first column is 4 mod 8 takes the 4 first)
-      auto chunk8 = [&](int c0, bool last) {
-        uint32_t rv[S][8];
-#pragma unroll
-        for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
+        for(int l = 0; l < S; l++) {
+          if constexpr(COLS == 16) sm100::tmem_ld16(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
+          else sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo, rv[l]);
+        }
         sm100::tmem_wait_ld();
-        if(last) release();
-        fold(rv, c0, std::integral_constant<int, 8>{});
-      };
-      auto chunk4 = [&](int c0, bool last) {
-        uint32_t rv[S][4];
-#pragma unroll
-        for(int l = 0; l < S; l++) sm100::tmem_ld4(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
-        sm100::tmem_wait_ld();
-        if(last) release();
-        fold(rv, c0, std::integral_constant<int, 4>{});
-      };
-      if constexpr(COLS % 8 == 0) {
-#pragma unroll
-        for(int c0 = 0; c0 < COLS; c0 += 8) chunk8(c0, c0 + 8 == COLS);
-      } else if((c_lo & 7) == 4) {
-        chunk4(0, false);
-#pragma unroll
-        for(int c0 = 4; c0 < COLS; c0 += 8) chunk8(c0, c0 + 8 == COLS);
+        release();
+        fold(rv, 0, std::integral_constant<int, COLS>{}, neg);
       } else {
+        // chunks of 8 columns and, when COLS % 8 == 4, one of 4; every TMEM access starts at a
+        // multiple of its own width (a thread whose first column is 4 mod 8 takes the 4 first)
+        auto chunk8 = [&](int c0, bool last) {
+          uint32_t rv[S][8];
 #pragma unroll
-        for(int c0 = 0; c0 + 8 <= COLS; c0 += 8) chunk8(c0, false);
-        chunk4(COLS - 4, true);
+          for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
+          sm100::tmem_wait_ld();
+          if(last) release();
+          fold(rv, c0, std::integral_constant<int, 8>{}, neg);
+        };
+        auto chunk4 = [&](int c0, bool last) {
+          uint32_t rv[S][4];
+#pragma unroll
+          for(int l = 0; l < S; l++) sm100::tmem_ld4(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
+          sm100::tmem_wait_ld();
+          if(last) release();
+          fold(rv, c0, std::integral_constant<int, 4>{}, neg);
+        };
+        if constexpr(COLS % 8 == 0) {
+#pragma unroll
+          for(int c0 = 0; c0 < COLS; c0 += 8) chunk8(c0, c0 + 8 == COLS);
+        } else if((c_lo & 7) == 4) {
+          chunk4(0, false);
+#pragma unroll
+          for(int c0 = 4; c0 < COLS; c0 += 8) chunk8(c0, c0 + 8 == COLS);
+        } else {
+#pragma unroll
+          for(int c0 = 0; c0 + 8 <= COLS; c0 += 8) chunk8(c0, false);
+          chunk4(COLS - 4, true);
+        }
       }
-    }
+    };
+    if(t < 2) run(false); // d-sum terms add, l-sum terms subtract
+    else run(true);
   }
-  if(vrow) {
+  if(y < v) {
 #pragma unroll
     for(int e = 0; e < COLS; e++) {
-      const int n = n0 + e;
+      const int   n = n0 + e;
       const float h = hi[e] + lo[e];
-      if(n < v) Cb[(long long) n * v2] = make_float2(h, lo[e] - (h - hi[e]));
+      if(n < v) Cb[(long long) n * v2] = make_float2(h * kScale, (lo[e] - (h - hi[e])) * kScale);
     }
   }
   return true;
@@ -308,6 +297,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
   unsigned* item_id    = reinterpret_cast<unsigned*>(drain + 1);
   uint32_t* tmem_slot  = item_id + PZ_IR;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  volatile int* gate_stop  = abort_flag + 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if(threadIdx.x == 0) {
@@ -317,7 +307,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     }
     for(int r = 0; r < PZ_IR; r++) {
       sm100::mbar_init(&item_full[r], 1);
-      sm100::mbar_init(&item_empty[r], 1 + PZ_EPI); // MMA thread + one arrival per epilogue warp
+      sm100::mbar_init(&item_empty[r], 1 + PZ_EPI); // gate + one arrival per epilogue warp
     }
     for(int b = 0; b < C::NBUF; b++) {
       sm100::mbar_init(&lvl_full[b], 1);
@@ -325,6 +315,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     }
     sm100::mbar_init(drain, 1);
     *abort_flag = 0;
+    *gate_stop  = 0;
     sm100::mbar_fence_init();
   }
   if(warp == 1) {
@@ -380,49 +371,80 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         if(!sm100::mbar_wait(&full[u % STAGES], (u / STAGES) & 1)) fail();
     }
   } else if(warp == 1) {
-    // ------------------------------------------------------------ MMA issuer
-    if(lane == 0) {
-      int stage_it = 0, term_it = 0;
-      for(int it = 0;; it++) {
-        const int r = it % PZ_IR;
-        if(!sm100::mbar_wait(&item_full[r], (it / PZ_IR) & 1)) {
-          fail();
-          break;
-        }
-        const unsigned id = item_id[r];
-        sm100::mbar_arrive(&item_empty[r]);
-        if(id == PZ_END) break;
-        for(int t = 0; t < PZ_TERMS; t++, term_it++) {
-          const int Kp  = t < 2 ? P.kp_v : P.kp_o;
-          const int buf = term_it % C::NBUF;
-          if(term_it >= C::NBUF && !sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1)) {
-            fail();
+    // ------------------------------------------------------------ MMA issuer (lane 0 issues)
+    // The MMAs need no item data: every item is the same sequence of terms and stages, and the
+    // gate says when the work ends.
+    int  stage_it = 0, term_it = 0;
+    bool go       = true;
+    while(go) {
+      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
+        const int      Kp    = t < 2 ? P.kp_v : P.kp_o;
+        const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
+        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
+          pz_gate_sync();
+          if(*gate_stop) {
+            go = false;
             break;
           }
-          sm100::tc_fence_after();
-          const uint32_t dbase = tmem + buf * S * NT;
-          for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
-            const int s = stage_it % STAGES, use = stage_it / STAGES;
-            if(!sm100::mbar_wait(&full[s], use & 1)) {
-              fail();
-              break;
-            }
+          if(lane == 0) {
             sm100::tc_fence_after();
-            const uint32_t a = sm100::smem_u32(smem + s * C::STAGE_BYTES);
+            const uint32_t a = sm100::smem_u32(smem + (stage_it % STAGES) * C::STAGE_BYTES);
             pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, k0 == 0);
-            sm100::mma_commit(&empty[s]);
+            sm100::mma_commit(&empty[stage_it % STAGES]);
           }
-          sm100::mma_commit(&lvl_full[buf]);
+          __syncwarp();
         }
-        if(*abort_flag) break;
+        if(go && lane == 0) sm100::mma_commit(&lvl_full[term_it % C::NBUF]);
+        __syncwarp();
       }
+    }
+    if(lane == 0) {
       sm100::mma_commit(drain);
       if(!sm100::mbar_wait(drain, 0)) fail();
+    }
+  } else if(warp == 2) {
+    // ------------------------------------------------------------ gate: the MMA issuer's waits
+    int  stage_it = 0, term_it = 0;
+    bool go       = true;
+    for(int it = 0; go; it++) {
+      const int r  = it % PZ_IR;
+      int       ok = 1;
+      unsigned  id = PZ_END;
+      if(lane == 0) {
+        ok = sm100::mbar_wait(&item_full[r], (it / PZ_IR) & 1);
+        if(ok) {
+          id = item_id[r];
+          sm100::mbar_arrive(&item_empty[r]);
+        } else
+          fail();
+        if(!ok || id == PZ_END) *gate_stop = 1;
+      }
+      if(__shfl_sync(0xffffffffu, ok && id != PZ_END, 0) == 0) { // the issuer's next rendezvous ends it
+        pz_gate_sync();
+        break;
+      }
+      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
+        const int Kp  = t < 2 ? P.kp_v : P.kp_o;
+        const int buf = term_it % C::NBUF;
+        if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1);
+        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
+          if(lane == 0) {
+            if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1);
+            if(!ok) fail();
+            if(!ok || *abort_flag) *gate_stop = 1;
+          }
+          pz_gate_sync();
+          if(*gate_stop) {
+            go = false;
+            break;
+          }
+        }
+      }
     }
   } else {
     // ------------------------------------------------------------ epilogue: PZ_EPI warps
     // Thread = one tile row (TMEM lane) x a quarter of the tile's columns (pz_epilogue_item).
-    const int      q = warp & 3, cq = (warp - 2) >> 2;     // TMEM lane quarter, column quarter
+    const int      q = warp & 3, cq = (warp - PZ_EPI_W0) >> 2; // TMEM lane quarter, column quarter
     const int      row = q * 32 + lane;
     const uint32_t lane_base = tmem + ((uint32_t) (q * 32) << 16);
     const int      c_lo = cq * C::COLS;

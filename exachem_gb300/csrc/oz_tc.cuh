@@ -29,10 +29,10 @@ struct TcTerm {
   int        mapA, mapB;         // indices into TcBatch::maps
   int        az;                 // A coordinate of the slab (dim 3); dims 1, 2 are the tile's (y, x)
   int        by, bx;             // B coordinates of the single rows (dims 2, 3 of map B)
-  const int* eA;                 // exponent of A row: eA[rid]
+  const int* eA;                 // exponent of A row: eA[rid] (nullptr: the digits carry it)
   long long  eA_x, eA_y;         // rid = eA_base + x * eA_x + y * eA_y
   long long  eA_base;
-  const int* eB;                 // exponent of B row n: eB[n]
+  const int* eB;                 // exponent of B row n: eB[n] (nullptr: the digits carry it)
   int        Kp;                 // contraction length (multiple of 64, <= 512)
   float      sign;
 };
@@ -196,13 +196,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
         break;
       }
       sm100::tc_fence_after();
-      const int ea = vrow ? T.eA[T.eA_base + (long long) x * T.eA_x + (long long) y * T.eA_y] : 0;
+      const int ea = vrow && T.eA ? T.eA[T.eA_base + (long long) x * T.eA_x + (long long) y * T.eA_y] : 0;
       const bool last = (t == J.nterms - 1);
       for(int c0 = 0; c0 < NT; c0 += 16) {
         float hi[16], lo[16];
         int   eb[16];
 #pragma unroll
-        for(int e = 0; e < 16; e++) eb[e] = (n0 + c0 + e < v) ? T.eB[n0 + c0 + e] : 0;
+        for(int e = 0; e < 16; e++) eb[e] = (T.eB && n0 + c0 + e < v) ? T.eB[n0 + c0 + e] : 0;
         if(t == 0) {
 #pragma unroll
           for(int e = 0; e < 16; e++) hi[e] = lo[e] = 0.f;

@@ -81,35 +81,45 @@ __device__ __forceinline__ float oz_pow2(int e) {
   return e < -126 ? 0.f : __int_as_float((min(e, 128) + 127) << 23);
 }
 
-// Horner fold of S exact level sums (integers held in FP32, most significant first) into
-// float-float: returns X = sum_l L[l] 2^{7 (S - 1 - l)}.  Each step multiplies by 2^7 (exact)
-// and adds the next level with an error-free two-sum, so the only rounding is in the low word
-// (relative 2^-48); X < 2^{24 + 7 (S - 1)} stays far inside the FP32 range.
+// Horner fold of S exact level sums (most significant first) into an unnormalised float-float
+// X = sum_l L[l] 2^{7 (S - 1 - l)}.  Each level is an integer multiple of one power of two g (the
+// element's row-scale product, carried by the BF16 digits), |L| < 2^24 g.  A step is Fast2Sum of
+// a = 128 hi (exact) and b = L[l]: s = fl(a + b), z = fl(s - a), e = b - z.  It is error-free
+// here in either order of |a|, |b|: for |a| >= |b| by Dekker's theorem; for |a| < |b| both are
+// integer multiples of g below 2^24 g, so the rounding error of s is 0 or +-g and s - a = b + error
+// is a multiple of g below 2^24 g, held exactly.  fma forms the 128 hi products without rounding
+// (4 operations per level; the first level's low word is e itself).  The result is exact for
+// S <= 4; at S = 5 the low-word update can round (relative < 2^-46).  The caller renormalises
+// once, after its last addition.
 template<int S, int W = 16>
 __device__ __forceinline__ ff oz_horner(const uint32_t (&L)[S][W], int e) {
   float hi = __uint_as_float(L[0][e]), lo = 0.f;
 #pragma unroll
   for(int l = 1; l < S; l++) {
-    const float a = hi * 128.f, b = __uint_as_float(L[l][e]);
-    const float s = a + b, z = s - a;
-    lo = fmaf(lo, 128.f, (a - (s - z)) + (b - z));
-    hi = s;
+    const float b = __uint_as_float(L[l][e]);
+    const float s = fmaf(hi, 128.f, b), z = fmaf(hi, -128.f, s);
+    lo            = l == 1 ? b - z : fmaf(lo, 128.f, b - z);
+    hi            = s;
   }
-  const float h = hi + lo;
-  return ff{h, lo - (h - hi)};
+  return ff{hi, lo};
 }
 
 // ---------------------------------------------------------------------------------- slicing
 // Rows of a dense FP64 array [R][K] -> S digit planes [S][R][Kp] (Kp >= K, zero padded) and
-// exponents e[R].  One warp per row.
+// exponents e[R].  One warp per row.  Row r ~ 2^e[r] sum_p d_p 2^{-7 (p + 1)} with integer digits
+// |d_0| <= 127, |d_p| <= 64.  BF16 planes hold d_p 2^e[r] (exact: 7 significant bits), so every
+// product in a contraction's dot product for output (y, n) carries the same power of two
+// 2^(e_y + e_n) and the level sums stay exact integer multiples of it; the epilogues need no row
+// or column scale.  Rows under 2^-126 flush to zero digits.  INT8 planes hold d_p and the kernels
+// that read them scale by the exponents.
 template<typename T>
-__device__ __forceinline__ T oz_digit(double d);
+__device__ __forceinline__ T oz_digit(double d, int e);
 template<>
-__device__ __forceinline__ __nv_bfloat16 oz_digit<__nv_bfloat16>(double d) {
-  return __float2bfloat16_rn((float) d);
+__device__ __forceinline__ __nv_bfloat16 oz_digit<__nv_bfloat16>(double d, int e) {
+  return __float2bfloat16_rn((float) d * oz_pow2(e));
 }
 template<>
-__device__ __forceinline__ int8_t oz_digit<int8_t>(double d) {
+__device__ __forceinline__ int8_t oz_digit<int8_t>(double d, int) {
   return (int8_t) (int) d;
 }
 
@@ -133,7 +143,7 @@ __global__ void oz_slice_rows_kernel(const double* __restrict__ x, long long R, 
         y        = y * 128.0;
         double d = rint(y);
         y        = y - d;
-        out[(long long) p * plane + r * Kp + k] = oz_digit<T>(d);
+        out[(long long) p * plane + r * Kp + k] = oz_digit<T>(d, e);
       }
     }
   }
@@ -152,7 +162,7 @@ inline OzRows oz_swapped(int q) { return OzRows{1, q, q}; } // r = x q + y -> y 
 
 struct OzTerm {
   const void* A;       // digit planes of A: plane stride planeA elements
-  const int*  eA;      // exponents, indexed by rid
+  const int*  eA;      // exponents, indexed by rid (nullptr: BF16 digits that carry their row scale)
   OzRows      ma;
   long long   planeA;
   const void* B;

@@ -251,7 +251,7 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   static_assert(sizeof(p.maps) == sizeof(tmaps), "the persistent kernel takes every map");
   std::memcpy(p.maps, tmaps, sizeof(p.maps));
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
-  p.F = bt_F, p.ex_t2 = ex_t2, p.ex_t2h = ex_t2h, p.ex_ovvv = ex_ovvv, p.ex_ooovh = ex_ooovh;
+  p.F = bt_F;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
   const int  NT  = pz_nt(S);
   const long per = items_per_slot(v, NT, pz_pair);

@@ -96,14 +96,14 @@ __global__ void __launch_bounds__(OZ_THREADS) oz_gemm_kernel(const __grid_consta
 #pragma unroll
       for(int h = 0; h < 2; h++) {
         long long m = m0 + wm + x * 16 + g + h * 8;
-        ea[x][h]    = m < J.M ? T_.eA[oz_rid(T_.ma, m)] : 0;
+        ea[x][h]    = m < J.M && T_.eA ? T_.eA[oz_rid(T_.ma, m)] : 0;
       }
 #pragma unroll
     for(int y = 0; y < 2; y++)
 #pragma unroll
       for(int e = 0; e < 2; e++) {
         long long n = n0 + wn + y * 8 + 2 * t + e;
-        eb[y][e]    = n < J.N ? T_.eB[oz_rid(T_.mb, n)] : 0;
+        eb[y][e]    = n < J.N && T_.eB ? T_.eB[oz_rid(T_.mb, n)] : 0;
       }
     const T* Ab = static_cast<const T*>(T_.A);
     const T* Bb = static_cast<const T*>(T_.B);
@@ -528,13 +528,14 @@ ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eo
   ccsdt_status s;
   if((s = ensure_tmaps(S, tc_nt(S)))) return s;
   const long long o = this->o, v = this->v, v2 = v * v;
+  // BF16 digit planes carry their rows' scales: no exponent tables
   auto hole = [&](int xx, bool nat, int yy, int zz) {
-    return TcTerm{nat ? MAP_T2H_NAT : MAP_T2H_SWP, MAP_OOOVH, xx, zz, yy, ex_t2h, nat ? v : 1, nat ? 1 : v,
-                  xx * v2, ex_ooovh + ((long long) yy * o + zz) * v, kp_o, -1.f};
+    return TcTerm{nat ? MAP_T2H_NAT : MAP_T2H_SWP, MAP_OOOVH, xx, zz, yy, nullptr, nat ? v : 1, nat ? 1 : v,
+                  xx * v2, nullptr, kp_o, -1.f};
   };
   auto part = [&](int z, bool nat, int xx, int yy) {
-    return TcTerm{nat ? MAP_OVVV_NAT : MAP_OVVV_SWP, MAP_T2, z, yy, xx, ex_ovvv, nat ? v : 1, nat ? 1 : v,
-                  z * v2, ex_t2 + ((long long) xx * o + yy) * v, kp_v, 1.f};
+    return TcTerm{nat ? MAP_OVVV_NAT : MAP_OVVV_SWP, MAP_T2, z, yy, xx, nullptr, nat ? v : 1, nat ? 1 : v,
+                  z * v2, nullptr, kp_v, 1.f};
   };
   TcBatch b;
   std::memcpy(b.maps, tmaps, sizeof(b.maps)); // the first six maps
@@ -581,11 +582,14 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
   const size_t    esz = variant == 0 ? 2 : 1;
   auto at = [&](const void* base, long long elems) { return (const void*) ((const char*) base + elems * esz); };
   // l-sum: rows of t2h are (x, (a, b)), rows of ooovh are (y, z, c)
+  // BF16 digit planes carry their rows' scales (no exponent tables); INT8 digits do not
+  const bool int8 = variant != 0;
   auto t2h_t = [&](int x, OzRows m) {
-    return std::make_tuple(at(sl_t2h, (long long) x * v2 * kp_o), ex_t2h + (long long) x * v2, m);
+    return std::make_tuple(at(sl_t2h, (long long) x * v2 * kp_o), int8 ? ex_t2h + (long long) x * v2 : nullptr, m);
   };
   auto ooh_t = [&](int y, int z) {
-    return std::make_tuple(at(sl_ooovh, ((long long) y * o + z) * v * kp_o), ex_ooovh + ((long long) y * o + z) * v);
+    return std::make_tuple(at(sl_ooovh, ((long long) y * o + z) * v * kp_o),
+                           int8 ? ex_ooovh + ((long long) y * o + z) * v : nullptr);
   };
   auto hole = [&](int xa, OzRows ma, int yb, int zb) {
     auto [A, eA, mA] = t2h_t(xa, ma);
@@ -604,7 +608,8 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
   // d-sum: rows of t2 are (x, y, a), rows of ovvv are (z, c, b)
   auto part_t = [&](int x, int y, int z, OzRows mb) {
     const long long ra = ((long long) x * o + y) * v, rb = (long long) z * v2;
-    return OzTerm{at(sl_t2, ra * kp_v), ex_t2 + ra, nat, pl_t2, at(sl_ovvv, rb * kp_v), ex_ovvv + rb, mb, pl_ovvv, kp_v, 1.f};
+    return OzTerm{at(sl_t2, ra * kp_v), int8 ? ex_t2 + ra : nullptr, nat, pl_t2, at(sl_ovvv, rb * kp_v),
+                  int8 ? ex_ovvv + rb : nullptr, mb, pl_ovvv, kp_v, 1.f};
   };
   OzBatch pb{};
   pb.S      = S;
