@@ -64,7 +64,6 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
   uint64_t* drain     = lvl_empty + 3;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  volatile int* gate_stop  = abort_flag + 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if(threadIdx.x == 0) {
@@ -78,7 +77,6 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
     }
     sm100::mbar_init(drain, 1);
     *abort_flag = 0;
-    *gate_stop  = 0;
     sm100::mbar_fence_init();
   }
   if(warp == 1) {
@@ -147,30 +145,26 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
         if(!sm100::mbar_wait(&empty[u % STAGES], (u / STAGES) & 1)) fail();
     }
   } else if(warp == 1) {
-    // ------------------------------------------------------------ MMA issuer (lane 0 issues; the
-    // gate warp does its waits, see pz_gate_sync)
-    int  stage_it = 0, term_it = 0;
-    bool go       = true;
-    for(unsigned kk = 0; go && kk < n_mine; kk++) { // the MMAs need no item data
-      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
-        const int      Kp    = t < 2 ? P.kp_v : P.kp_o;
+    // ------------------------------------------------------------ MMA issuer (the warp runs the
+    // loop, lane 0 issues; the gate warp does its waits, see pz_gate_sync).  The MMAs need no item data; between stages the
+    // loop does as little as it can (no modulo, no shared-memory reads).
+    const uint32_t a0 = sm100::smem_u32(smem);
+    uint32_t       a = a0;
+    int            s = 0, term_it = 0;
+    bool           stop = false;
+    for(unsigned kk = 0; !stop && kk < n_mine; kk++) {
+      for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
+        const int      nst   = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
         const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
-        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
-          pz_gate_sync();
-          if(*gate_stop) {
-            go = false;
-            break;
-          }
-          if(lane == 0) {
-            sm100::tc_fence_after();
-            const uint32_t a = sm100::smem_u32(smem + (stage_it % STAGES) * C::STAGE_BYTES);
-            pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, k0 == 0);
-            sm100::mma_commit_mc(&empty[stage_it % STAGES], kBoth); // stage free here, as seen by both producers
-          }
-          __syncwarp();
+        for(int u = 0; u < nst; u++) {
+          if((stop = pz_gate_sync(false))) break;
+          sm100::tc_fence_after();
+          pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
+          sm100::mma_commit_mc_if(&empty[s], kBoth, lane == 0); // stage free here, as seen by both producers
+          a += C::STAGE_BYTES;
+          if(++s == STAGES) s = 0, a = a0;
         }
-        if(go && lane == 0) sm100::mma_commit(&lvl_full[term_it % C::NBUF]);
-        __syncwarp();
+        if(!stop) sm100::mma_commit_if(&lvl_full[term_it % C::NBUF], lane == 0);
       }
     }
     if(lane == 0) {
@@ -180,24 +174,22 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
   } else if(warp == 2) {
     // ------------------------------------------------------------ gate: the MMA issuer's waits
     int  stage_it = 0, term_it = 0;
-    bool go       = true;
-    for(unsigned kk = 0; go && kk < n_mine; kk++) {
-      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
-        const int Kp  = t < 2 ? P.kp_v : P.kp_o;
+    bool stop     = false;
+    for(unsigned kk = 0; !stop && kk < n_mine; kk++) {
+      for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
+        const int nst = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
         const int buf = term_it % C::NBUF;
         int       ok  = 1;
         if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1);
-        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
+        for(int u = 0; u < nst; u++, stage_it++) {
+          bool mine = false;
           if(lane == 0) {
             if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1);
             if(!ok) fail();
-            if(!ok || *abort_flag) *gate_stop = 1;
+            mine = !ok || *abort_flag;
           }
-          pz_gate_sync();
-          if(*gate_stop) {
-            go = false;
-            break;
-          }
+          __syncwarp();
+          if((stop = pz_gate_sync(mine))) break;
         }
       }
     }

@@ -35,10 +35,19 @@ constexpr int PZ_BM = 128, PZ_KC = 64, PZ_EPI = 16, PZ_EPI_W0 = 3, PZ_THREADS = 
 // long: an mbarrier wait there, even on a completed phase, measured 170 - 550 cycles per stage on
 // GB300, against none for a named-barrier rendezvous with a warp that has already done the waits.
 // So the gate warp does every wait of the MMA loop (stage full, TMEM level buffer empty, work
-// items) and the MMA warp only rendezvouses.  Both walk the same stage sequence; a gate that must
-// stop (a bounded wait gave up, the abort flag, the end of the work) sets *stop before the
-// rendezvous and both leave at that same rendezvous, so neither is left waiting at the barrier.
-__device__ __forceinline__ void pz_gate_sync() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+// items) and the MMA warp only rendezvouses.  Both walk the same stage sequence; the rendezvous
+// is an OR-reduction of a stop bit (bar.red: no shared-memory flag to read back), which the gate
+// sets when it must stop (a bounded wait gave up, the abort flag, the end of the work), and both
+// leave at that same rendezvous, so neither is left waiting at the barrier.  Like bar.sync it
+// orders the gate's observations (the TMA bytes have landed) before the MMA warp's later work.
+__device__ __forceinline__ bool pz_gate_sync(bool stop) {
+  uint32_t r;
+  asm volatile("{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, 1, 64, q;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+               : "=r"(r)
+               : "r"((uint32_t) stop)
+               : "memory");
+  return r != 0;
+}
 constexpr unsigned PZ_END = 0xffffffffu;
 
 // map indices (the handle's map table): the d-sum uses 0-2, the l-sum 6-8
@@ -253,17 +262,19 @@ __device__ __forceinline__ void pz_flush_tail(float* tail, int slot, float tsq, 
 // MMAs A_p x [B_1 .. B_{S+1-p}] into the level columns (p - 1) NT ...  The descriptors are built
 // once per stage: the start-address field (bits 0-13, address >> 4) is linear, so the plane and
 // k-step offsets (multiples of 16 B, all inside the 228 KB window) are added to it directly.
-// `first`: the stage opens the term (its first MMA overwrites the accumulators).
+// `first`: the stage opens the term (its first MMA overwrites the accumulators).  The whole warp
+// calls it; the lanes with `issue` set (one) issue.
 template<int S, int NT>
-__device__ __forceinline__ void pz_issue_stage(uint32_t dbase, uint32_t a_smem, uint32_t b_smem, bool first) {
+__device__ __forceinline__ void pz_issue_stage(uint32_t dbase, uint32_t a_smem, uint32_t b_smem, bool first,
+                                               uint32_t issue) {
   const uint64_t da = sm100::desc_kmajor_sw128(a_smem), db = sm100::desc_kmajor_sw128(b_smem);
 #pragma unroll
   for(int ks = 0; ks < PZ_KC / 16; ks++)
 #pragma unroll
     for(int p = 1; p <= S; p++)
-      sm100::mma_bf16(dbase + (p - 1) * NT, da + (uint64_t) (((p - 1) * PZ_BM * 128 + ks * 32) >> 4),
-                      db + (uint64_t) ((ks * 32) >> 4), sm100::idesc_bf16_f32(PZ_BM, (S + 1 - p) * NT),
-                      (first && ks == 0 && p == 1) ? 0u : 1u);
+      sm100::mma_bf16_if(dbase + (p - 1) * NT, da + (uint64_t) (((p - 1) * PZ_BM * 128 + ks * 32) >> 4),
+                         db + (uint64_t) ((ks * 32) >> 4), sm100::idesc_bf16_f32(PZ_BM, (S + 1 - p) * NT),
+                         (first && ks == 0 && p == 1) ? 0u : 1u, issue);
 }
 
 template<int S, int NT, int STAGES>
@@ -297,7 +308,6 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
   unsigned* item_id    = reinterpret_cast<unsigned*>(drain + 1);
   uint32_t* tmem_slot  = item_id + PZ_IR;
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  volatile int* gate_stop  = abort_flag + 1;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if(threadIdx.x == 0) {
@@ -315,7 +325,6 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     }
     sm100::mbar_init(drain, 1);
     *abort_flag = 0;
-    *gate_stop  = 0;
     sm100::mbar_fence_init();
   }
   if(warp == 1) {
@@ -371,31 +380,27 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         if(!sm100::mbar_wait(&full[u % STAGES], (u / STAGES) & 1)) fail();
     }
   } else if(warp == 1) {
-    // ------------------------------------------------------------ MMA issuer (lane 0 issues)
-    // The MMAs need no item data: every item is the same sequence of terms and stages, and the
-    // gate says when the work ends.
-    int  stage_it = 0, term_it = 0;
-    bool go       = true;
-    while(go) {
-      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
-        const int      Kp    = t < 2 ? P.kp_v : P.kp_o;
+    // ------------------------------------------------------------ MMA issuer (the warp runs the
+    // loop, lane 0 issues).  The MMAs need no item data: every item is the same sequence of terms and stages, and the
+    // gate says when the work ends.  Between stages the loop does as little as it can (no
+    // modulo, no shared-memory reads): the tensor pipe idles for as long as it runs.
+    const uint32_t a0 = sm100::smem_u32(smem);
+    uint32_t       a = a0;
+    int            s = 0, term_it = 0;
+    bool           stop = false;
+    while(!stop) {
+      for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
+        const int      nst   = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
         const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
-        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
-          pz_gate_sync();
-          if(*gate_stop) {
-            go = false;
-            break;
-          }
-          if(lane == 0) {
-            sm100::tc_fence_after();
-            const uint32_t a = sm100::smem_u32(smem + (stage_it % STAGES) * C::STAGE_BYTES);
-            pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, k0 == 0);
-            sm100::mma_commit(&empty[stage_it % STAGES]);
-          }
-          __syncwarp();
+        for(int u = 0; u < nst; u++) {
+          if((stop = pz_gate_sync(false))) break;
+          sm100::tc_fence_after();
+          pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
+          sm100::mma_commit_if(&empty[s], lane == 0);
+          a += C::STAGE_BYTES;
+          if(++s == STAGES) s = 0, a = a0;
         }
-        if(go && lane == 0) sm100::mma_commit(&lvl_full[term_it % C::NBUF]);
-        __syncwarp();
+        if(!stop) sm100::mma_commit_if(&lvl_full[term_it % C::NBUF], lane == 0);
       }
     }
     if(lane == 0) {
@@ -405,8 +410,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
   } else if(warp == 2) {
     // ------------------------------------------------------------ gate: the MMA issuer's waits
     int  stage_it = 0, term_it = 0;
-    bool go       = true;
-    for(int it = 0; go; it++) {
+    bool stop     = false;
+    for(int it = 0; !stop; it++) {
       const int r  = it % PZ_IR;
       int       ok = 1;
       unsigned  id = PZ_END;
@@ -417,27 +422,24 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
           sm100::mbar_arrive(&item_empty[r]);
         } else
           fail();
-        if(!ok || id == PZ_END) *gate_stop = 1;
       }
       if(__shfl_sync(0xffffffffu, ok && id != PZ_END, 0) == 0) { // the issuer's next rendezvous ends it
-        pz_gate_sync();
+        pz_gate_sync(true);
         break;
       }
-      for(int t = 0; t < PZ_TERMS && go; t++, term_it++) {
-        const int Kp  = t < 2 ? P.kp_v : P.kp_o;
+      for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
+        const int nst = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
         const int buf = term_it % C::NBUF;
         if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1);
-        for(int k0 = 0; k0 < Kp; k0 += PZ_KC, stage_it++) {
+        for(int u = 0; u < nst; u++, stage_it++) {
+          bool mine = false;
           if(lane == 0) {
             if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1);
             if(!ok) fail();
-            if(!ok || *abort_flag) *gate_stop = 1;
+            mine = !ok || *abort_flag;
           }
-          pz_gate_sync();
-          if(*gate_stop) {
-            go = false;
-            break;
-          }
+          __syncwarp();
+          if((stop = pz_gate_sync(mine))) break;
         }
       }
     }

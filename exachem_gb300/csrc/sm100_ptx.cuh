@@ -94,6 +94,16 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
     "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
     : "memory");
 }
+// The same MMA from a whole warp, issued by the lanes with `issue` set (one lane): the warp runs
+// the issue loop without diverging.
+__device__ __forceinline__ void mma_bf16_if(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate, uint32_t issue) {
+  asm volatile(
+    "{\n\t.reg .pred p, e;\n\tsetp.ne.b32 p, %4, 0;\n\tsetp.ne.b32 e, %5, 0;\n\t"
+    "@e tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+    "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate), "r"(issue)
+    : "memory");
+}
 // arrive on `bar` once every previously issued tcgen05 op of this thread has completed
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -105,6 +115,20 @@ __device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t cta_mask) 
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
                  smem_u32(bar)),
                "h"(cta_mask)
+               : "memory");
+}
+
+__device__ __forceinline__ void mma_commit_if(uint64_t* bar, uint32_t issue) {
+  asm volatile("{\n\t.reg .pred e;\n\tsetp.ne.b32 e, %1, 0;\n\t"
+               "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(smem_u32(bar)),
+               "r"(issue)
+               : "memory");
+}
+__device__ __forceinline__ void mma_commit_mc_if(uint64_t* bar, uint16_t cta_mask, uint32_t issue) {
+  asm volatile("{\n\t.reg .pred e;\n\tsetp.ne.b32 e, %2, 0;\n\t"
+               "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;\n\t}" ::"r"(
+                 smem_u32(bar)),
+               "h"(cta_mask), "r"(issue)
                : "memory");
 }
 
