@@ -161,25 +161,29 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
   // element (y, n) of the tile: P[n][x][y] (consecutive rows -> consecutive addresses)
   float2* Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
   float hi[COLS], lo[COLS];
-#pragma unroll
-  for(int e = 0; e < COLS; e++) hi[e] = lo[e] = 0.f;
 #pragma unroll 1
   for(int t = 0; t < PZ_TERMS; t++, term_it++) {
     const int  buf = term_it % NBUF;
     const bool okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it / NBUF) & 1) && !*abort_flag);
     if(!okw) return false;
     sm100::tc_fence_after();
-    // fold `W` columns starting at c0 whose S levels are in rv; `neg`: an l-sum term
-    auto fold = [&](auto& rv, int c0, auto wtag, bool neg) {
+    // fold `W` columns starting at c0 whose S levels are in rv; `neg`: an l-sum term; `first`: the
+    // item's first term (the accumulators start from it)
+    auto fold = [&](auto& rv, int c0, auto wtag, bool neg, bool first) {
       constexpr int W = decltype(wtag)::value;
 #pragma unroll
       for(int e = 0; e < W; e++) {
         const ff    x  = oz_horner<S, W>(rv, e);
         const float xh = neg ? -x.hi : x.hi, xl = neg ? -x.lo : x.lo;
-        // two-sum of the high words, low words added; the tile is renormalised before the store
-        const float s = hi[c0 + e] + xh, z = s - hi[c0 + e];
-        lo[c0 + e]    = lo[c0 + e] + (((hi[c0 + e] - (s - z)) + (xh - z)) + xl);
-        hi[c0 + e]    = s;
+        if(first) {
+          hi[c0 + e] = xh;
+          lo[c0 + e] = xl;
+        } else {
+          // two-sum of the high words, low words added; the tile is renormalised before the store
+          const float s = hi[c0 + e] + xh, z = s - hi[c0 + e];
+          lo[c0 + e]    = lo[c0 + e] + (((hi[c0 + e] - (s - z)) + (xh - z)) + xl);
+          hi[c0 + e]    = s;
+        }
         if(P.tail) {
           const float tl = __uint_as_float(rv[S - 1][e]) * kScale;
           tsq            = fmaf(tl, tl, tsq);
@@ -193,7 +197,7 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
       __syncwarp();
       if(lane == 0) sm100::mbar_arrive(&lvl_empty[buf]);
     };
-    auto run = [&](bool neg) {
+    auto run = [&](bool neg, bool first) {
       if constexpr(S * COLS <= 32) {
         uint32_t rv[S][COLS]; // every level of the thread's columns in one TMEM round trip
 #pragma unroll
@@ -203,7 +207,7 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
         }
         sm100::tmem_wait_ld();
         release();
-        fold(rv, 0, std::integral_constant<int, COLS>{}, neg);
+        fold(rv, 0, std::integral_constant<int, COLS>{}, neg, first);
       } else {
         // chunks of 8 columns and, when COLS % 8 == 4, one of 4; every TMEM access starts at a
         // multiple of its own width (a thread whose first column is 4 mod 8 takes the 4 first)
@@ -213,7 +217,7 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
           for(int l = 0; l < S; l++) sm100::tmem_ld8(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
           sm100::tmem_wait_ld();
           if(last) release();
-          fold(rv, c0, std::integral_constant<int, 8>{}, neg);
+          fold(rv, c0, std::integral_constant<int, 8>{}, neg, first);
         };
         auto chunk4 = [&](int c0, bool last) {
           uint32_t rv[S][4];
@@ -221,7 +225,7 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
           for(int l = 0; l < S; l++) sm100::tmem_ld4(lane_base + buf * S * NT + l * NT + c_lo + c0, rv[l]);
           sm100::tmem_wait_ld();
           if(last) release();
-          fold(rv, c0, std::integral_constant<int, 4>{}, neg);
+          fold(rv, c0, std::integral_constant<int, 4>{}, neg, first);
         };
         if constexpr(COLS % 8 == 0) {
 #pragma unroll
@@ -237,8 +241,9 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
         }
       }
     };
-    if(t < 2) run(false); // d-sum terms add, l-sum terms subtract
-    else run(true);
+    if(t == 0) run(false, true); // d-sum terms add, l-sum terms subtract
+    else if(t == 1) run(false, false);
+    else run(true, false);
   }
   if(y < v) {
 #pragma unroll
