@@ -72,6 +72,8 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   __shared__ float2 dab[3][3][B * B];    // e_i + e_j + e_k - e_a - e_b (float-float), per block pair
   __shared__ int    blk0[3], blkn[3];
   __shared__ int    slot_on[6];
+  __shared__ long long cube0[3][6];      // offset of the slot's local (0, 0, 0) in pass p's array
+  __shared__ int    tile_full;
 
   const int       v = A.v, o = A.o, tid = threadIdx.x;
   const long long v2 = (long long) v * v;
@@ -80,6 +82,9 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
               *gOij = A.oovv + ((long long) i * o + j) * v2;
   ff    s4{0.f, 0.f}, s5{0.f, 0.f};
   float sens = 0.f; // first-order sensitivity of the energy to errors in W (a-posteriori estimate)
+  // this thread's cube positions r = tid and tid + 256: local (slowest, middle, fastest) index
+  // (r / 64, r / 8 % 8, r % 8) of every pass's array, as an element offset
+  const long long rel0 = ((long long) (tid >> 6) * v + ((tid >> 3) & 7)) * v + (tid & 7), rel1 = rel0 + 4 * v2;
 
   for(int tile = gblock; tile < A.ntiles; tile += gsize) {
     __syncthreads();
@@ -98,7 +103,14 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         if(blk0[P[0]] == blk0[Q[0]] && blk0[P[1]] == blk0[Q[1]] && blk0[P[2]] == blk0[Q[2]]) on = 0;
       }
       slot_on[tid] = on;
-    }
+    } else if(tid >= 32 && tid < 50) { // pass p reads its array with (slowest, middle, fastest)
+      const int  pp = (tid - 32) / 6, sl = (tid - 32) % 6; // = blocks (P0, P2, P1) / (P1, P0, P2) / (P2, P1, P0)
+      const int* P  = c_perm[sl];
+      const int  q0 = pp == 0 ? P[0] : pp == 1 ? P[1] : P[2], q1 = pp == 0 ? P[2] : pp == 1 ? P[0] : P[1],
+                 q2 = pp == 0 ? P[1] : pp == 1 ? P[2] : P[0];
+      cube0[pp][sl] = ((long long) blk0[q0] * v + blk0[q1]) * v + blk0[q2];
+    } else if(tid == 64)
+      tile_full = blkn[0] == B && blkn[1] == B && blkn[2] == B;
     // singles data of the three blocks
     for(int e = tid; e < 9 * B * B; e += ET_THREADS) {
       const int u = e / (3 * B * B), w = (e / (B * B)) % 3, x = (e / B) % B, y = e % B;
@@ -131,7 +143,8 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     // handles local positions r = tid and tid + 256 of every slot: (slowest, middle, fastest)
     // local index of the pass's array = (r / 64, r / 8 % 8, r % 8).
     static_assert(6 * B3 == 12 * ET_THREADS, "two positions of each of the six cubes per thread");
-    float2* Wf = &W[0][0];
+    float2*    Wf   = &W[0][0];
+    const bool full = tile_full;
 #pragma unroll
     for(int pass = 0; pass < 3; pass++) {
       __syncthreads();
@@ -144,22 +157,20 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         const int f = r & 7, m = (r >> 3) & 7, sl = r >> 6;
         int       la, lb, lc; // slot-local (a', b', c'): a in block P0, b in P1, c in P2
         const float2* src;
-        long long     off;
         if(pass == 0) { // P12[a][c][b]: b fastest
           la = sl, lc = m, lb = f;
           src = P12;
-          off = ((long long) (blk0[P0] + la) * v + blk0[P2] + lc) * v + blk0[P1] + lb;
         } else if(pass == 1) { // P34[b][a][c]: c fastest
           lb = sl, la = m, lc = f;
           src = P34;
-          off = ((long long) (blk0[P1] + lb) * v + blk0[P0] + la) * v + blk0[P2] + lc;
         } else { // P56[c][b][a]: a fastest
           lc = sl, lb = m, la = f;
           src = P56;
-          off = ((long long) (blk0[P2] + lc) * v + blk0[P1] + lb) * v + blk0[P0] + la;
         }
-        const bool ok = la < blkn[P0] && lb < blkn[P1] && lc < blkn[P2];
-        x[it]         = ok ? src[off] : make_float2(0.f, 0.f);
+        // (sl, m, f) of this thread do not depend on the tile: local offset rel0 (+ 4 v^2 for r >= 256)
+        const long long off = cube0[pass][s] + (it & 1 ? rel1 : rel0);
+        const bool      ok  = full || (la < blkn[P0] && lb < blkn[P1] && lc < blkn[P2]);
+        x[it]               = ok ? src[off] : make_float2(0.f, 0.f);
         int loc[3]    = {0, 0, 0};
         loc[P0] = la, loc[P1] = lb, loc[P2] = lc;
         widx[it] = s * B3 + kSwz(loc[0], loc[1], loc[2]);
@@ -167,7 +178,11 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
 #pragma unroll
       for(int it = 0; it < 12; it++) {
         if(pass == 0) Wf[widx[it]] = x[it];
-        else {
+        else if(pass == 1) { // two-sum of the high words, low words added; renormalised in pass 2
+          const float2 o = Wf[widx[it]];
+          const ff     h = ff_two_sum(o.x, x[it].x);
+          Wf[widx[it]]   = make_float2(h.hi, h.lo + (o.y + x[it].y));
+        } else {
           const float2 o = Wf[widx[it]];
           const ff     r = ff_add(ff{o.x, o.y}, ff{x[it].x, x[it].y});
           Wf[widx[it]]   = make_float2(r.hi, r.lo);
@@ -179,6 +194,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     // block 2 of the sorted triple) and all six of its orderings, which live in the six slots.
     // The six W values are read once, D is common to the orbit, and an ordering counts only if
     // its slot is a distinct ordered block triple (so every ordered (a, b, c) counts once).
+    const bool all_on = slot_on[0] & slot_on[1] & slot_on[2] & slot_on[3] & slot_on[4] & slot_on[5];
     for(int r = tid; r < B3; r += ET_THREADS) {
       const int la = r / (B * B), lb = (r / B) % B, lc = r % B;
       if(la >= blkn[0] || lb >= blkn[1] || lc >= blkn[2]) continue;
@@ -202,6 +218,22 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       const float sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
       ff    zy4{0.f, 0.f}, zys{0.f, 0.f};
       float sn = 0.f;
+      if(all_on && !A.want_sens) {
+        // All six orderings count: the orbit sums follow from the class sums.
+        //   sum_q Z_q Y4_q = 9 sum_q W_q^2 + 3 (C_a^2 + C_b^2) - 12 C_a C_b
+        //   sum_q Z_q ys_q = 3 sum_q W_q ys_q + 3 (C_a - C_b)(S_a - S_b)
+        // (class a: Z = 3 W + C_a, Y4 = 3 W - C_b, ys = 3 sg - S_b; class b with a and b swapped)
+        ff sq = ff_mul(w[0], w[0]), wy = ff_mul_f(w[0], 3.f * sg[0] - sgb);
+#pragma unroll
+        for(int q = 1; q < 6; q++) {
+          const bool in_a = q == 3 || q == 4;
+          sq = ff_add(sq, ff_mul(w[q], w[q]));
+          wy = ff_add(wy, ff_mul_f(w[q], 3.f * sg[q] - (in_a ? sgb : sga)));
+        }
+        zy4 = ff_add(ff_add(ff_mul_f(sq, 9.f), ff_mul_f(ff_add(ff_mul(ca, ca), ff_mul(cb, cb)), 3.f)),
+                     ff_neg(ff_mul_f(ff_mul(ca, cb), 12.f)));
+        zys = ff_add(ff_mul_f(wy, 3.f), ff_mul_f(ff_add(ca, ff_neg(cb)), 3.f * (sga - sgb)));
+      } else
 #pragma unroll
       for(int q = 0; q < 6; q++) {
         if(!slot_on[q]) continue;
