@@ -171,9 +171,16 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         const long long off = cube0[pass][s] + (it & 1 ? rel1 : rel0);
         const bool      ok  = full || (la < blkn[P0] && lb < blkn[P1] && lc < blkn[P2]);
         x[it]               = ok ? src[off] : make_float2(0.f, 0.f);
-        int loc[3]    = {0, 0, 0};
-        loc[P0] = la, loc[P1] = lb, loc[P2] = lc;
-        widx[it] = s * B3 + kSwz(loc[0], loc[1], loc[2]);
+        if(it & 1) {
+          // r + 256 sets bit 2 of the pass's slowest coordinate (sl < 4 for r < 256); kSwz is
+          // linear over GF(2) with disjoint fields, so the index changes by a constant XOR
+          const int q = pass == 0 ? P0 : pass == 1 ? P1 : P2; // argument of kSwz holding sl
+          widx[it]    = widx[it - 1] ^ (q == 0 ? 260 : q == 1 ? 36 : 4);
+        } else {
+          int loc[3] = {0, 0, 0};
+          loc[P0] = la, loc[P1] = lb, loc[P2] = lc;
+          widx[it] = s * B3 + kSwz(loc[0], loc[1], loc[2]);
+        }
       }
 #pragma unroll
       for(int it = 0; it < 12; it++) {
