@@ -225,18 +225,24 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       const float sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
       ff    zy4{0.f, 0.f}, zys{0.f, 0.f};
       float sn = 0.f;
-      if(all_on && !A.want_sens) {
+      if(all_on) {
         // All six orderings count: the orbit sums follow from the class sums.
         //   sum_q Z_q Y4_q = 9 sum_q W_q^2 + 3 (C_a^2 + C_b^2) - 12 C_a C_b
         //   sum_q Z_q ys_q = 3 sum_q W_q ys_q + 3 (C_a - C_b)(S_a - S_b)
         // (class a: Z = 3 W + C_a, Y4 = 3 W - C_b, ys = 3 sg - S_b; class b with a and b swapped)
-        ff sq = ff_mul(w[0], w[0]), wy = ff_mul_f(w[0], 3.f * sg[0] - sgb);
+        ffacc sqa, wya;
 #pragma unroll
-        for(int q = 1; q < 6; q++) {
-          const bool in_a = q == 3 || q == 4;
-          sq = ff_add(sq, ff_mul(w[q], w[q]));
-          wy = ff_add(wy, ff_mul_f(w[q], 3.f * sg[q] - (in_a ? sgb : sga)));
+        for(int q = 0; q < 6; q++) {
+          const bool  in_a = q == 0 || q == 3 || q == 4;
+          const float ys   = 3.f * sg[q] - (in_a ? sgb : sga);
+          sqa.add_sq(w[q]);
+          wya.add_mul_f(w[q], ys);
+          if(A.want_sens) { // the estimate needs Z and Y only to float precision
+            const float z = 3.f * w[q].hi + (in_a ? ca.hi : cb.hi), y5 = 3.f * w[q].hi - (in_a ? cb.hi : ca.hi) + ys;
+            sn = fmaf(18.f * y5, y5, fmaf(12.f * z, z, sn));
+          }
         }
+        const ff sq = sqa.get(), wy = wya.get();
         zy4 = ff_add(ff_add(ff_mul_f(sq, 9.f), ff_mul_f(ff_add(ff_mul(ca, ca), ff_mul(cb, cb)), 3.f)),
                      ff_neg(ff_mul_f(ff_mul(ca, cb), 12.f)));
         zys = ff_add(ff_mul_f(wy, 3.f), ff_mul_f(ff_add(ca, ff_neg(cb)), 3.f * (sga - sgb)));
@@ -261,7 +267,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       }
       const ff zy5 = ff_add(zy4, zys);
       const float2 dd = dab[0][1][la * B + lb], ec = evs[2][lc];
-      const ff     id = ff_div(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
+      const ff     id = ff_div_fast(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
       s4   = ff_add(s4, ff_mul(zy4, id));
       s5   = ff_add(s5, ff_mul(zy5, id));
       sens = fmaf(sn * id.hi, id.hi, sens);
