@@ -69,7 +69,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   __shared__ float  Ojk[3][3][B * B], Oik[3][3][B * B], Oij[3][3][B * B];
   __shared__ float  ti[3][B], tj[3][B], tk[3][B];
   __shared__ float2 evs[3][B];
-  __shared__ float2 dab[3][3][B * B];    // e_i + e_j + e_k - e_a - e_b (float-float), per block pair
+  __shared__ float2 dab[B * B];          // e_i + e_j + e_k - e_a - e_b (float-float), a in block 0, b in block 1
   __shared__ int    blk0[3], blkn[3];
   __shared__ int    slot_on[6];
   __shared__ long long cube0[3][6];      // offset of the slot's local (0, 0, 0) in pass p's array
@@ -111,9 +111,10 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       cube0[pp][sl] = ((long long) blk0[q0] * v + blk0[q1]) * v + blk0[q2];
     } else if(tid == 64)
       tile_full = blkn[0] == B && blkn[1] == B && blkn[2] == B;
-    // singles data of the three blocks
-    for(int e = tid; e < 9 * B * B; e += ET_THREADS) {
-      const int u = e / (3 * B * B), w = (e / (B * B)) % 3, x = (e / B) % B, y = e % B;
+    // singles data of the three blocks: the orbits read the six ordered pairs of distinct blocks
+    for(int e = tid; e < 6 * B * B; e += ET_THREADS) {
+      const int pi = e / (B * B), u = pi >> 1, w = (pi & 1) ? (u == 2 ? 1 : 2) : (u == 0 ? 1 : 0);
+      const int x = (e / B) % B, y = e % B;
       const bool ok = x < blkn[u] && y < blkn[w];
       const long long off = (long long) (blk0[u] + x) * v + blk0[w] + y;
       Ojk[u][w][x * B + y] = ok ? gOjk[off] : 0.f;
@@ -131,11 +132,11 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       evs[u][x] = make_float2(e.hi, e.lo);
     }
     __syncthreads();
-    for(int e = tid; e < 9 * B * B; e += ET_THREADS) {
-      const int    u = e / (3 * B * B), w = (e / (B * B)) % 3, x = (e / B) % B, y = e % B;
-      const float2 ea = evs[u][x], eb = evs[w][y];
+    if(tid < B * B) { // the orbit-wide part of D: a in block 0, b in block 1
+      const int    x = tid / B, y = tid % B;
+      const float2 ea = evs[0][x], eb = evs[1][y];
       const ff     d  = ff_add(ff_add(eijk, ff{-ea.x, -ea.y}), ff{-eb.x, -eb.y});
-      dab[u][w][x * B + y] = make_float2(d.hi, d.lo);
+      dab[tid]        = make_float2(d.hi, d.lo);
     }
     // W of the six slots, stored by orbit coordinates (loc[P[0]], loc[P[1]], loc[P[2]]) = the
     // slot's local (a', b', c'): three passes, each reading one array along its contiguous index
@@ -266,7 +267,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         }
       }
       const ff zy5 = ff_add(zy4, zys);
-      const float2 dd = dab[0][1][la * B + lb], ec = evs[2][lc];
+      const float2 dd = dab[la * B + lb], ec = evs[2][lc];
       const ff     id = ff_div_fast(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
       s4   = ff_add(s4, ff_mul(zy4, id));
       s5   = ff_add(s5, ff_mul(zy5, id));
