@@ -70,10 +70,8 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   __shared__ float  ti[3][B], tj[3][B], tk[3][B];
   __shared__ float2 evs[3][B];
   __shared__ float2 dab[B * B];          // e_i + e_j + e_k - e_a - e_b (float-float), a in block 0, b in block 1
-  __shared__ int    blk0[3], blkn[3];
   __shared__ int    slot_on[6];
   __shared__ long long cube0[3][6];      // offset of the slot's local (0, 0, 0) in pass p's array
-  __shared__ int    tile_full;
 
   const int       v = A.v, o = A.o, tid = threadIdx.x;
   const long long v2 = (long long) v * v;
@@ -87,44 +85,43 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   const long long rel0 = ((long long) (tid >> 6) * v + ((tid >> 3) & 7)) * v + (tid & 7), rel1 = rel0 + 4 * v2;
 
   for(int tile = gblock; tile < A.ntiles; tile += gsize) {
-    __syncthreads();
-    if(tid < 3) {
-      const int3 t = A.tiles[tile];
-      const int  b = tid == 0 ? t.x : tid == 1 ? t.y : t.z;
-      blk0[tid]    = b * B;
-      blkn[tid]    = min(B, v - b * B);
-    }
-    __syncthreads();
-    if(tid < 6) { // a slot counts once per distinct ordered block triple
-      const int* P  = c_perm[tid];
+    // every thread reads the block triple (one broadcast load) and keeps its bounds in registers
+    const int3 tt    = A.tiles[tile];
+    const int  rb0[3] = {tt.x * B, tt.y * B, tt.z * B};
+    const int  rbn[3] = {min(B, v - rb0[0]), min(B, v - rb0[1]), min(B, v - rb0[2])};
+    auto       b0    = [&](int u) { return u == 0 ? rb0[0] : u == 1 ? rb0[1] : rb0[2]; };
+    auto       bn    = [&](int u) { return u == 0 ? rbn[0] : u == 1 ? rbn[1] : rbn[2]; };
+    __syncthreads(); // the previous item's orbits are done with the shared arrays
+    if(tid >= 96 && tid < 102) { // a slot counts once per distinct ordered block triple
+      const int  t6 = tid - 96;
+      const int* P  = c_perm[t6];
       int        on = 1;
-      for(int q = 0; q < tid; q++) {
+      for(int q = 0; q < t6; q++) {
         const int* Q = c_perm[q];
-        if(blk0[P[0]] == blk0[Q[0]] && blk0[P[1]] == blk0[Q[1]] && blk0[P[2]] == blk0[Q[2]]) on = 0;
+        if(b0(P[0]) == b0(Q[0]) && b0(P[1]) == b0(Q[1]) && b0(P[2]) == b0(Q[2])) on = 0;
       }
-      slot_on[tid] = on;
+      slot_on[t6] = on;
     } else if(tid >= 32 && tid < 50) { // pass p reads its array with (slowest, middle, fastest)
       const int  pp = (tid - 32) / 6, sl = (tid - 32) % 6; // = blocks (P0, P2, P1) / (P1, P0, P2) / (P2, P1, P0)
       const int* P  = c_perm[sl];
       const int  q0 = pp == 0 ? P[0] : pp == 1 ? P[1] : P[2], q1 = pp == 0 ? P[2] : pp == 1 ? P[0] : P[1],
                  q2 = pp == 0 ? P[1] : pp == 1 ? P[2] : P[0];
-      cube0[pp][sl] = ((long long) blk0[q0] * v + blk0[q1]) * v + blk0[q2];
-    } else if(tid == 64)
-      tile_full = blkn[0] == B && blkn[1] == B && blkn[2] == B;
+      cube0[pp][sl] = ((long long) b0(q0) * v + b0(q1)) * v + b0(q2);
+    }
     // singles data of the three blocks: the orbits read the six ordered pairs of distinct blocks
     for(int e = tid; e < 6 * B * B; e += ET_THREADS) {
       const int pi = e / (B * B), u = pi >> 1, w = (pi & 1) ? (u == 2 ? 1 : 2) : (u == 0 ? 1 : 0);
       const int x = (e / B) % B, y = e % B;
-      const bool ok = x < blkn[u] && y < blkn[w];
-      const long long off = (long long) (blk0[u] + x) * v + blk0[w] + y;
+      const bool ok = x < bn(u) && y < bn(w);
+      const long long off = (long long) (b0(u) + x) * v + b0(w) + y;
       Ojk[u][w][x * B + y] = ok ? gOjk[off] : 0.f;
       Oik[u][w][x * B + y] = ok ? gOik[off] : 0.f;
       Oij[u][w][x * B + y] = ok ? gOij[off] : 0.f;
     }
     if(tid < 3 * B) {
       const int u = tid / B, x = tid % B;
-      const bool ok = x < blkn[u];
-      const int  a = blk0[u] + x;
+      const bool ok = x < bn(u);
+      const int  a = b0(u) + x;
       ti[u][x] = ok ? A.t1[(long long) i * v + a] : 0.f;
       tj[u][x] = ok ? A.t1[(long long) j * v + a] : 0.f;
       tk[u][x] = ok ? A.t1[(long long) k * v + a] : 0.f;
@@ -145,10 +142,12 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     // local index of the pass's array = (r / 64, r / 8 % 8, r % 8).
     static_assert(6 * B3 == 12 * ET_THREADS, "two positions of each of the six cubes per thread");
     float2*    Wf   = &W[0][0];
-    const bool full = tile_full;
+    const bool full = rbn[0] == B && rbn[1] == B && rbn[2] == B;
 #pragma unroll
     for(int pass = 0; pass < 3; pass++) {
-      __syncthreads();
+      // pass 0 needs no barrier: the one after the staging made cube0 visible, and the previous
+      // item's orbits finished with W before the barrier at the top of the item
+      if(pass > 0) __syncthreads();
       float2 x[12];
       int    widx[12];
 #pragma unroll
@@ -170,7 +169,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         }
         // (sl, m, f) of this thread do not depend on the tile: local offset rel0 (+ 4 v^2 for r >= 256)
         const long long off = cube0[pass][s] + (it & 1 ? rel1 : rel0);
-        const bool      ok  = full || (la < blkn[P0] && lb < blkn[P1] && lc < blkn[P2]);
+        const bool      ok  = full || (la < rbn[P0] && lb < rbn[P1] && lc < rbn[P2]);
         x[it]               = ok ? src[off] : make_float2(0.f, 0.f);
         if(it & 1) {
           // r + 256 sets bit 2 of the pass's slowest coordinate (sl < 4 for r < 256); kSwz is
@@ -205,7 +204,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     const bool all_on = slot_on[0] & slot_on[1] & slot_on[2] & slot_on[3] & slot_on[4] & slot_on[5];
     for(int r = tid; r < B3; r += ET_THREADS) {
       const int la = r / (B * B), lb = (r / B) % B, lc = r % B;
-      if(la >= blkn[0] || lb >= blkn[1] || lc >= blkn[2]) continue;
+      if(la >= rbn[0] || lb >= rbn[1] || lc >= rbn[2]) continue;
       const int loc[3] = {la, lb, lc};
       ff        w[6];
       float     sg[6];
