@@ -9,11 +9,13 @@
 // a device table, so the launch sequence of a batch is the same for every batch and can be
 // replayed from a CUDA graph.
 //
-// Roles (576 threads): warp 0 lane 0 fetches items and issues TMA loads (running ahead across
-// items), warp 1 lane 0 issues the MMAs, warps 2-17 fold the digit levels into float-float.  The
-// TMEM level accumulators are double buffered by term, so the fold of one term overlaps the MMAs
-// of the next; the float-float accumulator of a tile lives in registers (each epilogue thread owns
-// one row and a quarter of the tile's columns).  All waits are bounded (sm100::kSpinLimit).
+// Roles (608 threads): warp 0 lane 0 fetches items and issues TMA loads (running ahead across
+// items), warp 1 issues the MMAs (one lane, no mbarrier waits), warp 2 is its gate (does those
+// waits and hands each stage over at a named barrier), warps 3-18 fold the digit levels into
+// float-float.  The TMEM level accumulators are double buffered by term, so the fold of one term
+// overlaps the MMAs of the next; the float-float accumulator of a tile lives in registers (each
+// epilogue thread owns one row and a quarter of the tile's columns).  All mbarrier waits are
+// bounded (sm100::kSpinLimit); the named-barrier rendezvous ends when the gate's bounded waits do.
 #pragma once
 
 #include <cuda.h>

@@ -217,7 +217,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) oz_tc_gemm_kernel(const __grid_
             lo[e] = __uint_as_float(rl[e]);
           }
         }
-        // S exact levels -> float-float (oz_horner), scaled by 2^(e_row + e_col - 7 (S + 1))
+        // S exact levels -> float-float (oz_horner), scaled by 2^(e_row + e_col - 7 (S + 1)) (e_row = e_col
+        // = 0 for BF16 digits, which carry their row scales)
         uint32_t rv[S][16];
 #pragma unroll
         for(int l = 0; l < S; l++) sm100::tmem_ld16(lane_base + l * NT + c0, rv[l]);
