@@ -17,7 +17,8 @@ LIB = BUILD / "libccsdt_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
-CU_SOURCES = ["ccsdt_capi.cu", "split.cu", "persist.cu", "noalloc.cu", "mlp.cu", "learned.cu", "retile.cu"]
+CU_SOURCES = ["ccsdt_capi.cu", "split.cu", "persist.cu", "noalloc.cu", "mlp.cu", "learned.cu", "retile.cu",
+              "cholesky.cu"]
 CPP_SOURCES = ["refcount.cpp"]
 
 

@@ -52,7 +52,7 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet",
             "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc", "ccsdt_shard_triplets",
             "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates",
-            "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end"]
+            "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
@@ -78,6 +78,7 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_upload_blocks.argtypes = [vp, ctypes.c_int, ctypes.c_long, ip, ctypes.POINTER(ctypes.c_longlong), vp,
                                         ctypes.c_longlong, ctypes.c_int]
     lib.ccsdt_upload_end.argtypes = [vp]
+    lib.ccsdt_upload_cholesky.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int]
     lib.ccsdt_triplet_error_estimates.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp, dp]
     lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
@@ -93,7 +94,8 @@ def load_library(path: str | os.PathLike | None = None):
     for name in ("ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energies",
                  "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet",
                  "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
-                 "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end"):
+                 "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end",
+                 "ccsdt_upload_cholesky"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -162,6 +164,20 @@ class FusedTriples:
             raise TypeError("pass all inputs on the host or all on the device")
         self._keep = arrs
         self._check(self.lib.ccsdt_upload(self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs], on_dev))
+
+    def upload_cholesky(self, eps_occ, eps_vir, t1, t2, chol_oo, chol_ov, chol_vv):
+        """Inputs with oovv / ooov / ovvv built on the device from spatial Cholesky vectors
+        chol_oo[o][o][Q], chol_ov[o][v][Q], chol_vv[v][v][Q] (all on the host or all on the device)."""
+        arrs = [eps_occ, eps_vir, t1, t2, chol_oo, chol_ov, chol_vv]
+        on_dev = 0 if isinstance(arrs[0], np.ndarray) else 1
+        if any((isinstance(a, np.ndarray)) != (on_dev == 0) for a in arrs):
+            raise TypeError("pass all inputs on the host or all on the device")
+        if on_dev == 0:
+            arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
+        n_chol = int(arrs[4].shape[-1])
+        self._keep = arrs
+        self._check(self.lib.ccsdt_upload_cholesky(self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs[:4]], n_chol,
+                                                   *[ctypes.c_void_p(_ptr(a)) for a in arrs[4:]], on_dev))
 
     def upload_dict(self, d: dict):
         self.upload(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], d["oovv"], d["ooov"], d["ovvv"])

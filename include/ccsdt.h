@@ -136,6 +136,17 @@ ccsdt_status ccsdt_upload_blocks(ccsdt_handle* h, int kind, long n, const int* t
                                  const double* data, long long data_len, int on_device);
 ccsdt_status ccsdt_upload_end(ccsdt_handle* h);
 
+/* Inputs with the integral blocks built on the device from spatial Cholesky vectors
+ * L[p][q][Q] (the alpha-alpha block of the reference's cholVpr, symmetric in p, q):
+ *   chol_oo[o][o][n_chol], chol_ov[o][v][n_chol], chol_vv[v][v][n_chol]  (row-major, Q fastest)
+ *   oovv = (ia|jb), ooov = (ij|ka), ovvv = (ia|bc) = sum_Q L L       (FP64 DMMA GEMMs)
+ * eps_occ, eps_vir, t1, t2 as in ccsdt_upload.  Replaces exachem/cholesky/v2tensors.cpp:66-88
+ * (setupV2Tensors: v2ijab / v2ijka / v2iabc) for the blocks the closed-shell (T) reads, so the
+ * o v^3 ovvv block never crosses the host link.  Blocking; non-finite inputs -> CCSDT_E_NONFINITE. */
+ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
+                                   const double* t1, const double* t2, int n_chol, const double* chol_oo,
+                                   const double* chol_ov, const double* chol_vv, int on_device);
+
 /* Full (T): E[T] and E(T) over every occupied triplet of the shard in opts.  Blocking. */
 ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, ccsdt_result* out);
 

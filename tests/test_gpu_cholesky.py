@@ -1,0 +1,72 @@
+"""Integral blocks built on the device from spatial Cholesky vectors (ccsdt_upload_cholesky):
+oovv = (ia|jb), ooov = (ij|ka), ovvv = (ia|bc) = sum_Q L L (the closed-shell blocks of
+exachem/cholesky/v2tensors.cpp:66-88) must give the energies of the same blocks built on the host
+and uploaded with ccsdt_upload, and of the oracle."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+OCC, VIR = [4, 3], [16, 14]
+
+
+def _cholesky_system(o, v, nq, seed):
+    """The generator's amplitudes and orbital energies with integrals from random spatial Cholesky
+    vectors L[p][q][Q] (symmetric in p, q), and the host-built blocks."""
+    from exachem_gb300.generator import generate
+    d = generate(o, v, seed)
+    rng = np.random.default_rng(seed + 1000)
+    n = o + v
+    L = rng.normal(0.0, 0.05, size=(n, n, nq))
+    L = 0.5 * (L + L.transpose(1, 0, 2))
+    Loo, Lov, Lvv = (np.ascontiguousarray(x) for x in (L[:o, :o], L[:o, o:], L[o:, o:]))
+    d["oovv"] = np.einsum("iaQ,jbQ->ijab", Lov, Lov)
+    d["ooov"] = np.einsum("ijQ,kaQ->ijka", Loo, Lov)
+    d["ovvv"] = np.einsum("iaQ,bcQ->iabc", Lov, Lvv)
+    return d, (Loo, Lov, Lvv)
+
+
+def test_cholesky_blocks_match_host_blocks_and_oracle(built):
+    import oracle
+    from exachem_gb300.ccsd_t import FusedTriples
+    o, v = sum(OCC), sum(VIR)
+    d, (Loo, Lov, Lvv) = _cholesky_system(o, v, 40, 11)
+    ref = FusedTriples(o, v, OCC, VIR)
+    ref.upload_dict(d)
+    r = ref.energy("fp64")
+    ft = FusedTriples(o, v, OCC, VIR)
+    ft.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], Loo, Lov, Lvv)
+    g = ft.energy("fp64")
+    e4, e5 = oracle.energy(d)
+    for got, want, orc in ((g["e_bracket_T"], r["e_bracket_T"], e4), (g["e_paren_T"], r["e_paren_T"], e5)):
+        assert abs(got - want) <= 1e-12 * abs(want)
+        assert abs(got - orc) <= 1e-12 * abs(orc)
+    s3 = ft.energy("ozaki", slices=3)   # the split path on the device-built blocks
+    assert abs(s3["e_paren_T"] - e5) <= 1e-7 * abs(e5)
+
+
+def test_cholesky_from_device_vectors(built):
+    import torch
+    from exachem_gb300.ccsd_t import FusedTriples
+    o, v = sum(OCC), sum(VIR)
+    d, L = _cholesky_system(o, v, 17, 12)   # an n_chol that is not a multiple of the GEMM's k chunk
+    host = FusedTriples(o, v, OCC, VIR)
+    host.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], *L)
+    dev = FusedTriples(o, v, OCC, VIR)
+    on = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], *L)]
+    dev.upload_cholesky(*on)
+    a, b = host.energy("fp64"), dev.energy("fp64")
+    assert a["e_paren_T"] == b["e_paren_T"] and a["e_bracket_T"] == b["e_bracket_T"]
+
+
+def test_cholesky_rejects_bad_input(built):
+    from exachem_gb300.ccsd_t import CCSDTError, FusedTriples
+    o, v = sum(OCC), sum(VIR)
+    d, (Loo, Lov, Lvv) = _cholesky_system(o, v, 8, 13)
+    ft = FusedTriples(o, v, OCC, VIR)
+    bad = Lvv.copy()
+    bad[3, 5, 2] = np.nan
+    with pytest.raises(CCSDTError):                     # a non-finite vector reaches ovvv
+        ft.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], Loo, Lov, bad)
+    with pytest.raises(CCSDTError):                     # energy before a successful upload
+        ft.energy("fp64")
