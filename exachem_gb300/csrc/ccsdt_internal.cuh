@@ -43,7 +43,7 @@ struct ccsdt_handle {
   // tcgen05 path: TMA maps over the digit planes (built once per slicing) and an error flag
   CUtensorMap        tmaps[12];
   bool               tmaps_ready = false;
-  int                tmaps_S     = 0, tmaps_NT = 0;
+  int                tmaps_S     = 0, tmaps_NT = 0, tmaps_KC = 0;
   int*               d_err       = nullptr;
   int*               e_tiles     = nullptr; // sorted virtual block triples of the tiled energy
   int                e_ntiles    = 0;
@@ -78,7 +78,7 @@ struct ccsdt_handle {
   ccsdt_status run_split(const ccsdt_opts* opts, long n, const int* tri_host);
   ccsdt_status ensure_slices(int S, int variant);
   ccsdt_status run_triplet_split(int i, int j, int k, int S, int variant, double* eout);
-  ccsdt_status ensure_tmaps(int S, int NT);
+  ccsdt_status ensure_tmaps(int S, int NT, int KC);
   ccsdt_status run_triplet_tc(int i, int j, int k, int S, double* eout);
   bool         tc_eligible(int S, int variant) const;
   double*      part_buf() { return part; }

@@ -46,9 +46,9 @@ __device__ __forceinline__ int pz_plane_map(int mapA) {
   return mapA == PZ_OVVV_NAT ? PZ_OVVV_NAT_P1 : mapA == PZ_OVVV_SWP ? PZ_OVVV_SWP_P1 : PZ_OOOVH_A_P1;
 }
 
-template<int S, int NT, int STAGES>
+template<int S, int NT, int STAGES, int KC>
 __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_constant__ PzParams P) {
-  using C = PzCfg<S, NT, STAGES>;
+  using C = PzCfg<S, NT, STAGES, KC>;
   constexpr uint16_t kBoth = 0x3;
   const int      v = P.v, yblocks = (v + PZ_BM - 1) / PZ_BM, nblocks = (v + NT - 1) / NT, npairs = (nblocks + 1) / 2;
   const int      base = P.base ? *P.base : 0;
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
         for(int t = 0; t < PZ_TERMS && ok; t++) {
           const PzTerm T  = pz_term(P, w.job, t, i, j, k, w.x);
           const int    mA = pz_plane_map(T.mapA);
-          for(int k0 = 0; k0 < T.Kp; k0 += PZ_KC, stage_it++) {
+          for(int k0 = 0; k0 < T.Kp; k0 += KC, stage_it++) {
             const int s = stage_it % STAGES, use = stage_it / STAGES;
             if(use > 0 && !sm100::mbar_wait(&empty[s], (use - 1) & 1)) {
               fail();
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
 #pragma unroll
             for(int p = 0; p < S; p++)
               if((p & 1) == rank)
-                sm100::tma_load_5d_mc(a + p * PZ_BM * 128, &P.maps[mA], &full[s], k0, w.yb * PZ_BM, T.a2, T.a3, p, kBoth);
+                sm100::tma_load_5d_mc(a + p * PZ_BM * KC * 2, &P.maps[mA], &full[s], k0, w.yb * PZ_BM, T.a2, T.a3, p, kBoth);
             sm100::tma_load_5d(a + C::A_BYTES, &P.maps[T.mapB], &full[s], k0, w.nb * NT, T.b2, T.b3, 0);
           }
         }
@@ -154,12 +154,12 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
     bool           stop = false;
     for(unsigned kk = 0; !stop && kk < n_mine; kk++) {
       for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
-        const int      nst   = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
+        const int      nst   = (t < 2 ? P.kp_v : P.kp_o) / KC;
         const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
         for(int u = 0; u < nst; u++) {
           if((stop = pz_gate_sync(false))) break;
           sm100::tc_fence_after();
-          pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
+          pz_issue_stage<S, NT, KC>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
           sm100::mma_commit_mc_if(&empty[s], kBoth, lane == 0); // stage free here, as seen by both producers
           a += C::STAGE_BYTES;
           if(++s == STAGES) s = 0, a = a0;
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_pair_kernel(const __grid_con
     bool stop     = false;
     for(unsigned kk = 0; !stop && kk < n_mine; kk++) {
       for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
-        const int nst = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
+        const int nst = (t < 2 ? P.kp_v : P.kp_o) / KC;
         const int buf = term_it % C::NBUF;
         int       ok  = 1;
         if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1);

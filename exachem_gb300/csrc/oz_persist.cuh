@@ -28,7 +28,7 @@
 namespace ccsdt {
 
 // 3 role warps (TMA producer, MMA issuer, gate) + PZ_EPI epilogue warps (4 per TMEM lane quarter)
-constexpr int PZ_BM = 128, PZ_KC = 64, PZ_EPI = 16, PZ_EPI_W0 = 3, PZ_THREADS = 32 * (PZ_EPI_W0 + PZ_EPI), PZ_IR = 4,
+constexpr int PZ_BM = 128, PZ_EPI = 16, PZ_EPI_W0 = 3, PZ_THREADS = 32 * (PZ_EPI_W0 + PZ_EPI), PZ_IR = 4,
               PZ_TERMS = 4;
 
 // The MMA warp and its gate warp meet at named barrier 1 (64 threads) once per pipeline stage.
@@ -265,28 +265,34 @@ __device__ __forceinline__ void pz_flush_tail(float* tail, int slot, float tsq, 
   if(lane == 0 && tsq > 0.f) atomicAdd(tail + slot, tsq);
 }
 
-// The MMAs of one pipeline stage (PZ_KC = 64 along K, 4 k-steps of 16): for every k-step, S
-// MMAs A_p x [B_1 .. B_{S+1-p}] into the level columns (p - 1) NT ...  The descriptors are built
+// The MMAs of one pipeline stage (KC = 64 or 32 along K, KC / 16 k-steps of 16): for every
+// k-step, S MMAs A_p x [B_1 .. B_{S+1-p}] into the level columns (p - 1) NT ...  Rows are KC x 2
+// bytes (128 B under the 128-byte swizzle, 64 B under the 64-byte one).  The descriptors are built
 // once per stage: the start-address field (bits 0-13, address >> 4) is linear, so the plane and
 // k-step offsets (multiples of 16 B, all inside the 228 KB window) are added to it directly.
 // `first`: the stage opens the term (its first MMA overwrites the accumulators).  The whole warp
 // calls it; the lanes with `issue` set (one) issue.
-template<int S, int NT>
+template<int KC>
+__device__ __forceinline__ uint64_t pz_desc(uint32_t smem_addr) {
+  static_assert(KC == 64 || KC == 32, "K chunks of 64 (128-byte rows) or 32 (64-byte rows)");
+  return KC == 64 ? sm100::desc_kmajor_sw128(smem_addr) : sm100::desc_kmajor_sw64(smem_addr);
+}
+template<int S, int NT, int KC>
 __device__ __forceinline__ void pz_issue_stage(uint32_t dbase, uint32_t a_smem, uint32_t b_smem, bool first,
                                                uint32_t issue) {
-  const uint64_t da = sm100::desc_kmajor_sw128(a_smem), db = sm100::desc_kmajor_sw128(b_smem);
+  const uint64_t da = pz_desc<KC>(a_smem), db = pz_desc<KC>(b_smem);
 #pragma unroll
-  for(int ks = 0; ks < PZ_KC / 16; ks++)
+  for(int ks = 0; ks < KC / 16; ks++)
 #pragma unroll
     for(int p = 1; p <= S; p++)
-      sm100::mma_bf16_if(dbase + (p - 1) * NT, da + (uint64_t) (((p - 1) * PZ_BM * 128 + ks * 32) >> 4),
+      sm100::mma_bf16_if(dbase + (p - 1) * NT, da + (uint64_t) (((p - 1) * PZ_BM * KC * 2 + ks * 32) >> 4),
                          db + (uint64_t) ((ks * 32) >> 4), sm100::idesc_bf16_f32(PZ_BM, (S + 1 - p) * NT),
                          (first && ks == 0 && p == 1) ? 0u : 1u, issue);
 }
 
-template<int S, int NT, int STAGES>
+template<int S, int NT, int STAGES, int KC>
 struct PzCfg {
-  static constexpr int A_BYTES = S * PZ_BM * 128, B_BYTES = S * NT * 128, STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int A_BYTES = S * PZ_BM * KC * 2, B_BYTES = S * NT * KC * 2, STAGE_BYTES = A_BYTES + B_BYTES;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 512;
   static constexpr int COLS = NT / 4;   // columns per epilogue thread
   static constexpr uint32_t TMEM_COLS = 512;
@@ -297,9 +303,9 @@ struct PzCfg {
   static_assert(S * NT <= 256 && NT % 16 == 0, "MMA N limit / epilogue quarters of 4k columns");
 };
 
-template<int S, int NT, int STAGES>
+template<int S, int NT, int STAGES, int KC>
 __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_constant__ PzParams P) {
-  using C = PzCfg<S, NT, STAGES>;
+  using C = PzCfg<S, NT, STAGES, KC>;
   const int v = P.v, yblocks = (v + PZ_BM - 1) / PZ_BM, nblocks = (v + NT - 1) / NT;
   const int base = P.base ? *P.base : 0;
 
@@ -370,7 +376,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         const int    i = tp[0], j = tp[1], k = tp[2];
         for(int t = 0; t < PZ_TERMS; t++) {
           const PzTerm T = pz_term(P, w.job, t, i, j, k, w.x);
-          for(int k0 = 0; k0 < T.Kp; k0 += PZ_KC, stage_it++) {
+          for(int k0 = 0; k0 < T.Kp; k0 += KC, stage_it++) {
             const int s = stage_it % STAGES, use = stage_it / STAGES;
             if(use > 0 && !sm100::mbar_wait(&empty[s], (use - 1) & 1)) {
               fail();
@@ -397,12 +403,12 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     bool           stop = false;
     while(!stop) {
       for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
-        const int      nst   = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
+        const int      nst   = (t < 2 ? P.kp_v : P.kp_o) / KC;
         const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
         for(int u = 0; u < nst; u++) {
           if((stop = pz_gate_sync(false))) break;
           sm100::tc_fence_after();
-          pz_issue_stage<S, NT>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
+          pz_issue_stage<S, NT, KC>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
           sm100::mma_commit_if(&empty[s], lane == 0);
           a += C::STAGE_BYTES;
           if(++s == STAGES) s = 0, a = a0;
@@ -435,7 +441,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         break;
       }
       for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
-        const int nst = (t < 2 ? P.kp_v : P.kp_o) / PZ_KC;
+        const int nst = (t < 2 ? P.kp_v : P.kp_o) / KC;
         const int buf = term_it % C::NBUF;
         if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1);
         for(int u = 0; u < nst; u++, stage_it++) {

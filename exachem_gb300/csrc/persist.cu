@@ -28,23 +28,25 @@ template<int S>
 struct PzPick;
 template<>
 struct PzPick<1> {
-  static constexpr int NT = 64, ST = 4;
+  static constexpr int NT = 64, ST = 4, KC = 64;
 };
 template<>
 struct PzPick<2> {
-  static constexpr int NT = 64, ST = 4;
+  static constexpr int NT = 64, ST = 4, KC = 64;
 };
 template<>
 struct PzPick<3> {
-  static constexpr int NT = 64, ST = 3; // (NT = 48 with three level buffers measured 1.5x slower)
+  static constexpr int NT = 64, ST = 3, KC = 64; // (NT = 48 with three level buffers measured 1.5x slower)
 };
+// S = 4, 5: a 64-wide K chunk takes 96 / 100 KB a stage, so only two stages fit and the TMA latency
+// shows; 32-wide chunks (64-byte rows, 64-byte swizzle) give four stages in the same space
 template<>
 struct PzPick<4> {
-  static constexpr int NT = 64, ST = 2;
+  static constexpr int NT = 64, ST = 4, KC = 32;
 };
 template<>
 struct PzPick<5> {
-  static constexpr int NT = 32, ST = 2;
+  static constexpr int NT = 32, ST = 4, KC = 32;
 };
 
 int pz_nt(int S) {
@@ -57,14 +59,24 @@ int pz_nt(int S) {
   }
   return 0;
 }
+int pz_kc(int S) {
+  switch(S) {
+    case 1: return PzPick<1>::KC;
+    case 2: return PzPick<2>::KC;
+    case 3: return PzPick<3>::KC;
+    case 4: return PzPick<4>::KC;
+    case 5: return PzPick<5>::KC;
+  }
+  return 0;
+}
 
 template<int S>
 cudaError_t launch_pz(const PzParams& p, int grid, cudaStream_t st) {
-  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST;
-  using Cfg        = PzCfg<S, NT, ST>;
-  cudaError_t e = cudaFuncSetAttribute(oz_persist_kernel<S, NT, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
+  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST, KC = PzPick<S>::KC;
+  using Cfg        = PzCfg<S, NT, ST, KC>;
+  cudaError_t e = cudaFuncSetAttribute(oz_persist_kernel<S, NT, ST, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
   if(e != cudaSuccess) return e;
-  oz_persist_kernel<S, NT, ST><<<grid, PZ_THREADS, Cfg::SMEM, st>>>(p);
+  oz_persist_kernel<S, NT, ST, KC><<<grid, PZ_THREADS, Cfg::SMEM, st>>>(p);
   return cudaGetLastError();
 }
 
@@ -105,9 +117,9 @@ long items_per_slot(int v, int NT, bool pair) {
 
 template<int S>
 cudaError_t launch_pair(const PzParams& p, int ncl, cudaStream_t st) {
-  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST;
-  using Cfg        = PzCfg<S, NT, ST>;
-  cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
+  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST, KC = PzPick<S>::KC;
+  using Cfg        = PzCfg<S, NT, ST, KC>;
+  cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
   if(e != cudaSuccess) return e;
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute attr[1];
@@ -121,7 +133,7 @@ cudaError_t launch_pair(const PzParams& p, int ncl, cudaStream_t st) {
   cfg.stream               = st;
   cfg.attrs                = attr;
   cfg.numAttrs             = 1;
-  e = cudaLaunchKernelEx(&cfg, oz_pair_kernel<S, NT, ST>, p);
+  e = cudaLaunchKernelEx(&cfg, oz_pair_kernel<S, NT, ST, KC>, p);
   if(e != cudaSuccess) return e;
   return cudaGetLastError();
 }
@@ -140,9 +152,9 @@ cudaError_t launch_pair_any(int S, const PzParams& p, int ncl, cudaStream_t st) 
 // Co-resident two-CTA clusters of the cluster kernel for S planes (0: cannot run).
 template<int S>
 int pair_clusters() {
-  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST;
-  using Cfg        = PzCfg<S, NT, ST>;
-  if(cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM) !=
+  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST, KC = PzPick<S>::KC;
+  using Cfg        = PzCfg<S, NT, ST, KC>;
+  if(cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM) !=
      cudaSuccess) {
     cudaGetLastError();
     return 0;
@@ -162,7 +174,7 @@ int pair_clusters() {
   cfg.attrs                = attr;
   cfg.numAttrs             = 1;
   int n = 0;
-  if(cudaOccupancyMaxActiveClusters(&n, oz_pair_kernel<S, NT, ST>, &cfg) != cudaSuccess) {
+  if(cudaOccupancyMaxActiveClusters(&n, oz_pair_kernel<S, NT, ST, KC>, &cfg) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -243,7 +255,7 @@ int ccsdt_handle::energy_grid() {
 ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails,
                                         double* sens) {
   // the B-side TMA box must be exactly the kernel's N tile, or the loads overrun the smem slot
-  if(!tmaps_ready || tmaps_S != S || tmaps_NT != pz_nt(S))
+  if(!tmaps_ready || tmaps_S != S || tmaps_NT != pz_nt(S) || tmaps_KC != pz_kc(S))
     return fail(CCSDT_E_STATE, "tensor maps do not match the persistent kernel's tile");
   int sm = 0;
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
@@ -315,7 +327,7 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
   if(S >= 1 && S <= 5 && pair_clusters_by_S[S] < 0) pair_clusters_by_S[S] = pair_clusters_any(S);
   pz_pair_clusters = (S >= 1 && S <= 5) ? pair_clusters_by_S[S] : 0;
   pz_pair          = !force_single_cta && pz_pair_clusters > 0;
-  if((s = ensure_slices(std::max(S, slices_ready), 0)) || (s = ensure_tmaps(S, pz_nt(S)))) return s;
+  if((s = ensure_slices(std::max(S, slices_ready), 0)) || (s = ensure_tmaps(S, pz_nt(S), pz_kc(S)))) return s;
   // table of non-zero triplets (i < k); i = j = k contributes exactly zero
   std::vector<int> tab;
   for(long t = 0; t < n; t++) {

@@ -198,6 +198,18 @@ __device__ __forceinline__ uint64_t desc_kmajor_sw128(uint32_t smem_addr) {
   return d;
 }
 
+// The same for rows of 64 bytes (32 BF16 along K) under the 64-byte swizzle: 8-row groups 512 B
+// apart, layout type SWIZZLE_64B.
+__device__ __forceinline__ uint64_t desc_kmajor_sw64(uint32_t smem_addr) {
+  uint64_t d = 0;
+  d |= (uint64_t) ((smem_addr >> 4) & 0x3FFF);
+  d |= (uint64_t) 1 << 16;
+  d |= (uint64_t) (512 >> 4) << 32;
+  d |= (uint64_t) 1 << 46;
+  d |= (uint64_t) 4 << 61;
+  return d;
+}
+
 // Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major.
 __host__ __device__ constexpr uint32_t idesc_bf16_f32(uint32_t M, uint32_t N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);

@@ -444,27 +444,30 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 5-D BF16 map: dims (k, d1, d2, d3, plane), strides in elements for d1..d3 and plane.
+// kc: the box's K extent, 64 (128-byte rows, 128-byte swizzle) or 32 (64-byte rows, 64-byte swizzle)
 bool encode_map(CUtensorMap* m, const void* base, int Kp, long long d1, long long d2, long long d3, int planes,
-                long long s1, long long s2, long long s3, long long sp, int box1, int boxp) {
-  if(boxp > planes) return false;
+                long long s1, long long s2, long long s3, long long sp, int box1, int boxp, int kc) {
+  if(boxp > planes || (kc != 64 && kc != 32) || Kp % kc) return false;
   cuuint64_t dims[5]    = {(cuuint64_t) Kp, (cuuint64_t) d1, (cuuint64_t) d2, (cuuint64_t) d3, (cuuint64_t) planes};
   cuuint64_t strides[4] = {(cuuint64_t) s1 * 2, (cuuint64_t) s2 * 2, (cuuint64_t) s3 * 2, (cuuint64_t) sp * 2};
-  cuuint32_t box[5]     = {64, (cuuint32_t) box1, 1, 1, (cuuint32_t) boxp};
+  cuuint32_t box[5]     = {(cuuint32_t) kc, (cuuint32_t) box1, 1, 1, (cuuint32_t) boxp};
   cuuint32_t estr[5]    = {1, 1, 1, 1, 1};
   auto fn = encode_fn();
   if(!fn) return false;
   CUresult   r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides,
-                                        box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                        box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                        kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
                                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
 
 } // namespace
 
-// Tensor maps for S planes whose B-side box is NT rows: NT must equal the N tile of the kernel
-// that will use them (its shared-memory B slot holds exactly S x NT rows of 128 bytes).
-ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT) {
-  if(tmaps_ready && tmaps_S == S && tmaps_NT == NT) return CCSDT_OK;
+// Tensor maps for S planes whose B-side box is NT rows of KC elements: NT and KC must equal the
+// N tile and K chunk of the kernel that will use them (its shared-memory B slot holds exactly
+// S x NT rows of 2 KC bytes).
+ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT, int KC) {
+  if(tmaps_ready && tmaps_S == S && tmaps_NT == NT && tmaps_KC == KC) return CCSDT_OK;
   if(S > slices_ready) return fail(CCSDT_E_STATE, "tensor maps asked for more planes than were sliced");
   if(NT <= 0 || NT > 256 || NT % 16) return fail(CCSDT_E_INVALID, "bad N tile for the tensor maps");
   const long long o = this->o, v = this->v, S_ = S;
@@ -472,30 +475,31 @@ ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT) {
   const long long Kv = kp_v, Ko = kp_o;
   bool ok = true;
   // A side (pair rows, 128-row boxes): rows (z, x, y) natural = z v^2 + x v + y, swapped = z v^2 + y v + x
-  ok &= encode_map(&tmaps[MAP_OVVV_NAT], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
-  ok &= encode_map(&tmaps[MAP_OVVV_SWP], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_);
-  ok &= encode_map(&tmaps[MAP_T2H_NAT], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
-  ok &= encode_map(&tmaps[MAP_T2H_SWP], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_);
+  ok &= encode_map(&tmaps[MAP_OVVV_NAT], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_OVVV_SWP], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_T2H_NAT], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_T2H_SWP], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_, KC);
   // B side (single rows, NT-row boxes): t2 rows (xx, yy, a); ooovh rows (yy, zz, c)
-  ok &= encode_map(&tmaps[MAP_T2], sl_t2, (int) Kv, v, o, o, P, Kv, v * Kv, o * v * Kv, pl_t2, NT, (int) S_);
-  ok &= encode_map(&tmaps[MAP_OOOVH], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, NT, (int) S_);
-  ok &= encode_map(&tmaps[MAP_T2H_NAT_B], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, NT, (int) S_);
-  ok &= encode_map(&tmaps[MAP_T2H_SWP_B], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, NT, (int) S_);
-  ok &= encode_map(&tmaps[MAP_OOOVH_A], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, (int) S_);
-  ok &= encode_map(&tmaps[MAP_OVVV_NAT_P1], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, 1);
-  ok &= encode_map(&tmaps[MAP_OVVV_SWP_P1], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, 1);
-  ok &= encode_map(&tmaps[MAP_OOOVH_A_P1], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, 1);
+  ok &= encode_map(&tmaps[MAP_T2], sl_t2, (int) Kv, v, o, o, P, Kv, v * Kv, o * v * Kv, pl_t2, NT, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_OOOVH], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, NT, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_T2H_NAT_B], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, NT, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_T2H_SWP_B], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, NT, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_OOOVH_A], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_OVVV_NAT_P1], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, 1, KC);
+  ok &= encode_map(&tmaps[MAP_OVVV_SWP_P1], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, 1, KC);
+  ok &= encode_map(&tmaps[MAP_OOOVH_A_P1], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, 1, KC);
   if(!ok) return fail(CCSDT_E_CUDA, "cuTensorMapEncodeTiled failed for the digit planes");
   tmaps_ready = true;
   tmaps_S     = S;
   tmaps_NT    = NT;
+  tmaps_KC    = KC;
   return CCSDT_OK;
 }
 
 template<int S>
 static ccsdt_status launch_tc(ccsdt_handle* h, TcBatch& b) {
   constexpr int NT = TcPick<S>::NT, ST = TcPick<S>::ST;
-  if(!h->tmaps_ready || h->tmaps_S != S || h->tmaps_NT != NT)
+  if(!h->tmaps_ready || h->tmaps_S != S || h->tmaps_NT != NT || h->tmaps_KC != 64)
     return h->fail(CCSDT_E_STATE, "tensor maps do not match the tcgen05 kernel's tile");
   using Cfg        = TcCfg<S, NT, ST>;
   const int    v   = h->v;
@@ -526,7 +530,7 @@ bool ccsdt_handle::tc_eligible(int S, int variant) const {
 
 ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eout) {
   ccsdt_status s;
-  if((s = ensure_tmaps(S, tc_nt(S)))) return s;
+  if((s = ensure_tmaps(S, tc_nt(S), 64))) return s;
   const long long o = this->o, v = this->v, v2 = v * v;
   // BF16 digit planes carry their rows' scales: no exponent tables
   auto hole = [&](int xx, bool nat, int yy, int zz) {
