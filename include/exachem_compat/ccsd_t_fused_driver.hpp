@@ -16,6 +16,8 @@
 //        (ia|bc) = v2iabc(i_alpha, b_beta, a_alpha, c_beta)     (v2tensors.cpp:84-86)
 //    (in each the exchange part of the antisymmetrised block vanishes by spin).
 //    It is a template over the tensor types, so it needs only Tensor<T>::get.
+//  * gather_cholesky() + run_closed_shell_cholesky(): the alternative that skips V2 - the
+//    alpha-alpha blocks of the Cholesky tensor cholVpr, with the integral blocks built on the GPU.
 //  * CCSD_T_Fused_Driver<T>::execute(): the reference's signature, compiled when
 //    EXACHEM_GB300_WITH_TAMM is defined (inside an ExaChem build).  Each rank of the process
 //    group takes every size-th occupied triplet on its own GPU and returns its partial
@@ -55,10 +57,10 @@ inline std::vector<size_t> offsets(const std::vector<size_t>& ext) {
 
 // mo_tiles: extents of the MO tiles in the order occ_a, occ_b, virt_a, virt_b (as
 // TiledIndexSpace::input_tile_sizes() returns them); noa / nva: alpha occupied / virtual tiles.
-template<typename T, typename TensorT, typename V2T>
-SpatialInputs gather_closed_shell(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva,
-                                  TensorT& d_t1, TensorT& d_t2, V2T& d_v2,
-                                  const std::vector<T>& k_evl_sorted) {
+// The amplitudes and orbital energies only (the integral arrays stay empty).
+template<typename T, typename TensorT>
+SpatialInputs gather_amplitudes(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva, TensorT& d_t1,
+                                TensorT& d_t2, const std::vector<T>& k_evl_sorted) {
   if(mo_tiles.size() != 2 * noa + 2 * nva) throw std::invalid_argument("MO tiles != 2 noa + 2 nva");
   std::vector<size_t> ot(mo_tiles.begin(), mo_tiles.begin() + noa);
   std::vector<size_t> vt(mo_tiles.begin() + 2 * noa, mo_tiles.begin() + 2 * noa + nva);
@@ -78,9 +80,6 @@ SpatialInputs gather_closed_shell(const std::vector<size_t>& mo_tiles, size_t no
   S.eps_vir.assign(k_evl_sorted.begin() + 2 * o, k_evl_sorted.begin() + 2 * o + v);
   S.t1.assign(o * v, 0.0);
   S.t2.assign(o * o * v * v, 0.0);
-  S.oovv.assign(o * o * v * v, 0.0);
-  S.ooov.assign(o * o * o * v, 0.0);
-  S.ovvv.assign(o * v * v * v, 0.0);
   std::vector<T> buf;
   // block ids: O tiles 0..2noa-1 (beta = alpha + noa), V tiles 0..2nva-1 (beta = alpha + nva)
   for(size_t A = 0; A < nva; A++)
@@ -100,6 +99,28 @@ SpatialInputs gather_closed_shell(const std::vector<size_t>& mo_tiles, size_t no
                 for(size_t j = 0; j < ot[J]; j++)
                   S.t2[(((oo[I] + i) * o + oo[J] + j) * v + vo[A] + a) * v + vo[B] + b] =
                     buf[((a * vt[B] + b) * ot[I] + i) * ot[J] + j];
+        }
+  return S;
+}
+
+// gather_amplitudes plus the three integral blocks from the V2 tensors.
+template<typename T, typename TensorT, typename V2T>
+SpatialInputs gather_closed_shell(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva,
+                                  TensorT& d_t1, TensorT& d_t2, V2T& d_v2,
+                                  const std::vector<T>& k_evl_sorted) {
+  SpatialInputs       S = gather_amplitudes<T>(mo_tiles, noa, nva, d_t1, d_t2, k_evl_sorted);
+  std::vector<size_t> ot(mo_tiles.begin(), mo_tiles.begin() + noa);
+  std::vector<size_t> vt(mo_tiles.begin() + 2 * noa, mo_tiles.begin() + 2 * noa + nva);
+  const auto          oo = detail::offsets(ot), vo = detail::offsets(vt);
+  const size_t        o = S.o, v = S.v;
+  S.oovv.assign(o * o * v * v, 0.0);
+  S.ooov.assign(o * o * o * v, 0.0);
+  S.ovvv.assign(o * v * v * v, 0.0);
+  std::vector<T> buf;
+  for(size_t A = 0; A < nva; A++)
+    for(size_t B = 0; B < nva; B++)
+      for(size_t I = 0; I < noa; I++)
+        for(size_t J = 0; J < noa; J++) {
           d_v2.v2ijab.get({I, J + noa, A, B + nva}, buf); // [i][j][a][b]
           for(size_t i = 0; i < ot[I]; i++)
             for(size_t j = 0; j < ot[J]; j++)
@@ -271,6 +292,73 @@ inline std::tuple<double, double, double> run_closed_shell(const SpatialInputs& 
                     S.ooov.data(), S.ovvv.data(), 0);
   ccsdt_result r{};
   if(st == CCSDT_OK && slice_model) st = ccsdt_set_slice_model(h, slice_model->data());
+  if(st == CCSDT_OK) st = ccsdt_energy(h, &opts, &r);
+  if(st != CCSDT_OK) {
+    std::string msg = ccsdt_last_error(h);
+    ccsdt_destroy(h);
+    throw std::runtime_error("ccsdt: " + msg);
+  }
+  ccsdt_destroy(h);
+  return {r.e_bracket_T, r.e_paren_T, r.seconds};
+}
+
+// Spatial Cholesky vectors of the closed shell, row-major with the Cholesky index fastest.
+struct CholeskyInputs {
+  int                 o = 0, v = 0, nq = 0;
+  std::vector<double> L_oo, L_ov, L_vv; // [o][o][nq], [o][v][nq], [v][v][nq]
+};
+
+// Reads the alpha-alpha blocks (P, Q, C) of ExaChem's Cholesky tensor cholVpr {MO, MO, CI}
+// (ccsd_t.cpp:46, the tensor setupV2Tensors contracts at v2tensors.cpp:66-88) with Tensor::get.
+// mo_tiles / noa / nva as for gather_closed_shell; ci_tiles: the CI space's tile extents.
+template<typename T, typename TensorT>
+CholeskyInputs gather_cholesky(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva,
+                               const std::vector<size_t>& ci_tiles, TensorT& chol) {
+  if(mo_tiles.size() != 2 * noa + 2 * nva) throw std::invalid_argument("MO tiles != 2 noa + 2 nva");
+  std::vector<size_t> ot(mo_tiles.begin(), mo_tiles.begin() + noa);
+  std::vector<size_t> vt(mo_tiles.begin() + 2 * noa, mo_tiles.begin() + 2 * noa + nva);
+  const auto   oo = detail::offsets(ot), vo = detail::offsets(vt), co = detail::offsets(ci_tiles);
+  const size_t o = oo.empty() ? 0 : oo.back() + ot.back(), v = vo.empty() ? 0 : vo.back() + vt.back();
+  const size_t nq = co.empty() ? 0 : co.back() + ci_tiles.back();
+  CholeskyInputs L;
+  L.o = (int) o, L.v = (int) v, L.nq = (int) nq;
+  L.L_oo.assign(o * o * nq, 0.0);
+  L.L_ov.assign(o * v * nq, 0.0);
+  L.L_vv.assign(v * v * nq, 0.0);
+  std::vector<T> buf;
+  // one alpha-alpha block family: MO tile ids (P0 + X, Q0 + Y), rows of nr / cols of nc
+  auto family = [&](std::vector<double>& dst, size_t nx, size_t ny, size_t P0, size_t Q0,
+                    const std::vector<size_t>& xt, const std::vector<size_t>& yt, const std::vector<size_t>& xo,
+                    const std::vector<size_t>& yo, size_t ncols) {
+    for(size_t X = 0; X < nx; X++)
+      for(size_t Y = 0; Y < ny; Y++)
+        for(size_t C = 0; C < ci_tiles.size(); C++) {
+          chol.get({P0 + X, Q0 + Y, C}, buf); // [p][q][c]
+          for(size_t p = 0; p < xt[X]; p++)
+            for(size_t q = 0; q < yt[Y]; q++)
+              for(size_t c = 0; c < ci_tiles[C]; c++)
+                dst[((xo[X] + p) * ncols + yo[Y] + q) * nq + co[C] + c] = buf[(p * yt[Y] + q) * ci_tiles[C] + c];
+        }
+  };
+  family(L.L_oo, noa, noa, 0, 0, ot, ot, oo, oo, o);
+  family(L.L_ov, noa, nva, 0, 2 * noa, ot, vt, oo, vo, v);
+  family(L.L_vv, nva, nva, 2 * noa, 2 * noa, vt, vt, vo, vo, v);
+  return L;
+}
+
+// (T) with the integral blocks built on the device from Cholesky vectors (ccsdt_upload_cholesky);
+// the amplitudes and orbital energies come from gather_amplitudes.  Returns (E[T], E(T), device s).
+inline std::tuple<double, double, double> run_closed_shell_cholesky(const SpatialInputs& S, const CholeskyInputs& C,
+                                                                    int device, const ccsdt_opts& opts) {
+  if(C.o != S.o || C.v != S.v) throw std::invalid_argument("Cholesky vectors and amplitudes differ in o / v");
+  ccsdt_layout  L{S.o, S.v, (int) S.occ_tiles.size(), S.occ_tiles.data(), (int) S.vir_tiles.size(),
+                 S.vir_tiles.data()};
+  ccsdt_handle* h  = nullptr;
+  ccsdt_status  st = ccsdt_create(&h, &L, device);
+  if(st != CCSDT_OK) throw std::runtime_error(std::string("ccsdt_create: ") + ccsdt_status_string(st));
+  st = ccsdt_upload_cholesky(h, S.eps_occ.data(), S.eps_vir.data(), S.t1.data(), S.t2.data(), C.nq, C.L_oo.data(),
+                             C.L_ov.data(), C.L_vv.data(), 0);
+  ccsdt_result r{};
   if(st == CCSDT_OK) st = ccsdt_energy(h, &opts, &r);
   if(st != CCSDT_OK) {
     std::string msg = ccsdt_last_error(h);

@@ -2,10 +2,14 @@
 // spin-orbital tiled tensors (built with the oracle's spin_orbital.hpp on the TAMM stand-in)
 // -> gather_closed_shell() -> spatial arrays, and optionally run_closed_shell() on the GPU.
 //
-//   compat_driver <in.bin> <out.bin> [--run]
+//   compat_driver <in.bin> <out.bin> [--run | --run-tiled | --chol <chol.bin> [--run]]
 // in.bin : int32 o, v, noa, nva, occ tiles[noa], vir tiles[nva]; float64 eps_occ[o] eps_vir[v]
 //          t1 t2 oovv ooov ovvv (C-ABI layouts)
 // out.bin: the gathered float64 arrays in the same order; with --run also E[T], E(T).
+// --chol : chol.bin = int32 nq, nci, ci tiles[nci]; float64 L[o+v][o+v][nq] (spatial, occupied
+//          first).  The driver builds the spin-orbital Cholesky tensor cholVpr {MO, MO, CI} on the
+//          TAMM stand-in, gathers it with gather_cholesky and appends L_oo, L_ov, L_vv to out.bin;
+//          with --run also E[T], E(T) through run_closed_shell_cholesky.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -52,6 +56,46 @@ int main(int argc, char** argv) {
   std::ofstream g(argv[2], std::ios::binary);
   for(auto* a: {&S.eps_occ, &S.eps_vir, &S.t1, &S.t2, &S.oovv, &S.ooov, &S.ovvv})
     g.write(reinterpret_cast<const char*>(a->data()), sizeof(double) * a->size());
+  if(argc > 4 && std::string(argv[3]) == "--chol") {
+    std::ifstream c(argv[4], std::ios::binary);
+    int           h2[2];
+    rd(c, h2, 2);
+    const int        nq = h2[0], nci = h2[1];
+    std::vector<int> cit(nci);
+    rd(c, cit.data(), nci);
+    const size_t        n = (size_t) o + v;
+    std::vector<double> L(n * n * nq);
+    rd(c, L.data(), L.size());
+    if(!c) return 4;
+    std::vector<size_t> CT(cit.begin(), cit.end());
+    // spin-orbital MO index (occ_a | occ_b | virt_a | virt_b) -> (spatial index, spin)
+    auto sp = [&](size_t p, int& spin) -> size_t {
+      if(p < (size_t) 2 * o) return spin = (int) (p / o), p % o;
+      p -= 2 * o;
+      return spin = (int) (p / v), o + p % v;
+    };
+    tamm::Tensor<double> chol({mo, mo, CT});
+    for(size_t p = 0; p < 2 * n; p++)
+      for(size_t q = 0; q < 2 * n; q++) {
+        int          s1, s2;
+        const size_t a = sp(p, s1), b = sp(q, s2);
+        for(size_t Q = 0; Q < (size_t) nq; Q++) {
+          size_t idx[3] = {p, q, Q};
+          chol.at(idx)  = s1 == s2 ? L[(a * n + b) * nq + Q] : 0.0;
+        }
+      }
+    auto C = exachem_gb300::gather_cholesky<double>(mo, noa, nva, CT, chol);
+    for(auto* a: {&C.L_oo, &C.L_ov, &C.L_vv}) g.write(reinterpret_cast<const char*>(a->data()), sizeof(double) * a->size());
+    if(argc > 5 && std::string(argv[5]) == "--run") {
+      ccsdt_opts op{};
+      op.mode = CCSDT_MODE_FP64;
+      auto A = exachem_gb300::gather_amplitudes<double>(mo, noa, nva, d_t1, d_t2, k_evl);
+      auto [e4, e5, secs] = exachem_gb300::run_closed_shell_cholesky(A, C, 0, op);
+      g.write(reinterpret_cast<const char*>(&e4), sizeof(double));
+      g.write(reinterpret_cast<const char*>(&e5), sizeof(double));
+      std::printf("E[T] %.17g E(T) %.17g (%.3f s)\n", e4, e5, secs);
+    }
+  }
   if(argc > 3 && std::string(argv[3]) == "--run-tiled") {
     // the drop-in path: blocks through the device-side retile, then the (T) call
     ccsdt_opts op{};
