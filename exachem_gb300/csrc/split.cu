@@ -209,54 +209,6 @@ __global__ void __launch_bounds__(OZ_THREADS) oz_gemm_kernel(const __grid_consta
       }
 }
 
-// ----------------------------------------------------------------------------- energy (ff)
-struct SplitEnergyArgs {
-  const float2 *P12, *P34, *P56;
-  const float * oovv, *t1; // FP32 copies
-  const double *eo, *ev;
-  int           o, v, i, j, k;
-  double*       part;
-};
-
-__global__ void __launch_bounds__(E_THREADS) energy_split_kernel(const __grid_constant__ SplitEnergyArgs A) {
-  const int       v = A.v, o = A.o;
-  const long long v2 = (long long) v * v, n = v2 * v;
-  const int       i = A.i, j = A.j, k = A.k;
-  const ff        eijk = ff_add(ff_add(ff_from_double(A.eo[i]), ff_from_double(A.eo[j])), ff_from_double(A.eo[k]));
-  const float *   Ojk = A.oovv + ((long long) j * o + k) * v2, *Oik = A.oovv + ((long long) i * o + k) * v2,
-              *Oij = A.oovv + ((long long) i * o + j) * v2;
-  const float *ti = A.t1 + (long long) i * v, *tj = A.t1 + (long long) j * v, *tk = A.t1 + (long long) k * v;
-  ff           s4{0.f, 0.f}, s5{0.f, 0.f};
-  for(long long e = (long long) blockIdx.x * blockDim.x + threadIdx.x; e < n;
-      e += (long long) gridDim.x * blockDim.x) {
-    const int a = (int) (e / v2), b = (int) ((e / v) % v), c = (int) (e % v);
-    auto      W = [&](int x, int y, int z) {
-      float2 p = A.P12[((long long) x * v + z) * v + y], q = A.P34[((long long) y * v + x) * v + z],
-             r = A.P56[((long long) z * v + y) * v + x];
-      return ff_add(ff_add(ff{p.x, p.y}, ff{q.x, q.y}), ff{r.x, r.y});
-    };
-    auto SG = [&](int x, int y, int z) {
-      return Ojk[(long long) y * v + z] * ti[x] + Oik[(long long) x * v + z] * tj[y] + Oij[(long long) x * v + y] * tk[z];
-    };
-    const ff wabc = W(a, b, c), wbca = W(b, c, a), wcab = W(c, a, b);
-    const ff wacb = W(a, c, b), wbac = W(b, a, c), wcba = W(c, b, a);
-    const ff z    = ff_add(ff_add(ff_scale(wabc, 4.f), wbca), wcab);
-    const ff y4   = ff_add(ff_mul_f(wabc, 3.f), ff_neg(ff_add(ff_add(wacb, wbac), wcba)));
-    const float sgl = 3.f * SG(a, b, c) - SG(a, c, b) - SG(b, a, c) - SG(c, b, a);
-    const ff    y5  = ff_add_f(y4, sgl);
-    const ff    d   = ff_add(ff_add(ff_add(eijk, ff_from_double(-A.ev[a])), ff_from_double(-A.ev[b])),
-                        ff_from_double(-A.ev[c]));
-    s4 = ff_add(s4, ff_div(ff_mul(z, y4), d));
-    s5 = ff_add(s5, ff_div(ff_mul(z, y5), d));
-  }
-  CSum c4, c5;
-  c4.add((double) s4.hi);
-  c4.add((double) s4.lo);
-  c5.add((double) s5.hi);
-  c5.add((double) s5.lo);
-  block_reduce_csum(c4, c5, A.part + 4 * (long long) blockIdx.x);
-}
-
 __global__ void to_float_kernel(const double* x, float* y, long long n) {
   for(long long e = (long long) blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long) gridDim.x * blockDim.x)
     y[e] = (float) x[e];
@@ -531,7 +483,7 @@ bool ccsdt_handle::tc_eligible(int S, int variant) const {
 ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eout) {
   ccsdt_status s;
   if((s = ensure_tmaps(S, tc_nt(S), 64))) return s;
-  const long long o = this->o, v = this->v, v2 = v * v;
+  const long long v = this->v, v2 = v * v;
   // BF16 digit planes carry their rows' scales: no exponent tables
   auto hole = [&](int xx, bool nat, int yy, int zz) {
     return TcTerm{nat ? MAP_T2H_NAT : MAP_T2H_SWP, MAP_OOOVH, xx, zz, yy, nullptr, nat ? v : 1, nat ? 1 : v,
