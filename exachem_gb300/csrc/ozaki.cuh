@@ -43,8 +43,6 @@ __device__ __forceinline__ ff ff_add_f(ff a, float b) {
   float hi = s.hi + lo;
   return ff{hi, lo - (hi - s.hi)};
 }
-// a * s, exact only for s = +-2^k (both words scale without rounding)
-__device__ __forceinline__ ff ff_scale(ff a, float s) { return ff{a.hi * s, a.lo * s}; }
 // a * s for any float s: error-free product of the high word (fma), so the result keeps
 // float-float precision (for s = 3, say, a.hi * s alone would round at 2^-25)
 __device__ __forceinline__ ff ff_mul_f(ff a, float s) {
@@ -61,17 +59,9 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   float hi = p + e;
   return ff{hi, e - (hi - p)};
 }
-// a / b, one correction step
-__device__ __forceinline__ ff ff_div(ff a, ff b) {
-  float q1 = a.hi / b.hi;
-  ff    r  = ff_add(a, ff_scale(ff_mul(ff{q1, 0.f}, b), -1.f));
-  float q2 = r.hi / b.hi;
-  ff    s  = ff_two_sum(q1, q2);
-  return s;
-}
 // a / b from an approximate reciprocal (__fdividef: a few ulp) and one float-float correction
 // step: q1 = a.hi / b.hi (approx.), r = a - q1 b (float-float), q2 = r.hi / b.hi (approx.);
-// relative error ~2^-44 (against ~2^-48 for ff_div), at a fraction of two IEEE divisions.
+// relative error ~2^-44, at a fraction of the cost of two IEEE divisions.
 __device__ __forceinline__ ff ff_div_fast(ff a, ff b) {
   const float rb = __fdividef(1.f, b.hi);
   const float q1 = a.hi * rb;
