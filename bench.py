@@ -222,6 +222,8 @@ def main():
     ap.add_argument("--budget", type=float, default=1e-8,
                     help="learned mode: 3 sqrt(sum sigma_t^2) <= budget x sum |E(T)_t|")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-mode side measurement")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default tile configurations (no ccsdt_autotune before the timed region)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -283,6 +285,16 @@ def main():
     if mode == "learned":
         # each timed call is a part of the whole (T) over all triplets: its acceptance share
         kw = {"slices": 5, "energy_budget": args.budget, "budget_triplets": int(len(tri_all))}
+
+    # the contraction's tile configuration for each slice count this run uses, tuned on this system
+    # before anything is timed (every configuration gives bit-identical energies)
+    tile = None
+    if mode != "fp64" and not args.no_autotune:
+        tile = {}
+        for s_ in sorted({S} | (set(range(1, 6)) if model is not None else set())):
+            ms_c, chosen = ft.autotune(s_)
+            tile[str(s_)] = {"nt_st_kc": list(ct.FusedTriples.tile_configs(s_)[chosen]),
+                             "ms_per_config": [round(x, 3) for x in ms_c]}
 
     per_step = args.fp64_batch if mode == "fp64" else args.batch
     batches = [spread_sample(mine, per_step, offset=s) for s in range(args.steps)]
@@ -449,7 +461,7 @@ def main():
             "dtype": "f64" if mode == "fp64" else "bf16 digit planes (exact FP32 levels), float-float recombination",
             "data": "synthetic (seeded generator, built on GPU)",
             "config": {"workload": f"closed-shell (T) o={o} v={v} seed={seed} ragged tiles", "o": o, "v": v,
-                       "mode": mode, "slices": S if mode != "fp64" else None,
+                       "mode": mode, "slices": S if mode != "fp64" else None, "tile_config": tile,
                        "occ_tiles": occ_tiles, "vir_tiles": vir_tiles, "triplets_total": int(len(tri_all)),
                        "triplets_timed": int(timed_trip), "timed_fraction": frac,
                        "projection": None if frac >= 1 else "value = timed seconds / timed_fraction",

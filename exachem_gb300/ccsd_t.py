@@ -37,7 +37,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("slices", ctypes.c_int), ("slice_kind", ctypes.c_int),
                 ("use_graph", ctypes.c_int), ("shard_index", ctypes.c_int), ("shard_count", ctypes.c_int),
                 ("energy_budget", ctypes.c_double), ("budget_triplets", ctypes.c_int),
-                ("test_kernel", ctypes.c_int), ("test_single_cta", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("test_kernel", ctypes.c_int), ("test_single_cta", ctypes.c_int), ("autotune", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class Result(ctypes.Structure):
@@ -52,7 +53,8 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_last_error", "ccsdt_status_string", "ccsdt_set_stream", "ccsdt_profile_triplet",
             "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc", "ccsdt_shard_triplets",
             "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates",
-            "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky"]
+            "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky",
+            "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
@@ -79,6 +81,9 @@ def load_library(path: str | os.PathLike | None = None):
                                         ctypes.c_longlong, ctypes.c_int]
     lib.ccsdt_upload_end.argtypes = [vp]
     lib.ccsdt_upload_cholesky.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int]
+    lib.ccsdt_tile_configs.argtypes = [ctypes.c_int, ip, ip]
+    lib.ccsdt_autotune.argtypes = [vp, ctypes.c_int, dp, ip, ip]
+    lib.ccsdt_set_tile_config.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.ccsdt_triplet_error_estimates.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp, dp]
     lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
@@ -95,7 +100,7 @@ def load_library(path: str | os.PathLike | None = None):
                  "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet",
                  "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
                  "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end",
-                 "ccsdt_upload_cholesky"):
+                 "ccsdt_upload_cholesky", "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -179,12 +184,35 @@ class FusedTriples:
         self._check(self.lib.ccsdt_upload_cholesky(self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs[:4]], n_chol,
                                                    *[ctypes.c_void_p(_ptr(a)) for a in arrs[4:]], on_dev))
 
+    @staticmethod
+    def tile_configs(slices: int) -> list[tuple[int, int, int]]:
+        """(N tile, pipeline stages, K chunk) of the compiled contraction configurations for
+        `slices` digit planes; index 0 is the default."""
+        lib = load_library()
+        n = ctypes.c_int()
+        if lib.ccsdt_tile_configs(slices, ctypes.byref(n), None):
+            return []
+        buf = (ctypes.c_int * (3 * n.value))()
+        lib.ccsdt_tile_configs(slices, ctypes.byref(n), buf)
+        return [tuple(buf[3 * q:3 * q + 3]) for q in range(n.value)]
+
+    def autotune(self, slices: int):
+        """Times every configuration on one triplet, keeps the fastest: (ms per configuration,
+        index kept)."""
+        ms = (ctypes.c_double * 16)()
+        n, chosen = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.ccsdt_autotune(self.h, slices, ms, ctypes.byref(n), ctypes.byref(chosen)))
+        return list(ms[:n.value]), chosen.value
+
+    def set_tile_config(self, slices: int, index: int):
+        self._check(self.lib.ccsdt_set_tile_config(self.h, slices, index))
+
     def upload_dict(self, d: dict):
         self.upload(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], d["oovv"], d["ooov"], d["ovvv"])
 
     @staticmethod
     def opts(mode="fp64", slices=4, slice_kind="bf16", energy_budget=1e-9, use_graph=0,
-             shard_index=0, shard_count=1, legacy_mma=0, single_cta=0, budget_triplets=0) -> Opts:
+             shard_index=0, shard_count=1, legacy_mma=0, single_cta=0, budget_triplets=0, autotune=0) -> Opts:
         o = Opts()
         o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
         o.slices = slices
@@ -195,6 +223,7 @@ class FusedTriples:
         o.budget_triplets = budget_triplets
         o.test_kernel = legacy_mma       # 1: mma.sync slice kernel, 2: per-triplet tcgen05 kernel (testing)
         o.test_single_cta = single_cta   # 1: single-CTA persistent kernel, not the 2-CTA cluster one (testing)
+        o.autotune = autotune            # 1: tune the contraction's tile configuration on first use
         return o
 
     def energy(self, mode="fp64", **kw) -> dict:

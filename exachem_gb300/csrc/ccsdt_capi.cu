@@ -330,6 +330,20 @@ static bool valid_opts(const ccsdt_opts* o) {
   return o && (o->mode == CCSDT_MODE_FP64 || o->mode == CCSDT_MODE_OZAKI || o->mode == CCSDT_MODE_LEARNED);
 }
 
+// opts->autotune: the slice counts this call can use on the persistent tcgen05 path, each tuned
+// once per handle (before the caller's timed work)
+static ccsdt_status autotune_for(ccsdt_handle* h, const ccsdt_opts* opts) {
+  if(!opts->autotune || opts->mode == CCSDT_MODE_FP64 || opts->slice_kind != 0 || opts->test_kernel != 0)
+    return CCSDT_OK;
+  const int lo = opts->mode == CCSDT_MODE_LEARNED ? 1 : opts->slices, hi = std::min(opts->slices, 5);
+  for(int S = std::max(lo, 1); S <= hi; S++)
+    if(!h->pz_tuned[S]) {
+      ccsdt_status s = h->autotune(S, nullptr, nullptr, nullptr);
+      if(s) return s;
+    }
+  return CCSDT_OK;
+}
+
 ccsdt_status ccsdt_handle::run_list(const ccsdt_opts* opts, long n, const int* tri_host) {
   ccsdt_status s;
   if((s = ensure_scratch()) || (s = ensure_triplet_slots(n))) return s;
@@ -360,7 +374,9 @@ extern "C" ccsdt_status ccsdt_triplet_energies(ccsdt_handle* h, const ccsdt_opts
       return h->fail(CCSDT_E_INVALID, "triplet " + std::to_string(t) + " is not 0 <= i <= j <= k < o");
   }
   CK(cudaSetDevice(h->device));
-  ccsdt_status s = h->run_list(opts, n, tri);
+  ccsdt_status s = autotune_for(h, opts);
+  if(s) return s;
+  s = h->run_list(opts, n, tri);
   if(s) return s;
   std::vector<double> buf(2 * (size_t) n);
   if(n) CK(cudaMemcpyAsync(buf.data(), h->etrip, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, h->stream));
@@ -404,8 +420,10 @@ extern "C" ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, cc
   ccsdt_shard_triplets(o, opts->shard_index, nsh, &n, nullptr);
   std::vector<int> tri(3 * (size_t) n);
   ccsdt_shard_triplets(o, opts->shard_index, nsh, &n, tri.data());
+  ccsdt_status s = autotune_for(h, opts);
+  if(s) return s;
   CK(cudaEventRecord(h->ev0, h->stream));
-  ccsdt_status s = h->run_list(opts, n, tri.data());
+  s = h->run_list(opts, n, tri.data());
   if(s) return s;
   reduce_triplets_kernel<<<1, 32, 0, h->stream>>>(h->etrip, n, h->res);
   h->launches++;

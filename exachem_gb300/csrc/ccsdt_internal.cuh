@@ -108,7 +108,13 @@ struct ccsdt_handle {
   bool      pz_pair = false;         // this call runs the two-CTA cluster kernel
   bool      force_single_cta = false; // test knob: the single-CTA persistent kernel instead
   int       pz_pair_clusters = 0;    // co-resident clusters of the cluster kernel (this S)
-  int       pair_clusters_by_S[6] = {-1, -1, -1, -1, -1, -1};
+  int       pair_clusters_by_conf[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  // persistent-contraction configuration per S (index into kPzConfs, -1 = the default), set by
+  // the autotuner or ccsdt_set_tile_config; tuned[S]: the autotuner has run for S
+  int          pz_conf_idx[6] = {-1, -1, -1, -1, -1, -1};
+  bool         pz_tuned[6]    = {false, false, false, false, false, false};
+  int          pz_conf_index(int S) const;
+  ccsdt_status autotune(int S, double* ms, int* n, int* chosen);
   long      graph_replays = 0;
   ccsdt_status ensure_batch(int S, int B);
   ccsdt_status launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails, double* sens);

@@ -17,79 +17,12 @@
 #include "ccsdt_internal.cuh"
 #include "energy_tiled.cuh"
 #include "fp64_kernels.cuh"
-#include "oz_pair.cuh"
 #include "oz_persist.cuh"
+#include "pz_confs.h"
 
 using namespace ccsdt;
 
 namespace {
-
-template<int S>
-struct PzPick;
-template<>
-struct PzPick<1> {
-  static constexpr int NT = 64, ST = 4, KC = 64;
-};
-template<>
-struct PzPick<2> {
-  static constexpr int NT = 64, ST = 4, KC = 64;
-};
-template<>
-struct PzPick<3> {
-  static constexpr int NT = 64, ST = 3, KC = 64; // (NT = 48 with three level buffers measured 1.5x slower)
-};
-// S = 4, 5: a 64-wide K chunk takes 96 / 100 KB a stage, so only two stages fit and the TMA latency
-// shows; 32-wide chunks (64-byte rows, 64-byte swizzle) give four stages in the same space
-template<>
-struct PzPick<4> {
-  static constexpr int NT = 64, ST = 4, KC = 32;
-};
-template<>
-struct PzPick<5> {
-  static constexpr int NT = 32, ST = 4, KC = 32;
-};
-
-int pz_nt(int S) {
-  switch(S) {
-    case 1: return PzPick<1>::NT;
-    case 2: return PzPick<2>::NT;
-    case 3: return PzPick<3>::NT;
-    case 4: return PzPick<4>::NT;
-    case 5: return PzPick<5>::NT;
-  }
-  return 0;
-}
-int pz_kc(int S) {
-  switch(S) {
-    case 1: return PzPick<1>::KC;
-    case 2: return PzPick<2>::KC;
-    case 3: return PzPick<3>::KC;
-    case 4: return PzPick<4>::KC;
-    case 5: return PzPick<5>::KC;
-  }
-  return 0;
-}
-
-template<int S>
-cudaError_t launch_pz(const PzParams& p, int grid, cudaStream_t st) {
-  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST, KC = PzPick<S>::KC;
-  using Cfg        = PzCfg<S, NT, ST, KC>;
-  cudaError_t e = cudaFuncSetAttribute(oz_persist_kernel<S, NT, ST, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
-  if(e != cudaSuccess) return e;
-  oz_persist_kernel<S, NT, ST, KC><<<grid, PZ_THREADS, Cfg::SMEM, st>>>(p);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pz_any(int S, const PzParams& p, int grid, cudaStream_t st) {
-  switch(S) {
-    case 1: return launch_pz<1>(p, grid, st);
-    case 2: return launch_pz<2>(p, grid, st);
-    case 3: return launch_pz<3>(p, grid, st);
-    case 4: return launch_pz<4>(p, grid, st);
-    case 5: return launch_pz<5>(p, grid, st);
-  }
-  return cudaErrorInvalidValue;
-}
 
 // Item ids of B slots sorted by estimated cost (rows x columns of the tile), largest first; ties
 // keep the natural order (n-block fastest) so concurrently running CTAs share A tiles in L2.
@@ -115,89 +48,36 @@ long items_per_slot(int v, int NT, bool pair) {
   return 3L * v * yb * (pair ? (nb + 1) / 2 : nb);
 }
 
-template<int S>
-cudaError_t launch_pair(const PzParams& p, int ncl, cudaStream_t st) {
-  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST, KC = PzPick<S>::KC;
-  using Cfg        = PzCfg<S, NT, ST, KC>;
-  cudaError_t e = cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM);
-  if(e != cudaSuccess) return e;
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id               = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.gridDim              = dim3(2 * ncl, 1, 1);
-  cfg.blockDim             = dim3(PZ_THREADS, 1, 1);
-  cfg.dynamicSmemBytes     = Cfg::SMEM;
-  cfg.stream               = st;
-  cfg.attrs                = attr;
-  cfg.numAttrs             = 1;
-  e = cudaLaunchKernelEx(&cfg, oz_pair_kernel<S, NT, ST, KC>, p);
-  if(e != cudaSuccess) return e;
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pair_any(int S, const PzParams& p, int ncl, cudaStream_t st) {
-  switch(S) {
-    case 1: return launch_pair<1>(p, ncl, st);
-    case 2: return launch_pair<2>(p, ncl, st);
-    case 3: return launch_pair<3>(p, ncl, st);
-    case 4: return launch_pair<4>(p, ncl, st);
-    case 5: return launch_pair<5>(p, ncl, st);
-  }
-  return cudaErrorInvalidValue;
-}
-
-// Co-resident two-CTA clusters of the cluster kernel for S planes (0: cannot run).
-template<int S>
-int pair_clusters() {
-  constexpr int NT = PzPick<S>::NT, ST = PzPick<S>::ST, KC = PzPick<S>::KC;
-  using Cfg        = PzCfg<S, NT, ST, KC>;
-  if(cudaFuncSetAttribute(oz_pair_kernel<S, NT, ST, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM) !=
-     cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  int sm = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
-  cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute attr[1];
-  attr[0].id               = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = 2;
-  attr[0].val.clusterDim.y = 1;
-  attr[0].val.clusterDim.z = 1;
-  cfg.gridDim              = dim3(2 * (sm / 2), 1, 1);
-  cfg.blockDim             = dim3(PZ_THREADS, 1, 1);
-  cfg.dynamicSmemBytes     = Cfg::SMEM;
-  cfg.attrs                = attr;
-  cfg.numAttrs             = 1;
-  int n = 0;
-  if(cudaOccupancyMaxActiveClusters(&n, oz_pair_kernel<S, NT, ST, KC>, &cfg) != cudaSuccess) {
-    cudaGetLastError();
-    return 0;
-  }
-  return n;
-}
-
-int pair_clusters_any(int S) {
-  switch(S) {
-    case 1: return pair_clusters<1>();
-    case 2: return pair_clusters<2>();
-    case 3: return pair_clusters<3>();
-    case 4: return pair_clusters<4>();
-    case 5: return pair_clusters<5>();
-  }
-  return 0;
-}
-
 } // namespace
+
+namespace ccsdt {
+cudaError_t pz_launch_pair_a(int conf, const PzParams& p, int ncl, cudaStream_t st);
+cudaError_t pz_launch_single_a(int conf, const PzParams& p, int grid, cudaStream_t st);
+int         pz_pair_clusters_a(int conf);
+cudaError_t pz_launch_pair_b(int conf, const PzParams& p, int ncl, cudaStream_t st);
+cudaError_t pz_launch_single_b(int conf, const PzParams& p, int grid, cudaStream_t st);
+int         pz_pair_clusters_b(int conf);
+
+cudaError_t pz_launch_pair(int conf, const PzParams& p, int ncl, cudaStream_t st) {
+  return conf < kPzSplit ? pz_launch_pair_a(conf, p, ncl, st) : pz_launch_pair_b(conf, p, ncl, st);
+}
+cudaError_t pz_launch_single(int conf, const PzParams& p, int grid, cudaStream_t st) {
+  return conf < kPzSplit ? pz_launch_single_a(conf, p, grid, st) : pz_launch_single_b(conf, p, grid, st);
+}
+int pz_pair_clusters(int conf) { return conf < kPzSplit ? pz_pair_clusters_a(conf) : pz_pair_clusters_b(conf); }
+} // namespace ccsdt
+
+// The configuration in use for S digit planes: the one the autotuner kept, else the default.
+int ccsdt_handle::pz_conf_index(int S) const {
+  if(S < 1 || S > 5) return -1;
+  return pz_conf_idx[S] >= 0 ? pz_conf_idx[S] : pz_default_conf(S);
+}
 
 ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
   const long long v3 = (long long) v * v * v;
-  const int       NT = pz_nt(S);
-  if(!NT) return fail(CCSDT_E_INVALID, "no persistent configuration for this slice count");
+  const int conf = pz_conf_index(S);
+  if(conf < 0) return fail(CCSDT_E_INVALID, "no persistent configuration for this slice count");
+  const int NT = kPzConfs[conf].NT;
   if(bt_B != B) {
     if(bt_F) cudaFree(bt_F);
     if(bt_part) cudaFree(bt_part);
@@ -213,7 +93,7 @@ ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
     bt_B = B;
     bt_order_key = -1;
   }
-  const int key = (S * 100000 + B) * 2 + (pz_pair ? 1 : 0);
+  const int key = ((conf * 8 + S) * 100000 + B) * 2 + (pz_pair ? 1 : 0);
   if(bt_order_key != key) {
     auto ids = cost_order(B, v, NT, pz_pair);
     if(bt_order) cudaFree(bt_order);
@@ -255,7 +135,8 @@ int ccsdt_handle::energy_grid() {
 ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails,
                                         double* sens) {
   // the B-side TMA box must be exactly the kernel's N tile, or the loads overrun the smem slot
-  if(!tmaps_ready || tmaps_S != S || tmaps_NT != pz_nt(S) || tmaps_KC != pz_kc(S))
+  const int conf = pz_conf_index(S);
+  if(conf < 0 || !tmaps_ready || tmaps_S != S || tmaps_NT != kPzConfs[conf].NT || tmaps_KC != kPzConfs[conf].KC)
     return fail(CCSDT_E_STATE, "tensor maps do not match the persistent kernel's tile");
   int sm = 0;
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
@@ -265,7 +146,7 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
-  const int  NT  = pz_nt(S);
+  const int  NT  = kPzConfs[conf].NT;
   const long per = items_per_slot(v, NT, pz_pair);
   if(nitems_override <= 0) p.nitems = (unsigned) (per * nslots);
   // the cost-ordered table was built for bt_B slots; a smaller last batch has its own table
@@ -292,8 +173,8 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
     cudaEventRecord(prof_ev[1], stream); // no separate l-sum phase
   }
   if(e == cudaSuccess)
-    e = pz_pair ? launch_pair_any(S, p, (int) std::min<long>(pz_pair_clusters, (long) p.nitems), stream)
-                : launch_pz_any(S, p, sm, stream);
+    e = pz_pair ? pz_launch_pair(conf, p, (int) std::min<long>(pz_pair_clusters, (long) p.nitems), stream)
+                : pz_launch_single(conf, p, sm, stream);
   launches++;
   if(profiling) cudaEventRecord(prof_ev[2], stream);
   if(tv[1]) cudaEventRecord(tv[1], stream);
@@ -324,10 +205,12 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
   tev_used = 0; // events of a batch that failed earlier are not read
   tev_slots.clear();
   // the two-CTA cluster kernel when its clusters can be resident (and not switched off for a test)
-  if(S >= 1 && S <= 5 && pair_clusters_by_S[S] < 0) pair_clusters_by_S[S] = pair_clusters_any(S);
-  pz_pair_clusters = (S >= 1 && S <= 5) ? pair_clusters_by_S[S] : 0;
+  const int conf = pz_conf_index(S);
+  if(conf < 0) return fail(CCSDT_E_INVALID, "no persistent configuration for this slice count");
+  if(pair_clusters_by_conf[conf] < 0) pair_clusters_by_conf[conf] = ccsdt::pz_pair_clusters(conf);
+  pz_pair_clusters = pair_clusters_by_conf[conf];
   pz_pair          = !force_single_cta && pz_pair_clusters > 0;
-  if((s = ensure_slices(std::max(S, slices_ready), 0)) || (s = ensure_tmaps(S, pz_nt(S), pz_kc(S)))) return s;
+  if((s = ensure_slices(std::max(S, slices_ready), 0)) || (s = ensure_tmaps(S, kPzConfs[conf].NT, kPzConfs[conf].KC))) return s;
   // table of non-zero triplets (i < k); i = j = k contributes exactly zero
   std::vector<int> tab;
   for(long t = 0; t < n; t++) {
@@ -354,7 +237,7 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
     bt_tri_cap = m;
   }
   // natural-order table for a partial last batch
-  const int  NT  = pz_nt(S);
+  const int  NT  = kPzConfs[conf].NT;
   const long per = items_per_slot(v, NT, pz_pair);
   const long rem = m % B;
   if(rem) {
@@ -431,4 +314,101 @@ ccsdt_status ccsdt_handle::collect_phase_times() {
   tev_used = 0;
   tev_slots.clear();
   return CCSDT_OK;
+}
+
+static_assert(kPzNConfs <= 16, "pair_clusters_by_conf holds one entry per configuration");
+
+// Times every compiled configuration for S digit planes on one triplet of this system (the
+// contraction launch, CUDA events on the handle's stream, second of two runs) and keeps the
+// fastest for the handle's later calls.  Every configuration gives bit-identical energies.
+ccsdt_status ccsdt_handle::autotune(int S, double* ms, int* n, int* chosen) {
+  if(S < 1 || S > 5) return fail(CCSDT_E_INVALID, "autotune: slices must be 1 to 5");
+  if(!uploaded) return fail(CCSDT_E_STATE, "autotune before a successful upload");
+  std::vector<int> cands;
+  for(int c = 0; c < kPzNConfs; c++)
+    if(kPzConfs[c].S == S) cands.push_back(c);
+  if(n) *n = (int) cands.size();
+  if(o < 2) { // no triplet with i < k: nothing to time, keep the default
+    pz_tuned[S] = true;
+    if(chosen) *chosen = 0;
+    return CCSDT_OK;
+  }
+  ccsdt_status s;
+  if((s = ensure_scratch()) || (s = ensure_triplet_slots(1)) || (s = ensure_slices(std::max(S, slices_ready), 0)))
+    return s;
+  if(!d_err) return fail(CCSDT_E_STATE, "autotune: device error flag missing");
+  if(cudaMemsetAsync(d_err, 0, sizeof(int), stream) != cudaSuccess) return fail(CCSDT_E_CUDA, "autotune: memset");
+  const int tri[3] = {0, o / 2, o - 1};
+  // the phase timers serve the measurement; the caller's accumulated phase times are kept
+  const bool   pt = phase_timing;
+  const double saved[3] = {phase_ms[0], phase_ms[1], phase_ms[2]};
+  const long   sb = phase_batches, st = phase_triplets;
+  const bool   fs = force_single_cta;
+  phase_timing     = true;
+  force_single_cta = false;
+  int    best   = -1;
+  double best_t = 0.0;
+  for(size_t q = 0; q < cands.size() && !s; q++) {
+    pz_conf_idx[S] = cands[q];
+    double t = 0.0;
+    for(int rep = 0; rep < 2 && !s; rep++) {
+      phase_ms[0] = phase_ms[1] = phase_ms[2] = 0.0;
+      s = run_batched(S, 1, tri, false, nullptr, nullptr, nullptr);
+      t = phase_ms[0];
+    }
+    if(ms) ms[q] = t;
+    if(!s && (best < 0 || t < best_t)) best = (int) q, best_t = t;
+  }
+  phase_timing     = pt;
+  force_single_cta = fs;
+  for(int q = 0; q < 3; q++) phase_ms[q] = saved[q];
+  phase_batches  = sb;
+  phase_triplets = st;
+  if(!s) s = check_device_error();
+  if(s) {
+    pz_conf_idx[S] = -1;
+    return s;
+  }
+  pz_conf_idx[S] = cands[best];
+  pz_tuned[S]    = true;
+  if(chosen) *chosen = best;
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_tile_configs(int slices, int* n, int* nt_st_kc) {
+  if(!n) return CCSDT_E_INVALID;
+  int m = 0;
+  for(int c = 0; c < kPzNConfs; c++)
+    if(kPzConfs[c].S == slices) {
+      if(nt_st_kc) {
+        nt_st_kc[3 * m]     = kPzConfs[c].NT;
+        nt_st_kc[3 * m + 1] = kPzConfs[c].ST;
+        nt_st_kc[3 * m + 2] = kPzConfs[c].KC;
+      }
+      m++;
+    }
+  *n = m;
+  return m ? CCSDT_OK : CCSDT_E_INVALID;
+}
+
+extern "C" ccsdt_status ccsdt_autotune(ccsdt_handle* h, int slices, double* ms, int* n, int* chosen) {
+  if(!h) return CCSDT_E_INVALID;
+  if(cudaSetDevice(h->device) != cudaSuccess) return h->fail(CCSDT_E_CUDA, "cudaSetDevice");
+  return h->autotune(slices, ms, n, chosen);
+}
+
+extern "C" ccsdt_status ccsdt_set_tile_config(ccsdt_handle* h, int slices, int index) {
+  if(!h) return CCSDT_E_INVALID;
+  if(slices < 1 || slices > 5) return h->fail(CCSDT_E_INVALID, "ccsdt_set_tile_config: slices must be 1 to 5");
+  int m = 0;
+  for(int c = 0; c < kPzNConfs; c++)
+    if(kPzConfs[c].S == slices) {
+      if(m == index) {
+        h->pz_conf_idx[slices] = c;
+        h->pz_tuned[slices]    = true;
+        return CCSDT_OK;
+      }
+      m++;
+    }
+  return h->fail(CCSDT_E_INVALID, "ccsdt_set_tile_config: no configuration " + std::to_string(index));
 }

@@ -1,0 +1,33 @@
+// Instantiations of the persistent contraction for configurations [0, kPzSplit) of kPzConfs
+// (S = 1 to 3); pz_launch_b.cu holds the others, so the two compile in parallel.
+#include "pz_launch.cuh"
+
+namespace ccsdt {
+
+static_assert(kPzSplit == 6 && kPzConfs[5].S == 3 && kPzConfs[6].S == 4, "the split of the configurations");
+
+#define PZ_CASES(X) X(0) X(1) X(2) X(3) X(4) X(5)
+
+cudaError_t pz_launch_pair_a(int conf, const PzParams& p, int ncl, cudaStream_t st) {
+#define X(c) \
+  case c: return pz_launch_pair_t<c>(p, ncl, st);
+  switch(conf) { PZ_CASES(X) }
+#undef X
+  return cudaErrorInvalidValue;
+}
+cudaError_t pz_launch_single_a(int conf, const PzParams& p, int grid, cudaStream_t st) {
+#define X(c) \
+  case c: return pz_launch_single_t<c>(p, grid, st);
+  switch(conf) { PZ_CASES(X) }
+#undef X
+  return cudaErrorInvalidValue;
+}
+int pz_pair_clusters_a(int conf) {
+#define X(c) \
+  case c: return pz_pair_clusters_t<c>();
+  switch(conf) { PZ_CASES(X) }
+#undef X
+  return 0;
+}
+
+} // namespace ccsdt

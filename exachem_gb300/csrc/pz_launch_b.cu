@@ -1,0 +1,33 @@
+// Instantiations of the persistent contraction for configurations [kPzSplit, kPzNConfs) of kPzConfs
+// (S = 4, 5); pz_launch_a.cu holds the others, so the two compile in parallel.
+#include "pz_launch.cuh"
+
+namespace ccsdt {
+
+static_assert(kPzNConfs == 11, "the cases below list every configuration from kPzSplit on");
+
+#define PZ_CASES(X) X(6) X(7) X(8) X(9) X(10)
+
+cudaError_t pz_launch_pair_b(int conf, const PzParams& p, int ncl, cudaStream_t st) {
+#define X(c) \
+  case c: return pz_launch_pair_t<c>(p, ncl, st);
+  switch(conf) { PZ_CASES(X) }
+#undef X
+  return cudaErrorInvalidValue;
+}
+cudaError_t pz_launch_single_b(int conf, const PzParams& p, int grid, cudaStream_t st) {
+#define X(c) \
+  case c: return pz_launch_single_t<c>(p, grid, st);
+  switch(conf) { PZ_CASES(X) }
+#undef X
+  return cudaErrorInvalidValue;
+}
+int pz_pair_clusters_b(int conf) {
+#define X(c) \
+  case c: return pz_pair_clusters_t<c>();
+  switch(conf) { PZ_CASES(X) }
+#undef X
+  return 0;
+}
+
+} // namespace ccsdt

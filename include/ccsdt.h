@@ -78,7 +78,9 @@ typedef struct {
                           /* sqrt(budget_triplets / triplets of the call); 0 = the whole call   */
   int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05 */
   int    test_single_cta; /* testing: 1 = single-CTA persistent kernel, not the 2-CTA cluster  */
-  int    reserved[3];
+  int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
+                             slice count they use, once per handle, before the timed work      */
+  int    reserved[2];
 } ccsdt_opts;
 
 typedef struct {
@@ -146,6 +148,20 @@ ccsdt_status ccsdt_upload_end(ccsdt_handle* h);
 ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
                                    const double* t1, const double* t2, int n_chol, const double* chol_oo,
                                    const double* chol_ov, const double* chol_vv, int on_device);
+
+/* Tile configurations of the persistent split-precision contraction (tcgen05 path, slices 1-5):
+ *   ccsdt_tile_configs     lists the compiled ones for `slices`: *n of them, {N tile, pipeline
+ *                          stages, K chunk} each in nt_st_kc[3 n] (nullable); index 0 is the default;
+ *   ccsdt_autotune         times each on one triplet of the handle's system (CUDA events around the
+ *                          contraction launch), keeps the fastest for the handle's later calls with
+ *                          that slice count; ms[n] (nullable) the times, *chosen (nullable) the index;
+ *   ccsdt_set_tile_config  selects one by index (testing, or a stored autotune result).
+ * Every configuration gives bit-identical energies: the digit-level sums are exact integers
+ * whatever the tiling, and each element's float-float fold does not depend on the tile.  The
+ * reference has no counterpart (its kernels have fixed tile shapes). */
+ccsdt_status ccsdt_tile_configs(int slices, int* n, int* nt_st_kc);
+ccsdt_status ccsdt_autotune(ccsdt_handle* h, int slices, double* ms, int* n, int* chosen);
+ccsdt_status ccsdt_set_tile_config(ccsdt_handle* h, int slices, int index);
 
 /* Full (T): E[T] and E(T) over every occupied triplet of the shard in opts.  Blocking. */
 ccsdt_status ccsdt_energy(ccsdt_handle* h, const ccsdt_opts* opts, ccsdt_result* out);
