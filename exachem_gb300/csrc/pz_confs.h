@@ -5,7 +5,7 @@
 // the tiling, and each element's fold (four terms in a fixed order, Horner over the levels) does
 // not depend on the tile.  The autotuner (ccsdt_autotune) may therefore pick any of them.
 // Constraints a configuration meets: S NT <= 256 (MMA N), 2 S NT <= 512 (two TMEM level buffers),
-// NT a multiple of 32 (epilogue column quarters of 8), KC in {64, 32}, ST stages of
+// NT a multiple of 16 (epilogue column quarters of a multiple of 4), KC in {64, 32}, ST stages of
 // S 128 KC 2 + S NT KC 2 bytes within the 227 KB of shared memory.
 #pragma once
 
@@ -25,8 +25,8 @@ constexpr PzConf kPzConfs[] = {
   {1, 64, 4, 64}, {1, 32, 6, 64},                 // 0, 1
   {2, 64, 4, 64}, {2, 32, 5, 64},                 // 2, 3
   {3, 64, 3, 64}, {3, 32, 3, 64},                 // 4, 5
-  {4, 64, 4, 32}, {4, 32, 5, 32}, {4, 64, 2, 64}, // 6, 7, 8
-  {5, 32, 4, 32}, {5, 32, 2, 64},                 // 9, 10
+  {4, 64, 4, 32}, {4, 32, 5, 32}, {4, 64, 2, 64}, {4, 48, 5, 32}, // 6, 7, 8, 9
+  {5, 48, 4, 32}, {5, 32, 4, 32}, {5, 32, 2, 64},                 // 10, 11, 12
 };
 constexpr int kPzNConfs = sizeof(kPzConfs) / sizeof(kPzConfs[0]);
 constexpr int kPzSplit  = 6; // configurations [0, 6) live in pz_launch_a.cu, the rest in pz_launch_b.cu
@@ -40,7 +40,7 @@ constexpr int pz_smem_bytes(const PzConf& c) {
   return c.ST * (c.S * 128 * c.KC * 2 + c.S * c.NT * c.KC * 2) + 1024 + 512;
 }
 constexpr bool pz_conf_ok(const PzConf& c) {
-  return c.S >= 1 && c.S <= 5 && c.S * c.NT <= 256 && 2 * c.S * c.NT <= 512 && c.NT % 32 == 0 &&
+  return c.S >= 1 && c.S <= 5 && c.S * c.NT <= 256 && 2 * c.S * c.NT <= 512 && c.NT % 16 == 0 &&
          (c.KC == 64 || c.KC == 32) && c.ST >= 2 && pz_smem_bytes(c) <= 227 * 1024;
 }
 constexpr bool pz_all_ok() {

@@ -14,7 +14,7 @@ def test_tile_configs_fit_the_kernels():
         assert cfg, S
         for nt, st, kc in cfg:
             smem = st * (S * 128 * kc * 2 + S * nt * kc * 2) + 1536
-            assert S * nt <= 256 and 2 * S * nt <= 512 and nt % 32 == 0 and kc in (32, 64) and smem <= 227 * 1024
+            assert S * nt <= 256 and 2 * S * nt <= 512 and nt % 16 == 0 and kc in (32, 64) and smem <= 227 * 1024
     assert FusedTriples.tile_configs(6) == []
 
 
