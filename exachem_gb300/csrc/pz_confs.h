@@ -23,13 +23,13 @@ struct PzConf {
 // o=60 v=500 on GB300).
 constexpr PzConf kPzConfs[] = {
   {1, 64, 4, 64}, {1, 32, 6, 64},                 // 0, 1
-  {2, 64, 4, 64}, {2, 32, 5, 64},                 // 2, 3
-  {3, 64, 3, 64}, {3, 32, 3, 64},                 // 4, 5
-  {4, 64, 4, 32}, {4, 32, 5, 32}, {4, 64, 2, 64}, {4, 48, 5, 32}, // 6, 7, 8, 9
-  {5, 48, 4, 32}, {5, 32, 4, 32}, {5, 32, 2, 64},                 // 10, 11, 12
+  {2, 96, 4, 64}, {2, 64, 4, 64}, {2, 32, 5, 64}, // 2, 3, 4
+  {3, 64, 3, 64}, {3, 32, 3, 64}, {3, 48, 3, 64}, // 5, 6, 7
+  {4, 64, 4, 32}, {4, 32, 5, 32}, {4, 64, 2, 64}, {4, 48, 5, 32}, // 8, 9, 10, 11
+  {5, 48, 4, 32}, {5, 32, 4, 32}, {5, 32, 2, 64},                 // 12, 13, 14
 };
 constexpr int kPzNConfs = sizeof(kPzConfs) / sizeof(kPzConfs[0]);
-constexpr int kPzSplit  = 6; // configurations [0, 6) live in pz_launch_a.cu, the rest in pz_launch_b.cu
+constexpr int kPzSplit  = 8; // configurations [0, 8) live in pz_launch_a.cu, the rest in pz_launch_b.cu
 
 constexpr int pz_default_conf(int S) {
   for(int c = 0; c < kPzNConfs; c++)

@@ -4,9 +4,9 @@
 
 namespace ccsdt {
 
-static_assert(kPzSplit == 6 && kPzConfs[5].S == 3 && kPzConfs[6].S == 4, "the split of the configurations");
+static_assert(kPzSplit == 8 && kPzConfs[7].S == 3 && kPzConfs[8].S == 4, "the split of the configurations");
 
-#define PZ_CASES(X) X(0) X(1) X(2) X(3) X(4) X(5)
+#define PZ_CASES(X) X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7)
 
 cudaError_t pz_launch_pair_a(int conf, const PzParams& p, int ncl, cudaStream_t st) {
 #define X(c) \

@@ -4,9 +4,9 @@
 
 namespace ccsdt {
 
-static_assert(kPzNConfs == 13, "the cases below list every configuration from kPzSplit on");
+static_assert(kPzNConfs == 15, "the cases below list every configuration from kPzSplit on");
 
-#define PZ_CASES(X) X(6) X(7) X(8) X(9) X(10) X(11) X(12)
+#define PZ_CASES(X) X(8) X(9) X(10) X(11) X(12) X(13) X(14)
 
 cudaError_t pz_launch_pair_b(int conf, const PzParams& p, int ncl, cudaStream_t st) {
 #define X(c) \
