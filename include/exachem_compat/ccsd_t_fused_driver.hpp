@@ -199,6 +199,9 @@ inline ccsdt_opts opts_from_env() {
   op.slices      = sl ? std::atoi(sl) : (op.mode == CCSDT_MODE_LEARNED ? 5 : 3);
   const char* bu = std::getenv("EXACHEM_GB300_BUDGET");
   op.energy_budget = bu ? std::atof(bu) : 1e-8;
+  // the contraction's tile configuration tuned on this system on first use (results unchanged)
+  const char* at = std::getenv("EXACHEM_GB300_AUTOTUNE");
+  op.autotune    = at ? std::atoi(at) != 0 : 1;
   return op;
 }
 
