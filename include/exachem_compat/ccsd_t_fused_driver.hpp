@@ -3,7 +3,7 @@
 //   (exachem/cc/ccsd_t/ccsd_t_fused_driver.hpp:73-81, 91-546; called from ccsd_t.cpp:253-256)
 // backed by the GB300 library (include/ccsdt.h).
 //
-// Two layers:
+// Entry points:
 //  * gather_closed_shell(): reads the spin-orbital tiled blocks ExaChem holds - d_t1 {V,O},
 //    d_t2 {V,V,O,O}, v2ijab {O,O,V,V}, v2ijka {O,O,O,V}, v2iabc {O,V,V,V}, k_evl_sorted in MO
 //    order occ_a | occ_b | virt_a | virt_b - with Tensor::get(block ids, buffer), the same call
