@@ -7,7 +7,7 @@ import pytest
 OCC, VIR = [6, 5], [32, 24, 21]       # v = 77: the N tiles of 64 and 32 pad differently
 
 
-def test_tile_configs_fit_the_kernels():
+def test_tile_configs_fit_the_kernels(built):
     from exachem_gb300.ccsd_t import FusedTriples
     for S in range(1, 6):
         cfg = FusedTriples.tile_configs(S)
