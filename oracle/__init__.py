@@ -58,7 +58,28 @@ def ref():
         _ref = ctypes.CDLL(str(REF_LIB))
         _ref.ref_ccsd_t_energy.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _I, ctypes.c_int, _I] + \
             [_D] * 7 + [_D, _D, _D, ctypes.POINTER(ctypes.c_long)]
+        if hasattr(_ref, "ref_ccsd_t_energy_so"):
+            _ref.ref_ccsd_t_energy_so.argtypes = [ctypes.c_int, _I] * 4 + [_D] * 6 + \
+                [ctypes.c_int, _D, _D, ctypes.POINTER(ctypes.c_long)]
     return _ref
+
+
+def ref_energy_spin_orbital(tiles, eps, t1, t2, v2ijab, v2ijka, v2iabc, is_restricted=False):
+    """ExaChem's own CPU (T) on inputs given over spin orbitals (ref_ccsd_t_energy_so):
+    tiles = (occ_a, occ_b, virt_a, virt_b) tile extents; eps in MO order occ_a | occ_b | virt_a |
+    virt_b; dense arrays in the layouts of ExaChem's tensors.  Returns (E[T], E(T), tasks)."""
+    lib = ref()
+    ts = [np.ascontiguousarray(np.asarray(t, dtype=np.int32)) for t in tiles]
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (eps, t1, t2, v2ijab, v2ijka, v2iabc)]
+    args = []
+    for t in ts:
+        args += [len(t), t.ctypes.data_as(_I)]
+    e4, e5, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_long()
+    rc = lib.ref_ccsd_t_energy_so(*args, *[a.ctypes.data_as(_D) for a in arrs], int(bool(is_restricted)),
+                                  ctypes.byref(e4), ctypes.byref(e5), ctypes.byref(n))
+    if rc:
+        raise RuntimeError(f"ref_ccsd_t_energy_so failed ({rc})")
+    return e4.value, e5.value, n.value
 
 
 def _arrs(d):

@@ -53,53 +53,20 @@ std::vector<size_t> split_range(size_t n, size_t ts) {
 
 } // namespace
 
-extern "C" int ref_ccsd_t_energy(int o, int v, int n_occ_tiles, const int* occ_tiles, int n_vir_tiles,
-                                 const int* vir_tiles, const double* eps_occ, const double* eps_vir,
-                                 const double* t1, const double* t2, const double* oovv,
-                                 const double* ooov, const double* ovvv, double* e_bracket,
-                                 double* e_paren, double* ops_out, long* tasks_out) {
-  std::vector<size_t> otl(occ_tiles, occ_tiles + n_occ_tiles), vtl(vir_tiles, vir_tiles + n_vir_tiles);
-  size_t so = 0, sv = 0;
-  for(auto x: otl) so += x;
-  for(auto x: vtl) sv += x;
-  if((int) so != o || (int) sv != v) return 1;
-
-  // MO tiles: occ_a | occ_b | virt_a | virt_b
-  std::vector<size_t> k_range;
-  for(auto x: otl) k_range.push_back(x);
-  for(auto x: otl) k_range.push_back(x);
-  for(auto x: vtl) k_range.push_back(x);
-  for(auto x: vtl) k_range.push_back(x);
-  const Index noa = otl.size(), nva = vtl.size();
-  const Index noab = 2 * noa, nvab = 2 * nva;
-  std::vector<int> k_spin;
-  for(Index t = 0; t < noab; t++) k_spin.push_back(t < noa ? 1 : 2);
-  for(Index t = 0; t < nvab; t++) k_spin.push_back(t < nva ? 1 : 2);
-  std::vector<size_t> k_offset;
-  size_t              acc = 0;
-  for(auto x: k_range) {
-    k_offset.push_back(acc);
-    acc += x;
-  }
-  std::vector<double> k_evl_sorted;
-  for(int s = 0; s < 2; s++)
-    for(int i = 0; i < o; i++) k_evl_sorted.push_back(eps_occ[i]);
-  for(int s = 0; s < 2; s++)
-    for(int a = 0; a < v; a++) k_evl_sorted.push_back(eps_vir[a]);
-
-  std::vector<size_t> OT, VT; // tile lists of the spin-orbital occ / virt spaces
-  for(Index t = 0; t < noab; t++) OT.push_back(k_range[t]);
-  for(Index t = 0; t < nvab; t++) VT.push_back(k_range[noab + t]);
-  Tensor<double> d_t1, d_t2;
-  exachem::cholesky_2e::V2Tensors<double> d_v2;
-  build_spin_orbital(o, v, OT, VT, t1, t2, oovv, ooov, ovvv, d_t1, d_t2, d_v2);
-
-  // buffer sizes as in ccsd_t_fused_driver.hpp:176-195 (tilesize_opt = true)
+// The task loop of CCSD_T_Fused_Driver::execute restated for one rank
+// (cc/ccsd_t/ccsd_t_fused_driver.hpp:176-195 buffer sizes, :368-483 tasks), calling the
+// reference's total_fused_ccsd_t_cpu for every surviving tile block.
+static int run_tasks(std::vector<size_t>& k_range, Index noab, Index nvab, Index noa, Index nva,
+                     bool tilesize_opt, std::vector<int>& k_spin, std::vector<size_t>& k_offset,
+                     std::vector<double>& k_evl_sorted, Tensor<double>& d_t1, Tensor<double>& d_t2,
+                     exachem::cholesky_2e::V2Tensors<double>& d_v2, bool is_restricted, double* e_bracket,
+                     double* e_paren, double* ops_out, long* tasks_out) {
+  // buffer sizes as in ccsd_t_fused_driver.hpp:176-195
   size_t max_pdim = 0, max_hdim = 0;
   for(size_t t = noab; t < noab + nvab; t++) max_pdim = std::max(max_pdim, k_range[t]);
   for(size_t t = 0; t < noab; t++) max_hdim = std::max(max_hdim, k_range[t]);
-  size_t max_d1_kernels_pertask = 9 * noa;
-  size_t max_d2_kernels_pertask = 9 * nva;
+  size_t max_d1_kernels_pertask = tilesize_opt ? 9 * noa : 9 * noab;
+  size_t max_d2_kernels_pertask = tilesize_opt ? 9 * nva : 9 * nvab;
   size_t size_T_s1_t1           = 9 * max_pdim * max_hdim;
   size_t size_T_s1_v2           = 9 * (max_pdim * max_pdim) * (max_hdim * max_hdim);
   size_t size_T_d1_t2 = max_d1_kernels_pertask * (max_pdim * max_pdim) * (max_hdim * max_hdim);
@@ -115,7 +82,6 @@ extern "C" int ref_ccsd_t_energy(int o, int v, int n_occ_tiles, const int* occ_t
   LRUCache<Index, std::vector<double>> c1, c2, c3, c4, c5, c6;
   std::vector<double>                  energy_l(2, 0.0);
   long                                 ntasks = 0;
-  const bool                           is_restricted = true;
   std::vector<std::tuple<size_t, size_t, size_t, size_t, size_t, size_t, double>> task_list;
 
   // task loop: ccsd_t_fused_driver.hpp:368-395 (single rank, every task taken)
@@ -161,6 +127,51 @@ extern "C" int ref_ccsd_t_energy(int o, int v, int n_occ_tiles, const int* occ_t
   return 0;
 }
 
+extern "C" int ref_ccsd_t_energy(int o, int v, int n_occ_tiles, const int* occ_tiles, int n_vir_tiles,
+                                 const int* vir_tiles, const double* eps_occ, const double* eps_vir,
+                                 const double* t1, const double* t2, const double* oovv,
+                                 const double* ooov, const double* ovvv, double* e_bracket,
+                                 double* e_paren, double* ops_out, long* tasks_out) {
+  std::vector<size_t> otl(occ_tiles, occ_tiles + n_occ_tiles), vtl(vir_tiles, vir_tiles + n_vir_tiles);
+  size_t so = 0, sv = 0;
+  for(auto x: otl) so += x;
+  for(auto x: vtl) sv += x;
+  if((int) so != o || (int) sv != v) return 1;
+
+  // MO tiles: occ_a | occ_b | virt_a | virt_b
+  std::vector<size_t> k_range;
+  for(auto x: otl) k_range.push_back(x);
+  for(auto x: otl) k_range.push_back(x);
+  for(auto x: vtl) k_range.push_back(x);
+  for(auto x: vtl) k_range.push_back(x);
+  const Index noa = otl.size(), nva = vtl.size();
+  const Index noab = 2 * noa, nvab = 2 * nva;
+  std::vector<int> k_spin;
+  for(Index t = 0; t < noab; t++) k_spin.push_back(t < noa ? 1 : 2);
+  for(Index t = 0; t < nvab; t++) k_spin.push_back(t < nva ? 1 : 2);
+  std::vector<size_t> k_offset;
+  size_t              acc = 0;
+  for(auto x: k_range) {
+    k_offset.push_back(acc);
+    acc += x;
+  }
+  std::vector<double> k_evl_sorted;
+  for(int s = 0; s < 2; s++)
+    for(int i = 0; i < o; i++) k_evl_sorted.push_back(eps_occ[i]);
+  for(int s = 0; s < 2; s++)
+    for(int a = 0; a < v; a++) k_evl_sorted.push_back(eps_vir[a]);
+
+  std::vector<size_t> OT, VT; // tile lists of the spin-orbital occ / virt spaces
+  for(Index t = 0; t < noab; t++) OT.push_back(k_range[t]);
+  for(Index t = 0; t < nvab; t++) VT.push_back(k_range[noab + t]);
+  Tensor<double> d_t1, d_t2;
+  exachem::cholesky_2e::V2Tensors<double> d_v2;
+  build_spin_orbital(o, v, OT, VT, t1, t2, oovv, ooov, ovvv, d_t1, d_t2, d_v2);
+
+  return run_tasks(k_range, noab, nvab, noa, nva, true, k_spin, k_offset, k_evl_sorted, d_t1, d_t2, d_v2, true,
+                   e_bracket, e_paren, ops_out, tasks_out);
+}
+
 // the uniform tiling the reference builds from ccsdt_tilesize (cholesky_2e.cpp:230-285)
 extern "C" int ref_ccsd_t_energy_ts(int o, int v, int ts, const double* eps_occ,
                                     const double* eps_vir, const double* t1, const double* t2,
@@ -171,4 +182,47 @@ extern "C" int ref_ccsd_t_energy_ts(int o, int v, int ts, const double* eps_occ,
   std::vector<int> oti(ot.begin(), ot.end()), vti(vt.begin(), vt.end());
   return ref_ccsd_t_energy(o, v, (int) oti.size(), oti.data(), (int) vti.size(), vti.data(), eps_occ,
                            eps_vir, t1, t2, oovv, ooov, ovvv, e_bracket, e_paren, ops_out, tasks_out);
+}
+
+// Any (restricted or open-shell) input given directly over spin orbitals, in the layouts of
+// ExaChem's tensors: MO order occ_a | occ_b | virt_a | virt_b with the tile extents of each range;
+// eps[O + V] in that order; dense t1[V][O], t2[V][V][O][O], v2ijab[O][O][V][V] = <ij||ab>,
+// v2ijka[O][O][O][V] = <ij||ka>, v2iabc[O][V][V][V] = <ia||bc> over the spin-orbital occupied
+// (O = occ_a + occ_b) and virtual (V = virt_a + virt_b) ranges.  is_restricted selects the
+// reference's spin filter and factor (ccsd_t_fused_driver.hpp:383-392); the buffers are sized
+// for every tile (tilesize_opt = false, :181-182), as alpha and beta tile counts may differ.
+extern "C" int ref_ccsd_t_energy_so(int n_oa, const int* oa, int n_ob, const int* ob, int n_va, const int* va,
+                                    int n_vb, const int* vb, const double* eps, const double* t1,
+                                    const double* t2, const double* v2ijab, const double* v2ijka,
+                                    const double* v2iabc, int is_restricted, double* e_bracket,
+                                    double* e_paren, long* tasks_out) {
+  std::vector<size_t> k_range;
+  std::vector<int>    k_spin;
+  size_t              O = 0, V = 0;
+  for(int t = 0; t < n_oa; t++) k_range.push_back(oa[t]), k_spin.push_back(1), O += oa[t];
+  for(int t = 0; t < n_ob; t++) k_range.push_back(ob[t]), k_spin.push_back(2), O += ob[t];
+  for(int t = 0; t < n_va; t++) k_range.push_back(va[t]), k_spin.push_back(1), V += va[t];
+  for(int t = 0; t < n_vb; t++) k_range.push_back(vb[t]), k_spin.push_back(2), V += vb[t];
+  const Index noab = n_oa + n_ob, nvab = n_va + n_vb;
+  std::vector<size_t> k_offset;
+  size_t              acc = 0;
+  for(auto x: k_range) {
+    k_offset.push_back(acc);
+    acc += x;
+  }
+  std::vector<double> k_evl_sorted(eps, eps + O + V);
+  std::vector<size_t> OT(k_range.begin(), k_range.begin() + noab), VT(k_range.begin() + noab, k_range.end());
+  Tensor<double>                          d_t1({VT, OT}), d_t2({VT, VT, OT, OT});
+  exachem::cholesky_2e::V2Tensors<double> d_v2;
+  d_v2.v2ijab = Tensor<double>({OT, OT, VT, VT});
+  d_v2.v2ijka = Tensor<double>({OT, OT, OT, VT});
+  d_v2.v2iabc = Tensor<double>({OT, VT, VT, VT});
+  // the dense arrays are row-major in the tensors' own index order
+  std::copy(t1, t1 + V * O, d_t1.data());
+  std::copy(t2, t2 + V * V * O * O, d_t2.data());
+  std::copy(v2ijab, v2ijab + O * O * V * V, d_v2.v2ijab.data());
+  std::copy(v2ijka, v2ijka + O * O * O * V, d_v2.v2ijka.data());
+  std::copy(v2iabc, v2iabc + O * V * V * V, d_v2.v2iabc.data());
+  return run_tasks(k_range, noab, nvab, n_oa, n_va, false, k_spin, k_offset, k_evl_sorted, d_t1, d_t2, d_v2,
+                   is_restricted != 0, e_bracket, e_paren, nullptr, tasks_out);
 }

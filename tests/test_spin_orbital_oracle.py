@@ -1,0 +1,75 @@
+"""The spin-orbital (T) oracle (oracle/spin_orbital_oracle.py), the groundwork for an open-shell
+path.  Pinned two ways:
+- on closed-shell systems it equals the closed-shell oracle, which the reference's golden
+  vectors pin (tests/test_oracle_golden.py);
+- against ExaChem's own CPU (T) kernels (oracle/_ref, ref_ccsd_t_energy_so) given the same
+  spin-orbital tensors: restricted and unrestricted on RHF-derived inputs, unrestricted on
+  open-shell inputs (alpha and beta orbital sets of different sizes).
+CPU only; the comparisons with oracle/_ref skip where the reference tree is not built."""
+import numpy as np
+import pytest
+
+import oracle
+from exachem_gb300.generator import generate
+from oracle.spin_orbital_oracle import energy_spin_orbital, open_shell_system, spin_orbital_inputs
+
+needs_ref = pytest.mark.skipif(not oracle.REF_LIB.exists(), reason="reference tree not built here")
+
+
+def _tiles(n, t):
+    """Tile extents of n orbitals in tiles of at most t (the last one ragged)."""
+    return [t] * (n // t) + ([n % t] if n % t else [])
+
+
+@pytest.mark.parametrize("o,v,seed", [(3, 6, 1), (4, 7, 2), (2, 5, 3)])
+def test_spin_orbital_oracle_equals_closed_shell_oracle(o, v, seed):
+    d = generate(o, v, seed)
+    c4, c5 = oracle.energy(d)
+    s4, s5 = energy_spin_orbital(*spin_orbital_inputs(d))
+    assert s4 == pytest.approx(c4, rel=1e-12, abs=0)
+    assert s5 == pytest.approx(c5, rel=1e-12, abs=0)
+
+
+def test_open_shell_system_has_the_reference_symmetries():
+    eps_o, eps_v, t1, t2, v2ijab, v2ijka, v2iabc = open_shell_system(3, 2, 5, 4, 6, 9)
+    np.testing.assert_array_equal(t2, -t2.transpose(1, 0, 2, 3))
+    np.testing.assert_array_equal(t2, -t2.transpose(0, 1, 3, 2))
+    np.testing.assert_allclose(v2ijab, -v2ijab.transpose(0, 1, 3, 2), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(v2ijab, -v2ijab.transpose(1, 0, 2, 3), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(v2iabc, -v2iabc.transpose(0, 1, 3, 2), rtol=0, atol=1e-15)
+    # spin conservation: alpha occupied 0..2, beta 3..4; alpha virtual 0..4, beta 5..8
+    assert not t1[:5, 3:].any() and not t1[5:, :3].any()
+    assert not t2[:5, :5, 3:, 3:].any() and not v2ijab[:3, :3, 5:, 5:].any()
+
+
+@needs_ref
+@pytest.mark.parametrize("restricted", [True, False])
+@pytest.mark.parametrize("o,v,ot,vt,seed", [(4, 7, 2, 4, 2), (3, 6, 2, 4, 1), (5, 5, 3, 2, 4)])
+def test_reference_spin_orbital_kernels_on_closed_shell_inputs(o, v, ot, vt, seed, restricted):
+    d = generate(o, v, seed)
+    eps_o, eps_v, *rest = spin_orbital_inputs(d)
+    c4, c5 = oracle.energy(d)
+    tiles = (_tiles(o, ot), _tiles(o, ot), _tiles(v, vt), _tiles(v, vt))
+    r4, r5, ntask = oracle.ref_energy_spin_orbital(tiles, np.concatenate([eps_o, eps_v]), *rest,
+                                                   is_restricted=restricted)
+    assert ntask > 0
+    assert r4 == pytest.approx(c4, rel=1e-12, abs=0)
+    assert r5 == pytest.approx(c5, rel=1e-12, abs=0)
+
+
+@needs_ref
+@pytest.mark.parametrize("oa,ob,va,vb,ot,vt,seed", [
+    (3, 2, 5, 6, 2, 3, 5),
+    (4, 3, 6, 7, 2, 4, 6),
+    (2, 2, 4, 4, 1, 3, 7),
+    (5, 1, 3, 7, 3, 2, 8),
+])
+def test_open_shell_oracle_equals_reference_unrestricted(oa, ob, va, vb, ot, vt, seed):
+    sys_ = open_shell_system(oa, ob, va, vb, 7, seed)
+    e4, e5 = energy_spin_orbital(*sys_)
+    tiles = (_tiles(oa, ot), _tiles(ob, ot), _tiles(va, vt), _tiles(vb, vt))
+    r4, r5, ntask = oracle.ref_energy_spin_orbital(tiles, np.concatenate(sys_[:2]), *sys_[2:],
+                                                   is_restricted=False)
+    assert ntask > 0
+    assert e4 == pytest.approx(r4, rel=1e-12, abs=0)
+    assert e5 == pytest.approx(r5, rel=1e-12, abs=0)
