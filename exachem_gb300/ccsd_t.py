@@ -54,7 +54,7 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc", "ccsdt_shard_triplets",
             "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates",
             "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky",
-            "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config"]
+            "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config", "ccsdt_energy_spin_orbital"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
@@ -84,6 +84,7 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_tile_configs.argtypes = [ctypes.c_int, ip, ip]
     lib.ccsdt_autotune.argtypes = [vp, ctypes.c_int, dp, ip, ip]
     lib.ccsdt_set_tile_config.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.ccsdt_energy_spin_orbital.argtypes = [ctypes.c_int] * 4 + [vp] * 7 + [ctypes.c_int] * 3 + [dp, dp]
     lib.ccsdt_triplet_error_estimates.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp, dp]
     lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
@@ -100,7 +101,8 @@ def load_library(path: str | os.PathLike | None = None):
                  "ccsdt_reference_op_count", "ccsdt_set_stream", "ccsdt_profile_triplet",
                  "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
                  "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end",
-                 "ccsdt_upload_cholesky", "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config"):
+                 "ccsdt_upload_cholesky", "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config",
+                 "ccsdt_energy_spin_orbital"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -326,6 +328,34 @@ class FusedTriples:
             self.close()
         except Exception:
             pass
+
+
+def energy_spin_orbital(oa: int, ob: int, va: int, vb: int, eps_occ, eps_vir, t1, t2, v2ijab, v2ijka,
+                        v2iabc, shard_index: int = 0, shard_count: int = 1) -> dict:
+    """Open-shell (T) over spin orbitals (ccsdt_energy_spin_orbital): ExaChem's MO order
+    (occupied alpha | beta, virtual alpha | beta), arrays t1[V][O], t2[V][V][O][O],
+    v2ijab[O][O][V][V], v2ijka[O][O][O][V], v2iabc[O][V][V][V] as host numpy arrays or CUDA
+    tensors (all of one kind).  shard_index / shard_count select every shard_count-th occupied
+    triplet i < j < k."""
+    lib = load_library()
+    arrs = [eps_occ, eps_vir, t1, t2, v2ijab, v2ijka, v2iabc]
+    kinds = {isinstance(a, np.ndarray) for a in arrs}
+    if len(kinds) != 1:
+        raise TypeError("inputs must be all host arrays or all device tensors")
+    O, V = oa + ob, va + vb
+    shapes = [(O,), (V,), (V, O), (V, V, O, O), (O, O, V, V), (O, O, O, V), (O, V, V, V)]
+    for a, sh in zip(arrs, shapes):
+        if tuple(a.shape) != sh:
+            raise ValueError(f"expected shape {sh}, got {tuple(a.shape)}")
+    on_device = 0 if kinds == {True} else 1
+    e = (ctypes.c_double * 2)()
+    sec = ctypes.c_double()
+    st = lib.ccsdt_energy_spin_orbital(oa, ob, va, vb, *[_ptr(a) for a in arrs], on_device, shard_index,
+                                       shard_count, ctypes.cast(e, ctypes.POINTER(ctypes.c_double)),
+                                       ctypes.byref(sec))
+    if st:
+        raise CCSDTError(st, lib.ccsdt_status_string(st).decode())
+    return {"e_bracket_T": e[0], "e_paren_T": e[1], "seconds": sec.value}
 
 
 def all_triplets(o: int) -> np.ndarray:

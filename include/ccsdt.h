@@ -226,6 +226,32 @@ ccsdt_status ccsdt_energy_noalloc(int o, int v, const double* eps_occ, const dou
                                   const double* ooov, const double* ovvv, double* energies,
                                   void* stream);
 
+/* ---- open-shell (UHF) (T) over spin orbitals ------------------------------------------
+ * ExaChem's fused driver with is_restricted = false (ccsd_t_fused_driver.hpp:383-392, the
+ * spin filter and factor; its inputs come from ccsd_t.cpp:253-256).  Spin orbitals in
+ * ExaChem's MO order: occupied alpha (oa) | occupied beta (ob), virtual alpha (va) | virtual
+ * beta (vb); O = oa + ob, V = va + vb.  Dense row-major arrays in the index order of
+ * ExaChem's tensors (exachem/cholesky/v2tensors.cpp:67-86 for the V2 blocks):
+ *   eps_occ[O], eps_vir[V]      orbital energies
+ *   t1[V][O]                    t1(a, i)
+ *   t2[V][V][O][O]              t2(a, b, i, j)
+ *   v2ijab[O][O][V][V]          <ij||ab>
+ *   v2ijka[O][O][O][V]          <ij||ka>
+ *   v2iabc[O][V][V][V]          <ia||bc>
+ * Elements of spin-forbidden blocks are never read (they may hold anything).  FP64 DMMA
+ * contractions over the spin-allowed blocks only; energies[0] = E[T], energies[1] = E(T)
+ * (host memory).  on_device = 1: the arrays are device pointers on the current device;
+ * 0: host pointers, copied in by the call.  shard_index / shard_count: the call takes the
+ * occupied triplets i < j < k with t % shard_count == shard_index (t counts them in
+ * lexicographic order) and returns that part of the energies (shard_count 0 or 1: all).
+ * seconds (may be NULL) receives the device time of the call, copies included.
+ * Restricted (RHF) inputs in this form give the closed-shell energies. */
+ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb, const double* eps_occ,
+                                       const double* eps_vir, const double* t1, const double* t2,
+                                       const double* v2ijab, const double* v2ijka,
+                                       const double* v2iabc, int on_device, int shard_index,
+                                       int shard_count, double* energies, double* seconds);
+
 /* ---- learned slice count (no counterpart in the reference) --------------------------
  * A 12 -> 64 -> 64 -> 7 MLP (ReLU, softmax over slice counts 2..8) predicts, per occupied
  * triplet, the smallest digit-plane count that keeps the triplet's energy error under a

@@ -18,6 +18,9 @@
 //    It is a template over the tensor types, so it needs only Tensor<T>::get.
 //  * gather_cholesky() + run_closed_shell_cholesky(): the alternative that skips V2 - the
 //    alpha-alpha blocks of the Cholesky tensor cholVpr, with the integral blocks built on the GPU.
+//  * gather_spin_orbital() + run_spin_orbital(): the open-shell case (is_restricted = false) -
+//    every spin-allowed block of the same tensors, alpha and beta tile lists of their own, into
+//    the dense spin-orbital arrays of ccsdt_energy_spin_orbital.
 //  * CCSD_T_Fused_Driver<T>::execute(): the reference's signature, compiled when
 //    EXACHEM_GB300_WITH_TAMM is defined (inside an ExaChem build).  Each rank of the process
 //    group takes every size-th occupied triplet on its own GPU and returns its partial
@@ -411,6 +414,122 @@ std::tuple<T, T, double, double> run_tiled(const std::vector<size_t>& mo, size_t
   }
 }
 
+// ---- open shell (is_restricted = false) ----------------------------------------------------
+
+// Dense spin-orbital arrays of ccsdt_energy_spin_orbital (include/ccsdt.h): MO order occ_a | occ_b,
+// virt_a | virt_b; t1[V][O], t2[V][V][O][O], v2ijab[O][O][V][V], v2ijka[O][O][O][V], v2iabc[O][V][V][V].
+struct SpinOrbitalInputs {
+  int                 oa = 0, ob = 0, va = 0, vb = 0;
+  std::vector<double> eps_occ, eps_vir, t1, t2, v2ijab, v2ijka, v2iabc;
+};
+
+namespace detail {
+// One mode of a tiled tensor: tile extents, offsets and spins (0 alpha, 1 beta).
+struct ModeTiles {
+  std::vector<size_t> ext, off;
+  std::vector<int>    spin;
+  size_t              n = 0;
+};
+
+inline ModeTiles mode_tiles(const std::vector<size_t>& ext, size_t n_alpha_tiles) {
+  ModeTiles m;
+  m.ext = ext;
+  m.off = offsets(ext);
+  for(size_t t = 0; t < ext.size(); t++) {
+    m.spin.push_back(t >= n_alpha_tiles);
+    m.n += ext[t];
+  }
+  return m;
+}
+
+// Every block of a rank-R tensor whose spins pass `allowed` (TAMM's spin check: the spins of the
+// upper indices sum to those of the lower ones) is read with Tensor::get and scattered into the
+// dense row-major array `dst` over the full extents; other blocks are neither read nor stored.
+template<typename T, size_t R, typename TensorT, typename F>
+void gather_dense(TensorT& X, const ModeTiles* const (&modes)[R], F allowed, std::vector<double>& dst) {
+  size_t total = 1;
+  for(size_t m = 0; m < R; m++) total *= modes[m]->n;
+  dst.assign(total, 0.0);
+  std::vector<T> buf;
+  size_t         bid[R] = {};
+  for(;;) {
+    int sp[R];
+    for(size_t m = 0; m < R; m++) sp[m] = modes[m]->spin[bid[m]];
+    bool empty = false;
+    for(size_t m = 0; m < R; m++) empty = empty || modes[m]->ext[bid[m]] == 0;
+    if(!empty && allowed(sp)) {
+      static_assert(R == 2 || R == 4, "T1 / T2 / V2 tensors");
+      if constexpr(R == 2) X.get({bid[0], bid[1]}, buf); // tile ids as the closed-shell gathers pass them
+      else X.get({bid[0], bid[1], bid[2], bid[3]}, buf);
+      size_t c[R] = {}, nb = 1;
+      for(size_t m = 0; m < R; m++) nb *= modes[m]->ext[bid[m]];
+      for(size_t e = 0; e < nb; e++) {
+        size_t lin = 0;
+        for(size_t m = 0; m < R; m++) lin = lin * modes[m]->n + modes[m]->off[bid[m]] + c[m];
+        dst[lin] = (double) buf[e];
+        for(size_t m = R; m-- > 0;) {
+          if(++c[m] < modes[m]->ext[bid[m]]) break;
+          c[m] = 0;
+        }
+      }
+    }
+    size_t m = R;
+    while(m-- > 0) {
+      if(++bid[m] < modes[m]->ext.size()) break;
+      bid[m] = 0;
+    }
+    if(m == (size_t) -1) break;
+  }
+}
+} // namespace detail
+
+// mo_tiles: extents of the MO tiles in the order occ_a (noa tiles), occ_b (nob), virt_a (nva),
+// virt_b (nvb); k_evl_sorted in the same order.  Reads the spin-allowed blocks of the tensors the
+// reference driver takes (ccsd_t_fused_driver.hpp:73-81) into the dense arrays of
+// ccsdt_energy_spin_orbital.
+template<typename T, typename TensorT, typename V2T>
+SpinOrbitalInputs gather_spin_orbital(const std::vector<size_t>& mo_tiles, size_t noa, size_t nob, size_t nva,
+                                      size_t nvb, TensorT& d_t1, TensorT& d_t2, V2T& d_v2,
+                                      const std::vector<T>& k_evl_sorted) {
+  if(mo_tiles.size() != noa + nob + nva + nvb) throw std::invalid_argument("MO tiles != noa + nob + nva + nvb");
+  const auto Om = detail::mode_tiles({mo_tiles.begin(), mo_tiles.begin() + noa + nob}, noa);
+  const auto Vm = detail::mode_tiles({mo_tiles.begin() + noa + nob, mo_tiles.end()}, nva);
+  SpinOrbitalInputs S;
+  for(size_t t = 0; t < noa; t++) S.oa += (int) Om.ext[t];
+  for(size_t t = 0; t < nva; t++) S.va += (int) Vm.ext[t];
+  S.ob = (int) Om.n - S.oa;
+  S.vb = (int) Vm.n - S.va;
+  if(k_evl_sorted.size() < Om.n + Vm.n) throw std::invalid_argument("k_evl_sorted too short");
+  S.eps_occ.assign(k_evl_sorted.begin(), k_evl_sorted.begin() + Om.n);
+  S.eps_vir.assign(k_evl_sorted.begin() + Om.n, k_evl_sorted.begin() + Om.n + Vm.n);
+  const detail::ModeTiles *O = &Om, *V = &Vm;
+  const detail::ModeTiles* const m_t1[2]     = {V, O};
+  const detail::ModeTiles* const m_t2[4]     = {V, V, O, O};
+  const detail::ModeTiles* const m_ijab[4]   = {O, O, V, V};
+  const detail::ModeTiles* const m_ijka[4]   = {O, O, O, V};
+  const detail::ModeTiles* const m_iabc[4]   = {O, V, V, V};
+  auto                           pair_rule   = [](const int* s) { return s[0] + s[1] == s[2] + s[3]; };
+  detail::gather_dense<T>(d_t1, m_t1, [](const int* s) { return s[0] == s[1]; }, S.t1);
+  detail::gather_dense<T>(d_t2, m_t2, pair_rule, S.t2);
+  detail::gather_dense<T>(d_v2.v2ijab, m_ijab, pair_rule, S.v2ijab);
+  detail::gather_dense<T>(d_v2.v2ijka, m_ijka, pair_rule, S.v2ijka);
+  detail::gather_dense<T>(d_v2.v2iabc, m_iabc, pair_rule, S.v2iabc);
+  return S;
+}
+
+// (T) of a gathered open-shell system on the current device: (E[T], E(T), device seconds) of the
+// triplets t % shard_count == shard_index.
+inline std::tuple<double, double, double> run_spin_orbital(const SpinOrbitalInputs& S, int shard_index = 0,
+                                                           int shard_count = 1) {
+  double             e[2] = {0.0, 0.0}, secs = 0.0;
+  const ccsdt_status st =
+    ccsdt_energy_spin_orbital(S.oa, S.ob, S.va, S.vb, S.eps_occ.data(), S.eps_vir.data(), S.t1.data(),
+                              S.t2.data(), S.v2ijab.data(), S.v2ijka.data(), S.v2iabc.data(), 0, shard_index,
+                              shard_count, e, &secs);
+  if(st != CCSDT_OK) throw std::runtime_error(std::string("ccsdt_energy_spin_orbital: ") + ccsdt_status_string(st));
+  return {e[0], e[1], secs};
+}
+
 } // namespace exachem_gb300
 
 #ifdef EXACHEM_GB300_WITH_TAMM
@@ -429,14 +548,21 @@ public:
           bool seq_h3b = false, bool tilesize_opt = true) {
     (void) chem_env, (void) k_spin, (void) hf_ccsd_energy, (void) cache_s1t, (void) cache_s1v;
     (void) cache_d1t, (void) cache_d1v, (void) cache_d2t, (void) cache_d2v, (void) seq_h3b, (void) tilesize_opt;
-    if(!is_restricted) throw std::invalid_argument("the GB300 (T) path is closed-shell (RHF) only");
     auto                t0 = std::chrono::steady_clock::now();
     std::vector<size_t> mo;
     for(auto x: MO.input_tile_sizes()) mo.push_back((size_t) x);
     const size_t noa = MO("occ_alpha").num_tiles(), nva = MO("virt_alpha").num_tiles();
-    ccsdt_opts   op = exachem_gb300::opts_from_env();
-    op.shard_index  = (int) ec.pg().rank().value();
-    op.shard_count  = (int) ec.pg().size().value();
+    const int    rank = (int) ec.pg().rank().value(), size = (int) ec.pg().size().value();
+    if(!is_restricted) { // open shell: every spin case, FP64, this rank's share of the triplets
+      const size_t nob = MO("occ_beta").num_tiles(), nvb = MO("virt_beta").num_tiles();
+      auto S = exachem_gb300::gather_spin_orbital<T>(mo, noa, nob, nva, nvb, d_t1, d_t2, d_v2, k_evl_sorted);
+      auto [e4, e5, secs] = exachem_gb300::run_spin_orbital(S, rank, size);
+      const double total  = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      return {(T) e4, (T) e5, secs, total};
+    }
+    ccsdt_opts op  = exachem_gb300::opts_from_env();
+    op.shard_index = rank;
+    op.shard_count = size;
     return exachem_gb300::run_tiled<T>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl_sorted, op, t0);
   }
 };

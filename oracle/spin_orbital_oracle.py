@@ -166,3 +166,34 @@ def open_shell_system(oa: int, ob: int, va: int, vb: int, nq: int, seed: int):
     eps_o = -1.0 - rng.random(O)
     eps_v = 0.3 + rng.random(V)
     return eps_o, eps_v, t1, t2, v2ijab, v2ijka, v2iabc
+
+
+def spin_orbital_inputs_vec(d: dict):
+    """spin_orbital_inputs() with array operations (same result, element for element), for sizes
+    where the loops are too slow."""
+    o, v = int(d["o"]), int(d["v"])
+    so, sv = np.arange(2 * o) // o, np.arange(2 * v) // v     # spins
+    po, pv = np.arange(2 * o) % o, np.arange(2 * v) % v       # spatial indices
+    t1s, t2s, ovov, ooov, ovvv = d["t1"], d["t2"], d["oovv"], d["ooov"], d["ovvv"]
+    t1 = np.where(sv[:, None] == so[None, :], t1s.T[pv[:, None], po[None, :]], 0.0)
+    A, B, I, J = np.ix_(pv, pv, po, po)
+    sa, sb, si, sj = np.ix_(sv, sv, so, so)
+    same = (sa == sb) & (sb == si) & (si == sj)
+    t2 = np.where(same, t2s[I, J, A, B] - t2s[I, J, B, A], 0.0)
+    t2 = np.where((sa == si) & (sb == sj) & (sa != sb), t2s[I, J, A, B], t2)
+    t2 = np.where((sa == sj) & (sb == si) & (sa != sb), -t2s[J, I, A, B], t2)
+    I, J, A, B = np.ix_(po, po, pv, pv)
+    si, sj, sa, sb = np.ix_(so, so, sv, sv)
+    v2ijab = (np.where((si == sa) & (sj == sb), ovov[I, J, A, B], 0.0)
+              - np.where((si == sb) & (sj == sa), ovov[I, J, B, A], 0.0))
+    I, J, K, A = np.ix_(po, po, po, pv)
+    si, sj, sk, sa = np.ix_(so, so, so, sv)
+    v2ijka = (np.where((si == sk) & (sj == sa), ooov[I, K, J, A], 0.0)
+              - np.where((sj == sk) & (si == sa), ooov[J, K, I, A], 0.0))
+    I, A, B, C = np.ix_(po, pv, pv, pv)
+    si, sa, sb, sc = np.ix_(so, sv, sv, sv)
+    v2iabc = (np.where((si == sb) & (sa == sc), ovvv[I, B, A, C], 0.0)
+              - np.where((si == sc) & (sa == sb), ovvv[I, C, A, B], 0.0))
+    eps_o = np.concatenate([d["eps_occ"], d["eps_occ"]])
+    eps_v = np.concatenate([d["eps_vir"], d["eps_vir"]])
+    return eps_o, eps_v, t1, t2, v2ijab, v2ijka, v2iabc

@@ -23,7 +23,51 @@ static void rd(std::ifstream& f, X* p, size_t n) {
   f.read(reinterpret_cast<char*>(p), sizeof(X) * n);
 }
 
+// compat_driver --so <so.bin> <out.bin> [--run]: the open-shell case.
+// so.bin : int32 oa, ob, va, vb, n tiles of occ_a, occ_b, virt_a, virt_b, then those tile
+//          extents; float64 eps[O + V] (MO order), t1[V][O], t2[V][V][O][O], v2ijab[O][O][V][V],
+//          v2ijka[O][O][O][V], v2iabc[O][V][V][V] (dense spin-orbital arrays).
+// The arrays fill the TAMM stand-in tensors as they are (spin-forbidden blocks included, which
+// the gather must skip); out.bin = gather_spin_orbital's arrays in the same order, with --run
+// followed by E[T], E(T) from run_spin_orbital.
+static int open_shell(int argc, char** argv) {
+  std::ifstream f(argv[2], std::ios::binary);
+  int           hdr[8];
+  rd(f, hdr, 8);
+  std::vector<int> tl(hdr[4] + hdr[5] + hdr[6] + hdr[7]);
+  rd(f, tl.data(), tl.size());
+  const size_t        O = (size_t) hdr[0] + hdr[1], V = (size_t) hdr[2] + hdr[3];
+  std::vector<size_t> mo(tl.begin(), tl.end()), OT(tl.begin(), tl.begin() + hdr[4] + hdr[5]),
+    VT(tl.begin() + hdr[4] + hdr[5], tl.end());
+  std::vector<double> eps(O + V);
+  rd(f, eps.data(), eps.size());
+  tamm::Tensor<double>                    d_t1({VT, OT}), d_t2({VT, VT, OT, OT});
+  exachem::cholesky_2e::V2Tensors<double> d_v2;
+  d_v2.v2ijab = tamm::Tensor<double>({OT, OT, VT, VT});
+  d_v2.v2ijka = tamm::Tensor<double>({OT, OT, OT, VT});
+  d_v2.v2iabc = tamm::Tensor<double>({OT, VT, VT, VT});
+  rd(f, d_t1.data(), V * O);
+  rd(f, d_t2.data(), V * V * O * O);
+  rd(f, d_v2.v2ijab.data(), O * O * V * V);
+  rd(f, d_v2.v2ijka.data(), O * O * O * V);
+  rd(f, d_v2.v2iabc.data(), O * V * V * V);
+  if(!f) return 3;
+  auto S = exachem_gb300::gather_spin_orbital<double>(mo, hdr[4], hdr[5], hdr[6], hdr[7], d_t1, d_t2, d_v2, eps);
+  if((size_t) S.oa + S.ob != O || (size_t) S.va + S.vb != V) return 4;
+  std::ofstream g(argv[3], std::ios::binary);
+  for(auto* a: {&S.eps_occ, &S.eps_vir, &S.t1, &S.t2, &S.v2ijab, &S.v2ijka, &S.v2iabc})
+    g.write(reinterpret_cast<const char*>(a->data()), sizeof(double) * a->size());
+  if(argc > 4 && std::string(argv[4]) == "--run") {
+    auto [e4, e5, secs] = exachem_gb300::run_spin_orbital(S);
+    g.write(reinterpret_cast<const char*>(&e4), sizeof(double));
+    g.write(reinterpret_cast<const char*>(&e5), sizeof(double));
+    std::printf("E[T] %.17g E(T) %.17g (%.3f s)\n", e4, e5, secs);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
+  if(argc > 3 && std::string(argv[1]) == "--so") return open_shell(argc, argv);
   if(argc < 3) return 2;
   std::ifstream f(argv[1], std::ios::binary);
   int           hdr[4];

@@ -135,3 +135,69 @@ def test_adapter_cholesky_call_matches_oracle(tmp_path, built):
     _, extra = _read(tmp_path / "out.bin", d, extra=(o * o + o * v + v * v) * nq + 2)
     e4, e5 = oracle.energy(d)
     assert rel_close(extra[-2], e4, 1e-12) and rel_close(extra[-1], e5, 1e-12)
+
+
+SO_KEYS = ["eps_occ", "eps_vir", "t1", "t2", "v2ijab", "v2ijka", "v2iabc"]
+
+
+def _so_allowed(oa, ob, va, vb):
+    """Spin-allowed masks of t1 {V,O}, t2 {V,V,O,O}, v2ijab {O,O,V,V}, v2ijka {O,O,O,V},
+    v2iabc {O,V,V,V}: the spins of the first half of the indices sum to those of the second."""
+    so = np.array([0] * oa + [1] * ob)
+    sv = np.array([0] * va + [1] * vb)
+
+    def rule(*sp):
+        g = np.meshgrid(*sp, indexing="ij")
+        if len(g) == 2:
+            return g[0] == g[1]
+        return g[0] + g[1] == g[2] + g[3]
+    return [rule(sv, so), rule(sv, sv, so, so), rule(so, so, sv, sv), rule(so, so, so, sv), rule(so, sv, sv, sv)]
+
+
+def _write_so(path, tiles, arrs):
+    with open(path, "wb") as f:
+        dims = [sum(t) for t in tiles]
+        np.array(dims + [len(t) for t in tiles] + [x for t in tiles for x in t], dtype=np.int32).tofile(f)
+        np.concatenate([arrs[0], arrs[1]]).astype(np.float64).tofile(f)
+        for a in arrs[2:]:
+            np.ascontiguousarray(a, dtype=np.float64).tofile(f)
+
+
+def _read_so(path, arrs, extra=0):
+    raw = np.fromfile(path, dtype=np.float64)
+    out, off = [], 0
+    for a in arrs:
+        out.append(raw[off:off + a.size].reshape(a.shape))
+        off += a.size
+    return out, raw[off:off + extra]
+
+
+def test_adapter_open_shell_gather_is_exact(tmp_path, built):
+    """gather_spin_orbital reads every spin-allowed block of the open-shell tensors bit for bit
+    and none of the spin-forbidden ones (filled with NaN here; they come back as zeros)."""
+    from oracle.spin_orbital_oracle import open_shell_system
+    exe = _compile(tmp_path, link_lib=True)
+    for (oa, ob, va, vb, tiles, seed) in [(3, 2, 5, 6, ([2, 1], [2], [3, 2], [4, 2]), 3),
+                                          (4, 1, 3, 7, ([4], [1], [2, 1], [3, 3, 1]), 4)]:
+        arrs = list(open_shell_system(oa, ob, va, vb, 5, seed))
+        poisoned = arrs[:2] + [np.where(m, a, np.nan) for m, a in zip(_so_allowed(oa, ob, va, vb), arrs[2:])]
+        _write_so(tmp_path / "so.bin", tiles, poisoned)
+        subprocess.run([str(exe), "--so", str(tmp_path / "so.bin"), str(tmp_path / "out.bin")], check=True)
+        got, _ = _read_so(tmp_path / "out.bin", arrs)
+        for name, g, a in zip(SO_KEYS, got, arrs):
+            assert np.array_equal(g, a), name
+
+
+@pytest.mark.gpu
+def test_adapter_open_shell_call_matches_oracle(tmp_path, built):
+    """The open-shell drop-in end to end: tiled spin-orbital tensors -> gather_spin_orbital ->
+    ccsdt_energy_spin_orbital -> E[T], E(T) against the spin-orbital oracle."""
+    from oracle.spin_orbital_oracle import energy_spin_orbital, open_shell_system
+    exe = _compile(tmp_path, link_lib=True)
+    oa, ob, va, vb, tiles = 5, 3, 9, 11, ([3, 2], [3], [5, 4], [6, 5])
+    arrs = list(open_shell_system(oa, ob, va, vb, 8, 31))
+    _write_so(tmp_path / "so.bin", tiles, arrs)
+    subprocess.run([str(exe), "--so", str(tmp_path / "so.bin"), str(tmp_path / "out.bin"), "--run"], check=True)
+    _, extra = _read_so(tmp_path / "out.bin", arrs, extra=2)
+    e4, e5 = energy_spin_orbital(*arrs)
+    assert rel_close(extra[0], e4, 1e-12) and rel_close(extra[1], e5, 1e-12)

@@ -1,0 +1,89 @@
+"""The open-shell (UHF) (T) on the GPU (ccsdt_energy_spin_orbital) against the spin-orbital
+oracle, which the reference's own CPU kernels run unrestricted pin (test_spin_orbital_oracle.py).
+Relative tolerance 1e-12 on E[T] and E(T): FP64 contractions, compensated sums."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import rel_close
+from exachem_gb300 import ccsd_t
+from exachem_gb300.generator import generate
+from oracle.spin_orbital_oracle import (energy_spin_orbital, open_shell_system, spin_orbital_inputs,
+                                        spin_orbital_inputs_vec)
+
+pytestmark = pytest.mark.gpu
+
+CASES = [(3, 2, 5, 6, 5), (4, 3, 6, 7, 6), (5, 1, 3, 7, 8), (1, 3, 4, 3, 9), (2, 2, 4, 4, 7),
+         (6, 4, 10, 12, 10), (3, 0, 4, 0, 1), (0, 4, 0, 5, 2)]
+
+
+def _call(oa, ob, va, vb, arrs, **kw):
+    r = ccsd_t.energy_spin_orbital(oa, ob, va, vb, *arrs, **kw)
+    return r["e_bracket_T"], r["e_paren_T"]
+
+
+@pytest.mark.parametrize("oa,ob,va,vb,seed", CASES)
+def test_open_shell_matches_spin_orbital_oracle(built, oa, ob, va, vb, seed):
+    arrs = open_shell_system(oa, ob, va, vb, 7, seed)
+    e4, e5 = energy_spin_orbital(*arrs)
+    g4, g5 = _call(oa, ob, va, vb, arrs)
+    assert rel_close(g4, e4, 1e-12) and rel_close(g5, e5, 1e-12), (g4, e4, g5, e5)
+
+
+def test_fewer_than_three_occupied_gives_zero(built):
+    arrs = open_shell_system(1, 1, 3, 3, 4, 3)
+    assert _call(1, 1, 3, 3, arrs) == (0.0, 0.0)
+
+
+def test_spin_forbidden_blocks_are_not_read(built):
+    """NaN in every spin-forbidden element leaves the energies bit for bit unchanged."""
+    oa, ob, va, vb = 4, 3, 6, 7
+    arrs = list(open_shell_system(oa, ob, va, vb, 6, 12))
+    so, sv = np.array([0] * oa + [1] * ob), np.array([0] * va + [1] * vb)
+
+    def allowed(*sp):
+        g = np.meshgrid(*sp, indexing="ij")
+        return g[0] == g[1] if len(g) == 2 else g[0] + g[1] == g[2] + g[3]
+    masks = [allowed(sv, so), allowed(sv, sv, so, so), allowed(so, so, sv, sv), allowed(so, so, so, sv),
+             allowed(so, sv, sv, sv)]
+    poisoned = arrs[:2] + [np.ascontiguousarray(np.where(m, a, np.nan)) for m, a in zip(masks, arrs[2:])]
+    assert _call(oa, ob, va, vb, poisoned) == _call(oa, ob, va, vb, arrs)
+
+
+def test_device_inputs_match_host_inputs(built):
+    import torch
+    oa, ob, va, vb = 4, 2, 7, 8
+    arrs = open_shell_system(oa, ob, va, vb, 6, 13)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrs]
+    assert _call(oa, ob, va, vb, dev) == _call(oa, ob, va, vb, arrs)
+
+
+def test_shards_sum_to_the_whole(built):
+    oa, ob, va, vb = 5, 4, 8, 9
+    arrs = open_shell_system(oa, ob, va, vb, 6, 14)
+    w4, w5 = _call(oa, ob, va, vb, arrs)
+    parts = [_call(oa, ob, va, vb, arrs, shard_index=s, shard_count=3) for s in range(3)]
+    assert rel_close(sum(p[0] for p in parts), w4, 1e-13) and rel_close(sum(p[1] for p in parts), w5, 1e-13)
+
+
+@pytest.mark.parametrize("o,v,seed", [(3, 6, 1), (4, 9, 2)])
+def test_closed_shell_inputs_give_the_closed_shell_energies(built, o, v, seed):
+    d = generate(o, v, seed)
+    e4, e5 = oracle.energy(d)
+    g4, g5 = _call(o, o, v, v, spin_orbital_inputs(d))
+    assert rel_close(g4, e4, 1e-12) and rel_close(g5, e5, 1e-12)
+
+
+def test_closed_shell_inputs_match_the_closed_shell_gpu_path(built):
+    """A larger restricted case, where the oracle is slow: the spin-orbital path over all four
+    spin cases equals the closed-shell FP64 GPU path on the same system."""
+    o, v = 8, 40
+    d = generate(o, v, 3)
+    g4, g5 = _call(o, o, v, v, spin_orbital_inputs_vec(d))
+    ft = ccsd_t.FusedTriples(o, v, ts=16)
+    try:
+        ft.upload_dict(d)
+        r = ft.energy("fp64")
+    finally:
+        ft.close()
+    assert rel_close(g4, r["e_bracket_T"], 1e-11) and rel_close(g5, r["e_paren_T"], 1e-11)

@@ -73,3 +73,11 @@ def test_open_shell_oracle_equals_reference_unrestricted(oa, ob, va, vb, ot, vt,
     assert ntask > 0
     assert e4 == pytest.approx(r4, rel=1e-12, abs=0)
     assert e5 == pytest.approx(r5, rel=1e-12, abs=0)
+
+
+@pytest.mark.parametrize("o,v,seed", [(3, 6, 1), (2, 5, 3)])
+def test_vectorised_spin_orbital_inputs_equal_the_loops(o, v, seed):
+    from oracle.spin_orbital_oracle import spin_orbital_inputs_vec
+    d = generate(o, v, seed)
+    for a, b in zip(spin_orbital_inputs(d), spin_orbital_inputs_vec(d)):
+        assert np.array_equal(a, b)
