@@ -16,6 +16,7 @@
 //        (ia|bc) = v2iabc(i_alpha, b_beta, a_alpha, c_beta)     (v2tensors.cpp:84-86)
 //    (in each the exchange part of the antisymmetrised block vanishes by spin).
 //    It is a template over the tensor types, so it needs only Tensor<T>::get.
+//  * gather_cs_amplitudes(): the closed-shell CCSD's own t1_aa / t2_abab (no spin-orbital expansion).
 //  * gather_cholesky() + run_closed_shell_cholesky(): the alternative that skips V2 - the
 //    alpha-alpha blocks of the Cholesky tensor cholVpr, with the integral blocks built on the GPU.
 //  * gather_spin_orbital() + run_spin_orbital(): the open-shell case (is_restricted = false) -
@@ -58,12 +59,40 @@ inline std::vector<size_t> offsets(const std::vector<size_t>& ext) {
 }
 } // namespace detail
 
+namespace detail {
+// t1(a_alpha, i_alpha) and t2(a_alpha, b_beta, i_alpha, j_beta) into the spatial t1 / t2; the beta
+// tile ids of the tensors start at ob_base (occupied) / vb_base (virtual).
+template<typename T, typename TensorT>
+SpatialInputs gather_amplitudes_at(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva, TensorT& d_t1,
+                                   TensorT& d_t2, const std::vector<T>& k_evl_sorted, size_t ob_base,
+                                   size_t vb_base);
+} // namespace detail
+
 // mo_tiles: extents of the MO tiles in the order occ_a, occ_b, virt_a, virt_b (as
 // TiledIndexSpace::input_tile_sizes() returns them); noa / nva: alpha occupied / virtual tiles.
 // The amplitudes and orbital energies only (the integral arrays stay empty).
 template<typename T, typename TensorT>
 SpatialInputs gather_amplitudes(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva, TensorT& d_t1,
                                 TensorT& d_t2, const std::vector<T>& k_evl_sorted) {
+  return detail::gather_amplitudes_at<T>(mo_tiles, noa, nva, d_t1, d_t2, k_evl_sorted, noa, nva);
+}
+
+// The closed-shell CCSD's own amplitudes, without the spin-orbital expansion the reference runs
+// before (T) (cd_ccsd_cs_ann.cpp:932-975): t1_aa {v_alpha, o_alpha} and t2_abab {v_alpha, v_beta,
+// o_alpha, o_beta} as setupTensors_cs allocates them (ccsd_util.cpp:550-575), over the sub-spaces
+// o_alpha = {MO("occ"), range(noa)}, o_beta = {MO("occ"), range(noa, 2 noa)} (and the virtual
+// ones), whose tile ids start at 0 in each tensor.  The call then needs neither dt1_full / dt2_full
+// nor the six T2-sized temporaries of the expansion.
+template<typename T, typename TensorT>
+SpatialInputs gather_cs_amplitudes(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva, TensorT& t1_aa,
+                                   TensorT& t2_abab, const std::vector<T>& k_evl_sorted) {
+  return detail::gather_amplitudes_at<T>(mo_tiles, noa, nva, t1_aa, t2_abab, k_evl_sorted, 0, 0);
+}
+
+template<typename T, typename TensorT>
+SpatialInputs detail::gather_amplitudes_at(const std::vector<size_t>& mo_tiles, size_t noa, size_t nva,
+                                           TensorT& d_t1, TensorT& d_t2, const std::vector<T>& k_evl_sorted,
+                                           size_t ob_base, size_t vb_base) {
   if(mo_tiles.size() != 2 * noa + 2 * nva) throw std::invalid_argument("MO tiles != 2 noa + 2 nva");
   std::vector<size_t> ot(mo_tiles.begin(), mo_tiles.begin() + noa);
   std::vector<size_t> vt(mo_tiles.begin() + 2 * noa, mo_tiles.begin() + 2 * noa + nva);
@@ -95,7 +124,7 @@ SpatialInputs gather_amplitudes(const std::vector<size_t>& mo_tiles, size_t noa,
     for(size_t B = 0; B < nva; B++)
       for(size_t I = 0; I < noa; I++)
         for(size_t J = 0; J < noa; J++) {
-          d_t2.get({A, B + nva, I, J + noa}, buf); // [a][b][i][j], a,i alpha / b,j beta
+          d_t2.get({A, B + vb_base, I, J + ob_base}, buf); // [a][b][i][j], a,i alpha / b,j beta
           for(size_t a = 0; a < vt[A]; a++)
             for(size_t b = 0; b < vt[B]; b++)
               for(size_t i = 0; i < ot[I]; i++)

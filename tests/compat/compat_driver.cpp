@@ -2,10 +2,11 @@
 // spin-orbital tiled tensors (built with the oracle's spin_orbital.hpp on the TAMM stand-in)
 // -> gather_closed_shell() -> spatial arrays, and optionally run_closed_shell() on the GPU.
 //
-//   compat_driver <in.bin> <out.bin> [--run | --run-tiled | --chol <chol.bin> [--run]]
+//   compat_driver <in.bin> <out.bin> [--run | --run-tiled | --cs | --chol <chol.bin> [--run]]
 // in.bin : int32 o, v, noa, nva, occ tiles[noa], vir tiles[nva]; float64 eps_occ[o] eps_vir[v]
 //          t1 t2 oovv ooov ovvv (C-ABI layouts)
 // out.bin: the gathered float64 arrays in the same order; with --run also E[T], E(T).
+// --cs   : the closed-shell CCSD's t1_aa / t2_abab tensors instead, through gather_cs_amplitudes.
 // --chol : chol.bin = int32 nq, nci, ci tiles[nci]; float64 L[o+v][o+v][nq] (spatial, occupied
 //          first).  The driver builds the spin-orbital Cholesky tensor cholVpr {MO, MO, CI} on the
 //          TAMM stand-in, gathers it with gather_cholesky and appends L_oo, L_ov, L_vv to out.bin;
@@ -96,6 +97,24 @@ int main(int argc, char** argv) {
   exachem::cholesky_2e::V2Tensors<double> d_v2;
   build_spin_orbital(o, v, OT, VT, t1.data(), t2.data(), oovv.data(), ooov.data(), ovvv.data(), d_t1, d_t2, d_v2);
 
+  if(argc > 3 && std::string(argv[3]) == "--cs") {
+    // the closed-shell CCSD's own tensors: t1_aa {v_alpha, o_alpha}, t2_abab {v_alpha, v_beta,
+    // o_alpha, o_beta}, tile ids from 0 in each mode; out.bin = eps_occ, eps_vir, t1, t2
+    std::vector<size_t>  ota(ot.begin(), ot.end()), vta(vt.begin(), vt.end());
+    tamm::Tensor<double> t1_aa({vta, ota}), t2_abab({vta, vta, ota, ota});
+    for(int a = 0; a < v; a++)
+      for(int i = 0; i < o; i++) t1_aa.data()[(size_t) a * o + i] = t1[(size_t) i * v + a];
+    for(int a = 0; a < v; a++)
+      for(int b = 0; b < v; b++)
+        for(int i = 0; i < o; i++)
+          for(int j = 0; j < o; j++)
+            t2_abab.data()[(((size_t) a * v + b) * o + i) * o + j] = t2[(((size_t) i * o + j) * v + a) * v + b];
+    auto          A = exachem_gb300::gather_cs_amplitudes<double>(mo, noa, nva, t1_aa, t2_abab, k_evl);
+    std::ofstream g(argv[2], std::ios::binary);
+    for(auto* x: {&A.eps_occ, &A.eps_vir, &A.t1, &A.t2})
+      g.write(reinterpret_cast<const char*>(x->data()), sizeof(double) * x->size());
+    return 0;
+  }
   auto S = exachem_gb300::gather_closed_shell<double>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl);
   std::ofstream g(argv[2], std::ios::binary);
   for(auto* a: {&S.eps_occ, &S.eps_vir, &S.t1, &S.t2, &S.oovv, &S.ooov, &S.ovvv})

@@ -201,3 +201,21 @@ def test_adapter_open_shell_call_matches_oracle(tmp_path, built):
     _, extra = _read_so(tmp_path / "out.bin", arrs, extra=2)
     e4, e5 = energy_spin_orbital(*arrs)
     assert rel_close(extra[0], e4, 1e-12) and rel_close(extra[1], e5, 1e-12)
+
+
+def test_adapter_reads_the_closed_shell_ccsd_amplitudes(tmp_path, built):
+    """gather_cs_amplitudes takes the closed-shell CCSD's t1_aa {v_alpha, o_alpha} and t2_abab
+    {v_alpha, v_beta, o_alpha, o_beta} (ccsd_util.cpp:550-575) as they are - no expansion to the
+    spin-orbital d_t1 / d_t2 (cd_ccsd_cs_ann.cpp:932-975) - into the same spatial arrays."""
+    from exachem_gb300.generator import generate
+    exe = _compile(tmp_path, link_lib=True)
+    o, v, ot, vt = 5, 11, [2, 3], [4, 4, 3]
+    d = generate(o, v, 17)
+    _write(tmp_path / "in.bin", d, ot, vt)
+    subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), "--cs"], check=True)
+    raw = np.fromfile(tmp_path / "out.bin", dtype=np.float64)
+    off = 0
+    for k in ["eps_occ", "eps_vir", "t1", "t2"]:
+        got = raw[off:off + d[k].size].reshape(d[k].shape)
+        off += d[k].size
+        assert np.array_equal(got, d[k]), k
