@@ -54,7 +54,8 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_debug_triplet_w", "ccsdt_energy_noalloc", "ccsdt_shard_triplets",
             "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates",
             "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky",
-            "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config", "ccsdt_energy_spin_orbital"]
+            "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config", "ccsdt_energy_spin_orbital",
+            "ccsdt_debug_spin_orbital_plan"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
@@ -85,6 +86,7 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_autotune.argtypes = [vp, ctypes.c_int, dp, ip, ip]
     lib.ccsdt_set_tile_config.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.ccsdt_energy_spin_orbital.argtypes = [ctypes.c_int] * 4 + [vp] * 7 + [ctypes.c_int] * 3 + [dp, dp]
+    lib.ccsdt_debug_spin_orbital_plan.argtypes = [ctypes.c_int] * 7 + [ip, ctypes.POINTER(ctypes.c_longlong), ip]
     lib.ccsdt_triplet_error_estimates.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp, dp]
     lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
@@ -102,7 +104,7 @@ def load_library(path: str | os.PathLike | None = None):
                  "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
                  "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end",
                  "ccsdt_upload_cholesky", "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config",
-                 "ccsdt_energy_spin_orbital"):
+                 "ccsdt_energy_spin_orbital", "ccsdt_debug_spin_orbital_plan"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -356,6 +358,23 @@ def energy_spin_orbital(oa: int, ob: int, va: int, vb: int, eps_occ, eps_vir, t1
     if st:
         raise CCSDTError(st, lib.ccsdt_status_string(st).decode())
     return {"e_bracket_T": e[0], "e_paren_T": e[1], "seconds": sec.value}
+
+
+PLAN_FIELDS = ["x0", "y0", "z0", "nx", "ny", "nz", "has_d", "d_k", "d_a", "d_b", "has_s", "s_k", "s_a", "s_b"]
+
+
+def spin_orbital_plan(oa: int, ob: int, va: int, vb: int, i: int, j: int, k: int):
+    """The open-shell path's contraction plan for triplet i < j < k (host logic, no GPU):
+    (of[3][3] block index per permutation and position, list of block dicts)."""
+    lib = load_library()
+    of = (ctypes.c_int * 9)()
+    blocks = (ctypes.c_longlong * (9 * 14))()
+    n = ctypes.c_int()
+    st = lib.ccsdt_debug_spin_orbital_plan(oa, ob, va, vb, i, j, k, of, blocks, ctypes.byref(n))
+    if st:
+        raise CCSDTError(st, lib.ccsdt_status_string(st).decode())
+    return (np.array(list(of)).reshape(3, 3),
+            [dict(zip(PLAN_FIELDS, blocks[14 * b:14 * b + 14])) for b in range(n.value)])
 
 
 def all_triplets(o: int) -> np.ndarray:

@@ -174,26 +174,30 @@ __global__ void __launch_bounds__(kSoThreads) so_energy_kernel(const __grid_cons
 
 namespace {
 
-// Plans the contraction blocks of triplet (i, j, k), launches them on `st` into `slots` (at most
-// nine, each up to n_max^3 doubles) and fills the energy kernel's block table.
-cudaError_t so_contract(const SoSpins& S, const double* tt, const double* vv, const double* uu, const double* t2,
-                        double* const* slots, int i, int j, int k, SoBlock (&blk)[3][3], cudaStream_t st) {
+// The contraction blocks of one triplet, as offsets into the operand arrays (host logic only).
+// Block b is X[x - x0][(y - y0) nz + (z - z0)] over nx x (ny nz) elements:
+//   d-term  - sum_e tt[d_a + x' V + e'] vv[d_b + y' V^2 + z' V + e']          e' < d_k
+//   s-term  - sum_m uu[s_a + x' O + m'] t2[s_b + y' V O^2 + z' O^2 + m']       m' < s_k
+// with x', y', z' the indices within the block.  of[p][q] = the block the energy reads for
+// permutation p (ijk, jik, kji) at position q ((a; b c), (b; a c), (c; b a)), -1 where it is zero.
+struct SoPlanBlock {
+  int       x0, y0, z0, nx, ny, nz;
+  int       has_d, has_s, d_k, s_k;
+  long long d_a, d_b, s_a, s_b;
+};
+struct SoPlan {
+  int         nblk;
+  SoPlanBlock blk[9];
+  int         of[3][3];
+};
+
+SoPlan so_plan(const SoSpins& S, int i, int j, int k) {
   const long long O = S.O, V = S.V;
   const int       perm[3][3] = {{i, j, k}, {j, i, k}, {k, j, i}};
   const int       si = S.occ(i), sj = S.occ(j), sk = S.occ(k);
   // spins of (x, y, z) at the three positions; the virtual triple carries the pattern (s_i, s_j, s_k)
   const int pos[3][3] = {{si, sj, sk}, {sj, si, sk}, {sk, sj, si}};
-  GemmBatch batch{};
-  int       nj = 0, nslot = 0;
-  long long max_tiles = 0;
-  auto      flush = [&]() -> cudaError_t {
-    if(nj == 0) return cudaSuccess;
-    if(max_tiles > 0) dmma_gemm_kernel<<<dim3((unsigned) max_tiles, 1, (unsigned) nj), D_THREADS, 0, st>>>(batch);
-    batch     = GemmBatch{};
-    nj        = 0;
-    max_tiles = 0;
-    return cudaGetLastError();
-  };
+  SoPlan    P{};
   for(int p = 0; p < 3; p++) {
     const int ip = perm[p][0], jp = perm[p][1], kp = perm[p][2];
     const int s_i = S.occ(ip), s_j = S.occ(jp), s_k = S.occ(kp);
@@ -203,47 +207,80 @@ cudaError_t so_contract(const SoSpins& S, const double* tt, const double* vv, co
       for(int r = 0; r < q; r++)
         if(pos[r][0] == sx && pos[r][1] == sy && pos[r][2] == sz) same = r;
       if(same >= 0) {
-        blk[p][q] = blk[p][same];
+        P.of[p][q] = P.of[p][same];
         continue;
       }
-      GemmJob J{};
-      int     nt = 0;
+      SoPlanBlock B{S.vlo(sx), S.vlo(sy), S.vlo(sz), S.vn(sx), S.vn(sy), S.vn(sz), 0, 0, 0, 0, 0, 0, 0, 0};
       if(sx == s_j || sx == s_k) { // d-term: - sum_e tt[j'][k'][x][e] vv[i'][y][z][e]
         const int se = s_j + s_k - sx;
-        if(same_pair(s_i, se, sy, sz))
-          J.t[nt++] = GemmTerm{tt + (((long long) jp * O + kp) * V + S.vlo(sx)) * V + S.vlo(se), plain_rows(V),
-                               vv + (((long long) ip * V + S.vlo(sy)) * V + S.vlo(sz)) * V + S.vlo(se),
-                               RowMap{V * V, V, std::max(S.vn(sz), 1)}, S.vn(se), -1.0};
+        if(same_pair(s_i, se, sy, sz)) {
+          B.has_d = 1;
+          B.d_k   = S.vn(se);
+          B.d_a   = (((long long) jp * O + kp) * V + S.vlo(sx)) * V + S.vlo(se);
+          B.d_b   = (((long long) ip * V + S.vlo(sy)) * V + S.vlo(sz)) * V + S.vlo(se);
+        }
       }
       if(s_i == sy || s_i == sz) { // s-term: - sum_m uu[j'][k'][x][m] t2[y][z][i'][m]
-        const int sm = sy + sz - s_i, m0 = sm ? S.oa : 0, nm = sm ? S.O - S.oa : S.oa;
-        if(same_pair(s_j, s_k, sm, sx))
-          J.t[nt++] = GemmTerm{uu + (((long long) jp * O + kp) * V + S.vlo(sx)) * O + m0, plain_rows(O),
-                               t2 + ((long long) S.vlo(sy) * V + S.vlo(sz)) * O * O + (long long) ip * O + m0,
-                               RowMap{V * O * O, O * O, std::max(S.vn(sz), 1)}, nm, -1.0};
+        const int sm = sy + sz - s_i, m0 = sm ? S.oa : 0;
+        if(same_pair(s_j, s_k, sm, sx)) {
+          B.has_s = 1;
+          B.s_k   = sm ? S.O - S.oa : S.oa;
+          B.s_a   = (((long long) jp * O + kp) * V + S.vlo(sx)) * O + m0;
+          B.s_b   = ((long long) S.vlo(sy) * V + S.vlo(sz)) * O * O + (long long) ip * O + m0;
+        }
       }
-      if(nt == 0 || S.vn(sx) == 0 || S.vn(sy) == 0 || S.vn(sz) == 0) { // zero, or no point reads it
-        blk[p][q] = SoBlock{nullptr, 0, 0, 0, 0, 0};
+      if(!(B.has_d || B.has_s) || B.nx == 0 || B.ny == 0 || B.nz == 0) { // zero, or no point reads it
+        P.of[p][q] = -1;
         continue;
       }
-      double* C = slots[nslot++];
-      J.nterms  = nt;
-      J.C       = C;
-      J.M       = S.vn(sx);
-      J.N       = (long long) S.vn(sy) * S.vn(sz);
-      J.beta    = 0.0;
-      blk[p][q] = SoBlock{C, S.vlo(sx), S.vlo(sy), S.vlo(sz), S.vn(sy), S.vn(sz)};
-      const long long tiles = ((J.M + D_BM - 1) / D_BM) * ((J.N + D_BN - 1) / D_BN);
-      if(tiles >= (1LL << 31)) return cudaErrorInvalidConfiguration;
-      batch.job[nj++] = J;
-      max_tiles       = std::max(max_tiles, tiles);
-      if(nj == 3) {
-        const cudaError_t e = flush();
-        if(e != cudaSuccess) return e;
-      }
+      P.of[p][q]      = P.nblk;
+      P.blk[P.nblk++] = B;
     }
   }
-  return flush();
+  return P;
+}
+
+// Launches a triplet's plan on `st` (block b into slots[b], up to three GEMM jobs per launch) and
+// fills the energy kernel's block table.
+cudaError_t so_contract(const SoSpins& S, const SoPlan& P, const double* tt, const double* vv, const double* uu,
+                        const double* t2, double* const* slots, SoBlock (&blk)[3][3], cudaStream_t st) {
+  const long long O = S.O, V = S.V;
+  GemmBatch       batch{};
+  int             nj        = 0;
+  long long       max_tiles = 0;
+  for(int b = 0; b < P.nblk; b++) {
+    const SoPlanBlock& B = P.blk[b];
+    GemmJob            J{};
+    int                nt = 0;
+    if(B.has_d)
+      J.t[nt++] = GemmTerm{tt + B.d_a, plain_rows(V), vv + B.d_b, RowMap{V * V, V, B.nz}, B.d_k, -1.0};
+    if(B.has_s)
+      J.t[nt++] = GemmTerm{uu + B.s_a, plain_rows(O), t2 + B.s_b, RowMap{V * O * O, O * O, B.nz}, B.s_k, -1.0};
+    J.nterms = nt;
+    J.C      = slots[b];
+    J.M      = B.nx;
+    J.N      = (long long) B.ny * B.nz;
+    J.beta   = 0.0;
+    const long long tiles = ((J.M + D_BM - 1) / D_BM) * ((J.N + D_BN - 1) / D_BN);
+    if(tiles >= (1LL << 31)) return cudaErrorInvalidConfiguration;
+    batch.job[nj++] = J;
+    max_tiles       = std::max(max_tiles, tiles);
+    if(nj == 3 || b == P.nblk - 1) {
+      dmma_gemm_kernel<<<dim3((unsigned) max_tiles, 1, (unsigned) nj), D_THREADS, 0, st>>>(batch);
+      const cudaError_t e = cudaGetLastError();
+      if(e != cudaSuccess) return e;
+      batch     = GemmBatch{};
+      nj        = 0;
+      max_tiles = 0;
+    }
+  }
+  for(int p = 0; p < 3; p++)
+    for(int q = 0; q < 3; q++) {
+      const int b = P.of[p][q];
+      blk[p][q]   = b < 0 ? SoBlock{nullptr, 0, 0, 0, 0, 0}
+                          : SoBlock{slots[b], P.blk[b].x0, P.blk[b].y0, P.blk[b].z0, P.blk[b].ny, P.blk[b].nz};
+    }
+  return cudaSuccess;
 }
 
 // Device allocations of one call, released on every exit path.
@@ -357,7 +394,7 @@ extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb
         if((long long) na * nb * nc == 0) continue;
         const int    s  = (int) (n++ % kSoStreams);
         SoEnergyArgs A{};
-        e = so_contract(S, tt, vv, uu, d_t2, slots[s], i, j, k, A.blk, M.streams[s]);
+        e = so_contract(S, so_plan(S, i, j, k), tt, vv, uu, d_t2, slots[s], A.blk, M.streams[s]);
         if(e != cudaSuccess) break;
         A.eps_o = d_eo, A.eps_v = d_ev, A.t1 = d_t1, A.v2ijab = d_ijab;
         A.O = (int) O, A.V = (int) V, A.oa = oa, A.va = va;
@@ -396,5 +433,23 @@ extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb
     if(cudaEventElapsedTime(&ms, M.ev[0], M.ev[1]) == cudaSuccess) *seconds = ms * 1e-3;
   }
   if(!std::isfinite(energies[0]) || !std::isfinite(energies[1])) return CCSDT_E_NONFINITE;
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_debug_spin_orbital_plan(int oa, int ob, int va, int vb, int i, int j, int k, int* of,
+                                                      long long* blocks, int* nblk) {
+  if(oa < 0 || ob < 0 || va < 0 || vb < 0 || !of || !blocks || !nblk) return CCSDT_E_INVALID;
+  const int O = oa + ob, V = va + vb;
+  if(!(0 <= i && i < j && j < k && k < O)) return CCSDT_E_INVALID;
+  const SoPlan P = so_plan(SoSpins{oa, va, O, V}, i, j, k);
+  *nblk          = P.nblk;
+  for(int p = 0; p < 3; p++)
+    for(int q = 0; q < 3; q++) of[3 * p + q] = P.of[p][q];
+  for(int b = 0; b < P.nblk; b++) {
+    const SoPlanBlock& B = P.blk[b];
+    const long long    r[14] = {B.x0,  B.y0,  B.z0,  B.nx,  B.ny,  B.nz,  B.has_d,
+                                B.d_k, B.d_a, B.d_b, B.has_s, B.s_k, B.s_a, B.s_b};
+    for(int x = 0; x < 14; x++) blocks[14 * b + x] = r[x];
+  }
   return CCSDT_OK;
 }

@@ -252,6 +252,16 @@ ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb, const dou
                                        const double* v2iabc, int on_device, int shard_index,
                                        int shard_count, double* energies, double* seconds);
 
+/* Testing: the contraction plan of triplet i < j < k of an open-shell system (pure host logic).
+ * of[9]: for permutation p (ijk, jik, kji) and position q ((a; b c), (b; a c), (c; b a)) the
+ * block the energy reads at of[3p + q], -1 where it is zero; blocks[14 b + ...] for b < *nblk:
+ * x0, y0, z0, nx, ny, nz, has_d, d_k, d_a, d_b, has_s, s_k, s_a, s_b - block
+ * X[x - x0][(y - y0) nz + z - z0] = - sum_e tt[d_a + x' V + e] vv[d_b + y' V^2 + z' V + e]
+ * - sum_m uu[s_a + x' O + m] t2[s_b + y' V O^2 + z' O^2 + m], with tt[j][k][a][e] = t2(a,e,j,k),
+ * vv[i][b][c][e] = <ie||bc>, uu[j][k][a][m] = <jk||ma>. */
+ccsdt_status ccsdt_debug_spin_orbital_plan(int oa, int ob, int va, int vb, int i, int j, int k, int* of,
+                                           long long* blocks, int* nblk);
+
 /* ---- learned slice count (no counterpart in the reference) --------------------------
  * A 12 -> 64 -> 64 -> 7 MLP (ReLU, softmax over slice counts 2..8) predicts, per occupied
  * triplet, the smallest digit-plane count that keeps the triplet's energy error under a

@@ -1,0 +1,113 @@
+"""The open-shell path's host logic on the CPU: the library's own contraction plan
+(ccsdt_debug_spin_orbital_plan - the spin blocks, their ranges and operand offsets that the GPU
+launcher turns into GEMM jobs) is evaluated here with numpy, every operand row checked to lie
+inside its array, and the energy summed over a < b < c the way so_energy_kernel sums it.  The
+result must equal the spin-orbital oracle (1e-12), so the planning is proven without a GPU."""
+import itertools
+
+import numpy as np
+import pytest
+
+from exachem_gb300 import ccsd_t
+from oracle.spin_orbital_oracle import energy_spin_orbital, open_shell_system, spin_orbital_inputs
+from exachem_gb300.generator import generate
+
+
+def _gemm(A, a0, a_stride, B, b0, b_hi, b_lo, nz, K, M, N):
+    """- sum_kappa A[a0 + m a_stride + kappa] B[b0 + (n // nz) b_hi + (n % nz) b_lo + kappa]."""
+    ra = a0 + np.arange(M) * a_stride
+    n = np.arange(N)
+    rb = b0 + (n // nz) * b_hi + (n % nz) * b_lo
+    if K:
+        assert ra.min() >= 0 and ra.max() + K <= A.size
+        assert rb.min() >= 0 and rb.max() + K <= B.size
+    k = np.arange(K)
+    return -(A[ra[:, None] + k[None, :]] @ B[rb[:, None] + k[None, :]].T)
+
+
+def _plan_energy(oa, ob, va, vb, eps_o, eps_v, t1, t2, v2ijab, v2ijka, v2iabc):
+    O, V = oa + ob, va + vb
+    tt = np.ascontiguousarray(t2.transpose(2, 3, 0, 1)).ravel()      # tt[j][k][a][e]
+    vv = np.ascontiguousarray(v2iabc.transpose(0, 2, 3, 1)).ravel()  # vv[i][b][c][e]
+    uu = np.ascontiguousarray(v2ijka.transpose(0, 1, 3, 2)).ravel()  # uu[j][k][a][m]
+    t2f = t2.ravel()
+    so = lambda p: int(p >= oa)
+    sv = np.array([0] * va + [1] * vb)
+    rng = lambda s: (va, V) if s else (0, va)
+    e4 = e5 = 0.0
+    for i, j, k in itertools.combinations(range(O), 3):
+        si, sj, sk = so(i), so(j), so(k)
+        (a0, a1), (b0, b1), (c0, c1) = rng(si), rng(sj), rng(sk)
+        if (a1 - a0) * (b1 - b0) * (c1 - c0) == 0:
+            continue
+        of, blocks = ccsd_t.spin_orbital_plan(oa, ob, va, vb, i, j, k)
+        X = []
+        for B in blocks:
+            M, N = B["nx"], B["ny"] * B["nz"]
+            x = np.zeros((M, N))
+            if B["has_d"]:
+                x += _gemm(tt, B["d_a"], V, vv, B["d_b"], V * V, V, B["nz"], B["d_k"], M, N)
+            if B["has_s"]:
+                x += _gemm(uu, B["s_a"], O, t2f, B["s_b"], V * O * O, O * O, B["nz"], B["s_k"], M, N)
+            X.append((x.reshape(M, B["ny"], B["nz"]), B))
+        a, b, c = np.meshgrid(np.arange(a0, a1), np.arange(b0, b1), np.arange(c0, c1), indexing="ij")
+
+        def read(bi, x, y, z):
+            if bi < 0:
+                return np.zeros(x.shape)
+            arr, B = X[bi]
+            assert B["x0"] <= x.min() and x.max() < B["x0"] + B["nx"]
+            assert B["y0"] <= y.min() and y.max() < B["y0"] + B["ny"]
+            assert B["z0"] <= z.min() and z.max() < B["z0"] + B["nz"]
+            return arr[x - B["x0"], y - B["y0"], z - B["z0"]]
+        w = np.zeros(a.shape)
+        for p in range(3):
+            x = read(of[p][0], a, b, c) - read(of[p][1], b, a, c) - read(of[p][2], c, b, a)
+            w += -x if p else x
+        vt = np.zeros(a.shape)
+        for p, (ip, jp, kp) in enumerate([(i, j, k), (j, i, k), (k, j, i)]):
+            for q, (x, y, z) in enumerate([(a, b, c), (b, a, c), (c, b, a)]):
+                ok = (sv[x] == so(ip)) & (sv[y] + sv[z] == so(jp) + so(kp))
+                g = np.where(ok, t1[x, ip] * v2ijab[jp, kp, y, z], 0.0)
+                vt += g if (p == 0) == (q == 0) else -g
+        keep = np.ones(a.shape, dtype=bool)
+        if si == sj:
+            keep &= a < b
+        if sj == sk:
+            keep &= b < c
+        d = eps_o[i] + eps_o[j] + eps_o[k] - eps_v[a] - eps_v[b] - eps_v[c]
+        e4 += np.sum(np.where(keep, w * w / d, 0.0))
+        e5 += np.sum(np.where(keep, (w + vt) * w / d, 0.0))
+    return e4, e5
+
+
+@pytest.mark.parametrize("oa,ob,va,vb,seed", [(3, 2, 5, 6, 5), (4, 3, 6, 7, 6), (5, 1, 3, 7, 8), (1, 3, 4, 3, 9),
+                                              (3, 0, 4, 0, 1), (0, 3, 0, 4, 2), (3, 2, 0, 5, 3)])
+def test_open_shell_plan_reproduces_the_oracle(built, oa, ob, va, vb, seed):
+    arrs = open_shell_system(oa, ob, va, vb, 6, seed)
+    e4, e5 = energy_spin_orbital(*arrs)
+    g4, g5 = _plan_energy(oa, ob, va, vb, *arrs)
+    assert g4 == pytest.approx(e4, rel=1e-12, abs=1e-300) and g5 == pytest.approx(e5, rel=1e-12, abs=1e-300)
+
+
+def test_closed_shell_plan_reproduces_the_closed_shell_oracle(built):
+    import oracle
+    d = generate(3, 5, 2)
+    e4, e5 = oracle.energy(d)
+    g4, g5 = _plan_energy(3, 3, 5, 5, *spin_orbital_inputs(d))
+    assert g4 == pytest.approx(e4, rel=1e-12) and g5 == pytest.approx(e5, rel=1e-12)
+
+
+def test_plan_block_counts_follow_the_spin_cases(built):
+    """Distinct nonzero blocks: aaa / bbb one per permutation; aab two per permutation less one
+    (permutation kji at (c; b a): x is beta while j' and k' are alpha, and i' is beta while y and z
+    are alpha, so neither term survives); abb three per permutation less one."""
+    counts = {case: len(ccsd_t.spin_orbital_plan(3, 3, 4, 4, *tri)[1])
+              for case, tri in {"aaa": (0, 1, 2), "aab": (0, 1, 3), "abb": (0, 3, 4), "bbb": (3, 4, 5)}.items()}
+    assert counts == {"aaa": 3, "aab": 5, "abb": 8, "bbb": 3}
+
+
+def test_plan_rejects_bad_triplets(built):
+    for tri in [(1, 0, 2), (0, 0, 1), (0, 1, 6)]:
+        with pytest.raises(ccsd_t.CCSDTError):
+            ccsd_t.spin_orbital_plan(3, 3, 4, 4, *tri)
