@@ -18,9 +18,10 @@
 //           {s_i, s_e} = {s_y, s_z}
 //   s-term: m runs over the one spin with {s_y, s_z} = {s_i, s_m}; zero unless also
 //           {s_j, s_k} = {s_m, s_x}
-// Blocks with equal (p, s_x, s_y, s_z) are computed once (ααα: one block per permutation).
+// Blocks with equal (p, s_x, s_y, s_z) are computed once (aaa: one block per permutation).
 // Against dense spin-orbital GEMMs this is about five times less work, and no element of a
-// spin-forbidden block of the inputs is read.
+// spin-forbidden block of the inputs is read.  The plan of a triplet (so_plan) is host logic,
+// exposed for tests as ccsdt_debug_spin_orbital_plan.
 //
 // GEMM operands need the contraction index contiguous; three one-time permuted copies give that:
 //   tt[j][k][a][e] = t2(a,e,j,k),  vv[i][b][c][e] = <ie||bc>,  uu[j][k][a][m] = <jk||ma>

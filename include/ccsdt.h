@@ -1,5 +1,6 @@
 /*
- * ccsdt.h - C ABI of the GB300 closed-shell CCSD(T) perturbative-triples library.
+ * ccsdt.h - C ABI of the GB300 CCSD(T) perturbative-triples library (closed shell; open shell
+ * through ccsdt_energy_spin_orbital).
  *
  * This is the drop-in boundary for ExaChem's fused (T) driver:
  *
