@@ -111,3 +111,19 @@ def test_plan_rejects_bad_triplets(built):
     for tri in [(1, 0, 2), (0, 0, 1), (0, 1, 6)]:
         with pytest.raises(ccsd_t.CCSDTError):
             ccsd_t.spin_orbital_plan(3, 3, 4, 4, *tri)
+
+
+@pytest.mark.parametrize("oa,ob,va,vb", [(3, 2, 5, 6), (4, 4, 7, 7), (5, 1, 3, 7), (3, 0, 4, 0)])
+def test_bench_flop_count_is_the_planned_work(built, oa, ob, va, vb):
+    """The open-shell roofline numerator (bench.spin_orbital_flops) equals 2 x the multiply-adds
+    of the GEMM blocks the library plans, summed over every triplet."""
+    import bench
+    total = 0
+    O = oa + ob
+    for tri in itertools.combinations(range(O), 3):
+        s = [int(p >= oa) for p in tri]
+        if min((vb if x else va) for x in s) == 0:
+            continue
+        for B in ccsd_t.spin_orbital_plan(oa, ob, va, vb, *tri)[1]:
+            total += 2 * B["nx"] * B["ny"] * B["nz"] * (B["has_d"] * B["d_k"] + B["has_s"] * B["s_k"])
+    assert bench.spin_orbital_flops(oa, ob, va, vb) == total
