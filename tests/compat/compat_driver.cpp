@@ -24,13 +24,31 @@ static void rd(std::ifstream& f, X* p, size_t n) {
   f.read(reinterpret_cast<char*>(p), sizeof(X) * n);
 }
 
+// A stand-in tensor that, like a block-sparse TAMM tensor, holds no spin-forbidden blocks:
+// Tensor::get of one throws.  spins[m][t] = spin of tile t of mode m; a block is allowed when the
+// spins of the first half of its modes sum to those of the second half.
+struct SpinCheckedTensor {
+  const tamm::Tensor<double>*   t = nullptr;
+  std::vector<std::vector<int>> spins;
+  void get(const tamm::IndexVector& bid, std::vector<double>& buf) const {
+    int lo = 0, hi = 0;
+    for(size_t m = 0; m < bid.size(); m++) (m < bid.size() / 2 ? lo : hi) += spins[m][bid[m]];
+    if(lo != hi) throw std::runtime_error("Tensor::get of a spin-forbidden block");
+    t->get(bid, buf);
+  }
+};
+struct SpinCheckedV2 {
+  SpinCheckedTensor v2ijab, v2ijka, v2iabc;
+};
+
 // compat_driver --so <so.bin> <out.bin> [--run]: the open-shell case.
 // so.bin : int32 oa, ob, va, vb, n tiles of occ_a, occ_b, virt_a, virt_b, then those tile
 //          extents; float64 eps[O + V] (MO order), t1[V][O], t2[V][V][O][O], v2ijab[O][O][V][V],
 //          v2ijka[O][O][O][V], v2iabc[O][V][V][V] (dense spin-orbital arrays).
-// The arrays fill the TAMM stand-in tensors as they are (spin-forbidden blocks included, which
-// the gather must skip); out.bin = gather_spin_orbital's arrays in the same order, with --run
-// followed by E[T], E(T) from run_spin_orbital.
+// The arrays fill the TAMM stand-in tensors as they are, and each tensor is read through a
+// SpinCheckedTensor, which throws on a spin-forbidden block (the gather must never ask for one);
+// out.bin = gather_spin_orbital's arrays in the same order, with --run followed by E[T], E(T)
+// from run_spin_orbital.
 static int open_shell(int argc, char** argv) {
   std::ifstream f(argv[2], std::ios::binary);
   int           hdr[8];
@@ -53,7 +71,14 @@ static int open_shell(int argc, char** argv) {
   rd(f, d_v2.v2ijka.data(), O * O * O * V);
   rd(f, d_v2.v2iabc.data(), O * V * V * V);
   if(!f) return 3;
-  auto S = exachem_gb300::gather_spin_orbital<double>(mo, hdr[4], hdr[5], hdr[6], hdr[7], d_t1, d_t2, d_v2, eps);
+  std::vector<int> so_t, sv_t; // tile spins of the occupied / virtual modes
+  for(int t = 0; t < hdr[4] + hdr[5]; t++) so_t.push_back(t >= hdr[4]);
+  for(int t = 0; t < hdr[6] + hdr[7]; t++) sv_t.push_back(t >= hdr[6]);
+  SpinCheckedTensor c_t1{&d_t1, {sv_t, so_t}}, c_t2{&d_t2, {sv_t, sv_t, so_t, so_t}};
+  SpinCheckedV2     c_v2{{&d_v2.v2ijab, {so_t, so_t, sv_t, sv_t}},
+                         {&d_v2.v2ijka, {so_t, so_t, so_t, sv_t}},
+                         {&d_v2.v2iabc, {so_t, sv_t, sv_t, sv_t}}};
+  auto S = exachem_gb300::gather_spin_orbital<double>(mo, hdr[4], hdr[5], hdr[6], hdr[7], c_t1, c_t2, c_v2, eps);
   if((size_t) S.oa + S.ob != O || (size_t) S.va + S.vb != V) return 4;
   std::ofstream g(argv[3], std::ios::binary);
   for(auto* a: {&S.eps_occ, &S.eps_vir, &S.t1, &S.t2, &S.v2ijab, &S.v2ijka, &S.v2iabc})

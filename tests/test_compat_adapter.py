@@ -174,7 +174,8 @@ def _read_so(path, arrs, extra=0):
 
 def test_adapter_open_shell_gather_is_exact(tmp_path, built):
     """gather_spin_orbital reads every spin-allowed block of the open-shell tensors bit for bit
-    and none of the spin-forbidden ones (filled with NaN here; they come back as zeros)."""
+    and never asks for a spin-forbidden one: the harness's tensors throw on such a get, as a
+    block-sparse TAMM tensor has no such blocks (and their elements are NaN here besides)."""
     from oracle.spin_orbital_oracle import open_shell_system
     exe = _compile(tmp_path, link_lib=True)
     for (oa, ob, va, vb, tiles, seed) in [(3, 2, 5, 6, ([2, 1], [2], [3, 2], [4, 2]), 3),
