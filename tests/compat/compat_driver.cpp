@@ -1,6 +1,8 @@
 // Exercises include/exachem_compat/ccsd_t_fused_driver.hpp the way ExaChem would feed it:
 // spin-orbital tiled tensors (built with the oracle's spin_orbital.hpp on the TAMM stand-in)
 // -> gather_closed_shell() -> spatial arrays, and optionally run_closed_shell() on the GPU.
+// Every gather reads the tensors through SpinCheckedTensor, which throws on a spin-forbidden
+// block as a block-sparse TAMM tensor would.
 //
 //   compat_driver <in.bin> <out.bin> [--run | --run-tiled | --cs | --chol <chol.bin> [--run]]
 // in.bin : int32 o, v, noa, nva, occ tiles[noa], vir tiles[nva]; float64 eps_occ[o] eps_vir[v]
@@ -121,6 +123,14 @@ int main(int argc, char** argv) {
   tamm::Tensor<double>                    d_t1, d_t2;
   exachem::cholesky_2e::V2Tensors<double> d_v2;
   build_spin_orbital(o, v, OT, VT, t1.data(), t2.data(), oovv.data(), ooov.data(), ovvv.data(), d_t1, d_t2, d_v2);
+  // every read below goes through tensors that throw on a spin-forbidden block
+  std::vector<int> so_t, sv_t;
+  for(size_t t = 0; t < OT.size(); t++) so_t.push_back(t >= (size_t) noa);
+  for(size_t t = 0; t < VT.size(); t++) sv_t.push_back(t >= (size_t) nva);
+  SpinCheckedTensor c_t1{&d_t1, {sv_t, so_t}}, c_t2{&d_t2, {sv_t, sv_t, so_t, so_t}};
+  SpinCheckedV2     c_v2{{&d_v2.v2ijab, {so_t, so_t, sv_t, sv_t}},
+                         {&d_v2.v2ijka, {so_t, so_t, so_t, sv_t}},
+                         {&d_v2.v2iabc, {so_t, sv_t, sv_t, sv_t}}};
 
   if(argc > 3 && std::string(argv[3]) == "--cs") {
     // the closed-shell CCSD's own tensors: t1_aa {v_alpha, o_alpha}, t2_abab {v_alpha, v_beta,
@@ -140,7 +150,7 @@ int main(int argc, char** argv) {
       g.write(reinterpret_cast<const char*>(x->data()), sizeof(double) * x->size());
     return 0;
   }
-  auto S = exachem_gb300::gather_closed_shell<double>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl);
+  auto S = exachem_gb300::gather_closed_shell<double>(mo, noa, nva, c_t1, c_t2, c_v2, k_evl);
   std::ofstream g(argv[2], std::ios::binary);
   for(auto* a: {&S.eps_occ, &S.eps_vir, &S.t1, &S.t2, &S.oovv, &S.ooov, &S.ovvv})
     g.write(reinterpret_cast<const char*>(a->data()), sizeof(double) * a->size());
@@ -177,7 +187,7 @@ int main(int argc, char** argv) {
     if(argc > 5 && std::string(argv[5]) == "--run") {
       ccsdt_opts op{};
       op.mode = CCSDT_MODE_FP64;
-      auto A = exachem_gb300::gather_amplitudes<double>(mo, noa, nva, d_t1, d_t2, k_evl);
+      auto A = exachem_gb300::gather_amplitudes<double>(mo, noa, nva, c_t1, c_t2, k_evl);
       auto [e4, e5, secs] = exachem_gb300::run_closed_shell_cholesky(A, C, 0, op);
       g.write(reinterpret_cast<const char*>(&e4), sizeof(double));
       g.write(reinterpret_cast<const char*>(&e5), sizeof(double));
@@ -188,7 +198,7 @@ int main(int argc, char** argv) {
     // the drop-in path: blocks through the device-side retile, then the (T) call
     ccsdt_opts op{};
     op.mode = CCSDT_MODE_FP64;
-    auto [e4, e5, secs, total] = exachem_gb300::run_tiled<double>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl, op,
+    auto [e4, e5, secs, total] = exachem_gb300::run_tiled<double>(mo, noa, nva, c_t1, c_t2, c_v2, k_evl, op,
                                                                  std::chrono::steady_clock::now(), 0);
     g.write(reinterpret_cast<const char*>(&e4), sizeof(double));
     g.write(reinterpret_cast<const char*>(&e5), sizeof(double));
