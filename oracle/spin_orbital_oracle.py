@@ -125,20 +125,24 @@ def spin_orbital_inputs(d: dict):
     return eps_o, eps_v, t1, t2, v2ijab, v2ijka, v2iabc
 
 
-def open_shell_system(oa: int, ob: int, va: int, vb: int, nq: int, seed: int):
+def open_shell_system(oa: int, ob: int, va: int, vb: int, nq: int, seed: int, exact: bool = False):
     """A synthetic open-shell (UHF-like) system over spin orbitals: separate alpha and beta orbital
     sets (oa / ob occupied, va / vb virtual), integrals from spin-blocked Cholesky vectors
     (L_alpha over the oa + va alpha orbitals, L_beta over the ob + vb beta ones, zero between spins),
     antisymmetrised as v2tensors.cpp:67-86 does, spin-conserving antisymmetric T2 and T1.
     Spin-orbital order: occupied alpha then beta, virtual alpha then beta (ExaChem's MO order).
+    exact: the vectors are rounded to multiples of 2^-12 and t1 / t2 to multiples of 2^-20, so that
+    every integral and amplitude is exact in FP64 and the arrays are the same bits on any machine.
     Returns (eps_o, eps_v, t1, t2, v2ijab, v2ijka, v2iabc)."""
     rng = np.random.default_rng(seed)
     O, V = oa + ob, va + vb
     spin_o = np.array([0] * oa + [1] * ob)
     spin_v = np.array([0] * va + [1] * vb)
+    grid = (lambda x, b: np.round(x * 2.0 ** b) / 2.0 ** b) if exact else (lambda x, b: x)
     La = rng.normal(0.0, 0.05, size=(oa + va, oa + va, nq))
     Lb = rng.normal(0.0, 0.05, size=(ob + vb, ob + vb, nq))
-    La, Lb = 0.5 * (La + La.transpose(1, 0, 2)), 0.5 * (Lb + Lb.transpose(1, 0, 2))
+    La = grid(0.5 * (La + La.transpose(1, 0, 2)), 12)
+    Lb = grid(0.5 * (Lb + Lb.transpose(1, 0, 2)), 12)
     # spin-orbital vectors over occupied then virtual spin orbitals: index -> (spin, orbital of that spin)
     n = O + V
     orb = [(0, p) for p in range(oa)] + [(1, p) for p in range(ob)] + \
@@ -155,8 +159,8 @@ def open_shell_system(oa: int, ob: int, va: int, vb: int, nq: int, seed: int):
     v2ijka = np.ascontiguousarray(asym[o_, o_, o_, v_])
     v2iabc = np.ascontiguousarray(asym[o_, v_, v_, v_])
     same = spin_v[:, None] == spin_o[None, :]
-    t1 = np.where(same, rng.normal(0.0, 0.02, size=(V, O)), 0.0)
-    r = rng.normal(0.0, 0.05, size=(V, V, O, O))
+    t1 = grid(np.where(same, rng.normal(0.0, 0.02, size=(V, O)), 0.0), 20)
+    r = grid(rng.normal(0.0, 0.05, size=(V, V, O, O)), 20)
     sa, sb = spin_v[:, None, None, None], spin_v[None, :, None, None]
     si, sj = spin_o[None, None, :, None], spin_o[None, None, None, :]
     mask = ((sa == si) & (sb == sj)) | ((sa == sj) & (sb == si))
@@ -166,6 +170,12 @@ def open_shell_system(oa: int, ob: int, va: int, vb: int, nq: int, seed: int):
     eps_o = -1.0 - rng.random(O)
     eps_v = 0.3 + rng.random(V)
     return eps_o, eps_v, t1, t2, v2ijab, v2ijka, v2iabc
+
+
+def golden_checksums(arrs) -> dict:
+    """Exact sums of the t2 and v2iabc of an open_shell_system(exact=True) (every term and partial
+    sum is representable in FP64, so any summation order gives the same bits)."""
+    return {"t2": float(np.sum(arrs[3])), "v2iabc": float(np.sum(arrs[6]))}
 
 
 def spin_orbital_inputs_vec(d: dict):

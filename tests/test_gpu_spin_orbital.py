@@ -87,3 +87,19 @@ def test_closed_shell_inputs_match_the_closed_shell_gpu_path(built):
     finally:
         ft.close()
     assert rel_close(g4, r["e_bracket_T"], 1e-11) and rel_close(g5, r["e_paren_T"], 1e-11)
+
+
+def test_open_shell_matches_reference_golden(built):
+    """Against ExaChem's own CPU (T) run unrestricted (tests/golden/open_shell_energies.json, made by
+    tests/golden/make_open_shell_golden.py from oracle/_ref) on systems the dense oracle cannot
+    hold, up to 14 occupied and 84 virtual spin orbitals with ragged alpha / beta tiles."""
+    import json
+    from conftest import ROOT
+    from oracle.spin_orbital_oracle import golden_checksums as checksums
+    cases = json.loads((ROOT / "tests" / "golden" / "open_shell_energies.json").read_text())["cases"]
+    for c in cases:
+        arrs = open_shell_system(c["oa"], c["ob"], c["va"], c["vb"], c["nq"], c["seed"], exact=True)
+        assert checksums(arrs) == c["checksums"], c["name"]
+        g4, g5 = _call(c["oa"], c["ob"], c["va"], c["vb"], arrs)
+        assert rel_close(g4, c["e_bracket_T"], 1e-12) and rel_close(g5, c["e_paren_T"], 1e-12), \
+            (c["name"], g4, c["e_bracket_T"], g5, c["e_paren_T"])

@@ -81,3 +81,34 @@ def test_vectorised_spin_orbital_inputs_equal_the_loops(o, v, seed):
     d = generate(o, v, seed)
     for a, b in zip(spin_orbital_inputs(d), spin_orbital_inputs_vec(d)):
         assert np.array_equal(a, b)
+
+
+def _open_shell_golden():
+    import json
+    from conftest import ROOT
+    return json.loads((ROOT / "tests" / "golden" / "open_shell_energies.json").read_text())["cases"]
+
+
+def test_open_shell_golden_inputs_regenerate_bit_for_bit():
+    """The fixtures' systems come back with the recorded exact checksums (the GPU tests rebuild
+    them on another machine and compare with the reference's energies)."""
+    from oracle.spin_orbital_oracle import golden_checksums as checksums
+    for c in _open_shell_golden():
+        arrs = open_shell_system(c["oa"], c["ob"], c["va"], c["vb"], c["nq"], c["seed"], exact=True)
+        assert checksums(arrs) == c["checksums"], c["name"]
+
+
+def test_open_shell_golden_matches_the_oracle():
+    for c in _open_shell_golden()[:2]:
+        arrs = open_shell_system(c["oa"], c["ob"], c["va"], c["vb"], c["nq"], c["seed"], exact=True)
+        e4, e5 = energy_spin_orbital(*arrs)
+        assert e4 == pytest.approx(c["e_bracket_T"], rel=1e-12, abs=0)
+        assert e5 == pytest.approx(c["e_paren_T"], rel=1e-12, abs=0)
+
+
+@needs_ref
+def test_reference_reruns_its_open_shell_golden():
+    c = _open_shell_golden()[2]
+    arrs = open_shell_system(c["oa"], c["ob"], c["va"], c["vb"], c["nq"], c["seed"], exact=True)
+    r4, r5, n = oracle.ref_energy_spin_orbital(c["tiles"], np.concatenate(arrs[:2]), *arrs[2:], is_restricted=False)
+    assert (r4, r5, n) == (c["e_bracket_T"], c["e_paren_T"], c["ref_tasks"])
