@@ -127,3 +127,17 @@ def test_bench_flop_count_is_the_planned_work(built, oa, ob, va, vb):
         for B in ccsd_t.spin_orbital_plan(oa, ob, va, vb, *tri)[1]:
             total += 2 * B["nx"] * B["ny"] * B["nz"] * (B["has_d"] * B["d_k"] + B["has_s"] * B["s_k"])
     assert bench.spin_orbital_flops(oa, ob, va, vb) == total
+
+
+def test_plan_reproduces_the_reference_open_shell_golden(built):
+    """The library's plan, evaluated here, against ExaChem's own CPU (T) run unrestricted on the
+    golden systems (tests/golden/open_shell_energies.json, up to 14 occupied and 84 virtual spin
+    orbitals): the planning the GPU launches is pinned to the reference beyond the dense oracle."""
+    import json
+    from conftest import ROOT
+    cases = json.loads((ROOT / "tests" / "golden" / "open_shell_energies.json").read_text())["cases"]
+    for c in cases:
+        arrs = open_shell_system(c["oa"], c["ob"], c["va"], c["vb"], c["nq"], c["seed"], exact=True)
+        g4, g5 = _plan_energy(c["oa"], c["ob"], c["va"], c["vb"], *arrs)
+        assert g4 == pytest.approx(c["e_bracket_T"], rel=1e-12) and g5 == pytest.approx(c["e_paren_T"], rel=1e-12), \
+            c["name"]
