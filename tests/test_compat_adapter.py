@@ -220,3 +220,16 @@ def test_adapter_reads_the_closed_shell_ccsd_amplitudes(tmp_path, built):
         got = raw[off:off + d[k].size].reshape(d[k].shape)
         off += d[k].size
         assert np.array_equal(got, d[k]), k
+
+
+def test_adapter_execute_compiles_with_the_reference_signature(tmp_path, built):
+    """CCSD_T_Fused_Driver<T>::execute - the drop-in itself, compiled only inside an ExaChem build
+    (EXACHEM_GB300_WITH_TAMM) - compiles and links for T = double against stand-ins for the types
+    of the reference's signature, restricted and open-shell branches included."""
+    exe = tmp_path / "execute_compile"
+    lib = ROOT / "exachem_gb300" / "_build"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-Wno-unused-parameter",
+                    str(ROOT / "tests" / "compat" / "execute_compile.cpp"), "-o", str(exe),
+                    "-I", str(ROOT / "include"), "-I", str(ROOT / "oracle" / "ref_shim"),
+                    "-L", str(lib), "-lccsdt_gb300", f"-Wl,-rpath,{lib}"], check=True, capture_output=True, text=True)
+    subprocess.run([str(exe)], check=True)
