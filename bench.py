@@ -229,6 +229,20 @@ def spin_orbital_flops(oa, ob, va, vb):
     return float(total)
 
 
+def spin_orbital_launches(oa, ob, va, vb):
+    """Kernel launches of one open-shell call: three permutes, then per triplet its GEMM launches
+    (up to three blocks each, from the library's own plan) and one energy launch."""
+    from itertools import combinations
+    from exachem_gb300 import ccsd_t as ct
+    nv, n = (va, vb), 3
+    for tri in combinations(range(oa + ob), 3):
+        if min(nv[int(p >= oa)] for p in tri) == 0:
+            continue
+        nblk = len(ct.spin_orbital_plan(oa, ob, va, vb, *tri)[1])
+        n += -(-nblk // 3) + 1
+    return n
+
+
 def run_open_shell(args):
     """The open-shell (UHF) (T) through ccsdt_energy_spin_orbital on synthetic spin-orbital inputs:
     value = device time per call with the inputs resident in HBM, e2e = the same call from host
@@ -250,9 +264,12 @@ def run_open_shell(args):
         ct.energy_spin_orbital(oa, ob, va, vb, *dev)
     torch.cuda.synchronize()
     secs, res = [], None
+    clocks = ClockSampler(0)
+    clocks.start()
     for _ in range(args.steps):
         res = ct.energy_spin_orbital(oa, ob, va, vb, *dev)
         secs.append(res["seconds"])
+    clk = clocks.stop()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         r2 = ct.energy_spin_orbital(oa, ob, va, vb, *host)
@@ -273,6 +290,7 @@ def run_open_shell(args):
             "cpu_baseline": None,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": sum(a.nbytes for a in host),
                     "d2h_bytes_per_step": 16},
+            "gpu_launches": spin_orbital_launches(oa, ob, va, vb) * args.steps, "clocks": clk,
             "energies": {"e_bracket_T": res["e_bracket_T"], "e_paren_T": res["e_paren_T"],
                          "host_equals_device": r2["e_paren_T"] == res["e_paren_T"]}}
     print(json.dumps(line))

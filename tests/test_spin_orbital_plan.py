@@ -141,3 +141,11 @@ def test_plan_reproduces_the_reference_open_shell_golden(built):
         g4, g5 = _plan_energy(c["oa"], c["ob"], c["va"], c["vb"], *arrs)
         assert g4 == pytest.approx(c["e_bracket_T"], rel=1e-12) and g5 == pytest.approx(c["e_paren_T"], rel=1e-12), \
             c["name"]
+
+
+def test_bench_launch_count(built):
+    """3 permutes + per triplet ceil(blocks / 3) GEMM launches + 1 energy launch: at oa=ob=3,
+    va=vb=4 one aaa and one bbb triplet (3 blocks: 2 launches), nine aab (5 blocks: 3) and nine abb
+    (8 blocks: 4)."""
+    import bench
+    assert bench.spin_orbital_launches(3, 3, 4, 4) == 3 + 2 * 2 + 9 * 3 + 9 * 4
