@@ -149,3 +149,27 @@ def test_bench_launch_count(built):
     (8 blocks: 4)."""
     import bench
     assert bench.spin_orbital_launches(3, 3, 4, 4) == 3 + 2 * 2 + 9 * 3 + 9 * 4
+
+
+def test_open_shell_entry_rejects_bad_arguments_without_gpu(built):
+    """ccsdt_energy_spin_orbital checks its arguments before any CUDA call: negative or oversized
+    orbital counts, a null output, a shard outside [0, count) and null arrays are CCSDT_E_INVALID;
+    fewer than three occupied or virtual spin orbitals give zero energies."""
+    import ctypes
+    lib = ccsd_t.load_library()
+    e = (ctypes.c_double * 2)(1.0, 1.0)
+    ep = ctypes.cast(e, ctypes.POINTER(ctypes.c_double))
+    x = np.zeros(1 << 16)
+    p = [x.ctypes.data] * 7
+    call = lambda oa, ob, va, vb, arrs, si, sc, out: lib.ccsdt_energy_spin_orbital(oa, ob, va, vb, *arrs, 0, si, sc,
+                                                                                    out, None)
+    assert call(-1, 2, 3, 3, p, 0, 1, ep) == 1
+    assert call(5000, 2, 3, 3, p, 0, 1, ep) == 1
+    assert call(2, 2, 3, 3, p, 0, 1, None) == 1
+    assert call(2, 2, 3, 3, p, 3, 3, ep) == 1
+    assert call(2, 2, 3, 3, p, -1, 2, ep) == 1
+    assert call(2, 2, 3, 3, [None] * 7, 0, 1, ep) == 1
+    e[0] = e[1] = 1.0
+    assert call(1, 1, 3, 3, [None] * 7, 0, 1, ep) == 0 and (e[0], e[1]) == (0.0, 0.0)
+    e[0] = e[1] = 1.0
+    assert call(2, 2, 1, 1, [None] * 7, 0, 1, ep) == 0 and (e[0], e[1]) == (0.0, 0.0)
