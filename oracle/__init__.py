@@ -43,7 +43,23 @@ def port():
         _port.oracle_triplets_slabs.argtypes = [ctypes.c_int, ctypes.c_int] + [_D] * 6 + \
             [ctypes.POINTER(ctypes.c_void_p), ctypes.c_long, _I, _D, _D]
         _port.oracle_num_threads.restype = ctypes.c_int
+        _port.so_oracle_energy.argtypes = [ctypes.c_int] * 4 + [_D] * 7 + [ctypes.c_long, _I, _D, _D]
     return _port
+
+
+def energy_spin_orbital_c(oa, ob, va, vb, arrs, tri=None) -> tuple[float, float]:
+    """oracle/spin_orbital_oracle.c: (E[T], E(T)) of an open-shell system (arrs = eps_o, eps_v,
+    t1, t2, v2ijab, v2ijka, v2iabc in the layouts of oracle/spin_orbital_oracle.py) over the
+    triplets tri ([n][3], i < j < k; None = all of them)."""
+    lib = port()
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in arrs]
+    t = None if tri is None else np.ascontiguousarray(np.asarray(tri, dtype=np.int32).reshape(-1, 3))
+    e4, e5 = ctypes.c_double(), ctypes.c_double()
+    rc = lib.so_oracle_energy(oa, ob, va, vb, *[x.ctypes.data_as(_D) for x in a], 0 if t is None else len(t),
+                              None if t is None else t.ctypes.data_as(_I), ctypes.byref(e4), ctypes.byref(e5))
+    if rc:
+        raise RuntimeError("so_oracle_energy failed")
+    return e4.value, e5.value
 
 
 def ref_available() -> bool:

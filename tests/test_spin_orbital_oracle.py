@@ -112,3 +112,32 @@ def test_reference_reruns_its_open_shell_golden():
     arrs = open_shell_system(c["oa"], c["ob"], c["va"], c["vb"], c["nq"], c["seed"], exact=True)
     r4, r5, n = oracle.ref_energy_spin_orbital(c["tiles"], np.concatenate(arrs[:2]), *arrs[2:], is_restricted=False)
     assert (r4, r5, n) == (c["e_bracket_T"], c["e_paren_T"], c["ref_tasks"])
+
+
+@pytest.mark.parametrize("oa,ob,va,vb,seed", [(3, 2, 5, 6, 5), (4, 3, 6, 7, 6), (3, 0, 4, 0, 1), (1, 3, 4, 3, 9)])
+def test_c_restatement_equals_the_numpy_oracle(oa, ob, va, vb, seed):
+    arrs = open_shell_system(oa, ob, va, vb, 6, seed)
+    e4, e5 = energy_spin_orbital(*arrs)
+    c4, c5 = oracle.energy_spin_orbital_c(oa, ob, va, vb, arrs)
+    assert c4 == pytest.approx(e4, rel=1e-12, abs=1e-300) and c5 == pytest.approx(e5, rel=1e-12, abs=1e-300)
+
+
+def test_c_restatement_matches_the_reference_golden():
+    for c in _open_shell_golden()[:4]:
+        arrs = open_shell_system(c["oa"], c["ob"], c["va"], c["vb"], c["nq"], c["seed"], exact=True)
+        g4, g5 = oracle.energy_spin_orbital_c(c["oa"], c["ob"], c["va"], c["vb"], arrs)
+        assert g4 == pytest.approx(c["e_bracket_T"], rel=1e-12) and g5 == pytest.approx(c["e_paren_T"], rel=1e-12), \
+            c["name"]
+
+
+def test_c_restatement_triplet_subsets_sum_to_the_whole():
+    import itertools
+    oa, ob, va, vb = 4, 3, 6, 7
+    arrs = open_shell_system(oa, ob, va, vb, 6, 21)
+    w4, w5 = oracle.energy_spin_orbital_c(oa, ob, va, vb, arrs)
+    tri = list(itertools.combinations(range(oa + ob), 3))
+    parts = [oracle.energy_spin_orbital_c(oa, ob, va, vb, arrs, tri[s::3]) for s in range(3)]
+    assert sum(p[0] for p in parts) == pytest.approx(w4, rel=1e-13)
+    assert sum(p[1] for p in parts) == pytest.approx(w5, rel=1e-13)
+    with pytest.raises(RuntimeError):
+        oracle.energy_spin_orbital_c(oa, ob, va, vb, arrs, [(1, 0, 2)])
