@@ -1,10 +1,12 @@
 // Batched, persistent split-precision (T): host orchestration.
 //
 // The non-zero triplets of a call (i < k) go into a device table (i, j, k, output index).  A batch
-// of B triplets runs as: l-sum contraction (persistent, work queue), d-sum contraction (persistent),
-// tiled energy of the B triplets, per-triplet reduction, advance of the device batch base.  With
-// opts->use_graph that sequence is captured once per call into a CUDA graph and replayed for every
-// full batch; the remainder batch is launched directly.
+// of B triplets runs as: work-queue reset, one persistent contraction launch (every tile of the
+// three partial arrays with its l-sum and d-sum terms), tiled energy of the B triplets,
+// per-triplet reduction, advance of the device batch base.  With opts->use_graph that sequence is
+// captured once per call into a CUDA graph and replayed for every full batch (the per-launch
+// phase-timing events are not recorded inside the capture); the remainder batch is launched
+// directly.
 #include <cuda.h>
 #include <cuda_runtime.h>
 

@@ -234,6 +234,9 @@ inline ccsdt_opts opts_from_env() {
   // the contraction's tile configuration tuned on this system on first use (results unchanged)
   const char* at = std::getenv("EXACHEM_GB300_AUTOTUNE");
   op.autotune    = at ? std::atoi(at) != 0 : 1;
+  // split and learned modes: replay the call's per-batch launch sequence from a CUDA graph
+  const char* gr = std::getenv("EXACHEM_GB300_GRAPH");
+  op.use_graph   = gr ? std::atoi(gr) != 0 : 0;
   return op;
 }
 

@@ -2,6 +2,7 @@
 // only an ExaChem build defines) against minimal stand-ins for the types of its signature
 // (ccsd_t_fused_driver.hpp:73-81), with the TAMM-shaped tensor of the oracle's shim.  Compile and
 // link only: the stand-ins carry just what execute() calls.
+#include <cstdio>
 #include <string>
 #include <vector>
 
@@ -30,7 +31,12 @@ struct TiledIndexSpace {
 #define EXACHEM_GB300_WITH_TAMM 1
 #include "exachem_compat/ccsd_t_fused_driver.hpp"
 
-int main(int argc, char**) {
+int main(int argc, char** argv) {
+  if(argc > 1 && std::string(argv[1]) == "--opts") { // the options execute() takes from the environment
+    const ccsdt_opts op = exachem_gb300::opts_from_env();
+    std::printf("%d %d %.3g %d %d\n", op.mode, op.slices, op.energy_budget, op.autotune, op.use_graph);
+    return 0;
+  }
   if(argc > 1) { // never run: the point is that execute() compiles and links for T = double
     CCSD_T_Fused_Driver<double>              drv;
     ChemEnv                                  env;

@@ -225,7 +225,8 @@ def test_adapter_reads_the_closed_shell_ccsd_amplitudes(tmp_path, built):
 def test_adapter_execute_compiles_with_the_reference_signature(tmp_path, built):
     """CCSD_T_Fused_Driver<T>::execute - the drop-in itself, compiled only inside an ExaChem build
     (EXACHEM_GB300_WITH_TAMM) - compiles and links for T = double against stand-ins for the types
-    of the reference's signature, restricted and open-shell branches included."""
+    of the reference's signature, restricted and open-shell branches included; and the options it
+    reads from the environment (EXACHEM_GB300_MODE / SLICES / BUDGET / AUTOTUNE / GRAPH)."""
     exe = tmp_path / "execute_compile"
     lib = ROOT / "exachem_gb300" / "_build"
     subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-Wno-unused-parameter",
@@ -233,3 +234,15 @@ def test_adapter_execute_compiles_with_the_reference_signature(tmp_path, built):
                     "-I", str(ROOT / "include"), "-I", str(ROOT / "oracle" / "ref_shim"),
                     "-L", str(lib), "-lccsdt_gb300", f"-Wl,-rpath,{lib}"], check=True, capture_output=True, text=True)
     subprocess.run([str(exe)], check=True)
+    import os
+    env = {k: v for k, v in os.environ.items() if not k.startswith("EXACHEM_GB300_")}
+
+    def opts(**kw):
+        out = subprocess.run([str(exe), "--opts"], check=True, capture_output=True, text=True,
+                             env=env | {f"EXACHEM_GB300_{k}": v for k, v in kw.items()}).stdout.split()
+        return int(out[0]), int(out[1]), float(out[2]), int(out[3]), int(out[4])
+    assert opts() == (0, 3, 1e-8, 1, 0)                                  # fp64 drop-in, autotune on, no graph
+    assert opts(MODE="ozaki", SLICES="4", GRAPH="1") == (1, 4, 1e-8, 1, 1)
+    assert opts(MODE="learned", BUDGET="1e-9", AUTOTUNE="0") == (2, 5, 1e-9, 0, 0)
+    assert subprocess.run([str(exe), "--opts"], env=env | {"EXACHEM_GB300_MODE": "int4"},
+                          capture_output=True).returncode != 0
