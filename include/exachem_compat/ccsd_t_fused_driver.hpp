@@ -22,7 +22,8 @@
 //  * gather_spin_orbital() + run_spin_orbital(): the open-shell case (is_restricted = false) -
 //    every spin-allowed block of the same tensors, alpha and beta tile lists of their own, into
 //    the dense spin-orbital arrays of ccsdt_energy_spin_orbital.
-//  * CCSD_T_Fused_Driver<T>::execute(): the reference's signature, compiled when
+//  * exachem::cc::ccsd_t::CCSD_T_Fused_Driver<T>::execute(): the reference's namespace, class and
+//    signature, compiled when
 //    EXACHEM_GB300_WITH_TAMM is defined (inside an ExaChem build).  Each rank of the process
 //    group takes every size-th occupied triplet on its own GPU and returns its partial
 //    energies; ccsd_t.cpp:262-263 already sums them with pg().reduce.
@@ -565,7 +566,10 @@ inline std::tuple<double, double, double> run_spin_orbital(const SpinOrbitalInpu
 } // namespace exachem_gb300
 
 #ifdef EXACHEM_GB300_WITH_TAMM
-// Inside an ExaChem build: same class name and signature as the reference driver.
+// Inside an ExaChem build: same namespace, class name and signature as the reference driver
+// (exachem/cc/ccsd_t/ccsd_t_fused_driver.hpp:19,61-81), so the call site at ccsd_t.cpp:253-256
+// compiles unchanged with this header included in place of that one.
+namespace exachem::cc::ccsd_t {
 template<typename T>
 class CCSD_T_Fused_Driver {
 public:
@@ -598,4 +602,5 @@ public:
     return exachem_gb300::run_tiled<T>(mo, noa, nva, d_t1, d_t2, d_v2, k_evl_sorted, op, t0);
   }
 };
+} // namespace exachem::cc::ccsd_t
 #endif

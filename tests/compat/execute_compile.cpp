@@ -38,7 +38,7 @@ int main(int argc, char** argv) {
     return 0;
   }
   if(argc > 1) { // never run: the point is that execute() compiles and links for T = double
-    CCSD_T_Fused_Driver<double>              drv;
+    exachem::cc::ccsd_t::CCSD_T_Fused_Driver<double> drv; // the reference's qualified name
     ChemEnv                                  env;
     ExecutionContext                         ec;
     std::vector<int>                         k_spin;
