@@ -23,8 +23,8 @@
 //    every spin-allowed block of the same tensors, alpha and beta tile lists of their own, into
 //    the dense spin-orbital arrays of ccsdt_energy_spin_orbital.
 //  * exachem::cc::ccsd_t::CCSD_T_Fused_Driver<T>::execute(): the reference's namespace, class and
-//    signature, compiled when
-//    EXACHEM_GB300_WITH_TAMM is defined (inside an ExaChem build).  Each rank of the process
+//    signature, compiled when EXACHEM_GB300_WITH_TAMM is defined (inside an ExaChem build).  Each
+//    rank of the process
 //    group takes every size-th occupied triplet on its own GPU and returns its partial
 //    energies; ccsd_t.cpp:262-263 already sums them with pg().reduce.
 #pragma once
