@@ -55,7 +55,7 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates",
             "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky",
             "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config", "ccsdt_energy_spin_orbital",
-            "ccsdt_debug_spin_orbital_plan"]
+            "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
@@ -87,6 +87,8 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_set_tile_config.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.ccsdt_energy_spin_orbital.argtypes = [ctypes.c_int] * 4 + [vp] * 7 + [ctypes.c_int] * 3 + [dp, dp]
     lib.ccsdt_debug_spin_orbital_plan.argtypes = [ctypes.c_int] * 7 + [ip, ctypes.POINTER(ctypes.c_longlong), ip]
+    lib.ccsdt_reference_op_count_so.argtypes = [ctypes.c_int, ip] * 4 + [ctypes.c_int, dp,
+                                                                         ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_triplet_error_estimates.argtypes = [vp, ctypes.POINTER(Opts), ctypes.c_long, ip, dp, dp, dp]
     lib.ccsdt_phase_times.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_shard_triplets.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long), ip]
@@ -104,7 +106,7 @@ def load_library(path: str | os.PathLike | None = None):
                  "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
                  "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end",
                  "ccsdt_upload_cholesky", "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config",
-                 "ccsdt_energy_spin_orbital", "ccsdt_debug_spin_orbital_plan"):
+                 "ccsdt_energy_spin_orbital", "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -128,6 +130,20 @@ def reference_op_count(o: int, v: int, occ_tiles, vir_tiles) -> tuple[float, int
     L, keep = make_layout(o, v, occ_tiles, vir_tiles)
     ops, nt = ctypes.c_double(), ctypes.c_long()
     st = lib.ccsdt_reference_op_count(ctypes.byref(L), ctypes.byref(ops), ctypes.byref(nt))
+    if st:
+        raise CCSDTError(st, lib.ccsdt_status_string(st).decode())
+    return ops.value, nt.value
+
+
+def reference_op_count_so(occ_a, occ_b, vir_a, vir_b, is_restricted: bool = False) -> tuple[float, int]:
+    """The reference's op count and task count over alpha / beta tile lists of their own."""
+    lib = load_library()
+    ts = [_tiles(0, t) for t in (occ_a, occ_b, vir_a, vir_b)]
+    args = []
+    for t in ts:
+        args += [len(t), t.ctypes.data_as(ctypes.POINTER(ctypes.c_int))]
+    ops, nt = ctypes.c_double(), ctypes.c_long()
+    st = lib.ccsdt_reference_op_count_so(*args, int(bool(is_restricted)), ctypes.byref(ops), ctypes.byref(nt))
     if st:
         raise CCSDTError(st, lib.ccsdt_status_string(st).decode())
     return ops.value, nt.value

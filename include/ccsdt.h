@@ -208,6 +208,12 @@ long ccsdt_last_launch_count(const ccsdt_handle* h);
  * exachem/cc/ccsd_t/fused_common.hpp:34-261 counts it.  Pure host arithmetic. */
 ccsdt_status ccsdt_reference_op_count(const ccsdt_layout* layout, double* ops, long* tasks);
 
+/* The same count over MO tiles occ_a | occ_b | virt_a | virt_b of their own (open shell), with
+ * is_restricted as the reference driver takes it (1: the two restricted spin filters; 0: none). */
+ccsdt_status ccsdt_reference_op_count_so(int n_occ_a, const int* occ_a, int n_occ_b, const int* occ_b,
+                                         int n_vir_a, const int* vir_a, int n_vir_b, const int* vir_b,
+                                         int is_restricted, double* ops, long* tasks);
+
 /* Allocation-free FP64 (T) for small problems.  No counterpart in the reference: it is
  * for callers that cannot call cudaMalloc - a host runtime whose device memory is owned
  * by a pooled allocator (ExaChem's TAMM reserves the device through its RMM pool), code

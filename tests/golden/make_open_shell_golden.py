@@ -6,7 +6,9 @@ the arrays regenerate bit for bit on any machine).
 
 Run where the reference tree is present:  python tests/golden/make_open_shell_golden.py
 The JSON keeps the generator parameters, the alpha / beta tile lists, exact checksums of the
-generated t2 and v2iabc, E[T], E(T) and the reference's task count for each case.
+generated t2 and v2iabc, E[T], E(T) and the reference's task count for each case, and the op
+counts the reference's CI outputs hold for unrestricted (T) runs (total_num_ops), which pin the
+unrestricted task enumeration and spin filters.
 """
 from __future__ import annotations
 
@@ -33,8 +35,19 @@ CASES = [
 ]
 
 
-def main():
-    out = {"generator": "oracle.spin_orbital_oracle.open_shell_system(exact=True)", "cases": []}
+# unrestricted (T) runs in the reference's CI outputs: file, line of total_num_ops, alpha / beta
+# occupied and virtual counts (nelectrons_alpha / _beta, nbf - those), tile size, the value
+CI_OPS = [
+    ("ci/reference_output/ch4.def2-tzvp.ccsd_t.json", 484, 6, 4, 49, 51, 28, 37432196256),
+]
+
+
+def main(reference: str = "/root/reference"):
+    out = {"generator": "oracle.spin_orbital_oracle.open_shell_system(exact=True)", "cases": [], "ci_ops": []}
+    for f, line, oa, ob, va, vb, ts, want in CI_OPS:
+        text = (Path(reference) / f).read_text().splitlines()
+        assert str(want) in text[line - 1], (f, line, text[line - 1])
+        out["ci_ops"].append(dict(file=f, line=line, oa=oa, ob=ob, va=va, vb=vb, ts=ts, total_num_ops=want))
     for name, oa, ob, va, vb, nq, seed, tiles in CASES:
         arrs = open_shell_system(oa, ob, va, vb, nq, seed, exact=True)
         t0 = time.time()
@@ -50,4 +63,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(*sys.argv[1:])

@@ -141,3 +141,34 @@ def test_c_restatement_triplet_subsets_sum_to_the_whole():
     assert sum(p[1] for p in parts) == pytest.approx(w5, rel=1e-13)
     with pytest.raises(RuntimeError):
         oracle.energy_spin_orbital_c(oa, ob, va, vb, arrs, [(1, 0, 2)])
+
+
+def _open_shell_ci_ops():
+    import json
+    from conftest import ROOT
+    return json.loads((ROOT / "tests" / "golden" / "open_shell_energies.json").read_text())["ci_ops"]
+
+
+def test_unrestricted_op_count_matches_the_reference_ci(built):
+    """ccsdt_reference_op_count_so with is_restricted = 0 reproduces the total_num_ops of the
+    reference's CI run of an unrestricted (T) (CH4 triplet, def2-TZVP: 6 / 4 occupied, 49 / 51
+    virtual, tiles of 28) - the unrestricted task list and spin filters of ccsd_t_fused_driver.hpp."""
+    from exachem_gb300.ccsd_t import reference_op_count_so
+    from exachem_gb300.generator import tiles_uniform
+    for c in _open_shell_ci_ops():
+        ops, _ = reference_op_count_so(*(tiles_uniform(n, c["ts"]) for n in (c["oa"], c["ob"], c["va"], c["vb"])))
+        assert ops == c["total_num_ops"], c["file"]
+
+
+def test_unrestricted_task_count_matches_the_reference_runs(built):
+    from exachem_gb300.ccsd_t import reference_op_count_so
+    for c in _open_shell_golden():
+        assert reference_op_count_so(*c["tiles"])[1] == c["ref_tasks"], c["name"]
+
+
+def test_restricted_op_count_over_spin_tiles_equals_the_closed_shell_count(built):
+    from exachem_gb300.ccsd_t import reference_op_count, reference_op_count_so
+    ot, vt = [3, 5], [7, 13, 20]
+    assert reference_op_count_so(ot, ot, vt, vt, is_restricted=True) == reference_op_count(8, 40, ot, vt)
+    # unrestricted counts every spin case: more work than the restricted half
+    assert reference_op_count_so(ot, ot, vt, vt)[0] > reference_op_count(8, 40, ot, vt)[0]
