@@ -297,6 +297,8 @@ def run_open_shell(args):
     e2e = (time.perf_counter() - t0) / args.steps
     value = sum(secs) / len(secs)
     flops = spin_orbital_flops(oa, ob, va, vb)
+    from exachem_gb300.generator import tiles_uniform
+    ref_ops, _ = ct.reference_op_count_so(*(tiles_uniform(n, 40) for n in (oa, ob, va, vb)))
     ntri = O * (O - 1) * (O - 2) // 6
     line = {"metric": f"(T) wall-s open-shell (UHF) FP64 at oa={oa},ob={ob},va={va},vb={vb}", "value": value,
             "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
@@ -307,6 +309,8 @@ def run_open_shell(args):
             "roofline": {"bound": "fp64-tensor", "achieved": flops / value / 1e12, "peak": fp64_peak,
                          "unit": "TFLOP/s", "frac": flops / value / 1e12 / fp64_peak, "traffic": None,
                          "kernel": "dmma_gemm_kernel + so_energy_kernel", "flops_per_call": flops,
+                         "ref_equiv_tflops": ref_ops / value / 1e12,
+                         "ref_ops_per_call": ref_ops, "ref_ops_layout": "unrestricted, tiles of 40",
                          "peak_source": "cuBLAS DGEMM 8192^3 measured in this run, of measured"},
             "cpu_baseline": cpu_baseline_open_shell(oa, ob, va, vb, host) if args.cpu_sample > 0 else None,
             "e2e": {"value": e2e, "unit": "s", "h2d_bytes_per_step": sum(a.nbytes for a in host),
