@@ -29,6 +29,7 @@
 //    energies; ccsd_t.cpp:262-263 already sums them with pg().reduce.
 #pragma once
 
+#include <algorithm>
 #include <chrono>
 #include <cstddef>
 #include <cstdio>
@@ -494,13 +495,15 @@ void gather_dense(TensorT& X, const ModeTiles* const (&modes)[R], F allowed, std
       static_assert(R == 2 || R == 4, "T1 / T2 / V2 tensors");
       if constexpr(R == 2) X.get({bid[0], bid[1]}, buf); // tile ids as the closed-shell gathers pass them
       else X.get({bid[0], bid[1], bid[2], bid[3]}, buf);
-      size_t c[R] = {}, nb = 1;
+      // the block and dst are both row-major: copy runs along the last mode
+      size_t       c[R] = {}, nb = 1;
+      const size_t run = modes[R - 1]->ext[bid[R - 1]];
       for(size_t m = 0; m < R; m++) nb *= modes[m]->ext[bid[m]];
-      for(size_t e = 0; e < nb; e++) {
+      for(size_t e = 0; e < nb; e += run) {
         size_t lin = 0;
         for(size_t m = 0; m < R; m++) lin = lin * modes[m]->n + modes[m]->off[bid[m]] + c[m];
-        dst[lin] = (double) buf[e];
-        for(size_t m = R; m-- > 0;) {
+        std::copy(buf.begin() + e, buf.begin() + e + run, dst.begin() + lin);
+        for(size_t m = R - 1; m-- > 0;) {
           if(++c[m] < modes[m]->ext[bid[m]]) break;
           c[m] = 0;
         }
