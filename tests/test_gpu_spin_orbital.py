@@ -103,3 +103,19 @@ def test_open_shell_matches_reference_golden(built):
         g4, g5 = _call(c["oa"], c["ob"], c["va"], c["vb"], arrs)
         assert rel_close(g4, c["e_bracket_T"], 1e-12) and rel_close(g5, c["e_paren_T"], 1e-12), \
             (c["name"], g4, c["e_bracket_T"], g5, c["e_paren_T"])
+
+
+def test_open_shell_bench_line(built):
+    """bench.py --open-shell prints one JSON line with the contract's keys (small system)."""
+    import json
+    import subprocess
+    import sys
+    from conftest import ROOT
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--open-shell", "4,3,12,14", "--steps", "1",
+                          "--warmup", "3"], check=True, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "dtype",
+              "config", "roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks"):
+        assert k in line, k
+    assert line["value"] > 0 and line["e2e"]["value"] > 0 and line["gpu_launches"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["energies"]["host_equals_device"]
