@@ -81,9 +81,13 @@ def build_oracle(reference: str | None = None) -> None:
     own CPU (T) (oracle/_ref) only where the reference tree is present."""
     oracle = ROOT / "oracle"
     _run(["make", "-C", str(oracle), "port"])
-    ref = reference or os.environ.get("CCSDT_REFERENCE", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "exachem", "cc", "ccsd_t")):
+    ref = reference or os.environ.get("CCSDT_REFERENCE")
+    if not ref:
+        print("oracle/_ref not rebuilt: CCSDT_REFERENCE (the reference source tree) is not set", file=sys.stderr)
+    elif os.path.isdir(os.path.join(ref, "exachem", "cc", "ccsd_t")):
         _run(["make", "-C", str(oracle), "ref", f"REFERENCE={ref}"])
+    else:
+        print(f"oracle/_ref not rebuilt: {ref} holds no exachem/cc/ccsd_t", file=sys.stderr)
 
 
 if __name__ == "__main__":

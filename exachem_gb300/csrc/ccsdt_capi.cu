@@ -6,6 +6,8 @@
 // input stays resident in HBM and each occupied triplet i <= j <= k is one unit of work.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -47,9 +49,32 @@ ccsdt_status ccsdt_handle::fail(ccsdt_status s, const std::string& msg) {
   return s;
 }
 
+namespace {
+std::atomic<long> g_alloc_countdown{0}; // > 0: the call that brings it to 0 fails
+std::atomic<long> g_alloc_attempts{0};
+} // namespace
+
+cudaError_t ccsdt::dev_malloc(void** p, size_t bytes) {
+  g_alloc_attempts.fetch_add(1);
+  if(g_alloc_countdown.load() > 0 && g_alloc_countdown.fetch_sub(1) == 1) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if(e != cudaSuccess) *p = nullptr;
+  return e;
+}
+
+extern "C" ccsdt_status ccsdt_debug_fail_alloc(long nth, long* attempts) {
+  if(nth < 0) return CCSDT_E_INVALID;
+  if(attempts) *attempts = g_alloc_attempts.exchange(0);
+  g_alloc_countdown.store(nth);
+  return CCSDT_OK;
+}
+
 ccsdt_status ccsdt_handle::alloc(double** p, size_t n) {
   if(n == 0) n = 1;
-  cudaError_t e = cudaMalloc((void**) p, n * sizeof(double));
+  cudaError_t e = ccsdt::dev_malloc((void**) p, n * sizeof(double));
   if(e != cudaSuccess) {
     *p = nullptr;
     cudaGetLastError();
@@ -80,15 +105,17 @@ ccsdt_handle::~ccsdt_handle() {
 
 // Device arrays of the inputs (allocated once per handle).
 ccsdt_status ccsdt_handle::ensure_inputs() {
-  if(eo) return CCSDT_OK;
+  if(d_count) return CCSDT_OK; // the last one: every array is there
   const size_t o = this->o, v = this->v;
   const size_t n_t2 = o * o * v * v, n_ooov = o * o * o * v;
+  // allocate each array still missing (a call that failed part-way may have left some)
+  auto need = [&](double** p, size_t n) { return *p ? CCSDT_OK : alloc(p, n); };
   ccsdt_status s;
-  if((s = alloc(&eo, o)) || (s = alloc(&ev, v)) || (s = alloc(&t1, o * v)) || (s = alloc(&t2, n_t2)) ||
-     (s = alloc(&oovv, n_t2)) || (s = alloc(&ooov, n_ooov)) || (s = alloc(&ovvv, o * v * v * v)) ||
-     (s = alloc(&t2h, n_t2)) || (s = alloc(&ooovh, n_ooov)))
+  if((s = need(&eo, o)) || (s = need(&ev, v)) || (s = need(&t1, o * v)) || (s = need(&t2, n_t2)) ||
+     (s = need(&oovv, n_t2)) || (s = need(&ooov, n_ooov)) || (s = need(&ovvv, o * v * v * v)) ||
+     (s = need(&t2h, n_t2)) || (s = need(&ooovh, n_ooov)))
     return s;
-  if(cudaMalloc((void**) &d_count, sizeof(unsigned long long)) != cudaSuccess) {
+  if(ccsdt::dev_malloc((void**) &d_count, sizeof(unsigned long long)) != cudaSuccess) {
     d_count = nullptr;
     cudaGetLastError();
     return fail(CCSDT_E_OOM, "cudaMalloc of the error counter failed");
@@ -247,11 +274,11 @@ ccsdt_status ccsdt_upload(ccsdt_handle* h, const double* eps_occ, const double* 
 ccsdt_status ccsdt_handle::ensure_scratch() {
   const size_t v = this->v;
   ccsdt_status s;
-  if(!P12) {
-    if((s = alloc(&P12, v * v * v)) || (s = alloc(&P34, v * v * v)) || (s = alloc(&P56, v * v * v)))
-      return s;
-    if((s = alloc(&part, 4 * (size_t) kEnergyBlocks)) || (s = alloc(&res, 2))) return s;
-  }
+  // each buffer on its own: a call that failed part-way may have left some of them
+  auto need = [&](double** p, size_t n) { return *p ? CCSDT_OK : alloc(p, n); };
+  if((s = need(&P12, v * v * v)) || (s = need(&P34, v * v * v)) || (s = need(&P56, v * v * v)) ||
+     (s = need(&part, 4 * (size_t) kEnergyBlocks)) || (s = need(&res, 2)))
+    return s;
   return CCSDT_OK;
 }
 
@@ -318,7 +345,7 @@ ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
   EnergyArgs ea{P12, P34, P56, oovv, t1, eo, ev, (int) o, (int) v, i, j, k, part};
   energy_fp64_kernel<<<kEnergyBlocks, E_THREADS, 0, stream>>>(ea);
   if(profiling) cudaEventRecord(prof_ev[3], stream);
-  reduce_parts_kernel<<<1, 32, 0, stream>>>(part, kEnergyBlocks, multiplicity(i, j, k) / 9.0, eout);
+  reduce_parts_kernel<<<1, E_THREADS, 0, stream>>>(part, kEnergyBlocks, multiplicity(i, j, k) / 9.0, eout);
   if(profiling) cudaEventRecord(prof_ev[4], stream);
   launches += 2;
   cudaError_t e = cudaGetLastError();

@@ -9,6 +9,13 @@
 
 #include "../../include/ccsdt.h"
 
+namespace ccsdt {
+// Every device allocation of the handle-based paths goes through here: cudaMalloc, except that a
+// testing countdown (ccsdt_debug_fail_alloc) can make the n-th call fail as an out-of-memory
+// cudaMalloc would (*p = nullptr, cudaErrorMemoryAllocation), so the error paths can be exercised.
+cudaError_t dev_malloc(void** p, size_t bytes);
+} // namespace ccsdt
+
 constexpr int kEnergyBlocks = 1216; // 8 x 152 SMs
 constexpr int kTiledBlocks  = 1216; // upper bound of the tiled energy's persistent grid
 
@@ -41,7 +48,7 @@ struct ccsdt_handle {
   float *            oovv_f = nullptr, *t1_f = nullptr;
   float2 *           F12 = nullptr, *F34 = nullptr, *F56 = nullptr;
   // tcgen05 path: TMA maps over the digit planes (built once per slicing) and an error flag
-  CUtensorMap        tmaps[12];
+  CUtensorMap        tmaps[9];
   bool               tmaps_ready = false;
   int                tmaps_S     = 0, tmaps_NT = 0, tmaps_KC = 0;
   int*               d_err       = nullptr;
@@ -105,10 +112,8 @@ struct ccsdt_handle {
   int*      bt_tri = nullptr;        // triplet table (i, j, k, output index)
   long      bt_tri_cap = 0;
   int       batch_slots = 4;         // triplets per batch
-  bool      pz_pair = false;         // this call runs the two-CTA cluster kernel
-  bool      force_single_cta = false; // test knob: the single-CTA persistent kernel instead
-  int       pz_pair_clusters = 0;    // co-resident clusters of the cluster kernel (this S)
-  int       pair_clusters_by_conf[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  unsigned  test_spin_limit = 0;     // testing: bounded-wait poll limit of the persistent kernel (0: default)
+  int       test_skip_loads = 0;     // testing: the persistent kernel issues no TMA loads
   // persistent-contraction configuration per S (index into kPzConfs, -1 = the default), set by
   // the autotuner or ccsdt_set_tile_config; tuned[S]: the autotuner has run for S
   int          pz_conf_idx[6] = {-1, -1, -1, -1, -1, -1};

@@ -80,7 +80,7 @@ extern "C" ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps
   double*       scratch = nullptr;
   if(e == cudaSuccess && !on_device) {
     const long long n_oo = o * o * nq, n_ov = o * v * nq, n_vv = v * v * nq;
-    if(cudaMalloc((void**) &scratch, (n_oo + n_ov + n_vv) * sizeof(double)) != cudaSuccess) {
+    if(ccsdt::dev_malloc((void**) &scratch, (n_oo + n_ov + n_vv) * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
       return h->fail(CCSDT_E_OOM, "ccsdt_upload_cholesky: cudaMalloc of " +
                                      std::to_string((n_oo + n_ov + n_vv) * sizeof(double)) + " bytes for the vectors");

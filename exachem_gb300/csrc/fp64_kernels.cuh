@@ -211,18 +211,27 @@ static __global__ void __launch_bounds__(E_THREADS) energy_fp64_kernel(const __g
   block_reduce_csum(s4, s5, A.part + 4 * (long long) blockIdx.x);
 }
 
-// Sums nparts block partials (fixed order) for triplet slot `slot`, scales by m/9.
-static __global__ void reduce_parts_kernel(const double* part, int nparts, double scale, double* out) {
-  if(threadIdx.x != 0 || blockIdx.x != 0) return;
+// Sums nparts block partials for one triplet and scales by m/9: E_THREADS threads each take a
+// contiguous run of partials, then the fixed-shape block tree (deterministic for a given nparts).
+// Launch with one block of E_THREADS threads.
+static __global__ void __launch_bounds__(E_THREADS) reduce_parts_kernel(const double* part, int nparts, double scale,
+                                                                      double* out) {
   CSum a, b;
-  for(int q = 0; q < nparts; q++) {
+  const int per = (nparts + E_THREADS - 1) / E_THREADS;
+  const int q0 = threadIdx.x * per, q1 = min(nparts, q0 + per);
+  for(int q = q0; q < q1; q++) {
     a.add(part[4 * q + 0]);
     a.c += part[4 * q + 1];
     b.add(part[4 * q + 2]);
     b.c += part[4 * q + 3];
   }
-  out[0] = scale * a.value();
-  out[1] = scale * b.value();
+  __shared__ double tmp[4];
+  block_reduce_csum(a, b, tmp);
+  __syncthreads();
+  if(threadIdx.x == 0) {
+    out[0] = scale * (tmp[0] + tmp[1]);
+    out[1] = scale * (tmp[2] + tmp[3]);
+  }
 }
 
 // Compensated fixed-order sum of per-triplet energies e[2 n] -> out[2].

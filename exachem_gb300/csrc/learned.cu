@@ -99,7 +99,7 @@ ccsdt_status ccsdt_handle::ensure_stats() {
   const long long o = this->o, v = this->v;
   auto need = [&](int** p, size_t n) -> ccsdt_status {
     if(*p) return CCSDT_OK;
-    if(cudaMalloc((void**) p, n * sizeof(int)) != cudaSuccess) {
+    if(ccsdt::dev_malloc((void**) p, n * sizeof(int)) != cudaSuccess) {
       *p = nullptr;
       cudaGetLastError();
       return fail(CCSDT_E_OOM, "exponent statistics: cudaMalloc failed");
@@ -138,7 +138,7 @@ struct Scratch {
   template<typename T>
   T* get(size_t n) {
     void* q = nullptr;
-    if(cudaMalloc(&q, (n ? n : 1) * sizeof(T)) != cudaSuccess) {
+    if(ccsdt::dev_malloc(&q, (n ? n : 1) * sizeof(T)) != cudaSuccess) {
       cudaGetLastError();
       return nullptr;
     }
@@ -231,7 +231,6 @@ extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccs
      cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream) != cudaSuccess)
     return h->fail(CCSDT_E_CUDA, "estimate scratch init");
   h->force_mma_sync   = false;
-  h->force_single_cta = opts->test_single_cta == 1;
   if((s = h->run_batched(opts->slices, n, tri, false, dtail, dsens))) return s;
   std::vector<double> E(2 * n), sens(n);
   std::vector<float>  tail(n);
@@ -262,7 +261,7 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
   double*  dsens = sc.get<double>((size_t) n);
   if(!dt || !df || !dsl || !dtail || !dsens) return fail(CCSDT_E_OOM, "learned-mode scratch");
   if(!model_bf16) {
-    if(cudaMalloc(&model_bf16, CCSDT_MLP_NPARAM * sizeof(__nv_bfloat16)) != cudaSuccess) {
+    if(ccsdt::dev_malloc(&model_bf16, CCSDT_MLP_NPARAM * sizeof(__nv_bfloat16)) != cudaSuccess) {
       model_bf16 = nullptr;
       cudaGetLastError();
       return fail(CCSDT_E_OOM, "model buffer");

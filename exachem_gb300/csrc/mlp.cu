@@ -150,7 +150,7 @@ struct DevBuf {
     if(p) cudaFree(p);
   }
   bool alloc(size_t bytes) {
-    if(cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+    if(ccsdt::dev_malloc(&p, bytes ? bytes : 1) != cudaSuccess) {
       p = nullptr;
       cudaGetLastError();
       return false;

@@ -1,14 +1,18 @@
 // Allocation-free FP64 (T): the plain FP64 path run on a fixed, file-scope device scratch.
 //
 // For callers that cannot call cudaMalloc: a host runtime whose device memory is owned by a
-// pooled allocator (ExaChem's TAMM runs on an RMM pool that takes the device up front), code
-// inside a stream capture, or services under a fixed device-memory budget.  The caller passes
-// device inputs and a device output; every intermediate lives in `g_noalloc_scratch` below.
+// pooled allocator (ExaChem's TAMM runs on an RMM pool that takes the device up front, so a
+// cudaMalloc beside it fails or fragments the pool), or a service held to a fixed device-memory
+// budget.  The caller passes device inputs and a device output; every intermediate lives in
+// `g_noalloc_scratch` below.
 //
-// Limits: o <= CCSDT_NOALLOC_O_MAX (12), v <= CCSDT_NOALLOC_V_MAX (48).  The scratch is
-// NOALLOC_DOUBLES doubles (about 6.0 MB); every GPU that loads this library holds it until
-// the process exits.  All calls share it: two calls that overlap on the GPU (different
-// streams, or different host threads without ordering) race on it and give wrong results.
+// Limits: o <= 12, v <= 48.  The scratch is NOALLOC_DOUBLES doubles (about 6.0 MB); every GPU
+// that loads this library holds it until the process exits.  All calls share it: two calls that
+// overlap on the GPU (different streams, or different host threads without ordering) race on it
+// and give wrong results.  Nothing in it needs clearing between calls: each call writes every
+// element it reads before reading it.  The first call on a device looks up the array's device
+// address and keeps it for the process; after a cudaDeviceReset the module may load at another
+// address, so the entry point must not be used across a device reset.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -117,7 +121,7 @@ extern "C" ccsdt_status ccsdt_energy_noalloc(int o, int v, const double* eps_occ
         dmma_gemm_kernel<<<dim3((unsigned) pt, 1, 3), D_THREADS, 0, st>>>(pb);
         EnergyArgs ea{P12, P34, P56, oovv, t1, eps_occ, eps_vir, o, v, i, j, k, part};
         energy_fp64_kernel<<<kEnergyBlocks, E_THREADS, 0, st>>>(ea);
-        reduce_parts_kernel<<<1, 32, 0, st>>>(part, kEnergyBlocks, mult(i, j, k) / 9.0, eout);
+        reduce_parts_kernel<<<1, E_THREADS, 0, st>>>(part, kEnergyBlocks, mult(i, j, k) / 9.0, eout);
         if(cudaGetLastError() != cudaSuccess) return CCSDT_E_CUDA;
       }
   reduce_triplets_kernel<<<1, 32, 0, st>>>(etrip, ntri, energies);

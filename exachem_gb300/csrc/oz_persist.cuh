@@ -54,9 +54,7 @@ constexpr unsigned PZ_END = 0xffffffffu;
 
 // map indices (the handle's map table): the d-sum uses 0-2, the l-sum 6-8
 enum {
-  PZ_OVVV_NAT = 0, PZ_OVVV_SWP = 1, PZ_T2 = 2, PZ_T2H_NAT_B = 6, PZ_T2H_SWP_B = 7, PZ_OOOVH_A = 8,
-  // the A maps again with a one-plane box (the cluster kernel loads A plane by plane)
-  PZ_OVVV_NAT_P1 = 9, PZ_OVVV_SWP_P1 = 10, PZ_OOOVH_A_P1 = 11, PZ_NMAPS = 12
+  PZ_OVVV_NAT = 0, PZ_OVVV_SWP = 1, PZ_T2 = 2, PZ_T2H_NAT_B = 6, PZ_T2H_SWP_B = 7, PZ_OOOVH_A = 8, PZ_NMAPS = 9
 };
 
 struct PzParams {
@@ -72,6 +70,9 @@ struct PzParams {
   int*            err;        // set on a bounded-wait timeout
   float*          tail;       // optional: tail[output index] += sum of squares of the last
                               // kept level's terms (a-posteriori truncation estimate)
+  unsigned        spin;       // polls before a bounded mbarrier wait gives up (sm100::kSpinLimit)
+  int             skip_loads; // testing: announce each stage's bytes but issue no TMA load, so
+                              // the stage waits run out (the timeout path, CCSDT_E_TIMEOUT)
 };
 
 struct PzTerm {
@@ -141,7 +142,7 @@ __device__ __forceinline__ PzItem pz_decode(unsigned id, int v, int yblocks, int
   return it;
 }
 
-// Epilogue of one item (shared by the persistent kernels): thread = one tile row (TMEM lane
+// Epilogue of one item: thread = one tile row (TMEM lane
 // quarter q, row = 32 q + lane) x COLS = NT / 4 columns from c_lo.  Per term it waits for the MMAs
 // (lvl_full of the term's buffer), folds the S exact levels with oz_horner in chunks of 8 columns
 // and adds (d-sum terms) or subtracts (l-sum terms) them in float-float, releases the buffer
@@ -166,7 +167,7 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
 #pragma unroll 1
   for(int t = 0; t < PZ_TERMS; t++, term_it++) {
     const int  buf = term_it % NBUF;
-    const bool okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it / NBUF) & 1) && !*abort_flag);
+    const bool okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it / NBUF) & 1, P.spin) && !*abort_flag);
     if(!okw) return false;
     sm100::tc_fence_after();
     // fold `W` columns starting at c0 whose S levels are in rv; `neg`: an l-sum term; `first`: the
@@ -362,7 +363,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         const unsigned q  = atomicAdd(P.queue, 1u);
         const unsigned id = (q < P.nitems && !*abort_flag) ? P.order[q] : PZ_END;
         const int      r  = it % PZ_IR;
-        if(it >= PZ_IR && !sm100::mbar_wait(&item_empty[r], ((it / PZ_IR) - 1) & 1)) {
+        if(it >= PZ_IR && !sm100::mbar_wait(&item_empty[r], ((it / PZ_IR) - 1) & 1, P.spin)) {
           fail();
           item_id[r] = PZ_END;
           sm100::mbar_arrive(&item_full[r]);
@@ -378,19 +379,21 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
           const PzTerm T = pz_term(P, w.job, t, i, j, k, w.x);
           for(int k0 = 0; k0 < T.Kp; k0 += KC, stage_it++) {
             const int s = stage_it % STAGES, use = stage_it / STAGES;
-            if(use > 0 && !sm100::mbar_wait(&empty[s], (use - 1) & 1)) {
+            if(use > 0 && !sm100::mbar_wait(&empty[s], (use - 1) & 1, P.spin)) {
               fail();
               break;
             }
             unsigned char* a = smem + s * C::STAGE_BYTES;
             sm100::mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
-            sm100::tma_load_5d(a, &P.maps[T.mapA], &full[s], k0, w.yb * PZ_BM, T.a2, T.a3, 0);
-            sm100::tma_load_5d(a + C::A_BYTES, &P.maps[T.mapB], &full[s], k0, w.nb * NT, T.b2, T.b3, 0);
+            if(!P.skip_loads) {
+              sm100::tma_load_5d(a, &P.maps[T.mapA], &full[s], k0, w.yb * PZ_BM, T.a2, T.a3, 0);
+              sm100::tma_load_5d(a + C::A_BYTES, &P.maps[T.mapB], &full[s], k0, w.nb * NT, T.b2, T.b3, 0);
+            }
           }
         }
       }
       for(int u = (stage_it > STAGES ? stage_it - STAGES : 0); u < stage_it; u++)
-        if(!sm100::mbar_wait(&full[u % STAGES], (u / STAGES) & 1)) fail();
+        if(!sm100::mbar_wait(&full[u % STAGES], (u / STAGES) & 1, P.spin)) fail();
     }
   } else if(warp == 1) {
     // ------------------------------------------------------------ MMA issuer (the warp runs the
@@ -418,7 +421,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     }
     if(lane == 0) {
       sm100::mma_commit(drain);
-      if(!sm100::mbar_wait(drain, 0)) fail();
+      if(!sm100::mbar_wait(drain, 0, P.spin)) fail();
     }
   } else if(warp == 2) {
     // ------------------------------------------------------------ gate: the MMA issuer's waits
@@ -429,7 +432,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
       int       ok = 1;
       unsigned  id = PZ_END;
       if(lane == 0) {
-        ok = sm100::mbar_wait(&item_full[r], (it / PZ_IR) & 1);
+        ok = sm100::mbar_wait(&item_full[r], (it / PZ_IR) & 1, P.spin);
         if(ok) {
           id = item_id[r];
           sm100::mbar_arrive(&item_empty[r]);
@@ -443,11 +446,11 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
       for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
         const int nst = (t < 2 ? P.kp_v : P.kp_o) / KC;
         const int buf = term_it % C::NBUF;
-        if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1);
+        if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1, P.spin);
         for(int u = 0; u < nst; u++, stage_it++) {
           bool mine = false;
           if(lane == 0) {
-            if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1);
+            if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1, P.spin);
             if(!ok) fail();
             mine = !ok || *abort_flag;
           }
@@ -468,7 +471,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     int            tail_slot = -1;
     for(int it = 0;; it++) {
       const int  r  = it % PZ_IR;
-      const bool ok = __all_sync(0xffffffffu, sm100::mbar_wait(&item_full[r], (it / PZ_IR) & 1));
+      const bool ok = __all_sync(0xffffffffu, sm100::mbar_wait(&item_full[r], (it / PZ_IR) & 1, P.spin));
       if(!ok) {
         fail();
         break;

@@ -28,45 +28,33 @@ namespace {
 
 // Item ids of B slots sorted by estimated cost (rows x columns of the tile), largest first; ties
 // keep the natural order (n-block fastest) so concurrently running CTAs share A tiles in L2.
-// pair = true: items of the cluster kernel, one per pair of adjacent n-blocks.
-std::vector<unsigned> cost_order(int B, int v, int NT, bool pair) {
-  const int  yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT, nn = pair ? (nb + 1) / 2 : nb;
-  const long n  = (long) B * 3 * v * yb * nn;
+std::vector<unsigned> cost_order(int B, int v, int NT) {
+  const int  yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT;
+  const long n  = (long) B * 3 * v * yb * nb;
   std::vector<unsigned> ids(n);
   std::iota(ids.begin(), ids.end(), 0u);
-  auto cols = [&](int b) { return b < nb ? std::min(NT, v - b * NT) : 0; };
   auto cost = [&](unsigned id) {
-    const int n_b = id % nn, y_b = (id / nn) % yb;
-    const int rows = std::min(PZ_BM, v - y_b * PZ_BM);
-    return rows * (pair ? cols(2 * n_b) + cols(2 * n_b + 1) : cols(n_b));
+    const int n_b = id % nb, y_b = (id / nb) % yb;
+    return std::min(PZ_BM, v - y_b * PZ_BM) * std::min(NT, v - n_b * NT);
   };
   std::stable_sort(ids.begin(), ids.end(), [&](unsigned a, unsigned b) { return cost(a) > cost(b); });
   return ids;
 }
 
 // Items per triplet slot of one launch.
-long items_per_slot(int v, int NT, bool pair) {
-  const int yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT;
-  return 3L * v * yb * (pair ? (nb + 1) / 2 : nb);
+long items_per_slot(int v, int NT) {
+  return 3L * v * ((v + PZ_BM - 1) / PZ_BM) * ((v + NT - 1) / NT);
 }
 
 } // namespace
 
 namespace ccsdt {
-cudaError_t pz_launch_pair_a(int conf, const PzParams& p, int ncl, cudaStream_t st);
 cudaError_t pz_launch_single_a(int conf, const PzParams& p, int grid, cudaStream_t st);
-int         pz_pair_clusters_a(int conf);
-cudaError_t pz_launch_pair_b(int conf, const PzParams& p, int ncl, cudaStream_t st);
 cudaError_t pz_launch_single_b(int conf, const PzParams& p, int grid, cudaStream_t st);
-int         pz_pair_clusters_b(int conf);
 
-cudaError_t pz_launch_pair(int conf, const PzParams& p, int ncl, cudaStream_t st) {
-  return conf < kPzSplit ? pz_launch_pair_a(conf, p, ncl, st) : pz_launch_pair_b(conf, p, ncl, st);
-}
 cudaError_t pz_launch_single(int conf, const PzParams& p, int grid, cudaStream_t st) {
   return conf < kPzSplit ? pz_launch_single_a(conf, p, grid, st) : pz_launch_single_b(conf, p, grid, st);
 }
-int pz_pair_clusters(int conf) { return conf < kPzSplit ? pz_pair_clusters_a(conf) : pz_pair_clusters_b(conf); }
 } // namespace ccsdt
 
 // The configuration in use for S digit planes: the one the autotuner kept, else the default.
@@ -85,8 +73,9 @@ ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
     if(bt_part) cudaFree(bt_part);
     bt_F = nullptr;
     bt_part = nullptr;
-    if(cudaMalloc((void**) &bt_F, sizeof(float2) * 3 * v3 * B) != cudaSuccess ||
-       cudaMalloc((void**) &bt_part, sizeof(double) * 6 * kTiledBlocks * B) != cudaSuccess) {
+    bt_B = 0; // until both buffers exist
+    if(dev_malloc((void**) &bt_F, sizeof(float2) * 3 * v3 * B) != cudaSuccess ||
+       dev_malloc((void**) &bt_part, sizeof(double) * 6 * kTiledBlocks * B) != cudaSuccess) {
       cudaGetLastError();
       if(bt_F) cudaFree(bt_F);
       bt_F = nullptr;
@@ -95,12 +84,13 @@ ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
     bt_B = B;
     bt_order_key = -1;
   }
-  const int key = ((conf * 8 + S) * 100000 + B) * 2 + (pz_pair ? 1 : 0);
+  const int key = (conf * 8 + S) * 100000 + B;
   if(bt_order_key != key) {
-    auto ids = cost_order(B, v, NT, pz_pair);
+    auto ids = cost_order(B, v, NT);
     if(bt_order) cudaFree(bt_order);
-    bt_order = nullptr;
-    if(cudaMalloc((void**) &bt_order, ids.size() * sizeof(unsigned)) != cudaSuccess) {
+    bt_order     = nullptr;
+    bt_order_key = -1; // until the new table is in place
+    if(dev_malloc((void**) &bt_order, ids.size() * sizeof(unsigned)) != cudaSuccess) {
       cudaGetLastError();
       return fail(CCSDT_E_OOM, "work-queue table: cudaMalloc failed");
     }
@@ -110,7 +100,7 @@ ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
     bt_order_key = key;
   }
   if(!bt_ctrl) { // [0] queue l-sum, [1] queue d-sum, [2] batch base
-    if(cudaMalloc((void**) &bt_ctrl, 4 * sizeof(int)) != cudaSuccess) {
+    if(dev_malloc((void**) &bt_ctrl, 4 * sizeof(int)) != cudaSuccess) {
       bt_ctrl = nullptr;
       cudaGetLastError();
       return fail(CCSDT_E_OOM, "batch counters");
@@ -148,8 +138,10 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
+  p.spin       = test_spin_limit ? test_spin_limit : sm100::kSpinLimit;
+  p.skip_loads = test_skip_loads;
   const int  NT  = kPzConfs[conf].NT;
-  const long per = items_per_slot(v, NT, pz_pair);
+  const long per = items_per_slot(v, NT);
   if(nitems_override <= 0) p.nitems = (unsigned) (per * nslots);
   // the cost-ordered table was built for bt_B slots; a smaller last batch has its own table
   const bool partial = nslots != bt_B;
@@ -174,9 +166,7 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
     cudaEventRecord(prof_ev[0], stream);
     cudaEventRecord(prof_ev[1], stream); // no separate l-sum phase
   }
-  if(e == cudaSuccess)
-    e = pz_pair ? pz_launch_pair(conf, p, (int) std::min<long>(pz_pair_clusters, (long) p.nitems), stream)
-                : pz_launch_single(conf, p, sm, stream);
+  if(e == cudaSuccess) e = pz_launch_single(conf, p, sm, stream);
   launches++;
   if(profiling) cudaEventRecord(prof_ev[2], stream);
   if(tv[1]) cudaEventRecord(tv[1], stream);
@@ -206,12 +196,8 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
   ccsdt_status s;
   tev_used = 0; // events of a batch that failed earlier are not read
   tev_slots.clear();
-  // the two-CTA cluster kernel when its clusters can be resident (and not switched off for a test)
   const int conf = pz_conf_index(S);
   if(conf < 0) return fail(CCSDT_E_INVALID, "no persistent configuration for this slice count");
-  if(pair_clusters_by_conf[conf] < 0) pair_clusters_by_conf[conf] = ccsdt::pz_pair_clusters(conf);
-  pz_pair_clusters = pair_clusters_by_conf[conf];
-  pz_pair          = !force_single_cta && pz_pair_clusters > 0;
   if((s = ensure_slices(std::max(S, slices_ready), 0)) || (s = ensure_tmaps(S, kPzConfs[conf].NT, kPzConfs[conf].KC))) return s;
   // table of non-zero triplets (i < k); i = j = k contributes exactly zero
   std::vector<int> tab;
@@ -231,8 +217,9 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
   if((s = ensure_batch(S, B))) return s;
   if(bt_tri_cap < m) {
     if(bt_tri) cudaFree(bt_tri);
-    bt_tri = nullptr;
-    if(cudaMalloc((void**) &bt_tri, tab.size() * sizeof(int)) != cudaSuccess) {
+    bt_tri     = nullptr;
+    bt_tri_cap = 0; // until the new table is in place
+    if(dev_malloc((void**) &bt_tri, tab.size() * sizeof(int)) != cudaSuccess) {
       cudaGetLastError();
       return fail(CCSDT_E_OOM, "triplet table");
     }
@@ -240,13 +227,13 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
   }
   // natural-order table for a partial last batch
   const int  NT  = kPzConfs[conf].NT;
-  const long per = items_per_slot(v, NT, pz_pair);
+  const long per = items_per_slot(v, NT);
   const long rem = m % B;
   if(rem) {
-    auto ids = cost_order((int) rem, v, NT, pz_pair);
+    auto ids = cost_order((int) rem, v, NT);
     if(bt_order_partial) cudaFree(bt_order_partial);
     bt_order_partial = nullptr;
-    if(cudaMalloc((void**) &bt_order_partial, ids.size() * sizeof(unsigned)) != cudaSuccess) {
+    if(dev_malloc((void**) &bt_order_partial, ids.size() * sizeof(unsigned)) != cudaSuccess) {
       cudaGetLastError();
       return fail(CCSDT_E_OOM, "partial work-queue table");
     }
@@ -318,8 +305,6 @@ ccsdt_status ccsdt_handle::collect_phase_times() {
   return CCSDT_OK;
 }
 
-static_assert(kPzNConfs <= 16, "pair_clusters_by_conf holds one entry per configuration");
-
 // Times every compiled configuration for S digit planes on one triplet of this system (the
 // contraction launch, CUDA events on the handle's stream, second of two runs) and keeps the
 // fastest for the handle's later calls.  Every configuration gives bit-identical energies.
@@ -345,9 +330,7 @@ ccsdt_status ccsdt_handle::autotune(int S, double* ms, int* n, int* chosen) {
   const bool   pt = phase_timing;
   const double saved[3] = {phase_ms[0], phase_ms[1], phase_ms[2]};
   const long   sb = phase_batches, st = phase_triplets;
-  const bool   fs = force_single_cta;
   phase_timing     = true;
-  force_single_cta = false;
   int    best   = -1;
   double best_t = 0.0;
   for(size_t q = 0; q < cands.size() && !s; q++) {
@@ -362,7 +345,6 @@ ccsdt_status ccsdt_handle::autotune(int S, double* ms, int* n, int* chosen) {
     if(!s && (best < 0 || t < best_t)) best = (int) q, best_t = t;
   }
   phase_timing     = pt;
-  force_single_cta = fs;
   for(int q = 0; q < 3; q++) phase_ms[q] = saved[q];
   phase_batches  = sb;
   phase_triplets = st;
@@ -413,4 +395,11 @@ extern "C" ccsdt_status ccsdt_set_tile_config(ccsdt_handle* h, int slices, int i
       m++;
     }
   return h->fail(CCSDT_E_INVALID, "ccsdt_set_tile_config: no configuration " + std::to_string(index));
+}
+
+extern "C" ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin_limit, int skip_loads) {
+  if(!h) return CCSDT_E_INVALID;
+  h->test_spin_limit = spin_limit;
+  h->test_skip_loads = skip_loads ? 1 : 0;
+  return CCSDT_OK;
 }

@@ -50,10 +50,7 @@ constexpr bool pz_all_ok() {
 }
 static_assert(pz_all_ok(), "every compiled configuration must fit the kernels' limits, grouped by S");
 
-// Launch configuration `conf` (an index into kPzConfs): the two-CTA cluster kernel on `ncl`
-// clusters, or the single-CTA kernel on `grid` CTAs; resident clusters of the cluster kernel.
-cudaError_t pz_launch_pair(int conf, const PzParams& p, int ncl, cudaStream_t st);
+// Launch configuration `conf` (an index into kPzConfs) of the persistent kernel on `grid` CTAs.
 cudaError_t pz_launch_single(int conf, const PzParams& p, int grid, cudaStream_t st);
-int         pz_pair_clusters(int conf);
 
 } // namespace ccsdt

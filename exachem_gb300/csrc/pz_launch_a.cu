@@ -8,26 +8,12 @@ static_assert(kPzSplit == 8 && kPzConfs[7].S == 3 && kPzConfs[8].S == 4, "the sp
 
 #define PZ_CASES(X) X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7)
 
-cudaError_t pz_launch_pair_a(int conf, const PzParams& p, int ncl, cudaStream_t st) {
-#define X(c) \
-  case c: return pz_launch_pair_t<c>(p, ncl, st);
-  switch(conf) { PZ_CASES(X) }
-#undef X
-  return cudaErrorInvalidValue;
-}
 cudaError_t pz_launch_single_a(int conf, const PzParams& p, int grid, cudaStream_t st) {
 #define X(c) \
   case c: return pz_launch_single_t<c>(p, grid, st);
   switch(conf) { PZ_CASES(X) }
 #undef X
   return cudaErrorInvalidValue;
-}
-int pz_pair_clusters_a(int conf) {
-#define X(c) \
-  case c: return pz_pair_clusters_t<c>();
-  switch(conf) { PZ_CASES(X) }
-#undef X
-  return 0;
 }
 
 } // namespace ccsdt

@@ -8,26 +8,12 @@ static_assert(kPzNConfs == 15, "the cases below list every configuration from kP
 
 #define PZ_CASES(X) X(8) X(9) X(10) X(11) X(12) X(13) X(14)
 
-cudaError_t pz_launch_pair_b(int conf, const PzParams& p, int ncl, cudaStream_t st) {
-#define X(c) \
-  case c: return pz_launch_pair_t<c>(p, ncl, st);
-  switch(conf) { PZ_CASES(X) }
-#undef X
-  return cudaErrorInvalidValue;
-}
 cudaError_t pz_launch_single_b(int conf, const PzParams& p, int grid, cudaStream_t st) {
 #define X(c) \
   case c: return pz_launch_single_t<c>(p, grid, st);
   switch(conf) { PZ_CASES(X) }
 #undef X
   return cudaErrorInvalidValue;
-}
-int pz_pair_clusters_b(int conf) {
-#define X(c) \
-  case c: return pz_pair_clusters_t<c>();
-  switch(conf) { PZ_CASES(X) }
-#undef X
-  return 0;
 }
 
 } // namespace ccsdt

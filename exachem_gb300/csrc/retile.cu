@@ -102,7 +102,7 @@ extern "C" ccsdt_status ccsdt_upload_begin(ccsdt_handle* h, const double* eps_oc
       for(int x: ext) tt.push_back(off), off += x;
       tt.insert(tt.end(), ext.begin(), ext.end());
     }
-    if(cudaMalloc((void**) &h->blk_tiles, tt.size() * sizeof(int)) != cudaSuccess) {
+    if(ccsdt::dev_malloc((void**) &h->blk_tiles, tt.size() * sizeof(int)) != cudaSuccess) {
       h->blk_tiles = nullptr;
       cudaGetLastError();
       return h->fail(CCSDT_E_OOM, "tile table");
@@ -146,7 +146,7 @@ extern "C" ccsdt_status ccsdt_upload_blocks(ccsdt_handle* h, int kind, long n, c
   if(h->blk_meta_cap < (long) meta_bytes) {
     if(h->blk_meta) cudaFree(h->blk_meta);
     h->blk_meta = nullptr;
-    if(cudaMalloc((void**) &h->blk_meta, meta_bytes) != cudaSuccess) {
+    if(ccsdt::dev_malloc((void**) &h->blk_meta, meta_bytes) != cudaSuccess) {
       cudaGetLastError();
       h->blk_meta_cap = 0;
       return h->fail(CCSDT_E_OOM, "block metadata");
@@ -162,7 +162,7 @@ extern "C" ccsdt_status ccsdt_upload_blocks(ccsdt_handle* h, int kind, long n, c
     if(h->blk_stage_cap < data_len) {
       if(h->blk_stage) cudaFree(h->blk_stage);
       h->blk_stage = nullptr;
-      if(cudaMalloc((void**) &h->blk_stage, (size_t) data_len * sizeof(double)) != cudaSuccess) {
+      if(ccsdt::dev_malloc((void**) &h->blk_stage, (size_t) data_len * sizeof(double)) != cudaSuccess) {
         cudaGetLastError();
         h->blk_stage_cap = 0;
         return h->fail(CCSDT_E_OOM, "block staging buffer of " + std::to_string(data_len * 8) + " bytes");

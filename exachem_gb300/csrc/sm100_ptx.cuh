@@ -39,8 +39,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 // true on success, false when the poll limit ran out
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for(uint32_t it = 0; it < kSpinLimit; it++) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit = kSpinLimit) {
+  for(uint32_t it = 0; it < limit; it++) {
     if(mbar_try_wait(bar, parity)) return true;
     if(it > 64) __nanosleep(32);
   }
@@ -54,17 +54,6 @@ __device__ __forceinline__ void tma_load_5d(void* dst, const CUtensorMap* map, u
     "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], "
     "[%7];" ::"r"(smem_u32(dst)),
     "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar))
-    : "memory");
-}
-// The same load delivered to the same shared-memory offset in every CTA of `cta_mask` (this
-// GPU's own memory, within the cluster); each destination's mbarrier at `bar`'s offset receives
-// the byte count.
-__device__ __forceinline__ void tma_load_5d_mc(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1,
-                                               int c2, int c3, int c4, uint16_t cta_mask) {
-  asm volatile(
-    "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster [%0], [%1, {%2, "
-    "%3, %4, %5, %6}], [%7], %8;" ::"r"(smem_u32(dst)),
-    "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(smem_u32(bar)), "h"(cta_mask)
     : "memory");
 }
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
@@ -110,49 +99,12 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
                : "memory");
 }
 
-// the same, arriving on the mbarrier at `bar`'s offset in every CTA of `cta_mask`
-__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t cta_mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-                 smem_u32(bar)),
-               "h"(cta_mask)
-               : "memory");
-}
-
 __device__ __forceinline__ void mma_commit_if(uint64_t* bar, uint32_t issue) {
   asm volatile("{\n\t.reg .pred e;\n\tsetp.ne.b32 e, %1, 0;\n\t"
                "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n\t}" ::"r"(smem_u32(bar)),
                "r"(issue)
                : "memory");
 }
-__device__ __forceinline__ void mma_commit_mc_if(uint64_t* bar, uint16_t cta_mask, uint32_t issue) {
-  asm volatile("{\n\t.reg .pred e;\n\tsetp.ne.b32 e, %2, 0;\n\t"
-               "@e tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;\n\t}" ::"r"(
-                 smem_u32(bar)),
-               "h"(cta_mask), "r"(issue)
-               : "memory");
-}
-
-// ------------------------------------------------------------------------------ cluster
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ uint32_t cluster_id_x() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ uint32_t cluster_count_x() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
-  return r;
-}
-// every thread of every CTA of the cluster (release / acquire of shared-memory state)
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 // 32 lanes x 16 consecutive 32-bit columns: thread t of the warp gets lane (quarter*32 + t)
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(

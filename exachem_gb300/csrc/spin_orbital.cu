@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "../../include/ccsdt.h"
+#include "ccsdt_internal.cuh"
 #include "fp64_kernels.cuh"
 
 using namespace ccsdt;
@@ -291,7 +292,7 @@ struct SoArena {
   cudaEvent_t        ev[2 + kSoStreams]  = {};
   double*            alloc(size_t n, cudaError_t& e) {
     void* p = nullptr;
-    if(e == cudaSuccess && n) e = cudaMalloc(&p, n * sizeof(double));
+    if(e == cudaSuccess && n) e = ccsdt::dev_malloc(&p, n * sizeof(double));
     if(p) ptrs.push_back(p);
     return static_cast<double*>(p);
   }
@@ -366,6 +367,12 @@ extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb
     d_eo = h[0], d_ev = h[1], d_t1 = h[2], d_t2 = h[3], d_ijab = h[4];
   } else {
     if(e != cudaSuccess) return e == cudaErrorMemoryAllocation ? CCSDT_E_OOM : CCSDT_E_CUDA;
+    // the call's own streams are non-blocking, so nothing orders them after the caller's work that
+    // produced the inputs (on any stream, the legacy default one included): wait for all of it
+    if(cudaDeviceSynchronize() != cudaSuccess) {
+      cudaGetLastError();
+      return CCSDT_E_CUDA;
+    }
     cudaEventRecord(M.ev[0], st);
   }
   // contraction-index-contiguous copies (tt[j][k][a][e], vv[i][b][c][e], uu[j][k][a][m])

@@ -248,7 +248,7 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
   slices_ready = 0;
   tmaps_ready  = false;
   auto grab = [&](void** p, size_t bytes) -> ccsdt_status {
-    cudaError_t e = cudaMalloc(p, bytes ? bytes : 1);
+    cudaError_t e = ccsdt::dev_malloc(p, bytes ? bytes : 1);
     if(e != cudaSuccess) {
       cudaGetLastError();
       return fail(CCSDT_E_OOM, "slice planes: cudaMalloc of " + std::to_string(bytes) + " bytes failed");
@@ -306,7 +306,7 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
     e_ntiles = (int) (host.size() / 3);
     if((s = grab((void**) &e_tiles, host.size() * sizeof(int)))) return s;
     if(!e_part) {
-      cudaError_t ce = cudaMalloc((void**) &e_part, 6 * sizeof(double) * kTiledBlocks);
+      cudaError_t ce = ccsdt::dev_malloc((void**) &e_part, 6 * sizeof(double) * kTiledBlocks);
       if(ce != cudaSuccess) {
         e_part = nullptr;
         cudaGetLastError();
@@ -319,7 +319,7 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
     if(ce != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(ce));
   }
   if(!d_err) { // persistent: survives re-slicing
-    cudaError_t ce = cudaMalloc((void**) &d_err, sizeof(int));
+    cudaError_t ce = ccsdt::dev_malloc((void**) &d_err, sizeof(int));
     if(ce != cudaSuccess) {
       d_err = nullptr;
       cudaGetLastError();
@@ -340,9 +340,7 @@ enum {
   MAP_OVVV_NAT = 0, MAP_OVVV_SWP = 1, MAP_T2 = 2, MAP_T2H_NAT = 3, MAP_T2H_SWP = 4, MAP_OOOVH = 5,
   // the persistent kernel's l-sum runs with the single index on the tile rows: ooovh as the
   // 128-row A operand, t2h pair rows as the NT-row B operand
-  MAP_T2H_NAT_B = 6, MAP_T2H_SWP_B = 7, MAP_OOOVH_A = 8,
-  // A maps with a one-plane box: the cluster kernel multicasts A plane by plane
-  MAP_OVVV_NAT_P1 = 9, MAP_OVVV_SWP_P1 = 10, MAP_OOOVH_A_P1 = 11
+  MAP_T2H_NAT_B = 6, MAP_T2H_SWP_B = 7, MAP_OOOVH_A = 8
 };
 
 // tcgen05 configurations: digit planes S -> columns per level NT (S NT <= 256, (S + 2) NT <= 512)
@@ -437,9 +435,6 @@ ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT, int KC) {
   ok &= encode_map(&tmaps[MAP_T2H_NAT_B], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, NT, (int) S_, KC);
   ok &= encode_map(&tmaps[MAP_T2H_SWP_B], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, NT, (int) S_, KC);
   ok &= encode_map(&tmaps[MAP_OOOVH_A], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, (int) S_, KC);
-  ok &= encode_map(&tmaps[MAP_OVVV_NAT_P1], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, 1, KC);
-  ok &= encode_map(&tmaps[MAP_OVVV_SWP_P1], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, 1, KC);
-  ok &= encode_map(&tmaps[MAP_OOOVH_A_P1], sl_ooovh, (int) Ko, v, o, o, P, Ko, v * Ko, o * v * Ko, pl_ooovh, TC_BM, 1, KC);
   if(!ok) return fail(CCSDT_E_CUDA, "cuTensorMapEncodeTiled failed for the digit planes");
   tmaps_ready = true;
   tmaps_S     = S;
@@ -586,7 +581,6 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
   last_batched     = false;
   last_err_bound   = 0.0; // only the LEARNED mode estimates its error
-  force_single_cta = opts->test_single_cta == 1; // test knob: the single-CTA persistent kernel
   if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
   const int S       = opts->slices;
   const int variant = opts->slice_kind;

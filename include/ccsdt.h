@@ -78,10 +78,9 @@ typedef struct {
                           /* triplets (batched calls): the acceptance allowance is scaled by    */
                           /* sqrt(budget_triplets / triplets of the call); 0 = the whole call   */
   int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05 */
-  int    test_single_cta; /* testing: 1 = single-CTA persistent kernel, not the 2-CTA cluster  */
   int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
                              slice count they use, once per handle, before the timed work      */
-  int    reserved[2];
+  int    reserved[3];
 } ccsdt_opts;
 
 typedef struct {
@@ -200,6 +199,19 @@ ccsdt_status ccsdt_profile_triplet(ccsdt_handle* h, const ccsdt_opts* opts, int 
 ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts* opts, int i, int j, int k,
                                    double* w_host);
 
+/* Testing the failure paths (no counterpart in the reference, whose errors end the process:
+ * the exit(100) macros of ccsd_t_common.hpp:26-41).
+ *   ccsdt_debug_fail_alloc: the nth device allocation the library makes from now on (any handle,
+ *     any call) fails as an out-of-memory cudaMalloc would; 0 switches this off.  *attempts
+ *     (nullable) receives the number of allocations attempted since the previous call.  The
+ *     calls that meet the failure return CCSDT_E_OOM and leave their handle destroyable.
+ *   ccsdt_debug_set_wait_test: the split-precision persistent kernel's bounded waits give up after
+ *     spin_limit polls (0: the default limit), and with skip_loads != 0 it announces each stage's
+ *     bytes but issues no TMA load, so its stage waits run out: the call returns CCSDT_E_TIMEOUT,
+ *     the kernel having released its tensor memory, and the handle stays usable. */
+ccsdt_status ccsdt_debug_fail_alloc(long nth, long* attempts);
+ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin_limit, int skip_loads);
+
 /* Number of kernel launches issued by the last ccsdt_energy / ccsdt_triplet_energies. */
 long ccsdt_last_launch_count(const ccsdt_handle* h);
 
@@ -215,19 +227,20 @@ ccsdt_status ccsdt_reference_op_count_so(int n_occ_a, const int* occ_a, int n_oc
                                          int is_restricted, double* ops, long* tasks);
 
 /* Allocation-free FP64 (T) for small problems.  No counterpart in the reference: it is
- * for callers that cannot call cudaMalloc - a host runtime whose device memory is owned
- * by a pooled allocator (ExaChem's TAMM reserves the device through its RMM pool), code
- * running inside a CUDA stream capture, or a service held to a fixed device budget.
- * All pointers are device pointers on the current device: the inputs in the layouts
- * above and `energies`, which receives {E[T], E(T)}.  Work is queued on `stream` (a
+ * for callers that cannot call cudaMalloc - a host runtime whose device memory is owned by
+ * a pooled allocator (ExaChem's TAMM reserves the device through its RMM pool, so a
+ * cudaMalloc beside it fails or fragments the pool), or a service held to a fixed device
+ * budget.  All pointers are device pointers on the current device: the inputs in the
+ * layouts above and `energies`, which receives {E[T], E(T)}.  Work is queued on `stream` (a
  * cudaStream_t, NULL = legacy default stream) and is complete when that stream is.
  * Every intermediate lives in one fixed device array of about 6.0 MB defined in the
  * library, which each GPU that loads the library keeps until the process exits; sizes
  * beyond o = 12 or v = 48 are rejected with CCSDT_E_INVALID.  The first call on a device
- * looks up that array's device address (make that first call before any stream capture).
- * All calls share the array: calls that overlap on the GPU race and give wrong results,
- * so order them on one stream or synchronise between them.  It calls no cudaMalloc,
- * cudaFree or allocating library routine. */
+ * looks up that array's device address (make that first call before any stream capture)
+ * and keeps it for the rest of the process: do not use this entry point across a
+ * cudaDeviceReset.  All calls share the array: calls that overlap on the GPU race and give
+ * wrong results, so order them on one stream or synchronise between them.  It calls no
+ * cudaMalloc, cudaFree or allocating library routine. */
 ccsdt_status ccsdt_energy_noalloc(int o, int v, const double* eps_occ, const double* eps_vir,
                                   const double* t1, const double* t2, const double* oovv,
                                   const double* ooov, const double* ovvv, double* energies,
@@ -247,8 +260,10 @@ ccsdt_status ccsdt_energy_noalloc(int o, int v, const double* eps_occ, const dou
  *   v2iabc[O][V][V][V]          <ia||bc>
  * Elements of spin-forbidden blocks are never read (they may hold anything).  FP64 DMMA
  * contractions over the spin-allowed blocks only; energies[0] = E[T], energies[1] = E(T)
- * (host memory).  on_device = 1: the arrays are device pointers on the current device;
- * 0: host pointers, copied in by the call.  shard_index / shard_count: the call takes the
+ * (host memory).  on_device = 1: the arrays are device pointers on the current device; the
+ * call first waits for all work already submitted to that device (cudaDeviceSynchronize), so
+ * inputs still being written by the caller's kernels or copies on any stream are complete
+ * before they are read; 0: host pointers, copied in by the call.  shard_index / shard_count: the call takes the
  * occupied triplets i < j < k with t % shard_count == shard_index (t counts them in
  * lexicographic order) and returns that part of the energies (shard_count 0 or 1: all).
  * seconds (may be NULL) receives the device time of the call, copies included.

@@ -43,6 +43,8 @@ def port():
         _port.oracle_triplets_slabs.argtypes = [ctypes.c_int, ctypes.c_int] + [_D] * 6 + \
             [ctypes.POINTER(ctypes.c_void_p), ctypes.c_long, _I, _D, _D]
         _port.oracle_num_threads.restype = ctypes.c_int
+        _port.oracle_w_rows_sample.argtypes = [ctypes.c_int, ctypes.c_int] + [_D] * 6 + \
+            [ctypes.POINTER(ctypes.c_void_p)] + [ctypes.c_int] * 5
         _port.so_oracle_energy.argtypes = [ctypes.c_int] * 4 + [_D] * 7 + [ctypes.c_long, _I, _D, _D]
     return _port
 
@@ -150,6 +152,23 @@ def triplets_slabs(d, tri) -> tuple[np.ndarray, np.ndarray]:
     if rc:
         raise RuntimeError(f"oracle_triplets_slabs failed ({rc})")
     return e4, e5
+
+
+def w_rows_sample(d, tri, a0, a1) -> None:
+    """Timing sample: the contraction multiply-adds of triplet ``tri`` for first-virtual rows
+    [a0, a1) (``d`` as for ``triplets_slabs``); the result is discarded."""
+    o, v = int(d["o"]), int(d["v"])
+    a = [np.ascontiguousarray(d[k], dtype=np.float64) for k in KEYS[:6]]
+    slabs = (ctypes.c_void_p * o)()
+    keep = []
+    for i, s in d["ovvv_slabs"].items():
+        s = np.ascontiguousarray(s, dtype=np.float64)
+        keep.append(s)
+        slabs[i] = s.ctypes.data
+    i, j, k = (int(x) for x in tri)
+    rc = port().oracle_w_rows_sample(o, v, *[x.ctypes.data_as(_D) for x in a], slabs, i, j, k, int(a0), int(a1))
+    if rc:
+        raise RuntimeError(f"oracle_w_rows_sample failed ({rc})")
 
 
 def reference_energy(d, occ_tiles, vir_tiles) -> dict:

@@ -62,7 +62,7 @@ static inline void cs_add(csum_t* a, double x) {
 /* W[a][b][c] += sum_d t_xy^{alpha d} (z gamma|beta d) - sum_l t_xl^{alpha beta} (yl|z gamma)
  * for one of the six pair orderings; (alpha, beta, gamma) are the virtual indices that
  * pair with (x, y, z).  pos[] maps (alpha, beta, gamma) to the W slots (a, b, c). */
-static void add_perm(const sys_t* S, double* W, int x, int y, int z, const int pos[3]) {
+static void add_perm_rows(const sys_t* S, double* W, int x, int y, int z, const int pos[3], int a0, int a1) {
   const int     o = S->o, v = S->v;
   const size_t  v2 = (size_t) v * v;
   const double* T   = S->t2 + ((size_t) x * o + y) * v2; /* T[alpha][d] */
@@ -70,7 +70,7 @@ static void add_perm(const sys_t* S, double* W, int x, int y, int z, const int p
   const size_t  st[3] = {v2, (size_t) v, 1};
   const size_t  sa = st[pos[0]], sb = st[pos[1]], sc = st[pos[2]];
 #pragma omp parallel for schedule(static)
-  for(int al = 0; al < v; al++) {
+  for(int al = a0; al < a1; al++) {
     double* hol = (double*) malloc(sizeof(double) * (size_t) o * v); /* hol[l][gamma] = (yl|z gamma) */
     for(int l = 0; l < o; l++)
       for(int ga = 0; ga < v; ga++)
@@ -94,6 +94,9 @@ static void add_perm(const sys_t* S, double* W, int x, int y, int z, const int p
     }
     free(hol);
   }
+}
+static void add_perm(const sys_t* S, double* W, int x, int y, int z, const int pos[3]) {
+  add_perm_rows(S, W, x, y, z, pos, 0, S->v);
 }
 
 /* W for one ordered triplet (i, j, k): sum of the six pair orderings */
@@ -243,4 +246,23 @@ int oracle_num_threads(void) {
 #else
   return 1;
 #endif
+}
+
+/* Timing sample for the CPU baseline: the six pair orderings of triplet (i, j, k) restricted to
+ * the first-virtual rows alpha in [a0, a1), i.e. (a1 - a0) / v of the triplet's contraction
+ * multiply-adds (which are all but O(v^3) of its work), into a scratch W that is then discarded.
+ * slab as in oracle_triplets_slabs.  Returns 0 or an error code. */
+int oracle_w_rows_sample(int o, int v, const double* eo, const double* ev, const double* t1,
+                         const double* t2, const double* oovv, const double* ooov,
+                         const double* const* slab, int i, int j, int k, int a0, int a1) {
+  if(o <= 0 || v <= 0 || a0 < 0 || a1 > v || a0 > a1) return 1;
+  if(!(0 <= i && i <= j && j <= k && k < o) || !slab[i] || !slab[j] || !slab[k]) return 3;
+  sys_t   S = {o, v, eo, ev, t1, t2, oovv, ooov, slab};
+  double* W = (double*) calloc((size_t) v * v * v, sizeof(double));
+  if(!W) return 2;
+  const int p[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  const int x[6] = {i, i, j, j, k, k}, y[6] = {j, k, i, k, i, j}, z[6] = {k, j, k, i, j, i};
+  for(int q = 0; q < 6; q++) add_perm_rows(&S, W, x[q], y[q], z[q], p[q], a0, a1);
+  free(W);
+  return 0;
 }

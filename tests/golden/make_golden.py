@@ -13,6 +13,7 @@ and tile size of those runs, which pin the task enumeration and equation enablin
 from __future__ import annotations
 
 import json
+import os
 import sys
 import time
 from pathlib import Path
@@ -45,7 +46,10 @@ CI_OPS = [
 ]
 
 
-def main(reference: str = "/root/reference"):
+def main(reference: str | None = None):
+    reference = reference or os.environ.get("CCSDT_REFERENCE")
+    if not reference:
+        sys.exit("give the reference tree as the first argument or in CCSDT_REFERENCE")
     out = {"generator": "exachem_gb300.generator.generate", "cases": [], "ci_ops": []}
     for name, o, v, seed, ot, vt, sc in CASES:
         d = generate(o, v, seed, t2_scale=sc)

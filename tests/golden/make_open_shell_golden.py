@@ -13,6 +13,7 @@ unrestricted task enumeration and spin filters.
 from __future__ import annotations
 
 import json
+import os
 import sys
 import time
 from pathlib import Path
@@ -42,7 +43,10 @@ CI_OPS = [
 ]
 
 
-def main(reference: str = "/root/reference"):
+def main(reference: str | None = None):
+    reference = reference or os.environ.get("CCSDT_REFERENCE")
+    if not reference:
+        sys.exit("give the reference tree as the first argument or in CCSDT_REFERENCE")
     out = {"generator": "oracle.spin_orbital_oracle.open_shell_system(exact=True)", "cases": [], "ci_ops": []}
     for f, line, oa, ob, va, vb, ts, want in CI_OPS:
         text = (Path(reference) / f).read_text().splitlines()

@@ -91,19 +91,6 @@ def test_persistent_batches_cover_every_triplet(built):
     np.testing.assert_allclose(e5, r5, rtol=1e-12, atol=1e-12 * np.abs(r5).max())
 
 
-@pytest.mark.parametrize("o,v,seed", [(6, 40, 0), (5, 130, 2), (9, 70, 5), (4, 200, 7)])
-def test_cluster_kernel_equals_single_cta(built, o, v, seed):
-    """The two-CTA cluster kernel (A planes multicast to both CTAs of a cluster) computes every
-    tile with the same operations as the single-CTA kernel: energies are bit-identical.  The
-    shapes give odd and even numbers of N blocks (an odd count leaves the second CTA of the last
-    pair without columns)."""
-    ft = _ft(o, v, seed)
-    for S in (1, 2, 3, 4, 5):
-        a = ft.energy("ozaki", slices=S)
-        b = ft.energy("ozaki", slices=S, single_cta=1)
-        assert a["e_paren_T"] == b["e_paren_T"] and a["e_bracket_T"] == b["e_bracket_T"], (S, a, b)
-
-
 @pytest.mark.parametrize("o,v,seed", [(3, 9, 31), (2, 17, 32), (4, 65, 33), (1, 30, 34), (5, 129, 35)])
 def test_split_edge_shapes(built, o, v, seed):
     """Shapes at the edges of the tiling: v below one 8-wide energy block, below one N tile and
@@ -121,3 +108,34 @@ def test_split_edge_shapes(built, o, v, seed):
                 assert r[key] == 0.0
             else:
                 assert abs(r[key] - ref[key]) <= tol * abs(ref[key]), (S, key, r[key], ref[key])
+
+
+@pytest.mark.parametrize("o,v,seed,tri", [(4, 320, 41, [(0, 1, 3), (1, 1, 2)]), (3, 512, 42, [(0, 1, 2), (0, 2, 2)])])
+def test_split_large_v_against_oracle(built, o, v, seed, tri):
+    """Virtual extents of the headline range, up to the 512-wide contraction window the exact
+    level sums rely on (K = v for the d-sum terms): the persistent tcgen05 path at S = 3 and 4
+    and the FP64 path against the oracle's C restatement on the same triplets.  Inputs are built
+    on the GPU (bit-identical to the host generator); the oracle reads host copies of the slabs
+    the triplets need."""
+    import torch
+    import oracle
+    from exachem_gb300.ccsd_t import FusedTriples
+    from exachem_gb300.generator import generate_device
+    dev = generate_device(o, v, seed, device="cuda")
+    tri = np.array(tri, dtype=np.int32)
+    need = sorted(set(int(x) for x in tri.ravel()))
+    host = {k: dev[k].cpu().numpy() for k in ("eps_occ", "eps_vir", "t1", "t2", "oovv", "ooov")}
+    host.update(o=o, v=v, ovvv_slabs={i: dev["ovvv"][i].cpu().numpy() for i in need})
+    w4, w5 = oracle.triplets_slabs(host, tri)
+    ft = FusedTriples(o, v, ts=40)
+    ft.upload_dict(dev)
+    del dev
+    torch.cuda.empty_cache()
+    f4, f5 = ft.triplet_energies(tri, "fp64")
+    np.testing.assert_allclose(f5, w5, rtol=1e-11)
+    np.testing.assert_allclose(f4, w4, rtol=1e-11)
+    for S, tol in ((3, 1e-6), (4, 1e-8)):
+        s4, s5 = ft.triplet_energies(tri, "ozaki", slices=S)
+        np.testing.assert_allclose(s5, w5, rtol=tol)
+        np.testing.assert_allclose(s4, w4, rtol=tol)
+    ft.close()

@@ -1,10 +1,10 @@
 """The allocation-free entry point (ccsdt_energy_noalloc) against the handle-based one.
 
-It serves callers that cannot call cudaMalloc (a device owned by a pooled allocator, work
-inside a stream capture, a fixed memory budget): all its intermediates live in one fixed
-device array inside the library.  The test calls it through the C ABI twice in a row and
-compares with ccsdt_energy at the FP64 parity tolerance used by the other GPU tests.
-This file is collected last on purpose.
+It serves callers that cannot call cudaMalloc (a device owned by a pooled allocator, a fixed
+device-memory budget): all its intermediates live in one fixed device array inside the library.
+The test calls it through the C ABI twice in a row and compares with ccsdt_energy and with the
+oracle at the FP64 parity tolerance used by the other GPU tests.  This file is collected last on
+purpose.
 """
 import ctypes
 
@@ -28,10 +28,12 @@ def _noalloc(lib, d, out, stream):
 @pytest.mark.parametrize("o,v,seed", [(6, 20, 4), (12, 48, 5)])
 def test_noalloc_matches_handle_api_twice(built, o, v, seed):
     import torch
+    import oracle
     from exachem_gb300 import ccsd_t as ct
     from exachem_gb300.generator import generate
 
     d = generate(o, v, seed)
+    o4, o5 = oracle.energy(d)
     ref = ct.FusedTriples(o, v, ts=40)
     ref.upload_dict(d)
     want = ref.energy("fp64")
@@ -47,6 +49,7 @@ def test_noalloc_matches_handle_api_twice(built, o, v, seed):
         e4, e5 = out.tolist()
         assert abs(e4 - want["e_bracket_T"]) <= RTOL * abs(want["e_bracket_T"])
         assert abs(e5 - want["e_paren_T"]) <= RTOL * abs(want["e_paren_T"])
+        assert abs(e4 - o4) <= RTOL * abs(o4) and abs(e5 - o5) <= RTOL * abs(o5)
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(built):
