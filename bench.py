@@ -340,6 +340,67 @@ def run_open_shell(args):
     return 0
 
 
+def run_slice_sweep(args):
+    """Split precision swept over the slice count for BF16 digits (persistent tcgen05 kernel, FP32
+    level sums) and INT8 digits (mma.sync IMMA, INT32 level sums), on an evenly spread sample of
+    triplets: per (kind, S) the device time per triplet, the projected whole call, the speedup over
+    the FP64 path on the same sample and |dE(T)| of the sample against it."""
+    import torch
+    from exachem_gb300 import ccsd_t as ct
+    from exachem_gb300.generator import generate_device
+    torch.cuda.set_device(0)
+    o, v, seed = args.o, args.v, args.seed
+    wl = workload_config(o, v, seed)
+    dev = generate_device(o, v, seed, device="cuda")
+    ft = ct.FusedTriples(o, v, wl["occ_tiles"], wl["vir_tiles"], device=0)
+    ft.upload_dict(dev)
+    del dev
+    torch.cuda.empty_cache()
+    stream = torch.cuda.current_stream()
+    ft.set_stream(stream.cuda_stream)
+    tri_all = triplet_list(o)
+    samp = spread_sample(tri_all, args.sample, offset=len(tri_all) // (2 * args.sample))
+
+    def timed(mode, **kw):
+        ft.triplet_energies(samp[:2], mode, **kw)          # warm: slicing, tensor maps, tables
+        best, out = None, None
+        for _ in range(max(1, args.steps)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            out = ft.triplet_energies(samp, mode, **kw)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1) * 1e-3
+            best = t if best is None else min(best, t)
+        return best, out
+
+    t64, (f4, f5) = timed("fp64")
+    rows = []
+    for kind in args.sweep_kinds.split(","):
+        for S in [int(x) for x in args.sweep.split(",")]:
+            if kind == "bf16" and not args.no_autotune:
+                ft.autotune(S)
+            t, (s4, s5) = timed("ozaki", slices=S, slice_kind=kind)
+            rel = np.abs(s5 - f5) / np.abs(f5)
+            rows.append({"kind": kind, "slices": S, "s_per_triplet": t / len(samp),
+                         "whole_call_s": t / len(samp) * len(tri_all), "speedup_vs_fp64": t64 / t,
+                         "rel_error_of_sum": float(abs(s5.sum() - f5.sum()) / abs(f5.sum())),
+                         "max_rel_triplet": float(rel.max()),
+                         "kernel": "persistent tcgen05 (BF16 digits)" if kind == "bf16" else "mma.sync IMMA (INT8 digits)"})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    line = {"metric": f"(T) split-precision slice sweep at o={o},v={v}: |dE(T)| and speedup vs FP64 per slice count",
+            "unit": "s", "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "dtype": "f64 / bf16 / int8",
+            "data": "synthetic (seeded generator, built on GPU)",
+            "config": wl | {"sample_triplets": int(len(samp)), "triplets_total": int(len(tri_all)),
+                            "timing": "best of the timed repetitions, CUDA events around one call on the sample"},
+            "fp64": {"s_per_triplet": t64 / len(samp), "whole_call_s": t64 / len(samp) * len(tri_all),
+                     "sum_E(T)_sample": float(f5.sum())},
+            "sweep": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -360,6 +421,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1, help="triplets timed on the CPU baseline (0: skip)")
     ap.add_argument("--ref-row-parts", type=int, default=4,
                     help="--impl reference: each step times 1/q of one triplet's contraction rows")
+    ap.add_argument("--limit-triplets", type=int, default=0,
+                    help="profiling aid: run only this many evenly spread triplets of the call (projected)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--budget", type=float, default=1e-8,
                     help="learned mode: 3 sqrt(sum sigma_t^2) <= budget x sum |E(T)_t|")
@@ -368,6 +431,9 @@ def main():
                     help="keep the default tile configurations (no ccsdt_autotune before the timed region)")
     ap.add_argument("--open-shell", type=lambda x: tuple(int(y) for y in x.split(",")), default=None,
                     metavar="OA,OB,VA,VB", help="time the open-shell (UHF) path on this spin-orbital system instead")
+    ap.add_argument("--sweep", default=None, metavar="S1,S2,...",
+                    help="slice-count sweep on a triplet sample instead of the whole call (e.g. 4,5,6,7,8)")
+    ap.add_argument("--sweep-kinds", default="bf16,int8", help="digit kinds of the sweep")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -375,6 +441,8 @@ def main():
         return run_reference(args)
     if args.open_shell:
         return run_open_shell(args)
+    if args.sweep:
+        return run_slice_sweep(args)
 
     import torch
     from exachem_gb300 import ccsd_t as ct
@@ -404,6 +472,9 @@ def main():
 
     tri_all = triplet_list(o)
     mine = tri_all[rank::world]                       # independent triplets, no data-path collective
+    n_share = len(mine)
+    if args.limit_triplets > 0:                          # profiling runs: a spread subset, projected
+        mine = spread_sample(mine, min(len(mine), args.limit_triplets))
     cpu_samp = spread_sample(tri_all, max(1, args.cpu_sample), offset=len(tri_all) // 2)
     host_slabs = host_slabs_from_device(dev, cpu_samp) if (rank == 0 and args.cpu_sample > 0) else None
     keys = ["eps_occ", "eps_vir", "t1", "t2", "oovv", "ooov", "ovvv"]
@@ -497,7 +568,7 @@ def main():
         t = torch.tensor([elapsed, e2e_wall], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         elapsed, e2e_wall = (float(x) for x in t.tolist())
-    frac = timed_trip / len(mine)
+    frac = timed_trip / n_share
     value = elapsed / frac                               # == elapsed in split mode (frac 1)
     pt = None
     if split:
@@ -570,7 +641,16 @@ def main():
                              "rel_error_of_sum": float(abs(s5.sum() - f5.sum()) / abs(f5.sum())),
                              "abs_error_of_sum_Eh": float(abs(s5.sum() - f5.sum())),
                              "rel_error_of_sum_E[T]": float(abs(s4.sum() - f4.sum()) / abs(f4.sum()))}
+        # the learned mode's a-posteriori estimate sigma_t of each triplet's truncation error, against
+        # the measured error: how often the 3-sigma band misses (a statistical estimate, not a bound)
+        sigma = {}
+        for s_ in (2, 3):
+            _, e5s, est = ft.triplet_error_estimates(samp, s_)
+            err = np.abs(e5s[nz] - f5[nz])
+            sigma[f"S={s_}"] = {"miss_rate_3sigma": float(np.mean(err > 3 * est[nz])),
+                                "median_sigma_over_error": float(np.median(est[nz] / np.maximum(err, 1e-300)))}
         energy_sample = {"triplets": int(len(samp)), "spread": "evenly over the lexicographic list",
+                         "error_estimate": sigma,
                          "fp64_sum_E(T)_Eh": float(f5.sum()), "fp64_seconds": fp64_s, "vs_fp64": entries,
                          "tolerance": "|dE|/|E(T)| <= 1e-6 (the metric's 1e-6 Eh for any |E(T)| <= 1 Eh; the "
                                       "synthetic E(T) here is ~1e11 Eh, so absolute Eh bounds are below one ulp)"}

@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
 CU_SOURCES = ["ccsdt_capi.cu", "split.cu", "persist.cu", "noalloc.cu", "mlp.cu", "learned.cu", "retile.cu",
-              "cholesky.cu", "pz_launch_a.cu", "pz_launch_b.cu", "spin_orbital.cu"]
+              "cholesky.cu", "pz_launch_a.cu", "pz_launch_b.cu", "pz_launch_c.cu", "spin_orbital.cu"]
 CPP_SOURCES = ["refcount.cpp"]
 
 

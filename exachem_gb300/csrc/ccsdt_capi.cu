@@ -342,6 +342,14 @@ ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
     launches++;
   }
   if(profiling) cudaEventRecord(prof_ev[2], stream);
+  if(fp64_ff_energy) { // testing: the same P arrays through the split path's float-float energy
+    if(!F12 || !F34 || !F56) return fail(CCSDT_E_STATE, "float-float energy buffers missing");
+    to_ff_kernel<<<2048, 256, 0, stream>>>(P12, F12, v3);
+    to_ff_kernel<<<2048, 256, 0, stream>>>(P34, F34, v3);
+    to_ff_kernel<<<2048, 256, 0, stream>>>(P56, F56, v3);
+    launches += 3;
+    return launch_energy_tiled(i, j, k, eout);
+  }
   EnergyArgs ea{P12, P34, P56, oovv, t1, eo, ev, (int) o, (int) v, i, j, k, part};
   energy_fp64_kernel<<<kEnergyBlocks, E_THREADS, 0, stream>>>(ea);
   if(profiling) cudaEventRecord(prof_ev[3], stream);

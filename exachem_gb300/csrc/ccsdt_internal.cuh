@@ -87,7 +87,8 @@ struct ccsdt_handle {
   ccsdt_status run_triplet_split(int i, int j, int k, int S, int variant, double* eout);
   ccsdt_status ensure_tmaps(int S, int NT, int KC);
   ccsdt_status run_triplet_tc(int i, int j, int k, int S, double* eout);
-  bool         tc_eligible(int S, int variant) const;
+  bool         tc_eligible(int S, int variant) const; // per-triplet tcgen05 kernel
+  bool         pz_eligible(int S, int variant) const; // persistent tcgen05 kernel
   double*      part_buf() { return part; }
   ccsdt_status launch_energy_tiled(int i, int j, int k, double* eout);
   ccsdt_status run_triplet_S(int i, int j, int k, int S, double* eout);
@@ -114,10 +115,11 @@ struct ccsdt_handle {
   int       batch_slots = 4;         // triplets per batch
   unsigned  test_spin_limit = 0;     // testing: bounded-wait poll limit of the persistent kernel (0: default)
   int       test_skip_loads = 0;     // testing: the persistent kernel issues no TMA loads
+  int       test_window_k = 0;       // testing: shorter exact K windows than the slice count allows
   // persistent-contraction configuration per S (index into kPzConfs, -1 = the default), set by
   // the autotuner or ccsdt_set_tile_config; tuned[S]: the autotuner has run for S
-  int          pz_conf_idx[6] = {-1, -1, -1, -1, -1, -1};
-  bool         pz_tuned[6]    = {false, false, false, false, false, false};
+  int          pz_conf_idx[9] = {-1, -1, -1, -1, -1, -1, -1, -1, -1};
+  bool         pz_tuned[9]    = {false, false, false, false, false, false, false, false, false};
   int          pz_conf_index(int S) const;
   ccsdt_status autotune(int S, double* ms, int* n, int* chosen);
   long      graph_replays = 0;
@@ -131,6 +133,7 @@ struct ccsdt_handle {
   double             learned_cost_products = 0.0; // digit-plane products run, incl. escalations
   ccsdt_status check_device_error();
   bool         force_mma_sync = false; // use the mma.sync slice kernel even where tcgen05 applies
+  bool         fp64_ff_energy = false; // testing: FP64 contractions, then the float-float energy
   // live per-phase timing of the batched path: 3 events per batch, read after the call
   bool                     phase_timing = false, capturing = false;
   std::vector<cudaEvent_t> tev;

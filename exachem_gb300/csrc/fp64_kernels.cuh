@@ -234,6 +234,14 @@ static __global__ void __launch_bounds__(E_THREADS) reduce_parts_kernel(const do
   }
 }
 
+// x -> float-float (hi = x rounded to FP32, lo = the remainder rounded), element by element.
+static __global__ void to_ff_kernel(const double* x, float2* y, long long n) {
+  for(long long e = (long long) blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long) gridDim.x * blockDim.x) {
+    const float hi = (float) x[e];
+    y[e]           = make_float2(hi, (float) (x[e] - (double) hi));
+  }
+}
+
 // Compensated fixed-order sum of per-triplet energies e[2 n] -> out[2].
 static __global__ void reduce_triplets_kernel(const double* e, long long n, double* out) {
   if(threadIdx.x != 0 || blockIdx.x != 0) return;

@@ -212,8 +212,8 @@ extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccs
   if(!opts || opts->mode != CCSDT_MODE_OZAKI || n < 0 || (n && (!tri || !e_paren || !est)))
     return h->fail(CCSDT_E_INVALID, "ccsdt_triplet_error_estimates: needs CCSDT_MODE_OZAKI and output arrays");
   if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_triplet_error_estimates before ccsdt_upload");
-  if(!h->tc_eligible(opts->slices, opts->slice_kind))
-    return h->fail(CCSDT_E_INVALID, "error estimates need the tcgen05 path (BF16 digits, 1..5 planes)");
+  if(!h->pz_eligible(opts->slices, opts->slice_kind))
+    return h->fail(CCSDT_E_INVALID, "error estimates need the tcgen05 path (BF16 digits, 1..8 planes)");
   for(long t = 0; t < n; t++) {
     const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
     if(!(0 <= i && i <= j && j <= k && k < h->o)) return h->fail(CCSDT_E_INVALID, "triplet outside 0 <= i <= j <= k < o");
@@ -284,7 +284,7 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
      cudaStreamSynchronize(stream) != cudaSuccess)
     return fail(CCSDT_E_CUDA, "learned-mode slice readback");
   // run the triplets at their predicted counts, one persistent batched pass per count (the
-  // tcgen05 path, S <= 5); results, tails and sensitivities land at each triplet's own index
+  // persistent tcgen05 path); results, tails and sensitivities land at each triplet's own index
   force_mma_sync = false;
   const bool graph = opts->use_graph != 0;
   double     ssum  = 0;
@@ -295,7 +295,7 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
       for(int c = 0; c < 3; c++) sub[3 * q + c] = tri[3 * ids[q] + c];
       out[q] = (int) ids[q];
     }
-    if(tc_eligible(cnt, 0))
+    if(pz_eligible(cnt, 0))
       return run_batched(cnt, (long) ids.size(), sub.data(), graph, with_est ? dtail : nullptr,
                          with_est ? dsens : nullptr, out.data());
     for(size_t q = 0; q < ids.size(); q++) { // counts above the tcgen05 range: per-triplet slices
@@ -319,7 +319,7 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
   // collects it) run at the full count directly
   for(long t = 0; t < n; t++) {
     S[t] = std::min(std::max(S[t], 2), Sfull);
-    if(!tc_eligible(S[t], 0)) S[t] = Sfull;
+    if(!pz_eligible(S[t], 0)) S[t] = Sfull;
   }
   for(int cnt = 2; cnt <= Sfull; cnt++) {
     std::vector<long> ids;
@@ -350,7 +350,7 @@ ccsdt_status ccsdt_handle::run_learned(const ccsdt_opts* opts, long n, const int
        cudaStreamSynchronize(stream) != cudaSuccess)
       return fail(CCSDT_E_CUDA, "learned-mode readback");
     for(long t = 0; t < n; t++)
-      est[t] = (tri[3 * t] == tri[3 * t + 2] || !tc_eligible(S[t], 0)) ? 0.0 : truncation_estimate(tail[t], sens[t]);
+      est[t] = (tri[3 * t] == tri[3 * t + 2] || !pz_eligible(S[t], 0)) ? 0.0 : truncation_estimate(tail[t], sens[t]);
     return CCSDT_OK;
   };
   if((s = readback())) return s;

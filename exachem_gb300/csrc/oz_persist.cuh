@@ -70,6 +70,8 @@ struct PzParams {
   int*            err;        // set on a bounded-wait timeout
   float*          tail;       // optional: tail[output index] += sum of squares of the last
                               // kept level's terms (a-posteriori truncation estimate)
+  int             wst;        // stages (K chunks) per exact K window: a term longer than this is
+                              // accumulated and folded window by window (pz_window_k)
   unsigned        spin;       // polls before a bounded mbarrier wait gives up (sm100::kSpinLimit)
   int             skip_loads; // testing: announce each stage's bytes but issue no TMA load, so
                               // the stage waits run out (the timeout path, CCSDT_E_TIMEOUT)
@@ -78,6 +80,23 @@ struct PzParams {
 struct PzTerm {
   int mapA, mapB, a2, a3, b2, b3, Kp; // maps and their tile coordinates along dims 2, 3
 };
+
+// Longest contraction window (a multiple of kc) whose digit-level sums stay exact in an FP32
+// accumulator for S digit planes.  Level l = p + q (2 <= l <= S + 1) sums sigma_p tau_q over the
+// pairs p + q = l and the window's k, with |sigma_1| <= 127 and |sigma_p| <= 64 (p > 1): per k at
+// most 127^2 (l = 2) or 2 127 64 + (l - 3) 64^2 (l >= 3), growing with l, so the bound of level
+// S + 1 times the window length must stay <= 2^24.  S = 1..8 -> 1040, 1032, 824, 686, 587, 514,
+// 456, 410 before rounding down to kc.  A term longer than its window is accumulated window by
+// window, each window folded into the float-float result on its own.
+__host__ __device__ constexpr int pz_window_k(int S, int kc) {
+  const long per_k = S + 1 == 2 ? 127L * 127 : 2L * 127 * 64 + (long) (S + 1 - 3) * 64 * 64;
+  return (int) (((1L << 24) / per_k) / kc * kc);
+}
+static_assert(pz_window_k(3, 64) == 768 && pz_window_k(5, 32) == 576 && pz_window_k(6, 32) == 512 &&
+                pz_window_k(7, 32) == 448 && pz_window_k(8, 32) == 384, "exact windows");
+// passes of a term of nst stages with wst stages per window, and the stages of its pass w
+__device__ __forceinline__ int pz_npass(int nst, int wst) { return nst <= wst ? 1 : (nst + wst - 1) / wst; }
+__device__ __forceinline__ int pz_pass_st(int nst, int wst, int w) { return nst <= wst ? nst : min(wst, nst - w * wst); }
 
 // The four terms of a job's tile, from (job, t, i, j, k) and the item's x.  The tile holds
 // P[n][x][y] for 128 rows y and NT columns n (P12[a][c][b]: n = a, x = c, y = b; P34[b][a][c];
@@ -149,7 +168,7 @@ __device__ __forceinline__ PzItem pz_decode(unsigned id, int v, int yblocks, int
 // (lvl_empty); finally it renormalises, scales by 2^(-7 (S + 1)) and stores the tile once.  The
 // BF16 digits carry the row scales, so the levels need no per-row or per-column factor.  Returns
 // false when a bounded wait gave up.
-template<int S, int NT, int NBUF>
+template<int S, int NT, int NBUF, int KC>
 __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem& w, int nb, const int* tp,
                                                  uint32_t lane_base, int c_lo, int row, int lane, int& term_it,
                                                  float& tsq, uint64_t* lvl_full, uint64_t* lvl_empty,
@@ -164,8 +183,11 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
   // element (y, n) of the tile: P[n][x][y] (consecutive rows -> consecutive addresses)
   float2* Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
   float hi[COLS], lo[COLS];
+  const int np_d = pz_npass(P.kp_v / KC, P.wst), np_l = pz_npass(P.kp_o / KC, P.wst);
 #pragma unroll 1
-  for(int t = 0; t < PZ_TERMS; t++, term_it++) {
+  for(int tw = 0; tw < 2 * (np_d + np_l); tw++, term_it++) {
+    // pass tw: term t (two d-sum terms of np_d windows, then two l-sum terms of np_l windows)
+    const int  t   = tw < 2 * np_d ? tw / np_d : 2 + (tw - 2 * np_d) / np_l;
     const int  buf = term_it % NBUF;
     const bool okw = __all_sync(0xffffffffu, sm100::mbar_wait(&lvl_full[buf], (term_it / NBUF) & 1, P.spin) && !*abort_flag);
     if(!okw) return false;
@@ -244,8 +266,8 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
         }
       }
     };
-    if(t == 0) run(false, true); // d-sum terms add, l-sum terms subtract
-    else if(t == 1) run(false, false);
+    if(tw == 0) run(false, true); // d-sum terms add, l-sum terms subtract
+    else if(t < 2) run(false, false);
     else run(true, false);
   }
   if(y < v) {
@@ -405,18 +427,21 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
     int            s = 0, term_it = 0;
     bool           stop = false;
     while(!stop) {
-      for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
-        const int      nst   = (t < 2 ? P.kp_v : P.kp_o) / KC;
-        const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
-        for(int u = 0; u < nst; u++) {
-          if((stop = pz_gate_sync(false))) break;
-          sm100::tc_fence_after();
-          pz_issue_stage<S, NT, KC>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
-          sm100::mma_commit_if(&empty[s], lane == 0);
-          a += C::STAGE_BYTES;
-          if(++s == STAGES) s = 0, a = a0;
+      for(int t = 0; t < PZ_TERMS && !stop; t++) {
+        const int nst = (t < 2 ? P.kp_v : P.kp_o) / KC, np = pz_npass(nst, P.wst);
+        for(int w = 0; w < np && !stop; w++, term_it++) { // one TMEM level buffer per window
+          const int      ns    = pz_pass_st(nst, P.wst, w);
+          const uint32_t dbase = tmem + (term_it % C::NBUF) * S * NT;
+          for(int u = 0; u < ns; u++) {
+            if((stop = pz_gate_sync(false))) break;
+            sm100::tc_fence_after();
+            pz_issue_stage<S, NT, KC>(dbase, a, a + C::A_BYTES, u == 0, lane == 0);
+            sm100::mma_commit_if(&empty[s], lane == 0);
+            a += C::STAGE_BYTES;
+            if(++s == STAGES) s = 0, a = a0;
+          }
+          if(!stop) sm100::mma_commit_if(&lvl_full[term_it % C::NBUF], lane == 0);
         }
-        if(!stop) sm100::mma_commit_if(&lvl_full[term_it % C::NBUF], lane == 0);
       }
     }
     if(lane == 0) {
@@ -443,19 +468,22 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         pz_gate_sync(true);
         break;
       }
-      for(int t = 0; t < PZ_TERMS && !stop; t++, term_it++) {
-        const int nst = (t < 2 ? P.kp_v : P.kp_o) / KC;
-        const int buf = term_it % C::NBUF;
-        if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1, P.spin);
-        for(int u = 0; u < nst; u++, stage_it++) {
-          bool mine = false;
-          if(lane == 0) {
-            if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1, P.spin);
-            if(!ok) fail();
-            mine = !ok || *abort_flag;
+      for(int t = 0; t < PZ_TERMS && !stop; t++) {
+        const int nst = (t < 2 ? P.kp_v : P.kp_o) / KC, np = pz_npass(nst, P.wst);
+        for(int w = 0; w < np && !stop; w++, term_it++) {
+          const int ns  = pz_pass_st(nst, P.wst, w);
+          const int buf = term_it % C::NBUF;
+          if(lane == 0 && term_it >= C::NBUF) ok = sm100::mbar_wait(&lvl_empty[buf], ((term_it / C::NBUF) - 1) & 1, P.spin);
+          for(int u = 0; u < ns; u++, stage_it++) {
+            bool mine = false;
+            if(lane == 0) {
+              if(ok) ok = sm100::mbar_wait(&full[stage_it % STAGES], (stage_it / STAGES) & 1, P.spin);
+              if(!ok) fail();
+              mine = !ok || *abort_flag;
+            }
+            __syncwarp();
+            if((stop = pz_gate_sync(mine))) break;
           }
-          __syncwarp();
-          if((stop = pz_gate_sync(mine))) break;
         }
       }
     }
@@ -487,7 +515,7 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         tsq       = 0.f;
         tail_slot = tp[3];
       }
-      if(!pz_epilogue_item<S, NT, C::NBUF>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
+      if(!pz_epilogue_item<S, NT, C::NBUF, KC>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
                                   abort_flag)) {
         fail();
         break;

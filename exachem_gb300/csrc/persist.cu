@@ -51,15 +51,18 @@ long items_per_slot(int v, int NT) {
 namespace ccsdt {
 cudaError_t pz_launch_single_a(int conf, const PzParams& p, int grid, cudaStream_t st);
 cudaError_t pz_launch_single_b(int conf, const PzParams& p, int grid, cudaStream_t st);
+cudaError_t pz_launch_single_c(int conf, const PzParams& p, int grid, cudaStream_t st);
 
 cudaError_t pz_launch_single(int conf, const PzParams& p, int grid, cudaStream_t st) {
-  return conf < kPzSplit ? pz_launch_single_a(conf, p, grid, st) : pz_launch_single_b(conf, p, grid, st);
+  return conf < kPzSplit ? pz_launch_single_a(conf, p, grid, st)
+         : conf < kPzSplit2 ? pz_launch_single_b(conf, p, grid, st)
+                            : pz_launch_single_c(conf, p, grid, st);
 }
 } // namespace ccsdt
 
 // The configuration in use for S digit planes: the one the autotuner kept, else the default.
 int ccsdt_handle::pz_conf_index(int S) const {
-  if(S < 1 || S > 5) return -1;
+  if(S < 1 || S > OZ_MAX_SLICES) return -1;
   return pz_conf_idx[S] >= 0 ? pz_conf_idx[S] : pz_default_conf(S);
 }
 
@@ -138,6 +141,8 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
+  p.wst        = pz_window_k(S, kPzConfs[conf].KC) / kPzConfs[conf].KC;
+  if(test_window_k > 0) p.wst = std::max(1, std::min(p.wst, test_window_k / kPzConfs[conf].KC));
   p.spin       = test_spin_limit ? test_spin_limit : sm100::kSpinLimit;
   p.skip_loads = test_skip_loads;
   const int  NT  = kPzConfs[conf].NT;
@@ -309,7 +314,7 @@ ccsdt_status ccsdt_handle::collect_phase_times() {
 // contraction launch, CUDA events on the handle's stream, second of two runs) and keeps the
 // fastest for the handle's later calls.  Every configuration gives bit-identical energies.
 ccsdt_status ccsdt_handle::autotune(int S, double* ms, int* n, int* chosen) {
-  if(S < 1 || S > 5) return fail(CCSDT_E_INVALID, "autotune: slices must be 1 to 5");
+  if(S < 1 || S > OZ_MAX_SLICES) return fail(CCSDT_E_INVALID, "autotune: slices must be 1 to 8");
   if(!uploaded) return fail(CCSDT_E_STATE, "autotune before a successful upload");
   std::vector<int> cands;
   for(int c = 0; c < kPzNConfs; c++)
@@ -383,7 +388,8 @@ extern "C" ccsdt_status ccsdt_autotune(ccsdt_handle* h, int slices, double* ms, 
 
 extern "C" ccsdt_status ccsdt_set_tile_config(ccsdt_handle* h, int slices, int index) {
   if(!h) return CCSDT_E_INVALID;
-  if(slices < 1 || slices > 5) return h->fail(CCSDT_E_INVALID, "ccsdt_set_tile_config: slices must be 1 to 5");
+  if(slices < 1 || slices > OZ_MAX_SLICES)
+    return h->fail(CCSDT_E_INVALID, "ccsdt_set_tile_config: slices must be 1 to 8");
   int m = 0;
   for(int c = 0; c < kPzNConfs; c++)
     if(kPzConfs[c].S == slices) {
@@ -401,5 +407,11 @@ extern "C" ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin
   if(!h) return CCSDT_E_INVALID;
   h->test_spin_limit = spin_limit;
   h->test_skip_loads = skip_loads ? 1 : 0;
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_debug_set_window(ccsdt_handle* h, int k) {
+  if(!h || k < 0) return CCSDT_E_INVALID;
+  h->test_window_k = k;
   return CCSDT_OK;
 }

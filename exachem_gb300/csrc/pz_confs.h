@@ -23,13 +23,16 @@ struct PzConf {
 // o=60 v=500 on GB300).
 constexpr PzConf kPzConfs[] = {
   {1, 64, 4, 64}, {1, 32, 6, 64},                 // 0, 1
-  {2, 96, 4, 64}, {2, 64, 4, 64}, {2, 32, 5, 64}, // 2, 3, 4
-  {3, 64, 3, 64}, {3, 32, 3, 64}, {3, 48, 3, 64}, // 5, 6, 7
-  {4, 64, 4, 32}, {4, 32, 5, 32}, {4, 64, 2, 64}, {4, 48, 5, 32}, // 8, 9, 10, 11
-  {5, 48, 4, 32}, {5, 32, 4, 32}, {5, 32, 2, 64},                 // 12, 13, 14
+  {2, 96, 4, 64}, {2, 64, 4, 64}, {2, 32, 5, 64}, {2, 128, 3, 64}, // 2, 3, 4, 5
+  {3, 64, 3, 64}, {3, 32, 3, 64}, {3, 48, 3, 64},                  // 6, 7, 8
+  {4, 64, 4, 32}, {4, 32, 5, 32}, {4, 64, 2, 64}, {4, 48, 5, 32},  // 9, 10, 11, 12
+  {5, 48, 4, 32}, {5, 32, 4, 32}, {5, 32, 2, 64},                  // 13, 14, 15
+  {6, 32, 3, 32}, {7, 32, 3, 32}, {8, 32, 2, 32},                  // 16, 17, 18
 };
 constexpr int kPzNConfs = sizeof(kPzConfs) / sizeof(kPzConfs[0]);
-constexpr int kPzSplit  = 8; // configurations [0, 8) live in pz_launch_a.cu, the rest in pz_launch_b.cu
+// configurations [0, kPzSplit) live in pz_launch_a.cu, [kPzSplit, kPzSplit2) in pz_launch_b.cu,
+// the rest in pz_launch_c.cu (three translation units that compile in parallel)
+constexpr int kPzSplit = 9, kPzSplit2 = 16;
 
 constexpr int pz_default_conf(int S) {
   for(int c = 0; c < kPzNConfs; c++)
@@ -40,7 +43,7 @@ constexpr int pz_smem_bytes(const PzConf& c) {
   return c.ST * (c.S * 128 * c.KC * 2 + c.S * c.NT * c.KC * 2) + 1024 + 512;
 }
 constexpr bool pz_conf_ok(const PzConf& c) {
-  return c.S >= 1 && c.S <= 5 && c.S * c.NT <= 256 && 2 * c.S * c.NT <= 512 && c.NT % 16 == 0 &&
+  return c.S >= 1 && c.S <= 8 && c.S * c.NT <= 256 && 2 * c.S * c.NT <= 512 && c.NT % 16 == 0 &&
          (c.KC == 64 || c.KC == 32) && c.ST >= 2 && pz_smem_bytes(c) <= 227 * 1024;
 }
 constexpr bool pz_all_ok() {

@@ -4,9 +4,9 @@
 
 namespace ccsdt {
 
-static_assert(kPzSplit == 8 && kPzConfs[7].S == 3 && kPzConfs[8].S == 4, "the split of the configurations");
+static_assert(kPzSplit == 9 && kPzConfs[8].S == 3 && kPzConfs[9].S == 4, "the split of the configurations");
 
-#define PZ_CASES(X) X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7)
+#define PZ_CASES(X) X(0) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8)
 
 cudaError_t pz_launch_single_a(int conf, const PzParams& p, int grid, cudaStream_t st) {
 #define X(c) \

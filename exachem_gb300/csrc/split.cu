@@ -474,6 +474,10 @@ static ccsdt_status launch_tc_any(ccsdt_handle* h, TcBatch& b, int S) {
 bool ccsdt_handle::tc_eligible(int S, int variant) const {
   return variant == 0 && S >= 1 && S <= 5 && kp_v <= 512 && kp_o <= 512 && !force_mma_sync;
 }
+// the persistent tcgen05 path: BF16 digits, 1..8 planes, any contraction length (exact K windows)
+bool ccsdt_handle::pz_eligible(int S, int variant) const {
+  return variant == 0 && S >= 1 && S <= OZ_MAX_SLICES && !force_mma_sync;
+}
 
 ccsdt_status ccsdt_handle::run_triplet_tc(int i, int j, int k, int S, double* eout) {
   ccsdt_status s;
@@ -596,7 +600,20 @@ ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* 
   force_mma_sync        = kernel_kind == 1;
   cudaError_t e0 = cudaMemsetAsync(d_err, 0, sizeof(int), stream);
   if(e0 != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e0));
-  last_batched = kernel_kind == 0 && tc_eligible(S, variant);
+  if(kernel_kind == 3) { // testing: FP64 contractions with the float-float energy (its own error)
+    if((s = ensure_scratch())) return s;
+    fp64_ff_energy = true;
+    for(long t = 0; t < n && !s; t++) {
+      const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
+      if(i == k) {
+        if(cudaMemsetAsync(etrip + 2 * t, 0, 2 * sizeof(double), stream) != cudaSuccess) s = fail(CCSDT_E_CUDA, "memset");
+      } else
+        s = run_triplet_fp64(i, j, k, etrip + 2 * t);
+    }
+    fp64_ff_energy = false;
+    return s;
+  }
+  last_batched = kernel_kind == 0 && pz_eligible(S, variant);
   if(last_batched) return run_batched(S, n, tri, opts->use_graph != 0, nullptr, nullptr);
   for(long t = 0; t < n; t++) {
     const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];

@@ -1,11 +1,11 @@
 """Training data, training and use of the per-triplet slice-count model.
 
-Labels: for an occupied triplet, the smallest digit-plane count S in 2..smax whose triplet
-energy E_t(S) satisfies |E_t(S) - E_t(FP64)| <= budget * mean_t |E_t(FP64)| * sqrt(N) / 3,
-measured against the library's own FP64 path (the plain kernel is the yardstick); N is the
-system's number of occupied triplets and the mean is over its sampled triplets.  That is the
-equal share of the LEARNED mode's acceptance test 3 sqrt(sum_t sigma_t^2) <= budget sum_t |E_t|
-(independent per-triplet errors add like a random walk).  Features come from the library
+Labels: for the sampled triplets of a system, the digit-plane counts S in 2..smax that a greedy
+allocation gives under the LEARNED mode's own acceptance test 3 sqrt(sum_t sigma_t^2) <= budget
+sum_t |E_t| (sigma_t: the library's a-posteriori error estimate of triplet t at its count; the
+sample stands for the system's N triplets): all start at 2 and the triplet with the largest
+sigma_t moves up one count until the test passes (label_triplets).  The measured errors against
+the library's own FP64 path are kept beside the labels.  Features come from the library
 (ccsdt_triplet_features, 12 per triplet).  Training runs on the GPU through ccsdt_mlp_train
 (hand-written FP32 forward / backward / Adam kernels).
 
@@ -100,28 +100,44 @@ def learned_stats(ft: "ct.FusedTriples", with_products=False):
     return (m.value, f.value, p.value) if with_products else (m.value, f.value)
 
 
-def share(ft, ref, budget):
-    """Equal per-triplet share of the acceptance test: budget * mean|E_t| * sqrt(N) / 3."""
-    n_all = ft.o * (ft.o + 1) * (ft.o + 2) // 6
-    return budget * max(float(np.mean(np.abs(ref))), 1e-300) * np.sqrt(n_all) / 3.0
-
-
 def label_triplets(ft, tri, budget=1e-8, smax=7):
-    """Minimal S in 2..smax with |E_t(S) - E_t(fp64)| <= the equal share (smax if none).
-    Returns the labels, the errors [S-2][t] in units of that share, and the FP64 energies."""
+    """Slice-count labels of the sampled triplets `tri` of the handle's system: the counts a greedy
+    allocation gives under the LEARNED mode's own acceptance test.  With sigma_t(S) the library's
+    a-posteriori estimate of triplet t's error at S planes (ccsdt_triplet_error_estimates, what the
+    acceptance reads), the sample stands for the system's N triplets, and the test
+    3 sqrt(sum_t sigma_t^2) <= budget sum_t |E_t| over N triplets reads, per sample of n,
+        3 sqrt(sum_sample sigma_t^2) <= budget sqrt(N / n) sum_sample |E_t(FP64)|.
+    Every triplet starts at 2 planes; while the test fails, the triplet with the largest sigma_t
+    moves one count up (it buys the largest variance cut per extra product, as sigma falls by
+    ~2^-7 per plane), up to smax.  An equal per-triplet share of the allowance would leave most of
+    it unused (triplets at a higher count use a tiny part of theirs) and put nearly every triplet
+    one count higher than it needs.
+    Returns the labels, the measured errors |E_t(S) - E_t(FP64)| / |E_t(FP64)| [S - 2][t] and the
+    FP64 energies (the plain kernel is the yardstick)."""
     _, ref = ft.triplet_energies(tri, "fp64")
-    allow = share(ft, ref, budget)
-    errs = []
+    n_all = ft.o * (ft.o + 1) * (ft.o + 2) // 6
+    allow = budget * np.sqrt(n_all / max(1, len(ref))) * np.abs(ref).sum() / 3.0
+    sig, errs = [], []
     for S in range(2, smax + 1):
-        _, e = ft.triplet_energies(tri, "ozaki", slices=S)
-        errs.append(np.abs(e - ref) / allow)
-    errs = np.array(errs)                                   # [S-2][t]
-    ok = errs <= 1.0
-    lab = np.where(ok.any(0), ok.argmax(0) + 2, smax)
+        _, e, est = ft.triplet_error_estimates(tri, S)
+        sig.append(est)
+        errs.append(np.abs(e - ref) / np.maximum(np.abs(ref), 1e-300))
+    sig, errs = np.array(sig), np.array(errs)               # [S-2][t]
+    lab = np.full(len(ref), 2)
+    cur = sig[0].copy()
+    while np.sqrt(np.sum(cur ** 2)) > allow:
+        t = int(np.argmax(np.where(lab < smax, cur, -1.0)))
+        if lab[t] >= smax or cur[t] <= 0:
+            break
+        lab[t] += 1
+        cur[t] = sig[lab[t] - 2][t]
     return lab, errs, ref
 
 
-def training_systems(n=20, seed0=100, o_range=(10, 30), v_range=(60, 200), scale_range=(0.5, 3.0)):
+def training_systems(n=20, seed0=100, o_range=(20, 60), v_range=(150, 500), scale_range=(0.5, 3.0)):
+    """The training systems: seeds seed0.. with o, v and the T2 scale drawn uniformly from the
+    ranges (by default the ones the slice-count model is specified for: o in [20, 60], v in
+    [150, 500], T2 x [0.5, 3], seeds 100-119)."""
     rng = np.random.default_rng(12345)
     out = []
     for s in range(seed0, seed0 + n):
@@ -133,12 +149,17 @@ def training_systems(n=20, seed0=100, o_range=(10, 30), v_range=(60, 200), scale
 
 
 def build_training_set(systems, per_system=24, budget=1e-8, smax=7, log=print):
-    from .generator import generate
+    """Features and labels of per_system sampled triplets of each system (inputs built on the GPU,
+    bit-identical to the host generator)."""
+    import torch
+    from .generator import generate_device
     X, Y, meta = [], [], []
     for (o, v, seed, sc) in systems:
-        d = generate(o, v, seed, t2_scale=sc)
+        d = generate_device(o, v, seed, device="cuda", t2_scale=sc)
         ft = ct.FusedTriples(o, v, ts=40)
         ft.upload_dict(d)
+        del d
+        torch.cuda.empty_cache()
         allt = ct.all_triplets(o)
         allt = allt[allt[:, 0] != allt[:, 2]]
         rng = np.random.default_rng(seed)
@@ -161,17 +182,23 @@ def load_model(path=MODEL_PATH):
     return np.asarray(d["params"], np.float32), d.get("meta", {})
 
 
-def main():
-    """Train the shipped model on the GPU: python -m exachem_gb300.learned"""
+def main(argv=None):
+    """Train the shipped model on the GPU: python -m exachem_gb300.learned [--out PATH] [--per-system N]"""
+    import argparse
     import time
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=str(MODEL_PATH))
+    ap.add_argument("--per-system", type=int, default=24)
+    a = ap.parse_args(argv)
     t0 = time.time()
     systems = training_systems()
-    X, y, meta = build_training_set(systems)
+    X, y, meta = build_training_set(systems, per_system=a.per_system)
     params, loss = mlp_train(X, y, epochs=400, batch=64, lr=3e-3, seed=7)
     acc = float((mlp_predict(params, X) - 2 == y).mean())
     print(f"trained on {len(y)} triplets: loss {loss:.4f}, accuracy {acc:.3f}, {time.time() - t0:.0f} s")
     save_model(params, {"systems": meta, "budget": 1e-8, "loss": loss, "train_accuracy": acc,
-                        "label_histogram": np.bincount(y + 2, minlength=9).tolist()})
+                        "label_histogram": np.bincount(y + 2, minlength=9).tolist(),
+                        "per_system": a.per_system, "train_seconds": time.time() - t0}, a.out)
 
 
 if __name__ == "__main__":

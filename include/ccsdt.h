@@ -77,7 +77,8 @@ typedef struct {
   int    budget_triplets; /* LEARNED: the call is one part of a computation over this many    */
                           /* triplets (batched calls): the acceptance allowance is scaled by    */
                           /* sqrt(budget_triplets / triplets of the call); 0 = the whole call   */
-  int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05 */
+  int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05, */
+                          /* 3 FP64 contractions with the split path's float-float energy        */
   int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
                              slice count they use, once per handle, before the timed work      */
   int    reserved[3];
@@ -149,7 +150,7 @@ ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps_occ, const
                                    const double* t1, const double* t2, int n_chol, const double* chol_oo,
                                    const double* chol_ov, const double* chol_vv, int on_device);
 
-/* Tile configurations of the persistent split-precision contraction (tcgen05 path, slices 1-5):
+/* Tile configurations of the persistent split-precision contraction (tcgen05 path, slices 1-8):
  *   ccsdt_tile_configs     lists the compiled ones for `slices`: *n of them, {N tile, pipeline
  *                          stages, K chunk} each in nt_st_kc[3 n] (nullable); index 0 is the default;
  *   ccsdt_autotune         times each on one triplet of the handle's system (CUDA events around the
@@ -211,6 +212,12 @@ ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts* opts, int 
  *     the kernel having released its tensor memory, and the handle stays usable. */
 ccsdt_status ccsdt_debug_fail_alloc(long nth, long* attempts);
 ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin_limit, int skip_loads);
+
+/* Testing: the persistent split-precision kernel accumulates each contraction in windows of at most
+ * k (rounded down to its K chunk, at least one chunk) instead of the longest window whose digit-level
+ * sums stay exact for the slice count (0: that default).  Shorter windows are exact too; they
+ * exercise the window-by-window fold that long contractions (v beyond the exact window) need. */
+ccsdt_status ccsdt_debug_set_window(ccsdt_handle* h, int k);
 
 /* Number of kernel launches issued by the last ccsdt_energy / ccsdt_triplet_energies. */
 long ccsdt_last_launch_count(const ccsdt_handle* h);
@@ -316,7 +323,7 @@ ccsdt_status ccsdt_triplet_features(ccsdt_handle* h, long n, const int* tri, flo
  * opts->energy_budget the relative per-triplet budget of the a-posteriori check. */
 ccsdt_status ccsdt_set_slice_model(ccsdt_handle* h, const float* params);
 
-/* Per-triplet energies at opts->slices digit planes (CCSDT_MODE_OZAKI, BF16 digits, 1..5
+/* Per-triplet energies at opts->slices digit planes (CCSDT_MODE_OZAKI, BF16 digits, 1..8
  * planes) together with the a-posteriori estimate est[t] of |E(T)_t - E(T)_t,fp64| that the
  * LEARNED mode checks against its budget: the estimated standard deviation of the triplet's
  * truncation error, from the last kept level's terms and the energy's sensitivity (a statistical

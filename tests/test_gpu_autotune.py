@@ -9,13 +9,13 @@ OCC, VIR = [6, 5], [32, 24, 21]       # v = 77: the N tiles of 64 and 32 pad dif
 
 def test_tile_configs_fit_the_kernels(built):
     from exachem_gb300.ccsd_t import FusedTriples
-    for S in range(1, 6):
+    for S in range(1, 9):
         cfg = FusedTriples.tile_configs(S)
         assert cfg, S
         for nt, st, kc in cfg:
             smem = st * (S * 128 * kc * 2 + S * nt * kc * 2) + 1536
             assert S * nt <= 256 and 2 * S * nt <= 512 and nt % 16 == 0 and kc in (32, 64) and smem <= 227 * 1024
-    assert FusedTriples.tile_configs(6) == []
+    assert FusedTriples.tile_configs(9) == []
 
 
 @pytest.mark.gpu

@@ -70,6 +70,27 @@ def test_fp64_cfg1_shape_sampled_triplets(built):
     np.testing.assert_allclose(g5, o5, rtol=RTOL_TRIPLET, atol=RTOL_TRIPLET * np.abs(o5).max())
 
 
+def test_fp64_cfg1_whole_call_matches_golden(built):
+    """o=21, v=180, tiles of 40, seed 1 (the drop-in configuration): the whole call through
+    ccsdt_energy against the committed golden total (tests/golden/cfg1_energy.json, every triplet
+    of the oracle's C restatement, which matches ExaChem's own CPU (T) to 1e-14 on the fixtures of
+    reference_energies.json).  The configuration's 1e-9 Eh bound is below one ulp of E(T) here
+    (|E(T)| ~ 2e7 Eh), so the test holds FP64 to 1e-12 relative and split S = 5 to 1e-9."""
+    import json
+    from conftest import ROOT
+    from exachem_gb300.generator import generate
+    g = json.loads((ROOT / "tests" / "golden" / "cfg1_energy.json").read_text())
+    d = generate(g["o"], g["v"], g["seed"])
+    ft = _ft(d, g["occ_tiles"], g["vir_tiles"])
+    r = ft.energy("fp64")
+    assert rel_close(r["e_bracket_T"], g["e_bracket_T"], RTOL_FULL), (r, g["e_bracket_T"])
+    assert rel_close(r["e_paren_T"], g["e_paren_T"], RTOL_FULL), (r, g["e_paren_T"])
+    assert r["n_triplets"] == g["n_triplets"]
+    rs = ft.energy("ozaki", slices=5)
+    assert rel_close(rs["e_paren_T"], g["e_paren_T"], 1e-9), (rs, g["e_paren_T"])
+    ft.close()
+
+
 def test_fp64_deterministic_and_tiling_invariant(built):
     from exachem_gb300.generator import generate
     d = generate(7, 33, seed=9)
@@ -106,3 +127,18 @@ def test_nonfinite_inputs_rejected(built):
     with pytest.raises(CCSDTError) as e:
         ft.energy("fp64")
     assert e.value.status == 7
+
+
+def test_shards_sum_to_the_whole_call(built):
+    """The multi-GPU split (opts.shard_index / shard_count: every shard_count-th triplet, the
+    caller sums the partial energies, as ExaChem's ranks do with pg().reduce at ccsd_t.cpp:262-263)
+    run shard by shard on this GPU: the three parts add up to the whole call, FP64 and split."""
+    from exachem_gb300.generator import generate
+    d = generate(9, 48, seed=23)
+    ft = _ft(d)
+    for mode, kw in (("fp64", {}), ("ozaki", {"slices": 3})):
+        whole = ft.energy(mode, **kw)
+        parts = [ft.energy(mode, shard_index=s, shard_count=3, **kw) for s in range(3)]
+        assert sum(p["n_triplets"] for p in parts) == whole["n_triplets"]
+        for key in ("e_bracket_T", "e_paren_T"):
+            assert rel_close(sum(p[key] for p in parts), whole[key], 1e-13), (mode, key)

@@ -139,3 +139,76 @@ def test_split_large_v_against_oracle(built, o, v, seed, tri):
         np.testing.assert_allclose(s5, w5, rtol=tol)
         np.testing.assert_allclose(s4, w4, rtol=tol)
     ft.close()
+
+
+@pytest.mark.parametrize("o,v,seed", [(12, 70, 8), (4, 320, 9)])
+def test_float_float_energy_stage_error(built, o, v, seed):
+    """The split path's energy stage on its own: the FP64 contractions' P arrays, rounded to
+    float-float, through the tiled float-float energy (whose singles use FP32 copies of (ia|jb) and
+    t1), against the FP64 energy of the same arrays.  This isolates the error of the energy stage
+    (float-float W sums, 1/D and accumulation, FP32 singles) from the digit truncation."""
+    ft = _ft(o, v, seed)
+    ref = ft.energy("fp64")
+    got = ft.energy("ozaki", slices=1, legacy_mma=3)
+    for key in ("e_bracket_T", "e_paren_T"):
+        assert abs(got[key] - ref[key]) <= 2e-12 * abs(ref[key]), (key, got[key], ref[key])
+
+
+def _set_window(ft, k):
+    import ctypes
+    lib = ft.lib
+    lib.ccsdt_debug_set_window.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.ccsdt_debug_set_window.restype = ctypes.c_int
+    assert lib.ccsdt_debug_set_window(ft.h, k) == 0
+
+
+@pytest.mark.parametrize("o,v,seed", [(6, 40, 13), (5, 130, 14)])
+def test_six_to_eight_slices_on_tcgen05(built, o, v, seed):
+    """S = 6, 7, 8 run on the persistent tcgen05 kernel (32-column tiles, K chunks of 32) and agree
+    with the mma.sync slice kernel; the float-float fold is no longer exact above S = 4, so the
+    comparison is at 1e-12 relative, and both sit at the FP64 result to float-float precision."""
+    ft = _ft(o, v, seed)
+    ref = ft.energy("fp64")
+    for S in (6, 7, 8):
+        tc = ft.energy("ozaki", slices=S)
+        leg = ft.energy("ozaki", slices=S, legacy_mma=1)
+        assert tc["e_paren_T"] == pytest.approx(leg["e_paren_T"], rel=1e-12, abs=0), S
+        assert abs(tc["e_paren_T"] - ref["e_paren_T"]) <= 1e-11 * abs(ref["e_paren_T"]), (S, tc, ref)
+
+
+@pytest.mark.parametrize("o,v,seed", [(7, 96, 15), (5, 200, 16)])
+def test_contraction_windows(built, o, v, seed):
+    """Contractions accumulated window by window (here forced to windows of 64 and 32 along K, so
+    the d-sum terms take several and the l-sum terms one or two) give the single-window energies:
+    each window's level sums are exact, only the float-float folds of the partial sums differ."""
+    ft = _ft(o, v, seed)
+    for S in (3, 5):
+        one = ft.energy("ozaki", slices=S)
+        for k in (64, 32):
+            _set_window(ft, k)
+            win = ft.energy("ozaki", slices=S)
+            _set_window(ft, 0)
+            for key in ("e_bracket_T", "e_paren_T"):
+                assert win[key] == pytest.approx(one[key], rel=1e-12, abs=0), (S, k, key)
+
+
+def test_long_contraction_beyond_the_exact_window(built):
+    """v = 800: the d-sum contractions (K = 800) exceed the exact window of S = 3 (768) and of
+    S = 5 (576), so the persistent kernel folds two windows per term; one triplet against the FP64
+    path (v = 800 lies beyond the per-triplet tcgen05 kernel's 512)."""
+    import torch
+    from exachem_gb300.ccsd_t import FusedTriples
+    from exachem_gb300.generator import generate_device
+    o, v = 2, 800
+    dev = generate_device(o, v, 17, device="cuda")
+    ft = FusedTriples(o, v, ts=40)
+    ft.upload_dict(dev)
+    del dev
+    torch.cuda.empty_cache()
+    tri = np.array([(0, 0, 1), (0, 1, 1)], dtype=np.int32)
+    f4, f5 = ft.triplet_energies(tri, "fp64")
+    for S, tol in ((3, 1e-6), (5, 1e-9)):
+        s4, s5 = ft.triplet_energies(tri, "ozaki", slices=S)
+        np.testing.assert_allclose(s5, f5, rtol=tol)
+        np.testing.assert_allclose(s4, f4, rtol=tol)
+    ft.close()

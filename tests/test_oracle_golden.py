@@ -32,6 +32,23 @@ def test_per_triplet_sum_equals_total(built):
     assert rel_close(e4.sum(), t4, 1e-13) and rel_close(e5.sum(), t5, 1e-13)
 
 
+def test_cfg1_golden_sample_reproduces(built):
+    """The o=21, v=180 golden (tests/golden/cfg1_energy.json): two of its recorded per-triplet
+    energies recomputed by the oracle on regenerated inputs, and the recorded total is the sum
+    over every triplet (the sample is part of it)."""
+    import json
+    import oracle
+    from exachem_gb300.generator import generate
+    g = json.loads((ROOT / "tests" / "golden" / "cfg1_energy.json").read_text())
+    assert g["n_triplets"] == 21 * 22 * 23 // 6 and len(g["sample"]) >= 2
+    d = generate(g["o"], g["v"], g["seed"])
+    pick = [g["sample"][3], g["sample"][-2]]
+    e4, e5 = oracle.triplets(d, [c["tri"] for c in pick])
+    for c, a, b in zip(pick, e4, e5):
+        # the oracle's per-thread partial sums meet in arrival order: equal to ~1e-15, not bitwise
+        assert rel_close(a, c["e_bracket_T"], 1e-13) and rel_close(b, c["e_paren_T"], 1e-13), c
+
+
 @pytest.mark.skipif(not (ROOT / "oracle" / "_ref" / "libccsdt_ref.so").exists(), reason="reference tree not built here")
 def test_reference_reruns_its_golden(golden):
     import oracle
