@@ -92,8 +92,8 @@ __host__ __device__ constexpr int pz_window_k(int S, int kc) {
   const long per_k = S + 1 == 2 ? 127L * 127 : 2L * 127 * 64 + (long) (S + 1 - 3) * 64 * 64;
   return (int) (((1L << 24) / per_k) / kc * kc);
 }
-static_assert(pz_window_k(3, 64) == 768 && pz_window_k(5, 32) == 576 && pz_window_k(6, 32) == 512 &&
-                pz_window_k(7, 32) == 448 && pz_window_k(8, 32) == 384, "exact windows");
+static_assert(pz_window_k(3, 64) == 768 && pz_window_k(4, 64) == 640 && pz_window_k(5, 64) == 576 &&
+                pz_window_k(6, 64) == 512 && pz_window_k(7, 64) == 448 && pz_window_k(8, 64) == 384, "exact windows");
 // passes of a term of nst stages with wst stages per window, and the stages of its pass w
 __device__ __forceinline__ int pz_npass(int nst, int wst) { return nst <= wst ? 1 : (nst + wst - 1) / wst; }
 __device__ __forceinline__ int pz_pass_st(int nst, int wst, int w) { return nst <= wst ? nst : min(wst, nst - w * wst); }

@@ -141,7 +141,9 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
-  p.wst        = pz_window_k(S, kPzConfs[conf].KC) / kPzConfs[conf].KC;
+  // windows in multiples of 64 whatever the configuration's K chunk, so every configuration folds
+  // the same windows and the energies stay bit-identical across configurations
+  p.wst        = pz_window_k(S, 64) / kPzConfs[conf].KC;
   if(test_window_k > 0) p.wst = std::max(1, std::min(p.wst, test_window_k / kPzConfs[conf].KC));
   p.spin       = test_spin_limit ? test_spin_limit : sm100::kSpinLimit;
   p.skip_loads = test_skip_loads;
