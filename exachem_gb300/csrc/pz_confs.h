@@ -23,7 +23,7 @@ struct PzConf {
 // o=60 v=500 on GB300).
 constexpr PzConf kPzConfs[] = {
   {1, 64, 4, 64}, {1, 32, 6, 64},                 // 0, 1
-  {2, 96, 4, 64}, {2, 64, 4, 64}, {2, 32, 5, 64}, {2, 128, 3, 64}, // 2, 3, 4, 5
+  {2, 128, 3, 64}, {2, 96, 4, 64}, {2, 64, 4, 64}, {2, 32, 5, 64}, // 2, 3, 4, 5
   {3, 64, 3, 64}, {3, 32, 3, 64}, {3, 48, 3, 64},                  // 6, 7, 8
   {4, 64, 4, 32}, {4, 32, 5, 32}, {4, 64, 2, 64}, {4, 48, 5, 32},  // 9, 10, 11, 12
   {5, 48, 4, 32}, {5, 32, 4, 32}, {5, 32, 2, 64},                  // 13, 14, 15

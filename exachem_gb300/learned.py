@@ -189,16 +189,17 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=str(MODEL_PATH))
     ap.add_argument("--per-system", type=int, default=24)
+    ap.add_argument("--smax", type=int, default=6, help="largest label (digit-plane count) considered")
     a = ap.parse_args(argv)
     t0 = time.time()
     systems = training_systems()
-    X, y, meta = build_training_set(systems, per_system=a.per_system)
+    X, y, meta = build_training_set(systems, per_system=a.per_system, smax=a.smax)
     params, loss = mlp_train(X, y, epochs=400, batch=64, lr=3e-3, seed=7)
     acc = float((mlp_predict(params, X) - 2 == y).mean())
     print(f"trained on {len(y)} triplets: loss {loss:.4f}, accuracy {acc:.3f}, {time.time() - t0:.0f} s")
     save_model(params, {"systems": meta, "budget": 1e-8, "loss": loss, "train_accuracy": acc,
                         "label_histogram": np.bincount(y + 2, minlength=9).tolist(),
-                        "per_system": a.per_system, "train_seconds": time.time() - t0}, a.out)
+                        "per_system": a.per_system, "smax": a.smax, "train_seconds": time.time() - t0}, a.out)
 
 
 if __name__ == "__main__":

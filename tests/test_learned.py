@@ -51,11 +51,14 @@ def test_mlp_training_reduces_loss_and_bf16_inference(built):
 
 def test_learned_mode_meets_budget_and_saves_products(built):
     """LEARNED accepts when 3 sqrt(sum sigma_t^2) <= budget sum |E_t|: the measured error must
-    meet the budget, and the digit-plane products it runs (escalations included) must not exceed
-    those of the smallest fixed count that passes the same test."""
+    meet the budget, and the digit-plane products it runs (escalations included) must be strictly
+    fewer than those of the smallest fixed count that passes the same test.  The budget sits
+    between the fixed counts (2 planes miss it, 3 meet it with room to spare on these ~300-triplet
+    systems; the o=60 v=500 call is in the same regime at 1e-8), where a per-triplet choice can
+    gain: triplets with small energies stay at 2 planes."""
     from exachem_gb300 import ccsd_t as ct, learned
     from exachem_gb300.generator import generate
-    budget = 1e-8
+    budget = 1e-7
     systems = [(10, 60, 100, 1.0), (12, 70, 101, 2.0), (14, 64, 102, 0.7)]
     X, y, _ = learned.build_training_set(systems, per_system=30, budget=budget, smax=6, log=lambda *a: None)
     params, _ = learned.mlp_train(X, y, epochs=300, batch=32, lr=3e-3, seed=5)
