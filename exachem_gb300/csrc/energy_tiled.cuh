@@ -61,6 +61,86 @@ __device__ __forceinline__ int perm_slot(int p0, int p1, int p2) {
   return p0 * 2 + (p1 > p2 ? 1 : 0);
 }
 
+// One orbit {a, b, c} of a work item: the index triple (la, lb, lc) local to the sorted block
+// triple (a' in block 0, b' in block 1, c' in block 2) and all six of its orderings, which live in
+// the six slots of W.  The six W values are read once, D is common to the orbit, and an ordering
+// counts only if its slot is a distinct ordered block triple (so every ordered (a, b, c) counts
+// once).  Adds the orbit's E[T] and E(T) terms to s4 / s5 and, with want_sens, its first-order
+// sensitivity to sens.
+__device__ __forceinline__ void et_orbit(const float2 (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],
+                                         const float (*Oik)[3][ET_B * ET_B], const float (*Oij)[3][ET_B * ET_B],
+                                         const float (*ti)[ET_B], const float (*tj)[ET_B], const float (*tk)[ET_B],
+                                         const float2 (*evs)[ET_B], const float2* dab, bool all_on, const int* slot_on,
+                                         int la, int lb, int lc, int want_sens, ff& s4, ff& s5, float& sens) {
+  constexpr int B = ET_B;
+  const int loc[3] = {la, lb, lc};
+  ff        w[6];
+  float     sg[6];
+#pragma unroll
+  for(int q = 0; q < 6; q++) {
+    const int    p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
+    const int    x = loc[p0], y = loc[p1], z = loc[p2];
+    const float2 t = W[q][kSwz(la, lb, lc)]; // = W at (x, y, z) of slot q
+    w[q]           = ff{t.x, t.y};
+    // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z
+    sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
+  }
+  // The six orderings form two cyclic classes, {q, yzx(q), zxy(q)} and the three orderings
+  // one transposition away (xzy, yxz, zyx of q), which are the other class.  With the class
+  // sums C: Z_q = 4 W_q + W_yzx + W_zxy = 3 W_q + C_own, Y_q = 3 V_q - C_other(V).
+  const ff    ca  = ff_add(ff_add(w[0], w[3]), w[4]); // class of ordering 0: slots 0, 3, 4
+  const ff    cb  = ff_add(ff_add(w[1], w[2]), w[5]); // slots 1, 2, 5
+  const float sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
+  ff    zy4{0.f, 0.f}, zys{0.f, 0.f};
+  float sn = 0.f;
+  if(all_on) {
+    // All six orderings count: the orbit sums follow from the class sums.
+    //   sum_q Z_q Y4_q = 9 sum_q W_q^2 + 3 (C_a^2 + C_b^2) - 12 C_a C_b
+    //   sum_q Z_q ys_q = 3 sum_q W_q ys_q + 3 (C_a - C_b)(S_a - S_b)
+    // (class a: Z = 3 W + C_a, Y4 = 3 W - C_b, ys = 3 sg - S_b; class b with a and b swapped)
+    ffacc sqa, wya;
+#pragma unroll
+    for(int q = 0; q < 6; q++) {
+      const bool  in_a = q == 0 || q == 3 || q == 4;
+      const float ys   = 3.f * sg[q] - (in_a ? sgb : sga);
+      sqa.add_sq(w[q]);
+      wya.add_mul_f(w[q], ys);
+      if(want_sens) { // the estimate needs Z and Y only to float precision
+        const float z = 3.f * w[q].hi + (in_a ? ca.hi : cb.hi), y5 = 3.f * w[q].hi - (in_a ? cb.hi : ca.hi) + ys;
+        sn = fmaf(18.f * y5, y5, fmaf(12.f * z, z, sn));
+      }
+    }
+    const ff sq = sqa.get(), wy = wya.get();
+    zy4 = ff_add(ff_add(ff_mul_f(sq, 9.f), ff_mul_f(ff_add(ff_mul(ca, ca), ff_mul(cb, cb)), 3.f)),
+                 ff_neg(ff_mul_f(ff_mul(ca, cb), 12.f)));
+    zys = ff_add(ff_mul_f(wy, 3.f), ff_mul_f(ff_add(ca, ff_neg(cb)), 3.f * (sga - sgb)));
+  } else
+#pragma unroll
+  for(int q = 0; q < 6; q++) {
+    if(!slot_on[q]) continue;
+    const bool  in_a = q == 0 || q == 3 || q == 4;
+    const ff    t3 = ff_mul_f(w[q], 3.f);
+    const ff    z  = ff_add(t3, in_a ? ca : cb);
+    const ff    y4 = ff_add(t3, ff_neg(in_a ? cb : ca));
+    const float ys = 3.f * sg[q] - (in_a ? sgb : sga);   // singles part of Y
+    zy4 = ff_add(zy4, ff_mul(z, y4));
+    zys = ff_add(zys, ff_mul_f(z, ys));
+    // first-order sensitivity to errors in W: W_abc enters Z_abc (x4), Z_bca, Z_cab and,
+    // through V, Y_abc (x3), Y_acb, Y_bac, Y_cba; with uncorrelated signs
+    //   |dE/dW|^2 ~ (16 + 1 + 1) Y^2 / D^2 + (9 + 1 + 1 + 1) Z^2 / D^2
+    if(want_sens) {
+      const float y5 = y4.hi + ys;
+      sn = fmaf(18.f * y5, y5, fmaf(12.f * z.hi, z.hi, sn));
+    }
+  }
+  const ff zy5 = ff_add(zy4, zys);
+  const float2 dd = dab[la * B + lb], ec = evs[2][lc];
+  const ff     id = ff_div_fast(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
+  s4   = ff_add(s4, ff_mul(zy4, id));
+  s5   = ff_add(s5, ff_mul(zy5, id));
+  sens = fmaf(sn * id.hi, id.hi, sens);
+}
+
 __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, const float2* P12, const float2* P34,
                                                   const float2* P56, int i, int j, int k, double* part, int gblock,
                                                   int gsize) {
@@ -205,72 +285,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     for(int r = tid; r < B3; r += ET_THREADS) {
       const int la = r / (B * B), lb = (r / B) % B, lc = r % B;
       if(la >= rbn[0] || lb >= rbn[1] || lc >= rbn[2]) continue;
-      const int loc[3] = {la, lb, lc};
-      ff        w[6];
-      float     sg[6];
-#pragma unroll
-      for(int q = 0; q < 6; q++) {
-        const int    p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
-        const int    x = loc[p0], y = loc[p1], z = loc[p2];
-        const float2 t = W[q][kSwz(la, lb, lc)]; // = W at (x, y, z) of slot q
-        w[q]           = ff{t.x, t.y};
-        // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z
-        sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
-      }
-      // The six orderings form two cyclic classes, {q, yzx(q), zxy(q)} and the three orderings
-      // one transposition away (xzy, yxz, zyx of q), which are the other class.  With the class
-      // sums C: Z_q = 4 W_q + W_yzx + W_zxy = 3 W_q + C_own, Y_q = 3 V_q - C_other(V).
-      const ff    ca  = ff_add(ff_add(w[0], w[3]), w[4]); // class of ordering 0: slots 0, 3, 4
-      const ff    cb  = ff_add(ff_add(w[1], w[2]), w[5]); // slots 1, 2, 5
-      const float sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
-      ff    zy4{0.f, 0.f}, zys{0.f, 0.f};
-      float sn = 0.f;
-      if(all_on) {
-        // All six orderings count: the orbit sums follow from the class sums.
-        //   sum_q Z_q Y4_q = 9 sum_q W_q^2 + 3 (C_a^2 + C_b^2) - 12 C_a C_b
-        //   sum_q Z_q ys_q = 3 sum_q W_q ys_q + 3 (C_a - C_b)(S_a - S_b)
-        // (class a: Z = 3 W + C_a, Y4 = 3 W - C_b, ys = 3 sg - S_b; class b with a and b swapped)
-        ffacc sqa, wya;
-#pragma unroll
-        for(int q = 0; q < 6; q++) {
-          const bool  in_a = q == 0 || q == 3 || q == 4;
-          const float ys   = 3.f * sg[q] - (in_a ? sgb : sga);
-          sqa.add_sq(w[q]);
-          wya.add_mul_f(w[q], ys);
-          if(A.want_sens) { // the estimate needs Z and Y only to float precision
-            const float z = 3.f * w[q].hi + (in_a ? ca.hi : cb.hi), y5 = 3.f * w[q].hi - (in_a ? cb.hi : ca.hi) + ys;
-            sn = fmaf(18.f * y5, y5, fmaf(12.f * z, z, sn));
-          }
-        }
-        const ff sq = sqa.get(), wy = wya.get();
-        zy4 = ff_add(ff_add(ff_mul_f(sq, 9.f), ff_mul_f(ff_add(ff_mul(ca, ca), ff_mul(cb, cb)), 3.f)),
-                     ff_neg(ff_mul_f(ff_mul(ca, cb), 12.f)));
-        zys = ff_add(ff_mul_f(wy, 3.f), ff_mul_f(ff_add(ca, ff_neg(cb)), 3.f * (sga - sgb)));
-      } else
-#pragma unroll
-      for(int q = 0; q < 6; q++) {
-        if(!slot_on[q]) continue;
-        const bool  in_a = q == 0 || q == 3 || q == 4;
-        const ff    t3 = ff_mul_f(w[q], 3.f);
-        const ff    z  = ff_add(t3, in_a ? ca : cb);
-        const ff    y4 = ff_add(t3, ff_neg(in_a ? cb : ca));
-        const float ys = 3.f * sg[q] - (in_a ? sgb : sga);   // singles part of Y
-        zy4 = ff_add(zy4, ff_mul(z, y4));
-        zys = ff_add(zys, ff_mul_f(z, ys));
-        // first-order sensitivity to errors in W: W_abc enters Z_abc (x4), Z_bca, Z_cab and,
-        // through V, Y_abc (x3), Y_acb, Y_bac, Y_cba; with uncorrelated signs
-        //   |dE/dW|^2 ~ (16 + 1 + 1) Y^2 / D^2 + (9 + 1 + 1 + 1) Z^2 / D^2
-        if(A.want_sens) {
-          const float y5 = y4.hi + ys;
-          sn = fmaf(18.f * y5, y5, fmaf(12.f * z.hi, z.hi, sn));
-        }
-      }
-      const ff zy5 = ff_add(zy4, zys);
-      const float2 dd = dab[la * B + lb], ec = evs[2][lc];
-      const ff     id = ff_div_fast(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
-      s4   = ff_add(s4, ff_mul(zy4, id));
-      s5   = ff_add(s5, ff_mul(zy5, id));
-      sens = fmaf(sn * id.hi, id.hi, sens);
+      et_orbit(W, Ojk, Oik, Oij, ti, tj, tk, evs, dab, all_on, slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
     }
   }
   CSum c4, c5;

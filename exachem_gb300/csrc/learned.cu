@@ -220,6 +220,7 @@ extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccs
   }
   if(cudaSetDevice(h->device) != cudaSuccess) return h->fail(CCSDT_E_CUDA, "cudaSetDevice");
   if(n == 0) return CCSDT_OK;
+  h->energy_sync_kernel = opts->test_kernel == 4;
   ccsdt_status s;
   if((s = h->ensure_triplet_slots(n)) || (s = h->ensure_slices(opts->slices, 0))) return s;
   Scratch sc;

@@ -78,7 +78,8 @@ typedef struct {
                           /* triplets (batched calls): the acceptance allowance is scaled by    */
                           /* sqrt(budget_triplets / triplets of the call); 0 = the whole call   */
   int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05, */
-                          /* 3 FP64 contractions with the split path's float-float energy        */
+                          /* 3 FP64 contractions with the split path's float-float energy,       */
+                          /* 4 persistent path with the block-synchronous batched energy kernel  */
   int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
                              slice count they use, once per handle, before the timed work      */
   int    reserved[3];
