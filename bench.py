@@ -426,8 +426,9 @@ def main():
     ap.add_argument("--limit-triplets", type=int, default=0,
                     help="profiling aid: run only this many evenly spread triplets of the call (projected)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--budget", type=float, default=1e-8,
-                    help="learned mode: 3 sqrt(sum sigma_t^2) <= budget x sum |E(T)_t|")
+    ap.add_argument("--budget", type=float, default=1e-9,
+                    help="learned mode: 3 sqrt(sum sigma_t^2) <= budget x sum |E(T)_t| (1e-9: two planes miss it "
+                         "at o=60 v=500, three meet it)")
     ap.add_argument("--no-learned", action="store_true", help="no learned-mode entry in the parity sample")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile configurations (no ccsdt_autotune before the timed region)")

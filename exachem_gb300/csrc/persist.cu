@@ -27,16 +27,20 @@ using namespace ccsdt;
 
 namespace {
 
-// Item ids of B slots sorted by estimated cost (rows x columns of the tile), largest first; ties
-// keep the natural order (n-block fastest) so concurrently running CTAs share A tiles in L2.
+// Item ids of B slots sorted by estimated cost, largest first.  The cost is the tile's row count
+// (its A tile), not rows x columns: the items of one A tile - its n-blocks, the last of which may
+// be narrower - then stay adjacent in the natural order (n-block fastest), run at the same time on
+// neighbouring CTAs and read that A tile from L2 after the first load.  Ordering by rows x columns
+// moved the narrow last n-block of every A tile to the end of the queue, long after the tile had
+// left L2, and cost one more DRAM read of it.
 std::vector<unsigned> cost_order(int B, int v, int NT) {
   const int  yb = (v + PZ_BM - 1) / PZ_BM, nb = (v + NT - 1) / NT;
   const long n  = (long) B * 3 * v * yb * nb;
   std::vector<unsigned> ids(n);
   std::iota(ids.begin(), ids.end(), 0u);
   auto cost = [&](unsigned id) {
-    const int n_b = id % nb, y_b = (id / nb) % yb;
-    return std::min(PZ_BM, v - y_b * PZ_BM) * std::min(NT, v - n_b * NT);
+    const int y_b = (id / nb) % yb;
+    return std::min(PZ_BM, v - y_b * PZ_BM);
   };
   std::stable_sort(ids.begin(), ids.end(), [&](unsigned a, unsigned b) { return cost(a) > cost(b); });
   return ids;

@@ -4,7 +4,8 @@ Labels: for the sampled triplets of a system, the digit-plane counts S in 2..sma
 allocation gives under the LEARNED mode's own acceptance test 3 sqrt(sum_t sigma_t^2) <= budget
 sum_t |E_t| (sigma_t: the library's a-posteriori error estimate of triplet t at its count; the
 sample stands for the system's N triplets): all start at 2 and the triplet with the largest
-sigma_t moves up one count until the test passes (label_triplets).  The measured errors against
+sigma_t moves up one count until the test passes (label_triplets), against half the budget the
+model will run with (a safety margin: an underestimate costs a rerun).  The measured errors against
 the library's own FP64 path are kept beside the labels.  Features come from the library
 (ccsdt_triplet_features, 12 per triplet).  Training runs on the GPU through ccsdt_mlp_train
 (hand-written FP32 forward / backward / Adam kernels).
@@ -148,9 +149,15 @@ def training_systems(n=20, seed0=100, o_range=(20, 60), v_range=(150, 500), scal
     return out
 
 
-def build_training_set(systems, per_system=24, budget=1e-8, smax=7, log=print):
+LABEL_MARGIN = 0.5
+
+
+def build_training_set(systems, per_system=24, budget=1e-9, smax=7, log=print, margin=LABEL_MARGIN):
     """Features and labels of per_system sampled triplets of each system (inputs built on the GPU,
-    bit-identical to the host generator)."""
+    bit-identical to the host generator).  The labels are allocated against margin x budget: the
+    sample only estimates the system's error budget, and a triplet predicted one count too low
+    costs a rerun (the acceptance test escalates it), while one predicted too high costs only the
+    difference in digit-plane products."""
     import torch
     from .generator import generate_device
     X, Y, meta = [], [], []
@@ -164,7 +171,7 @@ def build_training_set(systems, per_system=24, budget=1e-8, smax=7, log=print):
         allt = allt[allt[:, 0] != allt[:, 2]]
         rng = np.random.default_rng(seed)
         tri = allt[np.sort(rng.choice(len(allt), size=min(per_system, len(allt)), replace=False))]
-        lab, errs, _ = label_triplets(ft, tri, budget, smax)
+        lab, errs, _ = label_triplets(ft, tri, budget * margin, smax)
         X.append(features(ft, tri))
         Y.append(lab - 2)
         meta.append({"o": o, "v": v, "seed": seed, "t2_scale": sc, "labels": np.bincount(lab, minlength=smax + 1).tolist()})
@@ -190,14 +197,16 @@ def main(argv=None):
     ap.add_argument("--out", default=str(MODEL_PATH))
     ap.add_argument("--per-system", type=int, default=24)
     ap.add_argument("--smax", type=int, default=6, help="largest label (digit-plane count) considered")
+    ap.add_argument("--budget", type=float, default=1e-9, help="the LEARNED mode's acceptance budget")
     a = ap.parse_args(argv)
     t0 = time.time()
     systems = training_systems()
-    X, y, meta = build_training_set(systems, per_system=a.per_system, smax=a.smax)
+    X, y, meta = build_training_set(systems, per_system=a.per_system, budget=a.budget, smax=a.smax)
     params, loss = mlp_train(X, y, epochs=400, batch=64, lr=3e-3, seed=7)
     acc = float((mlp_predict(params, X) - 2 == y).mean())
     print(f"trained on {len(y)} triplets: loss {loss:.4f}, accuracy {acc:.3f}, {time.time() - t0:.0f} s")
-    save_model(params, {"systems": meta, "budget": 1e-8, "loss": loss, "train_accuracy": acc,
+    save_model(params, {"systems": meta, "budget": a.budget, "label_margin": LABEL_MARGIN, "loss": loss,
+                        "train_accuracy": acc,
                         "label_histogram": np.bincount(y + 2, minlength=9).tolist(),
                         "per_system": a.per_system, "smax": a.smax, "train_seconds": time.time() - t0}, a.out)
 

@@ -54,7 +54,7 @@ def test_learned_mode_meets_budget_and_saves_products(built):
     meet the budget, and the digit-plane products it runs (escalations included) must be strictly
     fewer than those of the smallest fixed count that passes the same test.  The budget sits
     between the fixed counts (2 planes miss it, 3 meet it with room to spare on these ~300-triplet
-    systems; the o=60 v=500 call is in the same regime at 1e-8), where a per-triplet choice can
+    systems; the o=60 v=500 call is in the same regime at 1e-9), where a per-triplet choice can
     gain: triplets with small energies stay at 2 planes."""
     from exachem_gb300 import ccsd_t as ct, learned
     from exachem_gb300.generator import generate
