@@ -426,9 +426,9 @@ def main():
     ap.add_argument("--limit-triplets", type=int, default=0,
                     help="profiling aid: run only this many evenly spread triplets of the call (projected)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--budget", type=float, default=1e-9,
-                    help="learned mode: 3 sqrt(sum sigma_t^2) <= budget x sum |E(T)_t| (1e-9: two planes miss it "
-                         "at o=60 v=500, three meet it)")
+    ap.add_argument("--budget", type=float, default=1e-8,
+                    help="learned mode: 3 sum_t sigma_t <= budget x sum_t |E(T)_t| (1e-8: two planes miss it at "
+                         "o=60 v=500, three meet it)")
     ap.add_argument("--no-learned", action="store_true", help="no learned-mode entry in the parity sample")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default tile configurations (no ccsdt_autotune before the timed region)")
@@ -504,7 +504,7 @@ def main():
         learned.set_model(ft, model)
     lkw = {"slices": 5, "energy_budget": args.budget, "budget_triplets": int(len(tri_all))}
     if mode == "learned":
-        # each timed call is a part of the whole (T) over all triplets: its acceptance share
+        # each timed call is held to the same relative budget as the whole (T) (linear acceptance)
         kw = dict(lkw)
 
     # the contraction's tile configuration for each slice count this run uses, tuned on this system

@@ -144,7 +144,4 @@ struct ccsdt_handle {
   ccsdt_status collect_phase_times();
   int          energy_grid_ = 0; // resident CTAs of the tiled energy kernels (one full wave)
   int          energy_grid();
-  int          energy_ws_grid_ = -1; // the same for the warp-specialised batched energy kernel
-  int          energy_ws_grid();
-  bool         energy_sync_kernel = false; // testing: the block-synchronous batched energy kernel
 };

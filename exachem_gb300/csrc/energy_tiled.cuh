@@ -12,6 +12,8 @@
 // reduction, so the result is deterministic.
 #pragma once
 
+#include <type_traits>
+
 #include "fp64_kernels.cuh"
 #include "ozaki.cuh"
 
@@ -223,13 +225,9 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     static_assert(6 * B3 == 12 * ET_THREADS, "two positions of each of the six cubes per thread");
     float2*    Wf   = &W[0][0];
     const bool full = rbn[0] == B && rbn[1] == B && rbn[2] == B;
-#pragma unroll
-    for(int pass = 0; pass < 3; pass++) {
-      // pass 0 needs no barrier: the one after the staging made cube0 visible, and the previous
-      // item's orbits finished with W before the barrier at the top of the item
-      if(pass > 0) __syncthreads();
-      float2 x[12];
-      int    widx[12];
+    // pass p's loads (a thread's 12, all issued before any of them is used)
+    auto load_pass = [&](auto pass_tag, float2 (&x)[12], int (&widx)[12]) {
+      constexpr int pass = decltype(pass_tag)::value;
 #pragma unroll
       for(int it = 0; it < 12; it++) {
         const int s = it >> 1, r = tid + (it & 1) * ET_THREADS;
@@ -262,6 +260,10 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
           widx[it] = s * B3 + kSwz(loc[0], loc[1], loc[2]);
         }
       }
+    };
+    // pass p's shared-memory updates
+    auto apply_pass = [&](auto pass_tag, const float2 (&x)[12], const int (&widx)[12]) {
+      constexpr int pass = decltype(pass_tag)::value;
 #pragma unroll
       for(int it = 0; it < 12; it++) {
         if(pass == 0) Wf[widx[it]] = x[it];
@@ -275,6 +277,22 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
           Wf[widx[it]]   = make_float2(r.hi, r.lo);
         }
       }
+    };
+    // The next pass's loads are issued before the barrier that separates the passes' updates, so
+    // their latency overlaps the wait.  Pass 0 needs no barrier before it: the one after the
+    // staging made cube0 visible, and the previous item's orbits finished with W before the
+    // barrier at the top of the item.
+    {
+      float2 x[12];
+      int    widx[12];
+      load_pass(std::integral_constant<int, 0>{}, x, widx);
+      apply_pass(std::integral_constant<int, 0>{}, x, widx);
+      load_pass(std::integral_constant<int, 1>{}, x, widx);
+      __syncthreads();
+      apply_pass(std::integral_constant<int, 1>{}, x, widx);
+      load_pass(std::integral_constant<int, 2>{}, x, widx);
+      __syncthreads();
+      apply_pass(std::integral_constant<int, 2>{}, x, widx);
     }
     __syncthreads();
     // energies by orbit: a thread takes one index triple (a' in block 0, b' in block 1, c' in

@@ -18,7 +18,6 @@
 
 #include "ccsdt_internal.cuh"
 #include "energy_tiled.cuh"
-#include "energy_ws.cuh"
 #include "fp64_kernels.cuh"
 #include "oz_persist.cuh"
 #include "pz_confs.h"
@@ -131,20 +130,6 @@ int ccsdt_handle::energy_grid() {
   return energy_grid_;
 }
 
-// One full wave of the warp-specialised batched energy kernel (its two-buffer stage needs 65 KB of
-// dynamic shared memory, which the launch must be allowed first); 0 if it cannot be resident.
-int ccsdt_handle::energy_ws_grid() {
-  if(energy_ws_grid_ >= 0) return energy_ws_grid_;
-  int sm = 0, per = 0;
-  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
-  if(cudaFuncSetAttribute(energy_ws_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, EW_SMEM) != cudaSuccess ||
-     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_ws_batch_kernel, EW_THREADS, EW_SMEM) != cudaSuccess)
-    per = 0;
-  cudaGetLastError();
-  energy_ws_grid_ = std::min(kTiledBlocks, per * std::max(1, sm));
-  return energy_ws_grid_;
-}
-
 // Launch the sequence of one batch of `nslots` triplets starting at the device base counter.
 ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails,
                                         double* sens) {
@@ -201,11 +186,8 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
     ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
                                    o, v, 0, 0, 0, nullptr, sens != nullptr};
     ea.tri = bt_tri, ea.base = bt_ctrl + 2, ea.F = bt_F, ea.part = bt_part;
-    // the warp-specialised kernel unless a test asks for the block-synchronous one (same arithmetic)
-    const bool ws = !energy_sync_kernel && energy_ws_grid() > 0;
-    const int  G  = std::min(e_ntiles, ws ? energy_ws_grid() : energy_grid());
-    if(ws) energy_ws_batch_kernel<<<dim3(G, nslots), EW_THREADS, EW_SMEM, stream>>>(ea);
-    else energy_tiled_batch_kernel<<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
+    const int G = std::min(e_ntiles, energy_grid());
+    energy_tiled_batch_kernel<<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
     if(profiling) cudaEventRecord(prof_ev[3], stream);
     reduce_parts_batch_kernel<<<nslots, 256, 0, stream>>>(bt_part, G, bt_tri, bt_ctrl + 2, etrip, sens);
     if(advance) advance_base_kernel<<<1, 32, 0, stream>>>(bt_ctrl + 2, nslots);

@@ -583,9 +583,8 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 }
 
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
-  last_batched       = false;
-  last_err_bound     = 0.0; // only the LEARNED mode estimates its error
-  energy_sync_kernel = opts->test_kernel == 4; // testing: the block-synchronous batched energy
+  last_batched     = false;
+  last_err_bound   = 0.0; // only the LEARNED mode estimates its error
   if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
   const int S       = opts->slices;
   const int variant = opts->slice_kind;
@@ -614,7 +613,7 @@ ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* 
     fp64_ff_energy = false;
     return s;
   }
-  last_batched = (kernel_kind == 0 || kernel_kind == 4) && pz_eligible(S, variant);
+  last_batched = kernel_kind == 0 && pz_eligible(S, variant);
   if(last_batched) return run_batched(S, n, tri, opts->use_graph != 0, nullptr, nullptr);
   for(long t = 0; t < n; t++) {
     const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];

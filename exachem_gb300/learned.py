@@ -1,10 +1,10 @@
 """Training data, training and use of the per-triplet slice-count model.
 
 Labels: for the sampled triplets of a system, the digit-plane counts S in 2..smax that a greedy
-allocation gives under the LEARNED mode's own acceptance test 3 sqrt(sum_t sigma_t^2) <= budget
-sum_t |E_t| (sigma_t: the library's a-posteriori error estimate of triplet t at its count; the
-sample stands for the system's N triplets): all start at 2 and the triplet with the largest
-sigma_t moves up one count until the test passes (label_triplets), against half the budget the
+allocation gives under the LEARNED mode's own acceptance test 3 sum_t sigma_t <= budget
+sum_t |E_t| (sigma_t: the library's a-posteriori error estimate of triplet t at its count): all
+start at 2 and the triplet with the largest sigma_t moves up one count until the test passes
+(label_triplets), against half the budget the
 model will run with (a safety margin: an underestimate costs a rerun).  The measured errors against
 the library's own FP64 path are kept beside the labels.  Features come from the library
 (ccsdt_triplet_features, 12 per triplet).  Training runs on the GPU through ccsdt_mlp_train
@@ -103,21 +103,16 @@ def learned_stats(ft: "ct.FusedTriples", with_products=False):
 
 def label_triplets(ft, tri, budget=1e-8, smax=7):
     """Slice-count labels of the sampled triplets `tri` of the handle's system: the counts a greedy
-    allocation gives under the LEARNED mode's own acceptance test.  With sigma_t(S) the library's
-    a-posteriori estimate of triplet t's error at S planes (ccsdt_triplet_error_estimates, what the
-    acceptance reads), the sample stands for the system's N triplets, and the test
-    3 sqrt(sum_t sigma_t^2) <= budget sum_t |E_t| over N triplets reads, per sample of n,
-        3 sqrt(sum_sample sigma_t^2) <= budget sqrt(N / n) sum_sample |E_t(FP64)|.
-    Every triplet starts at 2 planes; while the test fails, the triplet with the largest sigma_t
-    moves one count up (it buys the largest variance cut per extra product, as sigma falls by
-    ~2^-7 per plane), up to smax.  An equal per-triplet share of the allowance would leave most of
-    it unused (triplets at a higher count use a tiny part of theirs) and put nearly every triplet
-    one count higher than it needs.
+    allocation gives under the LEARNED mode's own acceptance test 3 sum_t sigma_t <= budget
+    sum_t |E_t(FP64)| (sigma_t: the library's a-posteriori estimate of triplet t's error at its
+    count, ccsdt_triplet_error_estimates; the test is linear, so the sample stands for the system
+    without any rescaling).  Every triplet starts at 2 planes; while the test fails, the triplet with
+    the largest sigma_t moves one count up (it buys the largest cut per extra product, as sigma falls
+    by ~2^-7 per plane), up to smax.
     Returns the labels, the measured errors |E_t(S) - E_t(FP64)| / |E_t(FP64)| [S - 2][t] and the
     FP64 energies (the plain kernel is the yardstick)."""
     _, ref = ft.triplet_energies(tri, "fp64")
-    n_all = ft.o * (ft.o + 1) * (ft.o + 2) // 6
-    allow = budget * np.sqrt(n_all / max(1, len(ref))) * np.abs(ref).sum() / 3.0
+    allow = budget * np.abs(ref).sum() / 3.0
     sig, errs = [], []
     for S in range(2, smax + 1):
         _, e, est = ft.triplet_error_estimates(tri, S)
@@ -126,7 +121,7 @@ def label_triplets(ft, tri, budget=1e-8, smax=7):
     sig, errs = np.array(sig), np.array(errs)               # [S-2][t]
     lab = np.full(len(ref), 2)
     cur = sig[0].copy()
-    while np.sqrt(np.sum(cur ** 2)) > allow:
+    while np.sum(cur) > allow:
         t = int(np.argmax(np.where(lab < smax, cur, -1.0)))
         if lab[t] >= smax or cur[t] <= 0:
             break
@@ -152,7 +147,7 @@ def training_systems(n=20, seed0=100, o_range=(20, 60), v_range=(150, 500), scal
 LABEL_MARGIN = 0.5
 
 
-def build_training_set(systems, per_system=24, budget=1e-9, smax=7, log=print, margin=LABEL_MARGIN):
+def build_training_set(systems, per_system=24, budget=1e-8, smax=7, log=print, margin=LABEL_MARGIN):
     """Features and labels of per_system sampled triplets of each system (inputs built on the GPU,
     bit-identical to the host generator).  The labels are allocated against margin x budget: the
     sample only estimates the system's error budget, and a triplet predicted one count too low
@@ -197,7 +192,7 @@ def main(argv=None):
     ap.add_argument("--out", default=str(MODEL_PATH))
     ap.add_argument("--per-system", type=int, default=24)
     ap.add_argument("--smax", type=int, default=6, help="largest label (digit-plane count) considered")
-    ap.add_argument("--budget", type=float, default=1e-9, help="the LEARNED mode's acceptance budget")
+    ap.add_argument("--budget", type=float, default=1e-8, help="the LEARNED mode's acceptance budget")
     a = ap.parse_args(argv)
     t0 = time.time()
     systems = training_systems()

@@ -72,14 +72,12 @@ typedef struct {
   int    use_graph;     /* capture the per-call launch sequence in a CUDA graph               */
   int    shard_index;   /* process triplets t with t % shard_count == shard_index; the        */
   int    shard_count;   /* caller sums the partial energies (0 or 1 = every triplet)          */
-  double energy_budget; /* LEARNED: accept when 3 sqrt(sum_t sigma_t^2) <= budget x          */
-                        /* sum_t |E(T)_t| (sigma_t: estimated error of triplet t; default 1e-8) */
-  int    budget_triplets; /* LEARNED: the call is one part of a computation over this many    */
-                          /* triplets (batched calls): the acceptance allowance is scaled by    */
-                          /* sqrt(budget_triplets / triplets of the call); 0 = the whole call   */
+  double energy_budget; /* LEARNED: accept when 3 sum_t sigma_t <= budget x sum_t |E(T)_t|   */
+                        /* (sigma_t: estimated error of triplet t; default 1e-8)              */
+  int    budget_triplets; /* ignored (the linear acceptance test needs no share for a call that */
+                          /* is part of a larger computation); kept for the struct layout       */
   int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05, */
-                          /* 3 FP64 contractions with the split path's float-float energy,       */
-                          /* 4 persistent path with the block-synchronous batched energy kernel  */
+                          /* 3 FP64 contractions with the split path's float-float energy        */
   int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
                              slice count they use, once per handle, before the timed work      */
   int    reserved[3];

@@ -212,19 +212,3 @@ def test_long_contraction_beyond_the_exact_window(built):
         np.testing.assert_allclose(s5, f5, rtol=tol)
         np.testing.assert_allclose(s4, f4, rtol=tol)
     ft.close()
-
-
-@pytest.mark.parametrize("o,v,seed", [(7, 96, 18), (5, 203, 19)])
-def test_warp_specialised_energy_equals_block_synchronous(built, o, v, seed):
-    """The batched path's warp-specialised energy kernel (producer warps stage the next work item
-    while consumer warps evaluate the current one) and the block-synchronous kernel do the same
-    arithmetic per orbit; only the grouping of the per-CTA partial sums differs, so the energies
-    agree to rounding, triplet by triplet.  v = 203 leaves a ragged last 8-wide block."""
-    from exachem_gb300.ccsd_t import all_triplets
-    ft = _ft(o, v, seed)
-    tri = all_triplets(o)
-    for S in (2, 3):
-        w4, w5 = ft.triplet_energies(tri, "ozaki", slices=S)
-        s4, s5 = ft.triplet_energies(tri, "ozaki", slices=S, legacy_mma=4)
-        np.testing.assert_allclose(w5, s5, rtol=1e-13, atol=1e-13 * np.abs(s5).max())
-        np.testing.assert_allclose(w4, s4, rtol=1e-13, atol=1e-13 * np.abs(s4).max())

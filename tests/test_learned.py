@@ -50,15 +50,14 @@ def test_mlp_training_reduces_loss_and_bf16_inference(built):
 
 
 def test_learned_mode_meets_budget_and_saves_products(built):
-    """LEARNED accepts when 3 sqrt(sum sigma_t^2) <= budget sum |E_t|: the measured error must
-    meet the budget, and the digit-plane products it runs (escalations included) must be strictly
-    fewer than those of the smallest fixed count that passes the same test.  The budget sits
-    between the fixed counts (2 planes miss it, 3 meet it with room to spare on these ~300-triplet
-    systems; the o=60 v=500 call is in the same regime at 1e-9), where a per-triplet choice can
-    gain: triplets with small energies stay at 2 planes."""
+    """LEARNED accepts when 3 sum_t sigma_t <= budget sum |E_t|: the measured error must meet the
+    budget, and the digit-plane products it runs (escalations included) must be strictly fewer
+    than those of the smallest fixed count that passes the same test.  The budget sits between the
+    fixed counts (2 planes miss it, 3 meet it with room to spare on these ~300-triplet systems),
+    where a per-triplet choice can gain: triplets with small energies stay at 2 planes."""
     from exachem_gb300 import ccsd_t as ct, learned
     from exachem_gb300.generator import generate
-    budget = 1e-7
+    budget = 1e-6
     systems = [(10, 60, 100, 1.0), (12, 70, 101, 2.0), (14, 64, 102, 0.7)]
     X, y, _ = learned.build_training_set(systems, per_system=30, budget=budget, smax=6, log=lambda *a: None)
     params, _ = learned.mlp_train(X, y, epochs=300, batch=32, lr=3e-3, seed=5)
@@ -79,7 +78,7 @@ def test_learned_mode_meets_budget_and_saves_products(built):
     fixed = 5
     for S in (2, 3, 4):
         _, _, est = ft.triplet_error_estimates(tri, S)
-        if 3 * np.sqrt(np.sum(est ** 2)) <= allow:
+        if 3 * np.sum(est) <= allow:
             fixed = S
             break
     n = len(tri)
@@ -142,10 +141,10 @@ def test_error_estimate_covers_measured_error(built):
     assert q[2] <= 10
 
 
-def test_batched_call_takes_its_share_of_the_budget(built):
-    """A call that is one part of a larger computation (budget_triplets) is accepted against its
-    share of the whole allowance, sqrt(budget_triplets / n_call) times its own: never more
-    escalations than the same call judged as the whole computation."""
+def test_batched_call_is_held_to_the_same_relative_budget(built):
+    """The acceptance test is linear in the triplets (3 sum_t sigma_t <= budget sum_t |E_t|), so a
+    call that is one part of a larger computation is judged exactly as if it were the whole:
+    budget_triplets changes nothing."""
     from exachem_gb300 import ccsd_t as ct, learned
     from exachem_gb300.generator import generate
     params, _ = learned.load_model()
@@ -153,8 +152,9 @@ def test_batched_call_takes_its_share_of_the_budget(built):
     ft.upload_dict(generate(10, 64, 404))
     tri = ct.all_triplets(10)
     learned.set_model(ft, params)
-    ft.triplet_energies(tri, "learned", slices=5, energy_budget=1e-10)
+    a4, a5 = ft.triplet_energies(tri, "learned", slices=5, energy_budget=1e-9)
     _, esc_whole, prod_whole = learned.learned_stats(ft, with_products=True)
-    ft.triplet_energies(tri, "learned", slices=5, energy_budget=1e-10, budget_triplets=100 * len(tri))
+    b4, b5 = ft.triplet_energies(tri, "learned", slices=5, energy_budget=1e-9, budget_triplets=100 * len(tri))
     _, esc_part, prod_part = learned.learned_stats(ft, with_products=True)
-    assert esc_part <= esc_whole and prod_part <= prod_whole
+    assert esc_part == esc_whole and prod_part == prod_whole
+    assert np.array_equal(a5, b5) and np.array_equal(a4, b4)
