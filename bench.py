@@ -584,13 +584,14 @@ def main():
     fp64_eq = 12.0 * float(v) ** 4
     peaks = measured_peaks()
     if not split:
+        # the fused kernel: all twelve contractions of a triplet and its energy in one launch
         i, j, k = (int(x) for x in mine[len(mine) // 2])
         prof = [ft.profile_triplet(i, j, k, mode, **kw) for _ in range(3)]
         gemm_ms = statistics.median(p[1] for p in prof)
-        per_launch = fp64_eq
+        per_launch = 12.0 * float(v) ** 3 * (v + o)
         peak, peak_src = fp64_peak, "measured (cuBLAS DGEMM 8192^3 in this run; FP64 is not in MEASURED_PEAKS.json)"
-        kernel = "dmma_gemm_kernel"
-        phase = dict(zip(["l_sum", "d_sum", "energy", "reduce"], prof[1]))
+        kernel = "t3_fused_fp64_kernel"
+        phase = dict(zip(["l_sum", "fused_contraction_and_energy", "energy", "reduce"], prof[1]))
         timing = "profile_triplet: CUDA events around one triplet's launches, after the timed region"
     else:
         nb, ntr = max(1, pt["batches"]), max(1, pt["triplets"])

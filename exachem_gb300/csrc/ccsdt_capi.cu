@@ -18,6 +18,7 @@
 #include "../../include/ccsdt.h"
 #include "ccsdt_internal.cuh"
 #include "fp64_kernels.cuh"
+#include "fused_fp64.cuh"
 
 using namespace ccsdt;
 
@@ -292,7 +293,59 @@ ccsdt_status ccsdt_handle::ensure_triplet_slots(long n) {
   return CCSDT_OK;
 }
 
+// The sorted 8-wide virtual block triples (work units of the fused FP64 kernel), built once.
+ccsdt_status ccsdt_handle::ensure_fused_tiles() {
+  if(fx_tiles) return CCSDT_OK;
+  const int        nb = (v + ET_B - 1) / ET_B;
+  std::vector<int> host;
+  for(int X = 0; X < nb; X++)
+    for(int Y = X; Y < nb; Y++)
+      for(int Z = Y; Z < nb; Z++) host.insert(host.end(), {X, Y, Z});
+  int* d = nullptr;
+  if(ccsdt::dev_malloc((void**) &d, host.size() * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(CCSDT_E_OOM, "fused FP64 work units");
+  }
+  owned_bytes.push_back(d);
+  if(cudaMemcpy(d, host.data(), host.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess)
+    return fail(CCSDT_E_CUDA, "fused FP64 work-unit upload");
+  fx_tiles  = d;
+  fx_ntiles = (int) (host.size() / 3);
+  int sm = 0, per = 0;
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, t3_fused_fp64_kernel, FX_THREADS, 0);
+  cudaGetLastError();
+  fx_grid = std::max(1, std::min(kEnergyBlocks, std::max(1, per) * std::max(1, sm)));
+  return CCSDT_OK;
+}
+
+// One triplet on the fused FP64 kernel: contractions, the triples block kept on chip, energy.
+ccsdt_status ccsdt_handle::run_triplet_fp64_fused(int i, int j, int k, double* eout) {
+  ccsdt_status s;
+  if((s = ensure_fused_tiles())) return s;
+  FusedArgs fa{t2, t2h, ovvv, ooovh, oovv, t1, eo, ev, (const int3*) fx_tiles, fx_ntiles, o, v, i, j, k, part};
+  const int G = std::min(fx_ntiles, fx_grid);
+  if(profiling) {
+    cudaEventRecord(prof_ev[0], stream);
+    cudaEventRecord(prof_ev[1], stream); // contractions and energy are one launch
+  }
+  t3_fused_fp64_kernel<<<G, FX_THREADS, 0, stream>>>(fa);
+  if(profiling) {
+    cudaEventRecord(prof_ev[2], stream);
+    cudaEventRecord(prof_ev[3], stream);
+  }
+  reduce_parts_kernel<<<1, E_THREADS, 0, stream>>>(part, G, multiplicity(i, j, k) / 9.0, eout);
+  if(profiling) cudaEventRecord(prof_ev[4], stream);
+  launches += 2;
+  const cudaError_t e = cudaGetLastError();
+  if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("fused FP64 launch: ") + cudaGetErrorString(e));
+  return CCSDT_OK;
+}
+
 ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
+  // the fused kernel unless the partial arrays themselves are wanted (W debugging aid, the
+  // float-float energy test) or a test asks for the two-stage path
+  if(!fp64_unfused && !fp64_ff_energy) return run_triplet_fp64_fused(i, j, k, eout);
   const long long o = this->o, v = this->v, v2 = v * v, v3 = v2 * v;
   // ---- l-sum (hole) contractions: C[(pair)][single] = -sum_l t(pair, l) (..l|..)
   GemmBatch hb{};
@@ -370,7 +423,7 @@ static bool valid_opts(const ccsdt_opts* o) {
 static ccsdt_status autotune_for(ccsdt_handle* h, const ccsdt_opts* opts) {
   if(!opts->autotune || opts->mode == CCSDT_MODE_FP64 || opts->slice_kind != 0 || opts->test_kernel != 0)
     return CCSDT_OK;
-  const int lo = opts->mode == CCSDT_MODE_LEARNED ? 1 : opts->slices, hi = std::min(opts->slices, 5);
+  const int lo = opts->mode == CCSDT_MODE_LEARNED ? 1 : opts->slices, hi = std::min(opts->slices, 8);
   for(int S = std::max(lo, 1); S <= hi; S++)
     if(!h->pz_tuned[S]) {
       ccsdt_status s = h->autotune(S, nullptr, nullptr, nullptr);
@@ -384,6 +437,7 @@ ccsdt_status ccsdt_handle::run_list(const ccsdt_opts* opts, long n, const int* t
   if((s = ensure_scratch()) || (s = ensure_triplet_slots(n))) return s;
   launches = 0;
   if(opts->mode != CCSDT_MODE_FP64) return run_split(opts, n, tri_host);
+  fp64_unfused = opts->test_kernel == 5 || w_debug; // testing: the two-stage FP64 path
   for(long t = 0; t < n; t++) {
     const int i = tri_host[3 * t], j = tri_host[3 * t + 1], k = tri_host[3 * t + 2];
     if(i == k) {
@@ -521,7 +575,9 @@ extern "C" ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts*
   if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_debug_triplet_w before ccsdt_upload");
   CK(cudaSetDevice(h->device));
   const int    tri[3] = {i, j, k};
+  h->w_debug          = true; // the FP64 partial arrays must be written to HBM
   ccsdt_status s      = h->run_list(opts, 1, tri);
+  h->w_debug          = false;
   if(s) return s;
   CK(cudaStreamSynchronize(h->stream));
   if(opts->mode != CCSDT_MODE_FP64 && (s = h->check_device_error())) return s;

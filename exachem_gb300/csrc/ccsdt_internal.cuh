@@ -134,6 +134,12 @@ struct ccsdt_handle {
   ccsdt_status check_device_error();
   bool         force_mma_sync = false; // use the mma.sync slice kernel even where tcgen05 applies
   bool         fp64_ff_energy = false; // testing: FP64 contractions, then the float-float energy
+  bool         fp64_unfused   = false; // the two-stage FP64 path (partial arrays in HBM, then the energy)
+  bool         w_debug        = false; // ccsdt_debug_triplet_w is running
+  int*         fx_tiles       = nullptr; // work units of the fused FP64 kernel
+  int          fx_ntiles = 0, fx_grid = 0;
+  ccsdt_status ensure_fused_tiles();
+  ccsdt_status run_triplet_fp64_fused(int i, int j, int k, double* eout);
   // live per-phase timing of the batched path: 3 events per batch, read after the call
   bool                     phase_timing = false, capturing = false;
   std::vector<cudaEvent_t> tev;

@@ -77,7 +77,8 @@ typedef struct {
   int    budget_triplets; /* ignored (the linear acceptance test needs no share for a call that */
                           /* is part of a larger computation); kept for the struct layout       */
   int    test_kernel;     /* testing: 0 default, 1 mma.sync slice kernel, 2 per-triplet tcgen05, */
-                          /* 3 FP64 contractions with the split path's float-float energy        */
+                          /* 3 FP64 contractions with the split path's float-float energy,       */
+                          /* 5 (FP64 mode) the two-stage FP64 path: partial arrays, then energy  */
   int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
                              slice count they use, once per handle, before the timed work      */
   int    reserved[3];

@@ -142,3 +142,22 @@ def test_shards_sum_to_the_whole_call(built):
         assert sum(p["n_triplets"] for p in parts) == whole["n_triplets"]
         for key in ("e_bracket_T", "e_paren_T"):
             assert rel_close(sum(p[key] for p in parts), whole[key], 1e-13), (mode, key)
+
+
+@pytest.mark.parametrize("o,v,seed", [(6, 45, 31), (9, 64, 32), (4, 130, 33)])
+def test_fused_kernel_equals_two_stage_path(built, o, v, seed):
+    """The fused FP64 kernel (the six W cubes of a virtual block triple in shared memory, the
+    energy in the same kernel) against the two-stage FP64 path (partial arrays written to HBM by
+    DMMA GEMMs, then the energy kernel), triplet by triplet, including ragged last blocks
+    (v = 45, 130) and degenerate triplets: the same sums in another order, 1e-13."""
+    from exachem_gb300.ccsd_t import all_triplets
+    from exachem_gb300.generator import generate
+    ft = _ft(generate(o, v, seed=seed))
+    tri = all_triplets(o)
+    f4, f5 = ft.triplet_energies(tri, "fp64")
+    u4, u5 = ft.triplet_energies(tri, "fp64", legacy_mma=5)
+    np.testing.assert_allclose(f5, u5, rtol=1e-13, atol=1e-13 * np.abs(u5).max())
+    np.testing.assert_allclose(f4, u4, rtol=1e-13, atol=1e-13 * np.abs(u4).max())
+    for t in range(len(tri)):
+        if tri[t][0] == tri[t][2]:
+            assert f5[t] == 0.0 and f4[t] == 0.0
