@@ -426,6 +426,8 @@ def main():
     ap.add_argument("--limit-triplets", type=int, default=0,
                     help="profiling aid: run only this many evenly spread triplets of the call (projected)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--p-storage", default="auto", choices=["auto", "ff", "f32"],
+                    help="split path: partial arrays in FP32 (auto: at 1-2 digit planes) or float-float")
     ap.add_argument("--budget", type=float, default=1e-8,
                     help="learned mode: 3 sum_t sigma_t <= budget x sum_t |E(T)_t| (1e-8: two planes miss it at "
                          "o=60 v=500, three meet it)")
@@ -496,13 +498,14 @@ def main():
     torch.cuda.empty_cache()
     stream = torch.cuda.current_stream()
     ft.set_stream(stream.cuda_stream)
-    kw = {"slices": S} if split else {}
+    kw = {"slices": S, "p_storage": args.p_storage} if split else {}
     model = None
     if mode == "learned" or (mode == "ozaki" and not args.no_learned and args.sample > 0):
         from exachem_gb300 import learned
         model, _ = learned.load_model()                  # the shipped slice-count model
         learned.set_model(ft, model)
-    lkw = {"slices": 5, "energy_budget": args.budget, "budget_triplets": int(len(tri_all))}
+    lkw = {"slices": 5, "energy_budget": args.budget, "budget_triplets": int(len(tri_all)),
+           "p_storage": args.p_storage}
     if mode == "learned":
         # each timed call is held to the same relative budget as the whole (T) (linear acceptance)
         kw = dict(lkw)
@@ -635,7 +638,9 @@ def main():
         fp64_proj = fp64_s / len(samp) * len(tri_all) / world
         nz = np.abs(f5) > 0
         entries = {}
-        runs = [(f"S={s_}", "ozaki", {"slices": s_}) for s_ in sample_slices]
+        runs = [(f"S={s_}", "ozaki", {"slices": s_, "p_storage": args.p_storage}) for s_ in sample_slices]
+        if args.p_storage == "auto" and 2 in sample_slices:   # what the FP32 partial arrays cost in accuracy
+            runs.append(("S=2 float-float partial arrays", "ozaki", {"slices": 2, "p_storage": "ff"}))
         if model is not None:
             runs.append(("learned", "learned", lkw))
         for name, m_, k_ in runs:
@@ -688,6 +693,11 @@ def main():
             "dtype": "f64" if not split else "bf16 digit planes (exact FP32 levels), float-float recombination",
             "data": "synthetic (seeded generator, built on GPU)",
             "config": wl | {"mode": mode, "slices": S if mode == "ozaki" else None, "tile_config": tile,
+                            "partial_arrays": None if not split else (
+                                "FP32" if args.p_storage == "f32" or (args.p_storage == "auto" and mode == "ozaki"
+                                                                      and S <= 2)
+                                else "float-float" if mode == "ozaki" or args.p_storage == "ff"
+                                else "FP32 at 1-2 digit planes, float-float above"),
                             "triplets_total": int(len(tri_all)), "triplets_timed": int(timed_trip),
                             "timed_fraction": frac,
                             "projection": None if frac >= 1 else "value = timed seconds / timed_fraction",

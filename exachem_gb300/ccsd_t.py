@@ -37,7 +37,8 @@ class Opts(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("slices", ctypes.c_int), ("slice_kind", ctypes.c_int),
                 ("use_graph", ctypes.c_int), ("shard_index", ctypes.c_int), ("shard_count", ctypes.c_int),
                 ("energy_budget", ctypes.c_double), ("budget_triplets", ctypes.c_int),
-                ("test_kernel", ctypes.c_int), ("autotune", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("test_kernel", ctypes.c_int), ("autotune", ctypes.c_int), ("p_storage", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class Result(ctypes.Structure):
@@ -231,7 +232,7 @@ class FusedTriples:
 
     @staticmethod
     def opts(mode="fp64", slices=4, slice_kind="bf16", energy_budget=1e-9, use_graph=0,
-             shard_index=0, shard_count=1, legacy_mma=0, budget_triplets=0, autotune=0) -> Opts:
+             shard_index=0, shard_count=1, legacy_mma=0, budget_triplets=0, autotune=0, p_storage=0) -> Opts:
         o = Opts()
         o.mode = MODES[mode] if isinstance(mode, str) else int(mode)
         o.slices = slices
@@ -242,6 +243,7 @@ class FusedTriples:
         o.budget_triplets = budget_triplets
         o.test_kernel = legacy_mma       # 1: mma.sync slice kernel, 2: per-triplet tcgen05 kernel (testing)
         o.autotune = autotune            # 1: tune the contraction's tile configuration on first use
+        o.p_storage = {"auto": 0, "ff": 1, "f32": 2}[p_storage] if isinstance(p_storage, str) else int(p_storage)
         return o
 
     def energy(self, mode="fp64", **kw) -> dict:

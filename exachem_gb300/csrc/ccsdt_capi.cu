@@ -397,11 +397,17 @@ ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
   if(profiling) cudaEventRecord(prof_ev[2], stream);
   if(fp64_ff_energy) { // testing: the same P arrays through the split path's float-float energy
     if(!F12 || !F34 || !F56) return fail(CCSDT_E_STATE, "float-float energy buffers missing");
-    to_ff_kernel<<<2048, 256, 0, stream>>>(P12, F12, v3);
-    to_ff_kernel<<<2048, 256, 0, stream>>>(P34, F34, v3);
-    to_ff_kernel<<<2048, 256, 0, stream>>>(P56, F56, v3);
+    if(p_storage == 2) { // ... or its FP32 energy, from the arrays rounded to FP32
+      to_f32_kernel<<<2048, 256, 0, stream>>>(P12, reinterpret_cast<float*>(F12), v3);
+      to_f32_kernel<<<2048, 256, 0, stream>>>(P34, reinterpret_cast<float*>(F34), v3);
+      to_f32_kernel<<<2048, 256, 0, stream>>>(P56, reinterpret_cast<float*>(F56), v3);
+    } else {
+      to_ff_kernel<<<2048, 256, 0, stream>>>(P12, F12, v3);
+      to_ff_kernel<<<2048, 256, 0, stream>>>(P34, F34, v3);
+      to_ff_kernel<<<2048, 256, 0, stream>>>(P56, F56, v3);
+    }
     launches += 3;
-    return launch_energy_tiled(i, j, k, eout);
+    return launch_energy_tiled(i, j, k, eout, p_storage == 2);
   }
   EnergyArgs ea{P12, P34, P56, oovv, t1, eo, ev, (int) o, (int) v, i, j, k, part};
   energy_fp64_kernel<<<kEnergyBlocks, E_THREADS, 0, stream>>>(ea);
@@ -415,7 +421,8 @@ ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
 }
 
 static bool valid_opts(const ccsdt_opts* o) {
-  return o && (o->mode == CCSDT_MODE_FP64 || o->mode == CCSDT_MODE_OZAKI || o->mode == CCSDT_MODE_LEARNED);
+  return o && (o->mode == CCSDT_MODE_FP64 || o->mode == CCSDT_MODE_OZAKI || o->mode == CCSDT_MODE_LEARNED) &&
+         o->p_storage >= 0 && o->p_storage <= 2;
 }
 
 // opts->autotune: the slice counts this call can use on the persistent tcgen05 path, each tuned
@@ -435,7 +442,8 @@ static ccsdt_status autotune_for(ccsdt_handle* h, const ccsdt_opts* opts) {
 ccsdt_status ccsdt_handle::run_list(const ccsdt_opts* opts, long n, const int* tri_host) {
   ccsdt_status s;
   if((s = ensure_scratch()) || (s = ensure_triplet_slots(n))) return s;
-  launches = 0;
+  launches  = 0;
+  p_storage = opts->p_storage;
   if(opts->mode != CCSDT_MODE_FP64) return run_split(opts, n, tri_host);
   fp64_unfused = opts->test_kernel == 5 || w_debug; // testing: the two-stage FP64 path
   for(long t = 0; t < n; t++) {
@@ -588,15 +596,19 @@ extern "C" ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts*
     CK(cudaMemcpy(b.data(), h->P34, n * sizeof(double), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(c.data(), h->P56, n * sizeof(double), cudaMemcpyDeviceToHost));
   } else {
-    // the persistent path keeps slot 0's P12, P34, P56 consecutively in the batch scratch
+    // the persistent path keeps slot 0's P12, P34, P56 consecutively in the batch scratch, as
+    // float-float or FP32 elements
     std::vector<float2> f(n);
     const float2*       src[3] = {h->F12, h->F34, h->F56};
+    const bool          f32    = h->last_batched && h->last_p_f32;
     if(h->last_batched)
-      for(int q = 0; q < 3; q++) src[q] = h->bt_F + q * n;
+      for(int q = 0; q < 3; q++)
+        src[q] = f32 ? reinterpret_cast<const float2*>(reinterpret_cast<const float*>(h->bt_F) + q * n) : h->bt_F + q * n;
     for(int q = 0; q < 3; q++) {
-      CK(cudaMemcpy(f.data(), src[q], n * sizeof(float2), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(f.data(), src[q], n * (f32 ? sizeof(float) : sizeof(float2)), cudaMemcpyDeviceToHost));
       std::vector<double>& d = q == 0 ? a : q == 1 ? b : c;
-      for(size_t e = 0; e < n; e++) d[e] = (double) f[e].x + (double) f[e].y;
+      const float*         g = reinterpret_cast<const float*>(f.data());
+      for(size_t e = 0; e < n; e++) d[e] = f32 ? (double) g[e] : (double) f[e].x + (double) f[e].y;
     }
   }
   // W_xyz = P12[x][z][y] + P34[y][x][z] + P56[z][y][x]

@@ -90,7 +90,7 @@ struct ccsdt_handle {
   bool         tc_eligible(int S, int variant) const; // per-triplet tcgen05 kernel
   bool         pz_eligible(int S, int variant) const; // persistent tcgen05 kernel
   double*      part_buf() { return part; }
-  ccsdt_status launch_energy_tiled(int i, int j, int k, double* eout);
+  ccsdt_status launch_energy_tiled(int i, int j, int k, double* eout, bool f32 = false);
   ccsdt_status run_triplet_S(int i, int j, int k, int S, double* eout);
   // learned slice count
   ccsdt_status run_learned(const ccsdt_opts* opts, long n, const int* tri_host);
@@ -105,6 +105,11 @@ struct ccsdt_handle {
   // batched persistent path
   float2*   bt_F = nullptr;          // P arrays of the batch slots
   bool      last_batched = false;    // the last split-precision call ran the persistent path
+  bool      last_p_f32   = false;    // ... and stored its partial arrays in FP32
+  int       p_storage    = 0;        // the call's opts->p_storage
+  // FP32 partial arrays for S <= kPF32MaxS digit planes unless the call asks otherwise
+  static constexpr int kPF32MaxS = 2;
+  bool p_f32(int S) const { return p_storage == 2 || (p_storage == 0 && S <= kPF32MaxS); }
   double*   bt_part = nullptr;
   int       bt_B = 0, bt_order_key = -1;
   unsigned* bt_order = nullptr, *bt_order_partial = nullptr;
@@ -148,6 +153,6 @@ struct ccsdt_handle {
   double                   phase_ms[3]   = {0, 0, 0}; // contraction, energy + reduction, unused
   long                     phase_batches = 0, phase_triplets = 0;
   ccsdt_status collect_phase_times();
-  int          energy_grid_ = 0; // resident CTAs of the tiled energy kernels (one full wave)
-  int          energy_grid();
+  int          energy_grid_ = 0, energy_grid_f32_ = 0; // resident CTAs of the tiled energy kernels
+  int          energy_grid(bool f32 = false);            // (one full wave)
 };

@@ -22,7 +22,7 @@ namespace ccsdt {
 constexpr int ET_B = 8, ET_THREADS = 256;
 
 struct TiledEnergyArgs {
-  const float2 *P12, *P34, *P56;
+  const void *  P12, *P34, *P56; // float2 elements, or float for the FP32 form of the kernel
   const float * oovv, *t1; // FP32 copies
   const double *eo, *ev;
   const int3*   tiles;     // sorted block triples
@@ -143,11 +143,59 @@ __device__ __forceinline__ void et_orbit(const float2 (*W)[ET_B * ET_B * ET_B], 
   sens = fmaf(sn * id.hi, id.hi, sens);
 }
 
-__device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, const float2* P12, const float2* P34,
-                                                  const float2* P56, int i, int j, int k, double* part, int gblock,
-                                                  int gsize) {
-  constexpr int B = ET_B, B3 = B * B * B;
-  __shared__ float2 W[6][B3];            // [slot][a'][b'][c'] (a', b', c' local to the slot's blocks)
+// The same orbit from FP32 partial arrays (P stored rounded to FP32: the split path at few digit
+// planes, whose own contraction error is far above FP32's rounding).  Z and Y per ordering in FP32
+// (Z = 3 W + C_own, Y4 = 3 W - C_other directly: no class-sum identity, whose terms cancel), the
+// orbit's six products summed in FP32, one correctly rounded reciprocal of D, and the orbit's
+// share added to the thread's float-float sums.  The rounding errors are unbiased and average out
+// over the v^3 / 6 orbits of a triplet.
+__device__ __forceinline__ void et_orbit_f32(const float (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],
+                                             const float (*Oik)[3][ET_B * ET_B], const float (*Oij)[3][ET_B * ET_B],
+                                             const float (*ti)[ET_B], const float (*tj)[ET_B], const float (*tk)[ET_B],
+                                             const float2 (*evs)[ET_B], const float2* dab, bool all_on,
+                                             const int* slot_on, int la, int lb, int lc, int want_sens, ff& s4, ff& s5,
+                                             float& sens) {
+  constexpr int B = ET_B;
+  const int loc[3] = {la, lb, lc};
+  float     w[6], sg[6];
+#pragma unroll
+  for(int q = 0; q < 6; q++) {
+    const int p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
+    const int x = loc[p0], y = loc[p1], z = loc[p2];
+    w[q]  = W[q][kSwz(la, lb, lc)];
+    sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
+  }
+  const float ca = w[0] + w[3] + w[4], cb = w[1] + w[2] + w[5]; // the two cyclic classes
+  const float sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
+  float       zy4 = 0.f, zys = 0.f, sn = 0.f;
+#pragma unroll
+  for(int q = 0; q < 6; q++) {
+    if(!all_on && !slot_on[q]) continue;
+    const bool  in_a = q == 0 || q == 3 || q == 4;
+    const float z    = fmaf(3.f, w[q], in_a ? ca : cb);
+    const float y4   = fmaf(3.f, w[q], -(in_a ? cb : ca));
+    const float ys   = 3.f * sg[q] - (in_a ? sgb : sga);
+    zy4              = fmaf(z, y4, zy4);
+    zys              = fmaf(z, ys, zys);
+    if(want_sens) {
+      const float y5 = y4 + ys;
+      sn             = fmaf(18.f * y5, y5, fmaf(12.f * z, z, sn));
+    }
+  }
+  const float2 dd = dab[la * B + lb], ec = evs[2][lc];
+  const float  id = __frcp_rn(ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y}).hi); // 1 / D
+  s4   = ff_add_f(s4, zy4 * id);
+  s5   = ff_add_f(s5, (zy4 + zys) * id);
+  sens = fmaf(sn * id, id, sens);
+}
+
+// TP = float2: float-float partial arrays; TP = float: FP32 partial arrays
+template<typename TP>
+__device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, const TP* P12, const TP* P34, const TP* P56,
+                                                  int i, int j, int k, double* part, int gblock, int gsize) {
+  constexpr int  B = ET_B, B3 = B * B * B;
+  constexpr bool kF32 = std::is_same<TP, float>::value;
+  __shared__ TP  W[6][B3];               // [slot][a'][b'][c'] (a', b', c' local to the slot's blocks)
   __shared__ float  Ojk[3][3][B * B], Oik[3][3][B * B], Oij[3][3][B * B];
   __shared__ float  ti[3][B], tj[3][B], tk[3][B];
   __shared__ float2 evs[3][B];
@@ -223,10 +271,10 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     // handles local positions r = tid and tid + 256 of every slot: (slowest, middle, fastest)
     // local index of the pass's array = (r / 64, r / 8 % 8, r % 8).
     static_assert(6 * B3 == 12 * ET_THREADS, "two positions of each of the six cubes per thread");
-    float2*    Wf   = &W[0][0];
+    TP*        Wf   = &W[0][0];
     const bool full = rbn[0] == B && rbn[1] == B && rbn[2] == B;
     // pass p's loads (a thread's 12, all issued before any of them is used)
-    auto load_pass = [&](auto pass_tag, float2 (&x)[12], int (&widx)[12]) {
+    auto load_pass = [&](auto pass_tag, TP (&x)[12], int (&widx)[12]) {
       constexpr int pass = decltype(pass_tag)::value;
 #pragma unroll
       for(int it = 0; it < 12; it++) {
@@ -234,7 +282,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         const int P0 = kPerm(s, 0), P1 = kPerm(s, 1), P2 = kPerm(s, 2);
         const int f = r & 7, m = (r >> 3) & 7, sl = r >> 6;
         int       la, lb, lc; // slot-local (a', b', c'): a in block P0, b in P1, c in P2
-        const float2* src;
+        const TP* src;
         if(pass == 0) { // P12[a][c][b]: b fastest
           la = sl, lc = m, lb = f;
           src = P12;
@@ -248,7 +296,7 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
         // (sl, m, f) of this thread do not depend on the tile: local offset rel0 (+ 4 v^2 for r >= 256)
         const long long off = cube0[pass][s] + (it & 1 ? rel1 : rel0);
         const bool      ok  = full || (la < rbn[P0] && lb < rbn[P1] && lc < rbn[P2]);
-        x[it]               = ok ? src[off] : make_float2(0.f, 0.f);
+        x[it]               = ok ? src[off] : TP{};
         if(it & 1) {
           // r + 256 sets bit 2 of the pass's slowest coordinate (sl < 4 for r < 256); kSwz is
           // linear over GF(2) with disjoint fields, so the index changes by a constant XOR
@@ -262,11 +310,14 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
       }
     };
     // pass p's shared-memory updates
-    auto apply_pass = [&](auto pass_tag, const float2 (&x)[12], const int (&widx)[12]) {
+    auto apply_pass = [&](auto pass_tag, const TP (&x)[12], const int (&widx)[12]) {
       constexpr int pass = decltype(pass_tag)::value;
 #pragma unroll
       for(int it = 0; it < 12; it++) {
-        if(pass == 0) Wf[widx[it]] = x[it];
+        if constexpr(kF32) {
+          if(pass == 0) Wf[widx[it]] = x[it];
+          else Wf[widx[it]] += x[it];
+        } else if(pass == 0) Wf[widx[it]] = x[it];
         else if(pass == 1) { // two-sum of the high words, low words added; renormalised in pass 2
           const float2 o = Wf[widx[it]];
           const ff     h = ff_two_sum(o.x, x[it].x);
@@ -283,8 +334,8 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     // staging made cube0 visible, and the previous item's orbits finished with W before the
     // barrier at the top of the item.
     {
-      float2 x[12];
-      int    widx[12];
+      TP  x[12];
+      int widx[12];
       load_pass(std::integral_constant<int, 0>{}, x, widx);
       apply_pass(std::integral_constant<int, 0>{}, x, widx);
       load_pass(std::integral_constant<int, 1>{}, x, widx);
@@ -303,7 +354,10 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
     for(int r = tid; r < B3; r += ET_THREADS) {
       const int la = r / (B * B), lb = (r / B) % B, lc = r % B;
       if(la >= rbn[0] || lb >= rbn[1] || lc >= rbn[2]) continue;
-      et_orbit(W, Ojk, Oik, Oij, ti, tj, tk, evs, dab, all_on, slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
+      if constexpr(kF32)
+        et_orbit_f32(W, Ojk, Oik, Oij, ti, tj, tk, evs, dab, all_on, slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
+      else
+        et_orbit(W, Ojk, Oik, Oij, ti, tj, tk, evs, dab, all_on, slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
     }
   }
   CSum c4, c5;
@@ -326,27 +380,31 @@ __device__ __forceinline__ void energy_tiled_body(const TiledEnergyArgs& A, cons
   }
 }
 
+template<typename TP>
 static __global__ void __launch_bounds__(ET_THREADS, 4) energy_tiled_kernel(const __grid_constant__ TiledEnergyArgs A) {
-  energy_tiled_body(A, A.P12, A.P34, A.P56, A.i, A.j, A.k, A.part + 6 * (long long) blockIdx.x, blockIdx.x, gridDim.x);
+  energy_tiled_body<TP>(A, static_cast<const TP*>(A.P12), static_cast<const TP*>(A.P34), static_cast<const TP*>(A.P56),
+                        A.i, A.j, A.k, A.part + 6 * (long long) blockIdx.x, blockIdx.x, gridDim.x);
 }
 
 // Batched form: blockIdx.y = triplet slot; the triplet and its P arrays come from the batch
-// tables (4 ints per triplet: i, j, k, output index; P arrays of slot s at F + s * 3 v^3).
+// tables (4 ints per triplet: i, j, k, output index; P arrays of slot s at F + s * 3 v^3 elements
+// of TP: float2 for float-float, float for FP32 partial arrays).
 struct BatchEnergyArgs {
   TiledEnergyArgs base_args; // P12/P34/P56/i/j/k/part unused
   const int*      tri;
   const int*      base;
-  const float2*   F;
+  const void*     F;
   double*         part;      // [slot][gridDim.x][6]
 };
 
+template<typename TP>
 static __global__ void __launch_bounds__(ET_THREADS, 4) energy_tiled_batch_kernel(const __grid_constant__ BatchEnergyArgs A) {
   const int       slot = blockIdx.y, b0 = A.base ? *A.base : 0;
   const int*      tp   = A.tri + 4 * (b0 + slot);
   const long long v3   = (long long) A.base_args.v * A.base_args.v * A.base_args.v;
-  const float2*   F    = A.F + (long long) slot * 3 * v3;
-  energy_tiled_body(A.base_args, F, F + v3, F + 2 * v3, tp[0], tp[1], tp[2],
-                    A.part + 6 * ((long long) slot * gridDim.x + blockIdx.x), blockIdx.x, gridDim.x);
+  const TP*       F    = static_cast<const TP*>(A.F) + (long long) slot * 3 * v3;
+  energy_tiled_body<TP>(A.base_args, F, F + v3, F + 2 * v3, tp[0], tp[1], tp[2],
+                        A.part + 6 * ((long long) slot * gridDim.x + blockIdx.x), blockIdx.x, gridDim.x);
 }
 
 // Fixed-order parallel sum of per-CTA partials (6 doubles each) for one triplet -> out[2]

@@ -242,6 +242,11 @@ static __global__ void to_ff_kernel(const double* x, float2* y, long long n) {
   }
 }
 
+static __global__ void to_f32_kernel(const double* x, float* y, long long n) {
+  for(long long e = (long long) blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long) gridDim.x * blockDim.x)
+    y[e] = (float) x[e];
+}
+
 // Compensated fixed-order sum of per-triplet energies e[2 n] -> out[2].
 static __global__ void reduce_triplets_kernel(const double* e, long long n, double* out) {
   if(threadIdx.x != 0 || blockIdx.x != 0) return;

@@ -209,7 +209,8 @@ double ccsdt_handle::truncation_estimate(float tail_sq, double sens) const {
 extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccsdt_opts* opts, long n, const int* tri,
                                                       double* e_bracket, double* e_paren, double* est) {
   if(!h) return CCSDT_E_INVALID;
-  if(!opts || opts->mode != CCSDT_MODE_OZAKI || n < 0 || (n && (!tri || !e_paren || !est)))
+  if(!opts || opts->mode != CCSDT_MODE_OZAKI || opts->p_storage < 0 || opts->p_storage > 2 || n < 0 ||
+     (n && (!tri || !e_paren || !est)))
     return h->fail(CCSDT_E_INVALID, "ccsdt_triplet_error_estimates: needs CCSDT_MODE_OZAKI and output arrays");
   if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_triplet_error_estimates before ccsdt_upload");
   if(!h->pz_eligible(opts->slices, opts->slice_kind))
@@ -231,6 +232,7 @@ extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccs
      cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream) != cudaSuccess)
     return h->fail(CCSDT_E_CUDA, "estimate scratch init");
   h->force_mma_sync   = false;
+  h->p_storage = opts->p_storage;
   if((s = h->run_batched(opts->slices, n, tri, false, dtail, dsens))) return s;
   std::vector<double> E(2 * n), sens(n);
   std::vector<float>  tail(n);

@@ -64,6 +64,8 @@ struct PzParams {
   int             nslots;     // triplets per launch
   int             o, v, kp_v, kp_o;
   float2*         F;          // P arrays of slot s: F + s * 3 v^3 (P12, P34, P56 consecutive)
+  int             f32_out;    // store P rounded to FP32 (element e at ((float*) F)[e]) instead of
+                              // float-float (F[e])
   const unsigned* order;      // cost-ordered item ids, length nitems
   unsigned        nitems;
   unsigned*       queue;      // work counter, 0 at launch
@@ -181,7 +183,7 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
   const int       y = w.yb * PZ_BM + row, n0 = nb * NT + c_lo;
   (void) tp;
   // element (y, n) of the tile: P[n][x][y] (consecutive rows -> consecutive addresses)
-  float2* Cb = P.F + (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
+  const long long e0 = (long long) w.slot * 3 * v2 * v + (long long) w.job * v2 * v + (long long) w.x * v + y;
   float hi[COLS], lo[COLS];
   const int np_d = pz_npass(P.kp_v / KC, P.wst), np_l = pz_npass(P.kp_o / KC, P.wst);
 #pragma unroll 1
@@ -271,11 +273,19 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
     else run(true, false);
   }
   if(y < v) {
+    if(P.f32_out) { // one rounding of the float-float sum; the power-of-two scale is exact
+      float* Cf = reinterpret_cast<float*>(P.F) + e0;
 #pragma unroll
-    for(int e = 0; e < COLS; e++) {
-      const int   n = n0 + e;
-      const float h = hi[e] + lo[e];
-      if(n < v) Cb[(long long) n * v2] = make_float2(h * kScale, (lo[e] - (h - hi[e])) * kScale);
+      for(int e = 0; e < COLS; e++)
+        if(n0 + e < v) Cf[(long long) (n0 + e) * v2] = (hi[e] + lo[e]) * kScale;
+    } else {
+      float2* Cb = P.F + e0;
+#pragma unroll
+      for(int e = 0; e < COLS; e++) {
+        const int   n = n0 + e;
+        const float h = hi[e] + lo[e];
+        if(n < v) Cb[(long long) n * v2] = make_float2(h * kScale, (lo[e] - (h - hi[e])) * kScale);
+      }
     }
   }
   return true;

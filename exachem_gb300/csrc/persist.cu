@@ -118,16 +118,22 @@ ccsdt_status ccsdt_handle::ensure_batch(int S, int B) {
 
 // One full wave of the tiled energy kernels (resident CTAs per SM x SMs), capped at
 // kTiledBlocks: a grid-stride loop over more CTAs than fit at once would leave a partial wave.
-int ccsdt_handle::energy_grid() {
-  if(energy_grid_ > 0) return energy_grid_;
+int ccsdt_handle::energy_grid(bool f32) {
+  int& g = f32 ? energy_grid_f32_ : energy_grid_;
+  if(g > 0) return g;
   int sm = 0, per = 0, per1 = 0;
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tiled_batch_kernel, ET_THREADS, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, energy_tiled_kernel, ET_THREADS, 0);
-  per          = std::min(per, per1);
-  energy_grid_ = std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
+  if(f32) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tiled_batch_kernel<float>, ET_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, energy_tiled_kernel<float>, ET_THREADS, 0);
+  } else {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tiled_batch_kernel<float2>, ET_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, energy_tiled_kernel<float2>, ET_THREADS, 0);
+  }
+  per = std::min(per, per1);
+  g = std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
   cudaGetLastError();
-  return energy_grid_;
+  return g;
 }
 
 // Launch the sequence of one batch of `nslots` triplets starting at the device base counter.
@@ -144,6 +150,9 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   std::memcpy(p.maps, tmaps, sizeof(p.maps));
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F;
+  const bool f32 = p_f32(S);
+  p.f32_out      = f32;
+  last_p_f32     = f32;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
   // windows in multiples of 64 whatever the configuration's K chunk, so every configuration folds
   // the same windows and the energies stay bit-identical across configurations
@@ -186,8 +195,9 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
     ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
                                    o, v, 0, 0, 0, nullptr, sens != nullptr};
     ea.tri = bt_tri, ea.base = bt_ctrl + 2, ea.F = bt_F, ea.part = bt_part;
-    const int G = std::min(e_ntiles, energy_grid());
-    energy_tiled_batch_kernel<<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
+    const int G = std::min(e_ntiles, energy_grid(f32));
+    if(f32) energy_tiled_batch_kernel<float><<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
+    else energy_tiled_batch_kernel<float2><<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
     if(profiling) cudaEventRecord(prof_ev[3], stream);
     reduce_parts_batch_kernel<<<nslots, 256, 0, stream>>>(bt_part, G, bt_tri, bt_ctrl + 2, etrip, sens);
     if(advance) advance_base_kernel<<<1, 32, 0, stream>>>(bt_ctrl + 2, nslots);

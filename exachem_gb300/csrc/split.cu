@@ -640,11 +640,12 @@ ccsdt_status ccsdt_handle::check_device_error() {
   return CCSDT_OK;
 }
 
-ccsdt_status ccsdt_handle::launch_energy_tiled(int i, int j, int k, double* eout) {
-  const int       G = std::min(e_ntiles, energy_grid());
+ccsdt_status ccsdt_handle::launch_energy_tiled(int i, int j, int k, double* eout, bool f32) {
+  const int       G = std::min(e_ntiles, energy_grid(f32));
   TiledEnergyArgs ea{F12, F34, F56, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles, o, v, i, j, k, e_part,
                      cur_sens != nullptr};
-  energy_tiled_kernel<<<G, ET_THREADS, 0, stream>>>(ea);
+  if(f32) energy_tiled_kernel<float><<<G, ET_THREADS, 0, stream>>>(ea);
+  else energy_tiled_kernel<float2><<<G, ET_THREADS, 0, stream>>>(ea);
   if(profiling) cudaEventRecord(prof_ev[3], stream);
   reduce_parts_parallel_kernel<<<1, 256, 0, stream>>>(e_part, G, multiplicity(i, j, k) / 9.0, eout, cur_sens);
   cudaError_t e = cudaGetLastError();

@@ -81,7 +81,11 @@ typedef struct {
                           /* 5 (FP64 mode) the two-stage FP64 path: partial arrays, then energy  */
   int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
                              slice count they use, once per handle, before the timed work      */
-  int    reserved[3];
+  int    p_storage;       /* split path: element type of the triples' partial arrays between the
+                             contraction and the energy: 0 FP32 for 1..2 digit planes (whose own
+                             contraction error is ~100x FP32's rounding), float-float otherwise;
+                             1 float-float always; 2 FP32 always                               */
+  int    reserved[2];
 } ccsdt_opts;
 
 typedef struct {

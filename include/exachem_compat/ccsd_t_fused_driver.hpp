@@ -220,7 +220,8 @@ inline std::vector<float> read_slice_model(const std::string& path) {
 
 // Mode from the environment: EXACHEM_GB300_MODE = fp64 (default) | ozaki | learned,
 // EXACHEM_GB300_SLICES = digit planes (ozaki, default 3) or the largest count (learned, default 5),
-// EXACHEM_GB300_BUDGET = the learned mode's energy budget (default 1e-8).
+// EXACHEM_GB300_BUDGET = the learned mode's energy budget (default 1e-8),
+// EXACHEM_GB300_P_STORAGE = auto (default) | ff | f32: element type of the split path's partial arrays.
 inline ccsdt_opts opts_from_env() {
   ccsdt_opts  op{};
   const char* m = std::getenv("EXACHEM_GB300_MODE");
@@ -239,6 +240,12 @@ inline ccsdt_opts opts_from_env() {
   // split and learned modes: replay the call's per-batch launch sequence from a CUDA graph
   const char* gr = std::getenv("EXACHEM_GB300_GRAPH");
   op.use_graph   = gr ? std::atoi(gr) != 0 : 0;
+  const char* ps = std::getenv("EXACHEM_GB300_P_STORAGE");
+  std::string pst = ps ? ps : "auto";
+  if(pst == "auto") op.p_storage = 0;
+  else if(pst == "ff") op.p_storage = 1;
+  else if(pst == "f32") op.p_storage = 2;
+  else throw std::invalid_argument("EXACHEM_GB300_P_STORAGE must be auto, ff or f32: " + pst);
   return op;
 }
 

@@ -34,7 +34,7 @@ struct TiledIndexSpace {
 int main(int argc, char** argv) {
   if(argc > 1 && std::string(argv[1]) == "--opts") { // the options execute() takes from the environment
     const ccsdt_opts op = exachem_gb300::opts_from_env();
-    std::printf("%d %d %.3g %d %d\n", op.mode, op.slices, op.energy_budget, op.autotune, op.use_graph);
+    std::printf("%d %d %.3g %d %d %d\n", op.mode, op.slices, op.energy_budget, op.autotune, op.use_graph, op.p_storage);
     return 0;
   }
   if(argc > 1) { // never run: the point is that execute() compiles and links for T = double

@@ -240,9 +240,11 @@ def test_adapter_execute_compiles_with_the_reference_signature(tmp_path, built):
     def opts(**kw):
         out = subprocess.run([str(exe), "--opts"], check=True, capture_output=True, text=True,
                              env=env | {f"EXACHEM_GB300_{k}": v for k, v in kw.items()}).stdout.split()
-        return int(out[0]), int(out[1]), float(out[2]), int(out[3]), int(out[4])
-    assert opts() == (0, 3, 1e-8, 1, 0)                                  # fp64 drop-in, autotune on, no graph
-    assert opts(MODE="ozaki", SLICES="4", GRAPH="1") == (1, 4, 1e-8, 1, 1)
-    assert opts(MODE="learned", BUDGET="1e-9", AUTOTUNE="0") == (2, 5, 1e-9, 0, 0)
-    assert subprocess.run([str(exe), "--opts"], env=env | {"EXACHEM_GB300_MODE": "int4"},
-                          capture_output=True).returncode != 0
+        return int(out[0]), int(out[1]), float(out[2]), int(out[3]), int(out[4]), int(out[5])
+    assert opts() == (0, 3, 1e-8, 1, 0, 0)                               # fp64 drop-in, autotune on, no graph
+    assert opts(MODE="ozaki", SLICES="4", GRAPH="1") == (1, 4, 1e-8, 1, 1, 0)
+    assert opts(MODE="learned", BUDGET="1e-9", AUTOTUNE="0") == (2, 5, 1e-9, 0, 0, 0)
+    assert opts(MODE="ozaki", SLICES="2", P_STORAGE="ff")[5] == 1
+    assert opts(MODE="ozaki", SLICES="2", P_STORAGE="f32")[5] == 2
+    for bad in ({"EXACHEM_GB300_MODE": "int4"}, {"EXACHEM_GB300_P_STORAGE": "fp16"}):
+        assert subprocess.run([str(exe), "--opts"], env=env | bad, capture_output=True).returncode != 0

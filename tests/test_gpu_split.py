@@ -29,7 +29,7 @@ def _ft(o, v, seed, **kw):
 def test_tcgen05_equals_mma_sync_levels(built, o, v, seed):
     ft = _ft(o, v, seed)
     for S in (1, 2, 3, 4, 5):
-        tc = ft.energy("ozaki", slices=S)
+        tc = ft.energy("ozaki", slices=S, p_storage="ff")   # the other kernels keep float-float partial arrays
         leg = ft.energy("ozaki", slices=S, legacy_mma=1)
         assert tc["e_paren_T"] == pytest.approx(leg["e_paren_T"], rel=1e-13, abs=0)
         assert tc["e_bracket_T"] == pytest.approx(leg["e_bracket_T"], rel=1e-13, abs=0)
@@ -75,10 +75,12 @@ def test_persistent_queue_equals_per_triplet_tcgen05(built, o, v, seed):
     ft = _ft(o, v, seed)
     for S in (2, 3, 4):
         per = ft.energy("ozaki", slices=S, legacy_mma=2)
-        pers = ft.energy("ozaki", slices=S)
-        graph = ft.energy("ozaki", slices=S, use_graph=1)
+        pers = ft.energy("ozaki", slices=S, p_storage="ff")
+        graph = ft.energy("ozaki", slices=S, use_graph=1, p_storage="ff")
         assert pers["e_paren_T"] == pytest.approx(per["e_paren_T"], rel=1e-13, abs=0)
         assert graph["e_paren_T"] == pers["e_paren_T"]
+        # the default storage (FP32 partial arrays at S <= 2) through the graph as well
+        assert ft.energy("ozaki", slices=S, use_graph=1)["e_paren_T"] == ft.energy("ozaki", slices=S)["e_paren_T"]
 
 
 def test_persistent_batches_cover_every_triplet(built):
@@ -134,7 +136,7 @@ def test_split_large_v_against_oracle(built, o, v, seed, tri):
     f4, f5 = ft.triplet_energies(tri, "fp64")
     np.testing.assert_allclose(f5, w5, rtol=1e-11)
     np.testing.assert_allclose(f4, w4, rtol=1e-11)
-    for S, tol in ((3, 1e-6), (4, 1e-8)):
+    for S, tol in ((2, 2e-5), (3, 1e-6), (4, 1e-8)):
         s4, s5 = ft.triplet_energies(tri, "ozaki", slices=S)
         np.testing.assert_allclose(s5, w5, rtol=tol)
         np.testing.assert_allclose(s4, w4, rtol=tol)
@@ -152,6 +154,41 @@ def test_float_float_energy_stage_error(built, o, v, seed):
     got = ft.energy("ozaki", slices=1, legacy_mma=3)
     for key in ("e_bracket_T", "e_paren_T"):
         assert abs(got[key] - ref[key]) <= 2e-12 * abs(ref[key]), (key, got[key], ref[key])
+
+
+@pytest.mark.parametrize("o,v,seed", [(12, 70, 8), (4, 320, 9)])
+def test_fp32_energy_stage_error(built, o, v, seed):
+    """The FP32 form of the energy stage on its own: the FP64 contractions' P arrays rounded to
+    FP32 through the FP32 energy, against the FP64 energy of the same arrays.  Its error must sit
+    far below the two-plane contraction error it is used with (~1e-7 per triplet)."""
+    ft = _ft(o, v, seed)
+    ref = ft.energy("fp64")
+    got = ft.energy("ozaki", slices=1, legacy_mma=3, p_storage="f32")
+    for key in ("e_bracket_T", "e_paren_T"):
+        assert abs(got[key] - ref[key]) <= 1e-8 * abs(ref[key]), (key, got[key], ref[key])
+
+
+@pytest.mark.parametrize("o,v,seed", [(6, 40, 0), (5, 130, 2), (4, 320, 9)])
+def test_fp32_partial_arrays(built, o, v, seed):
+    """Partial arrays stored in FP32 (the default at one and two digit planes) against
+    float-float storage of the same contraction: the difference is the FP32 rounding, far below
+    the two-plane error; at S = 2 both stay within the split path's bound against FP64; the
+    debugging aid reads the FP32 arrays back."""
+    ft = _ft(o, v, seed)
+    ref = ft.energy("fp64")["e_paren_T"]
+    for S in (1, 2, 3):
+        a = ft.energy("ozaki", slices=S, p_storage="f32")
+        b = ft.energy("ozaki", slices=S, p_storage="ff")
+        for key in ("e_bracket_T", "e_paren_T"):
+            assert abs(a[key] - b[key]) <= 1e-8 * abs(b[key]), (S, key, a[key], b[key])
+    auto = ft.energy("ozaki", slices=2)["e_paren_T"]
+    assert auto == ft.energy("ozaki", slices=2, p_storage="f32")["e_paren_T"]
+    assert abs(auto - ref) <= BOUND[2] * abs(ref)
+    if v <= 130:
+        wf = ft.triplet_w(0, 1, 2, "ozaki", slices=2, p_storage="ff")
+        ws = ft.triplet_w(0, 1, 2, "ozaki", slices=2)
+        assert np.abs(ws - wf).max() <= 1e-6 * np.abs(wf).max()
+        assert np.abs(ws - wf).max() > 0      # the default really stored FP32
 
 
 def _set_window(ft, k):
