@@ -155,4 +155,13 @@ struct ccsdt_handle {
   ccsdt_status collect_phase_times();
   int          energy_grid_ = 0, energy_grid_f32_ = 0; // resident CTAs of the tiled energy kernels
   int          energy_grid(bool f32 = false);            // (one full wave)
+  // TMA map over the batch's partial arrays for energy_tma_batch_kernel (rebuilt when the batch
+  // scratch or the element type changes); false when the layout does not suit TMA
+  CUtensorMap  pmap;
+  const void*  pmap_base = nullptr;
+  int          pmap_B = 0, pmap_f32 = -1;
+  int          energy_tma_grid_[2] = {0, 0};
+  int          test_energy_passes = 0; // testing: 1 = the pass-by-pass energy kernel even where TMA suits
+  bool         ensure_pmap(bool f32);
+  int          energy_tma_grid(bool f32);
 };

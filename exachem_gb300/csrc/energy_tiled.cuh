@@ -63,30 +63,32 @@ __device__ __forceinline__ int perm_slot(int p0, int p1, int p2) {
   return p0 * 2 + (p1 > p2 ? 1 : 0);
 }
 
-// One orbit {a, b, c} of a work item: the index triple (la, lb, lc) local to the sorted block
-// triple (a' in block 0, b' in block 1, c' in block 2) and all six of its orderings, which live in
-// the six slots of W.  The six W values are read once, D is common to the orbit, and an ordering
-// counts only if its slot is a distinct ordered block triple (so every ordered (a, b, c) counts
-// once).  Adds the orbit's E[T] and E(T) terms to s4 / s5 and, with want_sens, its first-order
-// sensitivity to sens.
-__device__ __forceinline__ void et_orbit(const float2 (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],
-                                         const float (*Oik)[3][ET_B * ET_B], const float (*Oij)[3][ET_B * ET_B],
-                                         const float (*ti)[ET_B], const float (*tj)[ET_B], const float (*tk)[ET_B],
-                                         const float2 (*evs)[ET_B], const float2* dab, bool all_on, const int* slot_on,
-                                         int la, int lb, int lc, int want_sens, ff& s4, ff& s5, float& sens) {
+// Singles part of V at the six orderings of an orbit: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z
+// with (x, y, z) the ordering's local indices.
+__device__ __forceinline__ void et_singles(const float (*Ojk)[3][ET_B * ET_B], const float (*Oik)[3][ET_B * ET_B],
+                                           const float (*Oij)[3][ET_B * ET_B], const float (*ti)[ET_B],
+                                           const float (*tj)[ET_B], const float (*tk)[ET_B], int la, int lb, int lc,
+                                           float (&sg)[6]) {
   constexpr int B = ET_B;
   const int loc[3] = {la, lb, lc};
-  ff        w[6];
-  float     sg[6];
 #pragma unroll
   for(int q = 0; q < 6; q++) {
-    const int    p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
-    const int    x = loc[p0], y = loc[p1], z = loc[p2];
-    const float2 t = W[q][kSwz(la, lb, lc)]; // = W at (x, y, z) of slot q
-    w[q]           = ff{t.x, t.y};
-    // singles part of V_xyz: (jy|kz) t_i^x + (ix|kz) t_j^y + (ix|jy) t_k^z
+    const int p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
+    const int x = loc[p0], y = loc[p1], z = loc[p2];
     sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
   }
+}
+
+// One orbit {a, b, c} of a work item: the index triple (la, lb, lc) local to the sorted block
+// triple (a' in block 0, b' in block 1, c' in block 2) and all six of its orderings (the six
+// slots q; w[q] = W at the ordering's indices).  D is common to the orbit, and an ordering counts
+// only if its slot is a distinct ordered block triple (so every ordered (a, b, c) counts once).
+// Adds the orbit's E[T] and E(T) terms to s4 / s5 and, with want_sens, its first-order
+// sensitivity to sens.  Float-float W.
+__device__ __forceinline__ void et_orbit_values(const ff (&w)[6], const float (&sg)[6], const float2 (*evs)[ET_B],
+                                                const float2* dab, bool all_on, const int* slot_on, int la, int lb,
+                                                int lc, int want_sens, ff& s4, ff& s5, float& sens) {
+  constexpr int B = ET_B;
   // The six orderings form two cyclic classes, {q, yzx(q), zxy(q)} and the three orderings
   // one transposition away (xzy, yxz, zyx of q), which are the other class.  With the class
   // sums C: Z_q = 4 W_q + W_yzx + W_zxy = 3 W_q + C_own, Y_q = 3 V_q - C_other(V).
@@ -143,28 +145,33 @@ __device__ __forceinline__ void et_orbit(const float2 (*W)[ET_B * ET_B * ET_B], 
   sens = fmaf(sn * id.hi, id.hi, sens);
 }
 
+__device__ __forceinline__ void et_orbit(const float2 (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],
+                                         const float (*Oik)[3][ET_B * ET_B], const float (*Oij)[3][ET_B * ET_B],
+                                         const float (*ti)[ET_B], const float (*tj)[ET_B], const float (*tk)[ET_B],
+                                         const float2 (*evs)[ET_B], const float2* dab, bool all_on, const int* slot_on,
+                                         int la, int lb, int lc, int want_sens, ff& s4, ff& s5, float& sens) {
+  ff    w[6];
+  float sg[6];
+#pragma unroll
+  for(int q = 0; q < 6; q++) {
+    const float2 t = W[q][kSwz(la, lb, lc)]; // = W at the ordering's local (x, y, z) of slot q
+    w[q]           = ff{t.x, t.y};
+  }
+  et_singles(Ojk, Oik, Oij, ti, tj, tk, la, lb, lc, sg);
+  et_orbit_values(w, sg, evs, dab, all_on, slot_on, la, lb, lc, want_sens, s4, s5, sens);
+}
+
 // The same orbit from FP32 partial arrays (P stored rounded to FP32: the split path at few digit
 // planes, whose own contraction error is far above FP32's rounding).  Z and Y per ordering in FP32
 // (Z = 3 W + C_own, Y4 = 3 W - C_other directly: no class-sum identity, whose terms cancel), the
 // orbit's six products summed in FP32, one correctly rounded reciprocal of D, and the orbit's
 // share added to the thread's float-float sums.  The rounding errors are unbiased and average out
 // over the v^3 / 6 orbits of a triplet.
-__device__ __forceinline__ void et_orbit_f32(const float (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],
-                                             const float (*Oik)[3][ET_B * ET_B], const float (*Oij)[3][ET_B * ET_B],
-                                             const float (*ti)[ET_B], const float (*tj)[ET_B], const float (*tk)[ET_B],
-                                             const float2 (*evs)[ET_B], const float2* dab, bool all_on,
-                                             const int* slot_on, int la, int lb, int lc, int want_sens, ff& s4, ff& s5,
-                                             float& sens) {
+__device__ __forceinline__ void et_orbit_values_f32(const float (&w)[6], const float (&sg)[6],
+                                                    const float2 (*evs)[ET_B], const float2* dab, bool all_on,
+                                                    const int* slot_on, int la, int lb, int lc, int want_sens, ff& s4,
+                                                    ff& s5, float& sens) {
   constexpr int B = ET_B;
-  const int loc[3] = {la, lb, lc};
-  float     w[6], sg[6];
-#pragma unroll
-  for(int q = 0; q < 6; q++) {
-    const int p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
-    const int x = loc[p0], y = loc[p1], z = loc[p2];
-    w[q]  = W[q][kSwz(la, lb, lc)];
-    sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
-  }
   const float ca = w[0] + w[3] + w[4], cb = w[1] + w[2] + w[5]; // the two cyclic classes
   const float sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
   float       zy4 = 0.f, zys = 0.f, sn = 0.f;
@@ -187,6 +194,19 @@ __device__ __forceinline__ void et_orbit_f32(const float (*W)[ET_B * ET_B * ET_B
   s4   = ff_add_f(s4, zy4 * id);
   s5   = ff_add_f(s5, (zy4 + zys) * id);
   sens = fmaf(sn * id, id, sens);
+}
+
+__device__ __forceinline__ void et_orbit_f32(const float (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],
+                                             const float (*Oik)[3][ET_B * ET_B], const float (*Oij)[3][ET_B * ET_B],
+                                             const float (*ti)[ET_B], const float (*tj)[ET_B], const float (*tk)[ET_B],
+                                             const float2 (*evs)[ET_B], const float2* dab, bool all_on,
+                                             const int* slot_on, int la, int lb, int lc, int want_sens, ff& s4, ff& s5,
+                                             float& sens) {
+  float w[6], sg[6];
+#pragma unroll
+  for(int q = 0; q < 6; q++) w[q] = W[q][kSwz(la, lb, lc)];
+  et_singles(Ojk, Oik, Oij, ti, tj, tk, la, lb, lc, sg);
+  et_orbit_values_f32(w, sg, evs, dab, all_on, slot_on, la, lb, lc, want_sens, s4, s5, sens);
 }
 
 // TP = float2: float-float partial arrays; TP = float: FP32 partial arrays

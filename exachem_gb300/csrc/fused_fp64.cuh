@@ -19,7 +19,8 @@
 // Operands are read from L2 straight into the DMMA fragments (four consecutive kappa per row: one
 // 32-byte sector per fragment row): GB300's FP64 pipe retires ~3.5 flop per clock per SM, so each
 // SM needs only ~2 bytes per clock of operands and a staging copy through shared memory would buy
-// nothing.  Every unit costs 6 x 512 x (6 v + 6 o) multiply-adds.
+// nothing.  Every distinct cube costs 512 x (6 v + 6 o) multiply-adds; a unit with a repeated
+// block (X = Y or Y = Z) has equal cubes, computed once and read through `canon`.
 #pragma once
 
 #include "energy_tiled.cuh"
@@ -55,7 +56,7 @@ struct FusedArgs {
 static __global__ void __launch_bounds__(FX_THREADS, 3) t3_fused_fp64_kernel(const __grid_constant__ FusedArgs A) {
   constexpr int B = ET_B, B3 = B * B * B;
   __shared__ double W[6][B3];  // cube q: [a'][b'][c'] local to its blocks (blk(P0), blk(P1), blk(P2))
-  __shared__ int    slot_on[6];
+  __shared__ int    canon[6]; // first cube with the same ordered block triple (itself if distinct)
   __shared__ double red[4][FX_WARPS];
   const int        v = A.v, o = A.o, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int        g = lane >> 2, tq = lane & 3;
@@ -66,8 +67,18 @@ static __global__ void __launch_bounds__(FX_THREADS, 3) t3_fused_fp64_kernel(con
   for(int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
     const int3 tt  = A.tiles[tile];
     auto       blk = [&](int p) { return p == 0 ? tt.x : p == 1 ? tt.y : tt.z; }; // block at position p
+    if(tid < 6) { // a unit with a repeated block has equal cubes: each is computed and counted once
+      const int* P = c_perm[tid];
+      int        c = tid;
+      for(int p = tid - 1; p >= 0; p--) {
+        const int* Q = c_perm[p];
+        if(blk(P[0]) == blk(Q[0]) && blk(P[1]) == blk(Q[1]) && blk(P[2]) == blk(Q[2])) c = p;
+      }
+      canon[tid] = c;
+    }
+    __syncthreads();
     // ---------------------------------------------------------------- contractions: warp = cube q
-    {
+    if(canon[warp] == warp) {
       const int q = warp, P0 = c_perm[q][0], P1 = c_perm[q][1], P2 = c_perm[q][2];
       // first global index of role r (0 = a, 1 = b, 2 = c) and occupied index at position p, by
       // selects (a runtime index into a local array would live in local memory)
@@ -76,15 +87,6 @@ static __global__ void __launch_bounds__(FX_THREADS, 3) t3_fused_fp64_kernel(con
       auto      oc  = [&](int p) { return p == 0 ? A.i : p == 1 ? A.j : A.k; };
       double*   Wq    = W[q];
       for(int e = lane; e < B3; e += 32) Wq[e] = 0.0;
-      if(tid < 6) { // a cube counts once per distinct ordered block triple
-        const int* P  = c_perm[tid];
-        int        on = 1;
-        for(int p = 0; p < tid; p++) {
-          const int* Q = c_perm[p];
-          if(blk(P[0]) == blk(Q[0]) && blk(P[1]) == blk(Q[1]) && blk(P[2]) == blk(Q[2])) on = 0;
-        }
-        slot_on[tid] = on;
-      }
       __syncwarp();
 #pragma unroll 1
       for(int term = 0; term < 12; term++) {
@@ -131,18 +133,18 @@ static __global__ void __launch_bounds__(FX_THREADS, 3) t3_fused_fp64_kernel(con
         __syncwarp(); // the next term maps the cube's elements to other lanes
       }
     }
-    __syncthreads(); // all six cubes and slot_on are complete
+    __syncthreads(); // all distinct cubes are complete
     // ---------------------------------------------------------------- energy of the unit
     for(int e = tid; e < 6 * B3; e += FX_THREADS) {
       const int q = e / B3, r = e % B3;
-      if(!slot_on[q]) continue;
+      if(canon[q] != q) continue;
       const int* P  = c_perm[q];
       const int  la = r / (B * B), lb = (r / B) % B, lc = r % B;
       const int  a = blk(P[0]) * B + la, b = blk(P[1]) * B + lb, c = blk(P[2]) * B + lc;
       if(a >= v || b >= v || c >= v) continue;
       // W at the orderings of (a, b, c): the cube of the permuted positions, at the permuted local
       auto w_at = [&](int p0, int p1, int p2, int x, int y, int z) {
-        return W[kSlot(p0, p1, p2)][(x * B + y) * B + z];
+        return W[canon[kSlot(p0, p1, p2)]][(x * B + y) * B + z];
       };
       const double wabc = W[q][r];
       const double wbca = w_at(P[1], P[2], P[0], lb, lc, la), wcab = w_at(P[2], P[0], P[1], lc, la, lb);
@@ -161,7 +163,7 @@ static __global__ void __launch_bounds__(FX_THREADS, 3) t3_fused_fp64_kernel(con
       s4.add(z * y4 / d);
       s5.add(z * y5 / d);
     }
-    __syncthreads(); // the cubes are free for the next unit
+    __syncthreads(); // the cubes and canon are free for the next unit
   }
   // ---------------------------------------------------------------- fixed-order CTA reduction
 #pragma unroll

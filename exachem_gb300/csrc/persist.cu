@@ -18,6 +18,7 @@
 
 #include "ccsdt_internal.cuh"
 #include "energy_tiled.cuh"
+#include "energy_tma.cuh"
 #include "fp64_kernels.cuh"
 #include "oz_persist.cuh"
 #include "pz_confs.h"
@@ -136,6 +137,28 @@ int ccsdt_handle::energy_grid(bool f32) {
   return g;
 }
 
+int ccsdt_handle::energy_tma_grid(bool f32) {
+  int& g = energy_tma_grid_[f32 ? 1 : 0];
+  if(g > 0) return g;
+  int sm = 0, per = 0;
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+  // the float-float boxes (72 KB) exceed the default dynamic shared-memory limit
+  if(f32) {
+    cudaFuncSetAttribute(energy_tma_batch_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) em_smem_bytes<float>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tma_batch_kernel<float>, EM_THREADS,
+                                                  em_smem_bytes<float>());
+  } else {
+    cudaFuncSetAttribute(energy_tma_batch_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int) em_smem_bytes<float2>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tma_batch_kernel<float2>, EM_THREADS,
+                                                  em_smem_bytes<float2>());
+  }
+  g = std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
+  cudaGetLastError();
+  return g;
+}
+
 // Launch the sequence of one batch of `nslots` triplets starting at the device base counter.
 ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, bool advance, float* tails,
                                         double* sens) {
@@ -191,13 +214,25 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   if(profiling) cudaEventRecord(prof_ev[2], stream);
   if(tv[1]) cudaEventRecord(tv[1], stream);
   if(e == cudaSuccess) {
-    BatchEnergyArgs ea;
-    ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
-                                   o, v, 0, 0, 0, nullptr, sens != nullptr};
-    ea.tri = bt_tri, ea.base = bt_ctrl + 2, ea.F = bt_F, ea.part = bt_part;
-    const int G = std::min(e_ntiles, energy_grid(f32));
-    if(f32) energy_tiled_batch_kernel<float><<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
-    else energy_tiled_batch_kernel<float2><<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
+    int G = 0;
+    if(!test_energy_passes && ensure_pmap(f32)) {
+      // the partial arrays staged by TMA, eighteen 8 x 8 x 8 boxes per work unit
+      TmaEnergyArgs ta;
+      ta.pmap = pmap, ta.oovv = oovv_f, ta.t1 = t1_f, ta.eo = eo, ta.ev = ev, ta.tiles = (const int3*) e_tiles;
+      ta.ntiles = e_ntiles, ta.o = o, ta.v = v, ta.tri = bt_tri, ta.base = bt_ctrl + 2, ta.part = bt_part;
+      ta.want_sens = sens != nullptr, ta.err = d_err, ta.spin = sm100::kSpinLimit;
+      G = std::min(e_ntiles, energy_tma_grid(f32));
+      if(f32) energy_tma_batch_kernel<float><<<dim3(G, nslots), EM_THREADS, em_smem_bytes<float>(), stream>>>(ta);
+      else energy_tma_batch_kernel<float2><<<dim3(G, nslots), EM_THREADS, em_smem_bytes<float2>(), stream>>>(ta);
+    } else {
+      BatchEnergyArgs ea;
+      ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
+                                     o, v, 0, 0, 0, nullptr, sens != nullptr};
+      ea.tri = bt_tri, ea.base = bt_ctrl + 2, ea.F = bt_F, ea.part = bt_part;
+      G = std::min(e_ntiles, energy_grid(f32));
+      if(f32) energy_tiled_batch_kernel<float><<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
+      else energy_tiled_batch_kernel<float2><<<dim3(G, nslots), ET_THREADS, 0, stream>>>(ea);
+    }
     if(profiling) cudaEventRecord(prof_ev[3], stream);
     reduce_parts_batch_kernel<<<nslots, 256, 0, stream>>>(bt_part, G, bt_tri, bt_ctrl + 2, etrip, sens);
     if(advance) advance_base_kernel<<<1, 32, 0, stream>>>(bt_ctrl + 2, nslots);
@@ -423,6 +458,12 @@ extern "C" ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin
   if(!h) return CCSDT_E_INVALID;
   h->test_spin_limit = spin_limit;
   h->test_skip_loads = skip_loads ? 1 : 0;
+  return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_debug_set_energy_kernel(ccsdt_handle* h, int passes) {
+  if(!h || passes < 0 || passes > 1) return CCSDT_E_INVALID;
+  h->test_energy_passes = passes;
   return CCSDT_OK;
 }
 

@@ -413,6 +413,29 @@ bool encode_map(CUtensorMap* m, const void* base, int Kp, long long d1, long lon
 
 } // namespace
 
+// TMA map over the batch scratch's partial arrays: dims (v, v, v, 3 bt_B) of FP32 or float-float
+// (8-byte) elements, box 8 x 8 x 8 x 1, zero fill outside.  The row pitch must be a multiple of 16
+// bytes; out-of-range box elements are filled with zeros.
+bool ccsdt_handle::ensure_pmap(bool f32) {
+  if(!bt_F || bt_B <= 0 || v < ET_B) return false;
+  const long long es = f32 ? 4 : 8, vv = v;
+  if((vv * es) % 16) return false;
+  if(pmap_base == bt_F && pmap_B == bt_B && pmap_f32 == (int) f32) return true;
+  pmap_base      = nullptr;
+  auto fn        = encode_fn();
+  if(!fn) return false;
+  cuuint64_t dims[4]    = {(cuuint64_t) vv, (cuuint64_t) vv, (cuuint64_t) vv, (cuuint64_t) 3 * bt_B};
+  cuuint64_t strides[3] = {(cuuint64_t) (vv * es), (cuuint64_t) (vv * vv * es), (cuuint64_t) (vv * vv * vv * es)};
+  cuuint32_t box[4]     = {ET_B, ET_B, ET_B, 1};
+  cuuint32_t estr[4]    = {1, 1, 1, 1};
+  CUresult   r = fn(&pmap, f32 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, bt_F, dims,
+                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if(r != CUDA_SUCCESS) return false;
+  pmap_base = bt_F, pmap_B = bt_B, pmap_f32 = (int) f32;
+  return true;
+}
+
 // Tensor maps for S planes whose B-side box is NT rows of KC elements: NT and KC must equal the
 // N tile and K chunk of the kernel that will use them (its shared-memory B slot holds exactly
 // S x NT rows of 2 KC bytes).

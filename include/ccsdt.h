@@ -223,6 +223,12 @@ ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin_limit, int
  * exercise the window-by-window fold that long contractions (v beyond the exact window) need. */
 ccsdt_status ccsdt_debug_set_window(ccsdt_handle* h, int k);
 
+/* Testing: the persistent split-precision path's energy kernel.  0 (default): the partial arrays
+ * staged into shared memory by TMA tensor loads where their row pitch allows (v % 4 == 0 for FP32
+ * partial arrays, v even for float-float), else the pass-by-pass kernel; 1: the pass-by-pass
+ * kernel always (threads load the partial arrays and sum them into swizzled cubes). */
+ccsdt_status ccsdt_debug_set_energy_kernel(ccsdt_handle* h, int passes);
+
 /* Number of kernel launches issued by the last ccsdt_energy / ccsdt_triplet_energies. */
 long ccsdt_last_launch_count(const ccsdt_handle* h);
 

@@ -191,6 +191,28 @@ def test_fp32_partial_arrays(built, o, v, seed):
         assert np.abs(ws - wf).max() > 0      # the default really stored FP32
 
 
+@pytest.mark.parametrize("o,v,seed", [(6, 40, 0), (5, 132, 2), (4, 320, 9), (3, 130, 4)])
+def test_tma_energy_equals_pass_by_pass(built, o, v, seed):
+    """The energy kernel that stages the partial arrays by TMA against the pass-by-pass kernel, on
+    the same contraction: FP32 and float-float partial arrays, a ragged last block (v % 8 != 0)
+    and, at v = 130, a row pitch that FP32 TMA cannot take (float-float can).  The W values are
+    summed in the same order, so only the per-thread accumulation order differs."""
+    import ctypes
+    ft = _ft(o, v, seed)
+    lib = ft.lib
+    lib.ccsdt_debug_set_energy_kernel.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.ccsdt_debug_set_energy_kernel.restype = ctypes.c_int
+    tri = np.array([(0, 1, 2), (0, 0, 2), (1, 2, 2), (0, 1, o - 1)], dtype=np.int32)
+    for S, store in ((2, "f32"), (3, "ff"), (2, "ff")):
+        a4, a5 = ft.triplet_energies(tri, "ozaki", slices=S, p_storage=store)
+        assert lib.ccsdt_debug_set_energy_kernel(ft.h, 1) == 0
+        b4, b5 = ft.triplet_energies(tri, "ozaki", slices=S, p_storage=store)
+        assert lib.ccsdt_debug_set_energy_kernel(ft.h, 0) == 0
+        np.testing.assert_allclose(a5, b5, rtol=1e-12, atol=1e-13 * np.abs(b5).max())
+        np.testing.assert_allclose(a4, b4, rtol=1e-12, atol=1e-13 * np.abs(b4).max())
+    assert lib.ccsdt_debug_set_energy_kernel(ft.h, 2) != 0
+
+
 def _set_window(ft, k):
     import ctypes
     lib = ft.lib
