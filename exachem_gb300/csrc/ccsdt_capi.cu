@@ -105,17 +105,26 @@ ccsdt_handle::~ccsdt_handle() {
 }
 
 // Device arrays of the inputs (allocated once per handle).
-ccsdt_status ccsdt_handle::ensure_inputs() {
-  if(d_count) return CCSDT_OK; // the last one: every array is there
-  const size_t o = this->o, v = this->v;
-  const size_t n_t2 = o * o * v * v, n_ooov = o * o * o * v;
+ccsdt_status ccsdt_handle::ensure_inputs(long long nslab) {
+  const size_t    o = this->o, v = this->v;
+  const size_t    n_t2 = o * o * v * v, n_ooov = o * o * o * v;
+  const long long want = nslab < 0 ? (long long) o : nslab;
+  uploaded    = false;
+  ovvv_direct = nslab >= 0;
+  if(ovvv && ovvv_nslab != want) { // the other mode's ovvv: a different number of slabs
+    cudaFree(ovvv);
+    owned.erase(std::remove(owned.begin(), owned.end(), ovvv), owned.end());
+    ovvv = nullptr;
+  }
   // allocate each array still missing (a call that failed part-way may have left some)
   auto need = [&](double** p, size_t n) { return *p ? CCSDT_OK : alloc(p, n); };
   ccsdt_status s;
   if((s = need(&eo, o)) || (s = need(&ev, v)) || (s = need(&t1, o * v)) || (s = need(&t2, n_t2)) ||
-     (s = need(&oovv, n_t2)) || (s = need(&ooov, n_ooov)) || (s = need(&ovvv, o * v * v * v)) ||
+     (s = need(&oovv, n_t2)) || (s = need(&ooov, n_ooov)) || (s = need(&ovvv, (size_t) want * v * v * v)) ||
      (s = need(&t2h, n_t2)) || (s = need(&ooovh, n_ooov)))
     return s;
+  ovvv_nslab = want;
+  if(d_count) return CCSDT_OK;
   if(ccsdt::dev_malloc((void**) &d_count, sizeof(unsigned long long)) != cudaSuccess) {
     d_count = nullptr;
     cudaGetLastError();
@@ -133,9 +142,12 @@ ccsdt_status ccsdt_handle::finish_inputs(const char* who) {
     const double* p;
     size_t        n;
   } in[] = {{eo, o}, {ev, v}, {t1, o * v}, {t2, o * o * v * v}, {oovv, o * o * v * v}, {ooov, o * o * o * v},
-            {ovvv, o * v * v * v}};
+            // the direct mode forms ovvv later from the vectors, which are checked instead
+            {ovvv_direct ? chol_ov : ovvv, ovvv_direct ? o * v * (size_t) n_chol : o * v * v * v},
+            {ovvv_direct ? chol_vv : nullptr, ovvv_direct ? v * v * (size_t) n_chol : 0}};
   CK_H(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), stream));
   for(auto& c: in) {
+    if(!c.p) continue;
     nonfinite_count_kernel<<<1024, 256, 0, stream>>>(c.p, (long long) c.n, d_count);
     CK_H(cudaGetLastError());
   }
@@ -150,6 +162,8 @@ ccsdt_status ccsdt_handle::finish_inputs(const char* who) {
   if(bad) return fail(CCSDT_E_NONFINITE, std::string(who) + ": " + std::to_string(bad) + " non-finite input values");
   uploaded     = true;
   slices_ready = 0;
+  slabs.reset(o, ovvv_direct ? (int) ovvv_nslab : 0);
+  slab_sliced.assign(ovvv_direct ? ovvv_nslab : 0, 0);
   return CCSDT_OK;
 }
 

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "../../include/ccsdt.h"
+#include "ovvv_slabs.h"
 
 namespace ccsdt {
 // Every device allocation of the handle-based paths goes through here: cudaMalloc, except that a
@@ -66,11 +67,29 @@ struct ccsdt_handle {
   std::vector<double*> owned;
   std::vector<void*>   owned_bytes;
 
+  // Cholesky-direct mode (ccsdt_upload_cholesky_direct): (ia|bc) formed slab by slab (one occupied
+  // index: v^3 values) from the vectors into `ovvv`, which then holds ovvv_nslab slots
+  bool              ovvv_direct = false;
+  long long         ovvv_nslab  = 0;         // slabs `ovvv` holds (o outside the direct mode)
+  int               n_chol      = 0;
+  double *          chol_ov = nullptr, *chol_vv = nullptr; // L[i][a][Q], L[b][c][Q] (direct mode)
+  ccsdt::SlabCache  slabs;
+  std::vector<char> slab_sliced;             // the slot's digit planes are current
+  int*              d_slab_of   = nullptr;   // index -> slot table read by the contraction kernel
+  // makes the slabs of need[0..n) resident (formed and, with planes, sliced into digit planes)
+  // and the device table current; a no-op outside the direct mode
+  ccsdt_status      ensure_ovvv(const int* need, int n, bool planes);
+  const double*     ovvv_slab(int x) const {
+    return ovvv + (long long) (ovvv_direct ? slabs.slot(x) : x) * v * v * v;
+  }
+
   ~ccsdt_handle();
   ccsdt_status fail(ccsdt_status s, const std::string& msg);
   ccsdt_status alloc(double** p, size_t n);
   ccsdt_status ensure_scratch();
-  ccsdt_status ensure_inputs();
+  // nslab < 0: every array whole (ovvv = o slabs of v^3); nslab >= 3: the Cholesky-direct mode,
+  // ovvv a cache of nslab slabs formed from the vectors as the triplets need them
+  ccsdt_status ensure_inputs(long long nslab = -1);
   ccsdt_status finish_inputs(const char* who);
   // device-side retile of spin-orbital tile blocks (ccsdt_upload_blocks)
   double*      blk_stage = nullptr;    // device staging of a call's block data

@@ -14,11 +14,15 @@
 // over o v nQ + v^2 nQ + o^2 nQ doubles instead.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/ccsdt.h"
 #include "ccsdt_internal.cuh"
 #include "fp64_kernels.cuh"
+#include "ozaki.cuh"
 
 using namespace ccsdt;
 
@@ -52,20 +56,37 @@ cudaError_t gemm_abt(const double* A, const double* B, double* C, long long M, l
 
 } // namespace
 
-extern "C" ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
-                                             const double* t1, const double* t2, int n_chol,
-                                             const double* chol_oo, const double* chol_ov, const double* chol_vv,
-                                             int on_device) {
+// nslab < 0: every block built whole; nslab >= 3: the Cholesky-direct mode (ovvv a cache of nslab
+// slabs formed later by ensure_ovvv from persistent copies of L_ov and L_vv)
+static ccsdt_status upload_cholesky(ccsdt_handle* h, const char* who, const double* eps_occ, const double* eps_vir,
+                                    const double* t1, const double* t2, int n_chol, const double* chol_oo,
+                                    const double* chol_ov, const double* chol_vv, int on_device, long long nslab) {
   if(!h) return CCSDT_E_INVALID;
   if(!eps_occ || !eps_vir || !t1 || !t2 || !chol_oo || !chol_ov || !chol_vv)
-    return h->fail(CCSDT_E_INVALID, "ccsdt_upload_cholesky: null input pointer");
-  if(n_chol <= 0) return h->fail(CCSDT_E_INVALID, "ccsdt_upload_cholesky: n_chol must be positive");
+    return h->fail(CCSDT_E_INVALID, std::string(who) + ": null input pointer");
+  if(n_chol <= 0) return h->fail(CCSDT_E_INVALID, std::string(who) + ": n_chol must be positive");
   if(cudaSetDevice(h->device) != cudaSuccess) return h->fail(CCSDT_E_CUDA, "cudaSetDevice");
+  const long long o = h->o, v = h->v, nq = n_chol;
+  // the direct mode's persistent vectors (dropped by any other upload)
+  for(double** p: {&h->chol_ov, &h->chol_vv})
+    if(*p) {
+      cudaFree(*p);
+      *p = nullptr;
+    }
+  h->n_chol = 0;
   ccsdt_status s;
-  if((s = h->ensure_inputs())) return s;
+  if((s = h->ensure_inputs(nslab))) return s;
   h->blocks_open = false;
   h->uploaded    = false;
-  const long long o = h->o, v = h->v, nq = n_chol;
+  if(nslab >= 0) {
+    if(ccsdt::dev_malloc((void**) &h->chol_ov, o * v * nq * sizeof(double)) != cudaSuccess ||
+       ccsdt::dev_malloc((void**) &h->chol_vv, v * v * nq * sizeof(double)) != cudaSuccess ||
+       (!h->d_slab_of && ccsdt::dev_malloc((void**) &h->d_slab_of, o * sizeof(int)) != cudaSuccess)) {
+      cudaGetLastError();
+      return h->fail(CCSDT_E_OOM, std::string(who) + ": cudaMalloc of the Cholesky vectors failed");
+    }
+    h->n_chol = n_chol;
+  }
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   cudaError_t e = cudaSuccess;
   struct {
@@ -78,7 +99,19 @@ extern "C" ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps
   // the vectors on the device (copied from the host into one scratch allocation when needed)
   const double *L_oo = chol_oo, *L_ov = chol_ov, *L_vv = chol_vv;
   double*       scratch = nullptr;
-  if(e == cudaSuccess && !on_device) {
+  if(e == cudaSuccess && nslab >= 0) { // the direct mode keeps L_ov and L_vv
+    e = cudaMemcpyAsync(h->chol_ov, chol_ov, o * v * nq * sizeof(double), kind, h->stream);
+    if(e == cudaSuccess) e = cudaMemcpyAsync(h->chol_vv, chol_vv, v * v * nq * sizeof(double), kind, h->stream);
+    L_ov = h->chol_ov, L_vv = h->chol_vv;
+    if(e == cudaSuccess && !on_device) {
+      if(ccsdt::dev_malloc((void**) &scratch, o * o * nq * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        return h->fail(CCSDT_E_OOM, std::string(who) + ": cudaMalloc of the occupied-occupied vectors failed");
+      }
+      e    = cudaMemcpyAsync(scratch, chol_oo, o * o * nq * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+      L_oo = scratch;
+    }
+  } else if(e == cudaSuccess && !on_device) {
     const long long n_oo = o * o * nq, n_ov = o * v * nq, n_vv = v * v * nq;
     if(ccsdt::dev_malloc((void**) &scratch, (n_oo + n_ov + n_vv) * sizeof(double)) != cudaSuccess) {
       cudaGetLastError();
@@ -93,7 +126,7 @@ extern "C" ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps
     if(e == cudaSuccess) e = cudaMemcpyAsync(d_vv, chol_vv, n_vv * sizeof(double), cudaMemcpyHostToDevice, h->stream);
     L_oo = d_oo, L_ov = d_ov, L_vv = d_vv;
   }
-  if(e == cudaSuccess) e = gemm_abt(L_ov, L_vv, h->ovvv, o * v, v * v, (int) nq, h->stream); // (ia|bc)
+  if(e == cudaSuccess && nslab < 0) e = gemm_abt(L_ov, L_vv, h->ovvv, o * v, v * v, (int) nq, h->stream); // (ia|bc)
   if(e == cudaSuccess) e = gemm_abt(L_oo, L_ov, h->ooov, o * o, o * v, (int) nq, h->stream); // (ij|ka)
   if(e == cudaSuccess) e = gemm_abt(L_ov, L_ov, h->t2h, o * v, o * v, (int) nq, h->stream);  // [(i,a)][(j,b)]
   if(e == cudaSuccess) {
@@ -102,6 +135,92 @@ extern "C" ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps
   }
   if(e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if(scratch) cudaFree(scratch);
-  if(e != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string("ccsdt_upload_cholesky: ") + cudaGetErrorString(e));
-  return h->finish_inputs("ccsdt_upload_cholesky");
+  if(e != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string(who) + ": " + cudaGetErrorString(e));
+  return h->finish_inputs(who);
+}
+
+extern "C" ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
+                                             const double* t1, const double* t2, int n_chol,
+                                             const double* chol_oo, const double* chol_ov, const double* chol_vv,
+                                             int on_device) {
+  return upload_cholesky(h, "ccsdt_upload_cholesky", eps_occ, eps_vir, t1, t2, n_chol, chol_oo, chol_ov, chol_vv,
+                         on_device, -1);
+}
+
+extern "C" ccsdt_status ccsdt_upload_cholesky_direct(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
+                                                    const double* t1, const double* t2, int n_chol,
+                                                    const double* chol_oo, const double* chol_ov,
+                                                    const double* chol_vv, int on_device, int max_ovvv_slabs) {
+  if(h && (max_ovvv_slabs < 3))
+    return h->fail(CCSDT_E_INVALID, "ccsdt_upload_cholesky_direct: max_ovvv_slabs must be at least 3");
+  if(h) max_ovvv_slabs = std::min(max_ovvv_slabs, std::max(h->o, 3));
+  return upload_cholesky(h, "ccsdt_upload_cholesky_direct", eps_occ, eps_vir, t1, t2, n_chol, chol_oo, chol_ov,
+                         chol_vv, on_device, max_ovvv_slabs);
+}
+
+// Forms the missing slabs (index x into slot c: (x a|b c) = sum_Q L[x][a][Q] L[b][c][Q], one DMMA
+// GEMM of v x v^2 x n_chol), slices them into the digit-plane slots when `planes`, and updates
+// the device index -> slot table.  Stream-ordered: a slot is overwritten only after the kernels
+// launched before on the handle's stream have finished reading it.
+ccsdt_status ccsdt_handle::ensure_ovvv(const int* need, int n, bool planes) {
+  if(!ovvv_direct) return CCSDT_OK;
+  std::vector<std::pair<int, int>> todo;
+  if(!slabs.require(need, n, todo))
+    return fail(CCSDT_E_INVALID, "more distinct occupied indices at once than (ia|bc) slab slots");
+  const long long vv = v, v3 = vv * vv * vv;
+  for(auto& xc: todo) {
+    cudaError_t e = gemm_abt(chol_ov + (long long) xc.first * vv * n_chol, chol_vv, ovvv + xc.second * v3, vv, vv * vv,
+                             n_chol, stream);
+    if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("(ia|bc) slab: ") + cudaGetErrorString(e));
+    slab_sliced[xc.second] = 0;
+    launches++;
+  }
+  if(planes) {
+    if(!sl_ovvv || slices_ready <= 0 || slice_variant != 0)
+      return fail(CCSDT_E_STATE, "(ia|bc) slab planes asked for before the BF16 slicing");
+    for(int q = 0; q < n; q++) {
+      const int c = slabs.slot(need[q]);
+      if(slab_sliced[c]) continue;
+      oz_slice_rows_kernel<__nv_bfloat16><<<2048, 256, 0, stream>>>(
+        ovvv + c * v3, vv * vv, v, kp_v, slices_ready, (__nv_bfloat16*) sl_ovvv + (long long) c * vv * vv * kp_v,
+        pl_ovvv, ex_ovvv + (long long) c * vv * vv);
+      cudaError_t e = cudaGetLastError();
+      if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("(ia|bc) slab slicing: ") + cudaGetErrorString(e));
+      slab_sliced[c] = 1;
+      launches++;
+    }
+  }
+  if(!todo.empty()) { // pageable source: the copy is staged before the call returns
+    const std::vector<int>& tab = slabs.slots();
+    if(cudaMemcpyAsync(d_slab_of, tab.data(), tab.size() * sizeof(int), cudaMemcpyHostToDevice, stream) != cudaSuccess)
+      return fail(CCSDT_E_CUDA, "(ia|bc) slot table upload");
+  }
+  return CCSDT_OK;
+}
+
+extern "C" long ccsdt_ovvv_slab_builds(const ccsdt_handle* h) { return h ? h->slabs.builds() : -1; }
+
+extern "C" ccsdt_status ccsdt_debug_slab_schedule(int o, int max_ovvv_slabs, int batch, long n, const int* tri,
+                                                 long* order, long* builds) {
+  if(o <= 0 || max_ovvv_slabs < 3 || batch <= 0 || 3 * batch > max_ovvv_slabs || n < 0 || (n && (!tri || !order)) ||
+     !builds)
+    return CCSDT_E_INVALID;
+  for(long t = 0; t < n; t++)
+    if(!(0 <= tri[3 * t] && tri[3 * t] <= tri[3 * t + 1] && tri[3 * t + 1] <= tri[3 * t + 2] && tri[3 * t + 2] < o))
+      return CCSDT_E_INVALID;
+  const std::vector<long> ord = ccsdt::slab_order(tri, n, max_ovvv_slabs);
+  ccsdt::SlabCache        cache;
+  cache.reset(o, max_ovvv_slabs);
+  std::vector<std::pair<int, int>> todo;
+  for(long b0 = 0; b0 < n; b0 += batch) {
+    std::vector<int> need;
+    for(long t = b0; t < std::min(n, b0 + batch); t++)
+      for(int q = 0; q < 3; q++) need.push_back(tri[3 * ord[t] + q]);
+    if(!cache.require(need.data(), (int) need.size(), todo)) return CCSDT_E_STATE;
+    for(int x: need)
+      if(cache.slot(x) < 0 || cache.owner(cache.slot(x)) != x) return CCSDT_E_STATE;
+  }
+  for(long t = 0; t < n; t++) order[t] = ord[t];
+  *builds = cache.builds();
+  return CCSDT_OK;
 }

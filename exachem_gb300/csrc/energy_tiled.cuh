@@ -75,7 +75,8 @@ __device__ __forceinline__ void et_singles(const float (*Ojk)[3][ET_B * ET_B], c
   for(int q = 0; q < 6; q++) {
     const int p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
     const int x = loc[p0], y = loc[p1], z = loc[p2];
-    sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
+    sg[q] = __fmaf_rn(Ojk[p1][p2][y * B + z], ti[p0][x],
+                      __fmaf_rn(Oik[p0][p2][x * B + z], tj[p1][y], __fmul_rn(Oij[p0][p1][x * B + y], tk[p2][z])));
   }
 }
 
@@ -106,12 +107,13 @@ __device__ __forceinline__ void et_orbit_values(const ff (&w)[6], const float (&
 #pragma unroll
     for(int q = 0; q < 6; q++) {
       const bool  in_a = q == 0 || q == 3 || q == 4;
-      const float ys   = 3.f * sg[q] - (in_a ? sgb : sga);
+      const float ys   = __fmaf_rn(3.f, sg[q], -(in_a ? sgb : sga));
       sqa.add_sq(w[q]);
       wya.add_mul_f(w[q], ys);
       if(want_sens) { // the estimate needs Z and Y only to float precision
-        const float z = 3.f * w[q].hi + (in_a ? ca.hi : cb.hi), y5 = 3.f * w[q].hi - (in_a ? cb.hi : ca.hi) + ys;
-        sn = fmaf(18.f * y5, y5, fmaf(12.f * z, z, sn));
+        const float z  = __fmaf_rn(3.f, w[q].hi, in_a ? ca.hi : cb.hi);
+        const float y5 = __fadd_rn(__fmaf_rn(3.f, w[q].hi, -(in_a ? cb.hi : ca.hi)), ys);
+        sn = __fmaf_rn(__fmul_rn(18.f, y5), y5, __fmaf_rn(__fmul_rn(12.f, z), z, sn));
       }
     }
     const ff sq = sqa.get(), wy = wya.get();
@@ -126,15 +128,15 @@ __device__ __forceinline__ void et_orbit_values(const ff (&w)[6], const float (&
     const ff    t3 = ff_mul_f(w[q], 3.f);
     const ff    z  = ff_add(t3, in_a ? ca : cb);
     const ff    y4 = ff_add(t3, ff_neg(in_a ? cb : ca));
-    const float ys = 3.f * sg[q] - (in_a ? sgb : sga);   // singles part of Y
+    const float ys = __fmaf_rn(3.f, sg[q], -(in_a ? sgb : sga)); // singles part of Y
     zy4 = ff_add(zy4, ff_mul(z, y4));
     zys = ff_add(zys, ff_mul_f(z, ys));
     // first-order sensitivity to errors in W: W_abc enters Z_abc (x4), Z_bca, Z_cab and,
     // through V, Y_abc (x3), Y_acb, Y_bac, Y_cba; with uncorrelated signs
     //   |dE/dW|^2 ~ (16 + 1 + 1) Y^2 / D^2 + (9 + 1 + 1 + 1) Z^2 / D^2
     if(want_sens) {
-      const float y5 = y4.hi + ys;
-      sn = fmaf(18.f * y5, y5, fmaf(12.f * z.hi, z.hi, sn));
+      const float y5 = __fadd_rn(y4.hi, ys);
+      sn = __fmaf_rn(__fmul_rn(18.f, y5), y5, __fmaf_rn(__fmul_rn(12.f, z.hi), z.hi, sn));
     }
   }
   const ff zy5 = ff_add(zy4, zys);
@@ -142,7 +144,7 @@ __device__ __forceinline__ void et_orbit_values(const ff (&w)[6], const float (&
   const ff     id = ff_div_fast(ff{1.f, 0.f}, ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y})); // 1 / D (orbit-wide)
   s4   = ff_add(s4, ff_mul(zy4, id));
   s5   = ff_add(s5, ff_mul(zy5, id));
-  sens = fmaf(sn * id.hi, id.hi, sens);
+  sens = __fmaf_rn(__fmul_rn(sn, id.hi), id.hi, sens);
 }
 
 __device__ __forceinline__ void et_orbit(const float2 (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],
@@ -179,21 +181,21 @@ __device__ __forceinline__ void et_orbit_values_f32(const float (&w)[6], const f
   for(int q = 0; q < 6; q++) {
     if(!all_on && !slot_on[q]) continue;
     const bool  in_a = q == 0 || q == 3 || q == 4;
-    const float z    = fmaf(3.f, w[q], in_a ? ca : cb);
-    const float y4   = fmaf(3.f, w[q], -(in_a ? cb : ca));
-    const float ys   = 3.f * sg[q] - (in_a ? sgb : sga);
-    zy4              = fmaf(z, y4, zy4);
-    zys              = fmaf(z, ys, zys);
+    const float z    = __fmaf_rn(3.f, w[q], in_a ? ca : cb);
+    const float y4   = __fmaf_rn(3.f, w[q], -(in_a ? cb : ca));
+    const float ys   = __fmaf_rn(3.f, sg[q], -(in_a ? sgb : sga));
+    zy4              = __fmaf_rn(z, y4, zy4);
+    zys              = __fmaf_rn(z, ys, zys);
     if(want_sens) {
-      const float y5 = y4 + ys;
-      sn             = fmaf(18.f * y5, y5, fmaf(12.f * z, z, sn));
+      const float y5 = __fadd_rn(y4, ys);
+      sn             = __fmaf_rn(__fmul_rn(18.f, y5), y5, __fmaf_rn(__fmul_rn(12.f, z), z, sn));
     }
   }
   const float2 dd = dab[la * B + lb], ec = evs[2][lc];
   const float  id = __frcp_rn(ff_add(ff{dd.x, dd.y}, ff{-ec.x, -ec.y}).hi); // 1 / D
-  s4   = ff_add_f(s4, zy4 * id);
-  s5   = ff_add_f(s5, (zy4 + zys) * id);
-  sens = fmaf(sn * id, id, sens);
+  s4   = ff_add_f(s4, __fmul_rn(zy4, id));
+  s5   = ff_add_f(s5, __fmul_rn(__fadd_rn(zy4, zys), id));
+  sens = __fmaf_rn(__fmul_rn(sn, id), id, sens);
 }
 
 __device__ __forceinline__ void et_orbit_f32(const float (*W)[ET_B * ET_B * ET_B], const float (*Ojk)[3][ET_B * ET_B],

@@ -23,6 +23,9 @@ constexpr int OZ_BITS = 7;
 constexpr int OZ_MAX_SLICES = 8;
 
 // ---------------------------------------------------------------------------------- float-float
+// Products and sums that feed error terms are written with the _rn intrinsics, which the compiler
+// never contracts into fused multiply-adds, so every kernel that inlines these helpers rounds the
+// same way.
 struct ff {
   float hi, lo;
 };
@@ -46,17 +49,17 @@ __device__ __forceinline__ ff ff_add_f(ff a, float b) {
 // a * s for any float s: error-free product of the high word (fma), so the result keeps
 // float-float precision (for s = 3, say, a.hi * s alone would round at 2^-25)
 __device__ __forceinline__ ff ff_mul_f(ff a, float s) {
-  const float p = a.hi * s, e = fmaf(a.hi, s, -p);
-  const float lo = fmaf(a.lo, s, e);
-  const float hi = p + lo;
+  const float p = __fmul_rn(a.hi, s), e = __fmaf_rn(a.hi, s, -p);
+  const float lo = __fmaf_rn(a.lo, s, e);
+  const float hi = __fadd_rn(p, lo);
   return ff{hi, lo - (hi - p)};
 }
 __device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
-  float p = a.hi * b.hi;
-  float e = fmaf(a.hi, b.hi, -p);
-  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
-  float hi = p + e;
+  float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+  float hi = __fadd_rn(p, e);
   return ff{hi, e - (hi - p)};
 }
 // a / b from an approximate reciprocal (__fdividef: a few ulp) and one float-float correction
@@ -64,10 +67,10 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
 // relative error ~2^-44, at a fraction of the cost of two IEEE divisions.
 __device__ __forceinline__ ff ff_div_fast(ff a, ff b) {
   const float rb = __fdividef(1.f, b.hi);
-  const float q1 = a.hi * rb;
+  const float q1 = __fmul_rn(a.hi, rb);
   const ff    r  = ff_add(a, ff_neg(ff_mul(ff{q1, 0.f}, b)));
-  const float q2 = r.hi * rb;
-  const float h  = q1 + q2;
+  const float q2 = __fmul_rn(r.hi, rb);
+  const float h  = __fadd_rn(q1, q2);
   return ff{h, q2 - (h - q1)};
 }
 // Running float-float sum of products p + e (p rounded, e its error and low-order terms):
@@ -80,12 +83,12 @@ struct ffacc {
     hi = s;
   }
   __device__ __forceinline__ void add_sq(ff w) { // + w^2
-    const float p = w.hi * w.hi;
-    add(p, fmaf(w.hi, w.hi, -p) + 2.f * w.hi * w.lo);
+    const float p = __fmul_rn(w.hi, w.hi);
+    add(p, __fadd_rn(__fmaf_rn(w.hi, w.hi, -p), __fmul_rn(__fmul_rn(2.f, w.hi), w.lo)));
   }
   __device__ __forceinline__ void add_mul_f(ff w, float y) { // + w y
-    const float p = w.hi * y;
-    add(p, fmaf(w.hi, y, -p) + w.lo * y);
+    const float p = __fmul_rn(w.hi, y);
+    add(p, __fadd_rn(__fmaf_rn(w.hi, y, -p), __fmul_rn(w.lo, y)));
   }
   __device__ __forceinline__ ff get() const {
     const float h = hi + lo;
