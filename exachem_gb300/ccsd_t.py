@@ -55,7 +55,8 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_set_phase_timing", "ccsdt_phase_times", "ccsdt_triplet_error_estimates",
             "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky",
             "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config", "ccsdt_energy_spin_orbital",
-            "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so"]
+            "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so", "ccsdt_upload_cholesky_direct",
+            "ccsdt_ovvv_slab_builds", "ccsdt_debug_slab_schedule"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
@@ -82,6 +83,12 @@ def load_library(path: str | os.PathLike | None = None):
                                         ctypes.c_longlong, ctypes.c_int]
     lib.ccsdt_upload_end.argtypes = [vp]
     lib.ccsdt_upload_cholesky.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int]
+    lib.ccsdt_upload_cholesky_direct.argtypes = [vp, vp, vp, vp, vp, ctypes.c_int, vp, vp, vp, ctypes.c_int,
+                                                 ctypes.c_int]
+    lib.ccsdt_ovvv_slab_builds.argtypes = [vp]
+    lib.ccsdt_ovvv_slab_builds.restype = ctypes.c_long
+    lib.ccsdt_debug_slab_schedule.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_long, ip,
+                                              ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
     lib.ccsdt_tile_configs.argtypes = [ctypes.c_int, ip, ip]
     lib.ccsdt_autotune.argtypes = [vp, ctypes.c_int, dp, ip, ip]
     lib.ccsdt_set_tile_config.argtypes = [vp, ctypes.c_int, ctypes.c_int]
@@ -106,7 +113,8 @@ def load_library(path: str | os.PathLike | None = None):
                  "ccsdt_shard_triplets", "ccsdt_set_phase_timing", "ccsdt_phase_times",
                  "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end",
                  "ccsdt_upload_cholesky", "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config",
-                 "ccsdt_energy_spin_orbital", "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so"):
+                 "ccsdt_energy_spin_orbital", "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so",
+                 "ccsdt_upload_cholesky_direct", "ccsdt_debug_slab_schedule"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -190,9 +198,11 @@ class FusedTriples:
         self._keep = arrs
         self._check(self.lib.ccsdt_upload(self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs], on_dev))
 
-    def upload_cholesky(self, eps_occ, eps_vir, t1, t2, chol_oo, chol_ov, chol_vv):
+    def upload_cholesky(self, eps_occ, eps_vir, t1, t2, chol_oo, chol_ov, chol_vv, max_ovvv_slabs=None):
         """Inputs with oovv / ooov / ovvv built on the device from spatial Cholesky vectors
-        chol_oo[o][o][Q], chol_ov[o][v][Q], chol_vv[v][v][Q] (all on the host or all on the device)."""
+        chol_oo[o][o][Q], chol_ov[o][v][Q], chol_vv[v][v][Q] (all on the host or all on the device).
+        max_ovvv_slabs: the Cholesky-direct mode, (ia|bc) formed slab by slab into a cache of that
+        many v^3 slabs (ccsdt_upload_cholesky_direct)."""
         arrs = [eps_occ, eps_vir, t1, t2, chol_oo, chol_ov, chol_vv]
         on_dev = 0 if isinstance(arrs[0], np.ndarray) else 1
         if any((isinstance(a, np.ndarray)) != (on_dev == 0) for a in arrs):
@@ -201,8 +211,17 @@ class FusedTriples:
             arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in arrs]
         n_chol = int(arrs[4].shape[-1])
         self._keep = arrs
-        self._check(self.lib.ccsdt_upload_cholesky(self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs[:4]], n_chol,
-                                                   *[ctypes.c_void_p(_ptr(a)) for a in arrs[4:]], on_dev))
+        if max_ovvv_slabs is None:
+            self._check(self.lib.ccsdt_upload_cholesky(self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs[:4]], n_chol,
+                                                       *[ctypes.c_void_p(_ptr(a)) for a in arrs[4:]], on_dev))
+        else:
+            self._check(self.lib.ccsdt_upload_cholesky_direct(
+                self.h, *[ctypes.c_void_p(_ptr(a)) for a in arrs[:4]], n_chol,
+                *[ctypes.c_void_p(_ptr(a)) for a in arrs[4:]], on_dev, int(max_ovvv_slabs)))
+
+    def ovvv_slab_builds(self) -> int:
+        """(ia|bc) slabs formed since the last upload (Cholesky-direct mode)."""
+        return int(self.lib.ccsdt_ovvv_slab_builds(self.h))
 
     @staticmethod
     def tile_configs(slices: int) -> list[tuple[int, int, int]]:
@@ -346,6 +365,21 @@ class FusedTriples:
             self.close()
         except Exception:
             pass
+
+
+def slab_schedule(o: int, max_ovvv_slabs: int, batch: int, triplets) -> tuple[np.ndarray, int]:
+    """The Cholesky-direct mode's triplet order and slab count for a cache of max_ovvv_slabs slabs
+    and batches of `batch` triplets (host only, ccsdt_debug_slab_schedule)."""
+    lib = load_library()
+    tri = np.ascontiguousarray(np.asarray(triplets, dtype=np.int32).reshape(-1, 3))
+    order = np.zeros(len(tri), dtype=np.int64)
+    builds = ctypes.c_long()
+    st = lib.ccsdt_debug_slab_schedule(o, max_ovvv_slabs, batch, len(tri),
+                                       tri.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                       order.ctypes.data_as(ctypes.POINTER(ctypes.c_long)), ctypes.byref(builds))
+    if st:
+        raise CCSDTError(st, "ccsdt_debug_slab_schedule")
+    return order, builds.value
 
 
 def energy_spin_orbital(oa: int, ob: int, va: int, vb: int, eps_occ, eps_vir, t1, t2, v2ijab, v2ijka,

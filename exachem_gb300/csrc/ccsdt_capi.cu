@@ -91,7 +91,8 @@ ccsdt_handle::~ccsdt_handle() {
   for(void* p: owned) cudaFree(p);
   for(void* p: owned_bytes) cudaFree(p);
   for(void* p: slice_bufs) cudaFree(p);
-  for(void* p: {(void*) bt_F, (void*) bt_part, (void*) bt_order, (void*) bt_order_partial, (void*) bt_ctrl, (void*) bt_tri})
+  for(void* p: {(void*) bt_F, (void*) bt_part, (void*) bt_order, (void*) bt_order_partial, (void*) bt_ctrl, (void*) bt_tri,
+                (void*) chol_ov, (void*) chol_vv, (void*) d_slab_of})
     if(p) cudaFree(p);
   if(ev0) cudaEventDestroy(ev0);
   if(ev1) cudaEventDestroy(ev1);
@@ -111,6 +112,12 @@ ccsdt_status ccsdt_handle::ensure_inputs(long long nslab) {
   const long long want = nslab < 0 ? (long long) o : nslab;
   uploaded    = false;
   ovvv_direct = nslab >= 0;
+  if(!ovvv_direct)
+    for(double** p: {&chol_ov, &chol_vv}) // a previous direct-mode upload's vectors
+      if(*p) {
+        cudaFree(*p);
+        *p = nullptr;
+      }
   if(ovvv && ovvv_nslab != want) { // the other mode's ovvv: a different number of slabs
     cudaFree(ovvv);
     owned.erase(std::remove(owned.begin(), owned.end(), ovvv), owned.end());
@@ -337,7 +344,8 @@ ccsdt_status ccsdt_handle::ensure_fused_tiles() {
 ccsdt_status ccsdt_handle::run_triplet_fp64_fused(int i, int j, int k, double* eout) {
   ccsdt_status s;
   if((s = ensure_fused_tiles())) return s;
-  FusedArgs fa{t2, t2h, ovvv, ooovh, oovv, t1, eo, ev, (const int3*) fx_tiles, fx_ntiles, o, v, i, j, k, part};
+  FusedArgs fa{t2,        t2h, ovvv_slab(i), ovvv_slab(j), ovvv_slab(k), ooovh, oovv, t1, eo, ev, (const int3*) fx_tiles,
+               fx_ntiles, o,   v,            i,            j,            k,     part};
   const int G = std::min(fx_ntiles, fx_grid);
   if(profiling) {
     cudaEventRecord(prof_ev[0], stream);
@@ -388,7 +396,7 @@ ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
   // ---- d-sum (particle) contractions: C[single][(pair)] += sum_d t(single, d) (pair|d)
   GemmBatch pb{};
   auto      t2_of   = [&](int x, int y) { return t2 + ((long long) x * o + y) * v2; }; // [a][d]
-  auto      ovvv_of = [&](int z) { return ovvv + (long long) z * v3; };                 // [(g,b)][d]
+  auto      ovvv_of = [&](int z) { return ovvv_slab(z); };                              // [(g,b)][d]
   const RowMap arow = plain_rows(v), bnat = plain_rows(v), bswp = swapped_pair_rows((int) v, v);
   // P12[a][(c,b)] += t_ij^{ad} (kc|bd) + t_ik^{ad} (jb|cd)
   pb.job[0] = GemmJob{{GemmTerm{t2_of(i, j), arow, ovvv_of(k), bnat, (int) v, 1.0},
@@ -460,15 +468,25 @@ ccsdt_status ccsdt_handle::run_list(const ccsdt_opts* opts, long n, const int* t
   p_storage = opts->p_storage;
   if(opts->mode != CCSDT_MODE_FP64) return run_split(opts, n, tri_host);
   fp64_unfused = opts->test_kernel == 5 || w_debug; // testing: the two-stage FP64 path
-  for(long t = 0; t < n; t++) {
-    const int i = tri_host[3 * t], j = tri_host[3 * t + 1], k = tri_host[3 * t + 2];
+  return run_fp64_list(n, tri_host);
+}
+
+// The FP64 path over a triplet list; results at etrip[2 t].  In the Cholesky-direct mode the
+// triplets run by blocks of occupied indices, each after its three (ia|bc) slabs are resident.
+ccsdt_status ccsdt_handle::run_fp64_list(long n, const int* tri_host) {
+  ccsdt_status            s;
+  const std::vector<long> ord =
+    ovvv_direct ? ccsdt::slab_order(tri_host, n, (int) ovvv_nslab) : std::vector<long>();
+  for(long u = 0; u < n; u++) {
+    const long t = ovvv_direct ? ord[u] : u;
+    const int  i = tri_host[3 * t], j = tri_host[3 * t + 1], k = tri_host[3 * t + 2];
     if(i == k) {
       // i = j = k: W is symmetric in (a, b, c), so Z Y vanishes identically
       cudaError_t e = cudaMemsetAsync(etrip + 2 * t, 0, 2 * sizeof(double), stream);
       if(e != cudaSuccess) return fail(CCSDT_E_CUDA, cudaGetErrorString(e));
       continue;
     }
-    if((s = run_triplet_fp64(i, j, k, etrip + 2 * t))) return s;
+    if((s = ensure_ovvv(&tri_host[3 * t], 3, false)) || (s = run_triplet_fp64(i, j, k, etrip + 2 * t))) return s;
   }
   return CCSDT_OK;
 }

@@ -100,6 +100,7 @@ struct ccsdt_handle {
   bool         blocks_open = false;    // between ccsdt_upload_begin and ccsdt_upload_end
   ccsdt_status ensure_triplet_slots(long n);
   ccsdt_status run_triplet_fp64(int i, int j, int k, double* eout);
+  ccsdt_status run_fp64_list(long n, const int* tri_host);
   ccsdt_status run_list(const ccsdt_opts* opts, long n, const int* tri_host);
   ccsdt_status run_split(const ccsdt_opts* opts, long n, const int* tri_host);
   ccsdt_status ensure_slices(int S, int variant);

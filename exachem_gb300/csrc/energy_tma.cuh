@@ -10,6 +10,9 @@
 // box12_q[x][z][y] + box34_q[y][x][z] + box56_q[z][y][x], summed in the order of the
 // pass-by-pass kernel, so both kernels give the same W bit for bit.
 //
+// Two pipeline stages: unit n + 1's boxes are loaded (and its singles data read into registers)
+// while unit n is evaluated.
+//
 // Lane -> orbit: warp g (16 per unit, two per thread block warp), lane (u = lane % 8, w = lane / 8)
 // takes la = w + 4 (g % 2), lb = u, lc = (u + w + g / 2) % 8.  For every one of the eighteen reads
 // (each position of each box layout takes each of the three coordinates) the 32 lanes then touch
@@ -41,26 +44,45 @@ struct TmaEnergyArgs {
   unsigned      spin;
 };
 
-// bytes of dynamic shared memory: the eighteen boxes
+// bytes of dynamic shared memory: the eighteen boxes of each of the two pipeline stages
 template<typename TP>
-constexpr size_t em_smem_bytes() {
+constexpr size_t em_stage_bytes() {
   return (size_t) EM_BOXES * ET_B * ET_B * ET_B * sizeof(TP);
 }
+template<typename TP>
+constexpr size_t em_smem_bytes() {
+  return 2 * em_stage_bytes<TP>();
+}
+
+// Per-stage shared data of a unit besides the boxes: the singles' integrals and amplitudes of its
+// three blocks, its virtual orbital energies, the orbit-wide part of D and the distinct-cube flags.
+struct EmSingles {
+  float  Ojk[3][3][ET_B * ET_B], Oik[3][3][ET_B * ET_B], Oij[3][3][ET_B * ET_B];
+  float  ti[3][ET_B], tj[3][ET_B], tk[3][ET_B];
+  float2 evs[3][ET_B];
+  float2 dab[ET_B * ET_B];
+  int    slot_on[6];
+};
+
+// A thread's share of one unit's singles data, loaded from global memory into registers while the
+// previous unit is being evaluated and stored to that unit's stage afterwards.
+struct EmPrefetch {
+  float  o[2][3];  // (jk), (ik), (ij) integrals at the thread's two singles positions
+  float  t[3];     // t_i, t_j, t_k at (block, index) = (tid / 8, tid % 8), threads 0..23
+  float2 ev;       // e_v there
+  float2 dab;      // e_i + e_j + e_k - e_a - e_b, threads 64..127
+  int    on;       // distinct-cube flag, threads 96..101
+};
 
 template<typename TP>
-static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::value ? 4 : 2)
+static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::value ? 2 : 1)
   energy_tma_batch_kernel(const __grid_constant__ TmaEnergyArgs A) {
   constexpr int  B = ET_B, B3 = B * B * B;
   constexpr bool kF32 = std::is_same<TP, float>::value;
   extern __shared__ __align__(128) unsigned char em_dyn[];
-  TP* box = reinterpret_cast<TP*>(em_dyn); // [pass][slot q][512]: pass 0 = P12, 1 = P34, 2 = P56
-  __shared__ float    Ojk[3][3][B * B], Oik[3][3][B * B], Oij[3][3][B * B];
-  __shared__ float    ti[3][B], tj[3][B], tk[3][B];
-  __shared__ float2   evs[3][B];
-  __shared__ float2   dab[B * B];
-  __shared__ int      slot_on[6];
-  __shared__ uint64_t full;
-  __shared__ int      failed;
+  // stage st: boxes [pass][slot q][512] at em_dyn + st * em_stage_bytes (pass 0 = P12, 1 = P34, 2 = P56)
+  __shared__ EmSingles sgl[2];
+  __shared__ uint64_t  full[2];
 
   const int       slot = blockIdx.y, b0 = A.base ? *A.base : 0;
   const int*      tp   = A.tri + 4 * (b0 + slot);
@@ -71,15 +93,102 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
   const float *   gOjk = A.oovv + ((long long) j * o + k) * v2, *gOik = A.oovv + ((long long) i * o + k) * v2,
               *gOij = A.oovv + ((long long) i * o + j) * v2;
   if(tid == 0) {
-    sm100::mbar_init(&full, 1);
+    sm100::mbar_init(&full[0], 1);
+    sm100::mbar_init(&full[1], 1);
     sm100::mbar_fence_init();
     sm100::prefetch_tmap(&A.pmap);
-    failed = 0;
   }
   __syncthreads();
-  ff       s4{0.f, 0.f}, s5{0.f, 0.f};
-  float    sens  = 0.f;
-  uint32_t phase = 0;
+
+  // one thread issues a unit's eighteen box loads into stage st
+  auto issue = [&](int tile, int st) {
+    const int3 tt     = A.tiles[tile];
+    const int  rb0[3] = {tt.x * B, tt.y * B, tt.z * B};
+    auto       b0f    = [&](int p) { return p == 0 ? rb0[0] : p == 1 ? rb0[1] : rb0[2]; };
+    TP*        box    = reinterpret_cast<TP*>(em_dyn + st * em_stage_bytes<TP>());
+    // the stage was last read through the generic proxy; the TMA writes it through the async one
+    sm100::fence_proxy_async_smem();
+    sm100::mbar_arrive_expect_tx(&full[st], (uint32_t) em_stage_bytes<TP>());
+#pragma unroll 1
+    for(int b = 0; b < EM_BOXES; b++) {
+      const int  pass = b / 6, q = b % 6;
+      const int* P    = c_perm[q];
+      // (slowest, middle, fastest) block positions of the pass's array: P12[a][c][b],
+      // P34[b][a][c], P56[c][b][a] with a, b, c in the blocks at positions P[0], P[1], P[2]
+      const int q0 = pass == 0 ? P[0] : pass == 1 ? P[1] : P[2];
+      const int q1 = pass == 0 ? P[2] : pass == 1 ? P[0] : P[1];
+      const int q2 = pass == 0 ? P[1] : pass == 1 ? P[2] : P[0];
+      sm100::tma_load_4d(box + (size_t) b * B3, &A.pmap, &full[st], b0f(q2), b0f(q1), b0f(q0), 3 * slot + pass);
+    }
+  };
+  // every thread loads its share of a unit's singles data into registers
+  auto prefetch = [&](int tile, EmPrefetch& r) {
+    const int3 tt     = A.tiles[tile];
+    const int  rb0[3] = {tt.x * B, tt.y * B, tt.z * B};
+    const int  rbn[3] = {min(B, v - rb0[0]), min(B, v - rb0[1]), min(B, v - rb0[2])};
+    auto       b0f    = [&](int p) { return p == 0 ? rb0[0] : p == 1 ? rb0[1] : rb0[2]; };
+    auto       bnf    = [&](int p) { return p == 0 ? rbn[0] : p == 1 ? rbn[1] : rbn[2]; };
+#pragma unroll
+    for(int h = 0; h < 2; h++) { // the six ordered pairs of distinct blocks, 64 entries each
+      const int e = tid + h * EM_THREADS;
+      r.o[h][0] = r.o[h][1] = r.o[h][2] = 0.f;
+      if(e < 6 * B * B) {
+        const int       pi = e / (B * B), uu = pi >> 1, ww = (pi & 1) ? (uu == 2 ? 1 : 2) : (uu == 0 ? 1 : 0);
+        const int       x = (e / B) % B, y = e % B;
+        const long long off = (long long) (b0f(uu) + x) * v + b0f(ww) + y;
+        if(x < bnf(uu) && y < bnf(ww)) r.o[h][0] = gOjk[off], r.o[h][1] = gOik[off], r.o[h][2] = gOij[off];
+      }
+    }
+    if(tid < 3 * B) {
+      const int  uu = tid / B, x = tid % B;
+      const bool ok = x < bnf(uu);
+      const int  a  = b0f(uu) + x;
+      r.t[0] = ok ? A.t1[(long long) i * v + a] : 0.f;
+      r.t[1] = ok ? A.t1[(long long) j * v + a] : 0.f;
+      r.t[2] = ok ? A.t1[(long long) k * v + a] : 0.f;
+      const ff e = ok ? ff_from_double(A.ev[a]) : ff{0.f, 0.f};
+      r.ev       = make_float2(e.hi, e.lo);
+    } else if(tid >= 64 && tid < 64 + B * B) { // a in block 0, b in block 1
+      const int x = (tid - 64) / B, y = (tid - 64) % B;
+      const ff  ea = x < rbn[0] ? ff_from_double(A.ev[rb0[0] + x]) : ff{0.f, 0.f};
+      const ff  eb = y < rbn[1] ? ff_from_double(A.ev[rb0[1] + y]) : ff{0.f, 0.f};
+      const ff  d  = ff_add(ff_add(eijk, ff_neg(ea)), ff_neg(eb));
+      r.dab        = make_float2(d.hi, d.lo);
+      if(tid >= 96 && tid < 102) { // a cube counts once per distinct ordered block triple
+        const int  t6 = tid - 96;
+        const int* P  = c_perm[t6];
+        r.on          = 1;
+        for(int q = 0; q < t6; q++) {
+          const int* Q = c_perm[q];
+          if(b0f(P[0]) == b0f(Q[0]) && b0f(P[1]) == b0f(Q[1]) && b0f(P[2]) == b0f(Q[2])) r.on = 0;
+        }
+      }
+    }
+  };
+  auto store = [&](const EmPrefetch& r, EmSingles& S_) {
+#pragma unroll
+    for(int h = 0; h < 2; h++) {
+      const int e = tid + h * EM_THREADS;
+      if(e < 6 * B * B) {
+        const int pi = e / (B * B), uu = pi >> 1, ww = (pi & 1) ? (uu == 2 ? 1 : 2) : (uu == 0 ? 1 : 0);
+        const int x = (e / B) % B, y = e % B;
+        S_.Ojk[uu][ww][x * B + y] = r.o[h][0];
+        S_.Oik[uu][ww][x * B + y] = r.o[h][1];
+        S_.Oij[uu][ww][x * B + y] = r.o[h][2];
+      }
+    }
+    if(tid < 3 * B) {
+      const int uu = tid / B, x = tid % B;
+      S_.ti[uu][x] = r.t[0], S_.tj[uu][x] = r.t[1], S_.tk[uu][x] = r.t[2];
+      S_.evs[uu][x] = r.ev;
+    } else if(tid >= 64 && tid < 64 + B * B) {
+      S_.dab[tid - 64] = r.dab;
+      if(tid >= 96 && tid < 102) S_.slot_on[tid - 96] = r.on;
+    }
+  };
+
+  ff    s4{0.f, 0.f}, s5{0.f, 0.f};
+  float sens = 0.f;
   // this thread's two orbits of every unit (warps g = warp and warp + 8)
   const int u = lane & 7, w = lane >> 3;
   int       la_[2], lb_[2], lc_[2];
@@ -88,79 +197,41 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
     const int g = warp + 8 * h;
     la_[h] = w + 4 * (g & 1), lb_[h] = u, lc_[h] = (u + w + (g >> 1)) & 7;
   }
-
-  for(int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
-    const int3 tt     = A.tiles[tile];
-    const int  rb0[3] = {tt.x * B, tt.y * B, tt.z * B};
-    const int  rbn[3] = {min(B, v - rb0[0]), min(B, v - rb0[1]), min(B, v - rb0[2])};
-    auto       b0f    = [&](int p) { return p == 0 ? rb0[0] : p == 1 ? rb0[1] : rb0[2]; };
-    auto       bnf    = [&](int p) { return p == 0 ? rbn[0] : p == 1 ? rbn[1] : rbn[2]; };
-    __syncthreads(); // the previous unit's orbits are done with the boxes and the singles
-    if(tid == 0) {
-      // the boxes were last read through the generic proxy; the TMA writes them through the async one
-      sm100::fence_proxy_async_smem();
-      sm100::mbar_arrive_expect_tx(&full, (uint32_t) em_smem_bytes<TP>());
-#pragma unroll 1
-      for(int b = 0; b < EM_BOXES; b++) {
-        const int  pass = b / 6, q = b % 6;
-        const int* P    = c_perm[q];
-        // (slowest, middle, fastest) block positions of the pass's array: P12[a][c][b],
-        // P34[b][a][c], P56[c][b][a] with a, b, c in the blocks at positions P[0], P[1], P[2]
-        const int q0 = pass == 0 ? P[0] : pass == 1 ? P[1] : P[2];
-        const int q1 = pass == 0 ? P[2] : pass == 1 ? P[0] : P[1];
-        const int q2 = pass == 0 ? P[1] : pass == 1 ? P[2] : P[0];
-        sm100::tma_load_4d(box + (size_t) b * B3, &A.pmap, &full, b0f(q2), b0f(q1), b0f(q0), 3 * slot + pass);
-      }
-    } else if(tid >= 96 && tid < 102) { // a slot counts once per distinct ordered block triple
-      const int  t6 = tid - 96;
-      const int* P  = c_perm[t6];
-      int        on = 1;
-      for(int q = 0; q < t6; q++) {
-        const int* Q = c_perm[q];
-        if(b0f(P[0]) == b0f(Q[0]) && b0f(P[1]) == b0f(Q[1]) && b0f(P[2]) == b0f(Q[2])) on = 0;
-      }
-      slot_on[t6] = on;
+  bool       failed = false;
+  EmPrefetch pre{};
+  if((int) blockIdx.x < A.ntiles) {
+    if(tid == 0) issue(blockIdx.x, 0);
+    prefetch(blockIdx.x, pre);
+  }
+  // Pipeline: while unit n is evaluated from stage n % 2, unit n + 1's boxes are in flight into the
+  // other stage and its singles data in registers.
+  int n = 0;
+  for(int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x, n++) {
+    const int st = n & 1;
+    store(pre, sgl[st]);
+    __syncthreads(); // stage st's singles are visible; unit n - 1's orbits are done with stage st ^ 1
+    const int next = tile + gridDim.x;
+    if(next < A.ntiles) {
+      if(tid == 0) issue(next, st ^ 1);
+      prefetch(next, pre);
     }
-    // singles data of the three blocks (the orbits read the six ordered pairs of distinct blocks)
-    for(int e = tid; e < 6 * B * B; e += EM_THREADS) {
-      const int       pi = e / (B * B), uu = pi >> 1, ww = (pi & 1) ? (uu == 2 ? 1 : 2) : (uu == 0 ? 1 : 0);
-      const int       x = (e / B) % B, y = e % B;
-      const bool      ok  = x < bnf(uu) && y < bnf(ww);
-      const long long off = (long long) (b0f(uu) + x) * v + b0f(ww) + y;
-      Ojk[uu][ww][x * B + y] = ok ? gOjk[off] : 0.f;
-      Oik[uu][ww][x * B + y] = ok ? gOik[off] : 0.f;
-      Oij[uu][ww][x * B + y] = ok ? gOij[off] : 0.f;
+    const bool ok = sm100::mbar_wait(&full[st], (n >> 1) & 1, A.spin);
+    if(__syncthreads_or(!ok)) { // the boxes never arrived: give up on the call
+      failed = true;
+      break;
     }
-    if(tid < 3 * B) {
-      const int  uu = tid / B, x = tid % B;
-      const bool ok = x < bnf(uu);
-      const int  a  = b0f(uu) + x;
-      ti[uu][x] = ok ? A.t1[(long long) i * v + a] : 0.f;
-      tj[uu][x] = ok ? A.t1[(long long) j * v + a] : 0.f;
-      tk[uu][x] = ok ? A.t1[(long long) k * v + a] : 0.f;
-      const ff e = ok ? ff_from_double(A.ev[a]) : ff{0.f, 0.f};
-      evs[uu][x] = make_float2(e.hi, e.lo);
-    } else if(tid >= 64 && tid < 64 + B * B) { // the orbit-wide part of D: a in block 0, b in block 1
-      const int x = (tid - 64) / B, y = (tid - 64) % B;
-      const ff  ea = x < rbn[0] ? ff_from_double(A.ev[rb0[0] + x]) : ff{0.f, 0.f};
-      const ff  eb = y < rbn[1] ? ff_from_double(A.ev[rb0[1] + y]) : ff{0.f, 0.f};
-      const ff  d  = ff_add(ff_add(eijk, ff_neg(ea)), ff_neg(eb));
-      dab[tid - 64] = make_float2(d.hi, d.lo);
-    }
-    // the boxes: every thread waits (bounded) for the unit's TMA bytes
-    const bool ok = sm100::mbar_wait(&full, phase, A.spin);
-    phase ^= 1;
-    if(!ok) failed = 1;
-    __syncthreads(); // singles staged; every thread's wait has finished
-    if(failed) break;
-    const bool all_on = slot_on[0] & slot_on[1] & slot_on[2] & slot_on[3] & slot_on[4] & slot_on[5];
+    const EmSingles& S_ = sgl[st];
+    const TP*        box = reinterpret_cast<const TP*>(em_dyn + st * em_stage_bytes<TP>());
+    const int3       tt  = A.tiles[tile];
+    const int        rbn[3] = {min(B, v - tt.x * B), min(B, v - tt.y * B), min(B, v - tt.z * B)};
+    const bool       all_on = S_.slot_on[0] & S_.slot_on[1] & S_.slot_on[2] & S_.slot_on[3] & S_.slot_on[4] & S_.slot_on[5];
 #pragma unroll
     for(int h = 0; h < 2; h++) {
       const int la = la_[h], lb = lb_[h], lc = lc_[h];
       if(la >= rbn[0] || lb >= rbn[1] || lc >= rbn[2]) continue;
       const int loc[3] = {la, lb, lc};
       float     sg[6];
-      et_singles(Ojk, Oik, Oij, ti, tj, tk, la, lb, lc, sg);
+      et_singles(S_.Ojk, S_.Oik, S_.Oij, S_.ti, S_.tj, S_.tk, la, lb, lc, sg);
       if constexpr(kF32) {
         float wv[6];
 #pragma unroll
@@ -170,7 +241,7 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
           wv[q] += box[(1 * 6 + q) * B3 + (y * B + x) * B + z];
           wv[q] += box[(2 * 6 + q) * B3 + (z * B + y) * B + x];
         }
-        et_orbit_values_f32(wv, sg, evs, dab, all_on, slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
+        et_orbit_values_f32(wv, sg, S_.evs, S_.dab, all_on, S_.slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
       } else {
         ff wv[6];
 #pragma unroll
@@ -181,10 +252,10 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
           const float2 p56 = box[(2 * 6 + q) * B3 + (z * B + y) * B + x];
           // the pass-by-pass kernel's order: two-sum of the high words with the low words added,
           // then a float-float add of the third array
-          const ff h = ff_two_sum(p12.x, p34.x);
-          wv[q]      = ff_add(ff{h.hi, h.lo + (p12.y + p34.y)}, ff{p56.x, p56.y});
+          const ff hs = ff_two_sum(p12.x, p34.x);
+          wv[q]       = ff_add(ff{hs.hi, hs.lo + (p12.y + p34.y)}, ff{p56.x, p56.y});
         }
-        et_orbit_values(wv, sg, evs, dab, all_on, slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
+        et_orbit_values(wv, sg, S_.evs, S_.dab, all_on, S_.slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
       }
     }
   }

@@ -46,7 +46,9 @@ __device__ __constant__ FxTerm c_fx_terms[12] = {
 };
 
 struct FusedArgs {
-  const double *t2, *t2h, *ovvv, *ooovh, *oovv, *t1, *eo, *ev;
+  const double *t2, *t2h;
+  const double *ov_i, *ov_j, *ov_k; // (ia|bc) slabs (v^3 each) of the triplet's occupied indices
+  const double *ooovh, *oovv, *t1, *eo, *ev;
   const int3*   tiles; // sorted block triples
   int           ntiles;
   int           o, v, i, j, k;
@@ -98,7 +100,8 @@ static __global__ void __launch_bounds__(FX_THREADS, 3) t3_fused_fp64_kernel(con
                                   : A.ooovh + ((long long) oc(T.s0) * o + oc(T.s1)) * v * o + (long long) gs * o;
         const bool    sv = gs < v;
         // pair operand rows (M index = (r1, r2), 16 rows per tile t: r1 local 2 t + h, r2 local g)
-        const double* pbase = T.dsum ? A.ovvv + (long long) oc(T.pz) * v2 * v : A.t2h + (long long) oc(T.pz) * v2 * o;
+        const double* pbase = T.dsum ? (T.pz == 0 ? A.ov_i : T.pz == 1 ? A.ov_j : A.ov_k)
+                                     : A.t2h + (long long) oc(T.pz) * v2 * o;
         // row (r1 local n1, r2 local g) at p0 + n1 v K; rows with a global index >= v read as zero
         const int       g2   = rb(T.r2) + g;
         const int       nlim = g2 < v ? v - rb(T.r1) : 0; // local r1 rows < nlim exist

@@ -66,6 +66,8 @@ struct PzParams {
   float2*         F;          // P arrays of slot s: F + s * 3 v^3 (P12, P34, P56 consecutive)
   int             f32_out;    // store P rounded to FP32 (element e at ((float*) F)[e]) instead of
                               // float-float (F[e])
+  const int*      ovvv_slot;  // (ia|bc) digit planes by slot: slot of occupied index z (nullable:
+                              // slot = z; the Cholesky-direct mode's slab cache otherwise)
   const unsigned* order;      // cost-ordered item ids, length nitems
   unsigned        nitems;
   unsigned*       queue;      // work counter, 0 at launch
@@ -134,7 +136,8 @@ __device__ __forceinline__ PzTerm pz_term(const PzParams& P, int job, int t, int
   PzTerm T;
   if(t < 2) {
     const int z = e0, xx = e2, yy = e3;
-    T.mapA = nat ? PZ_OVVV_NAT : PZ_OVVV_SWP, T.a2 = x, T.a3 = z;     // rows (z, x, y) or (z, y, x)
+    T.mapA = nat ? PZ_OVVV_NAT : PZ_OVVV_SWP, T.a2 = x;              // rows (z, x, y) or (z, y, x)
+    T.a3   = P.ovvv_slot ? __ldg(P.ovvv_slot + z) : z;
     T.mapB = PZ_T2, T.b2 = yy, T.b3 = xx;                            // rows (xx, yy, n)
     T.Kp = P.kp_v;
   } else {

@@ -176,6 +176,7 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   const bool f32 = p_f32(S);
   p.f32_out      = f32;
   last_p_f32     = f32;
+  p.ovvv_slot    = ovvv_direct ? d_slab_of : nullptr;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
   // windows in multiples of 64 whatever the configuration's K chunk, so every configuration folds
   // the same windows and the energies stay bit-identical across configurations
@@ -267,9 +268,31 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
     }
     tab.insert(tab.end(), {i, j, k, out});
   }
-  const long m = (long) tab.size() / 4;
+  long m = (long) tab.size() / 4;
   if(m == 0) return CCSDT_OK;
-  const int B = (int) std::min<long>(batch_slots, m);
+  int B = (int) std::min<long>(batch_slots, m);
+  if(ovvv_direct) {
+    // Cholesky-direct mode: triplets by blocks of occupied indices, and batches whose slabs fit
+    // the cache together (3 per triplet at most)
+    B = std::max(1, std::min(B, (int) (ovvv_nslab / 3)));
+    std::vector<int> ijk(3 * m);
+    for(long t = 0; t < m; t++)
+      for(int q = 0; q < 3; q++) ijk[3 * t + q] = tab[4 * t + q];
+    const std::vector<long> ord = ccsdt::slab_order(ijk.data(), m, (int) ovvv_nslab);
+    std::vector<int>        sorted(tab.size());
+    for(long t = 0; t < m; t++)
+      for(int q = 0; q < 4; q++) sorted[4 * t + q] = tab[4 * ord[t] + q];
+    tab.swap(sorted);
+    use_graph = false; // every batch may form slabs first
+  }
+  // the slabs batch b reads (direct mode), formed before its launch
+  auto slabs_for = [&](long b0, long cnt) -> ccsdt_status {
+    if(!ovvv_direct) return CCSDT_OK;
+    std::vector<int> need;
+    for(long t = b0; t < b0 + cnt; t++)
+      for(int q = 0; q < 3; q++) need.push_back(tab[4 * t + q]);
+    return ensure_ovvv(need.data(), (int) need.size(), true);
+  };
   if((s = ensure_batch(S, B))) return s;
   if(bt_tri_cap < m) {
     if(bt_tri) cudaFree(bt_tri);
@@ -334,11 +357,12 @@ ccsdt_status ccsdt_handle::run_batched(int S, long n, const int* tri, bool use_g
       cudaGraphDestroy(g);
     } else {
       for(long b = 0; b < full; b++)
-        if((s = launch_batch(S, B, 0, true, tails, sens))) return s;
+        if((s = slabs_for(b * B, B)) || (s = launch_batch(S, B, 0, true, tails, sens))) return s;
     }
   }
   if(rem) {
-    if((s = launch_batch(S, (int) rem, (int) (per * rem), true, tails, sens))) return s;
+    if((s = slabs_for(full * B, rem)) || (s = launch_batch(S, (int) rem, (int) (per * rem), true, tails, sens)))
+      return s;
   }
   return collect_phase_times();
 }

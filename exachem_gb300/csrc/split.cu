@@ -265,13 +265,17 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
     long long*    plane;
   } src[4] = {{t2, o * o * v, (int) v, Kpv, &sl_t2, &ex_t2, &pl_t2},
               {t2h, o * v * v, (int) o, Kpo, &sl_t2h, &ex_t2h, &pl_t2h},
-              {ovvv, o * v * v, (int) v, Kpv, &sl_ovvv, &ex_ovvv, &pl_ovvv},
+              {ovvv, ovvv_nslab * v * v, (int) v, Kpv, &sl_ovvv, &ex_ovvv, &pl_ovvv}, // slots in the direct mode
               {ooovh, o * o * v, (int) o, Kpo, &sl_ooovh, &ex_ooovh, &pl_ooovh}};
   ccsdt_status s;
   for(auto& q: src) {
     *q.plane = q.R * q.Kp;
     if((s = grab(q.planes, (size_t) S * q.R * q.Kp * esz)) || (s = grab((void**) q.exps, (size_t) q.R * sizeof(int))))
       return s;
+    if(ovvv_direct && q.planes == &sl_ovvv) { // its slabs are sliced as they are formed (ensure_ovvv)
+      std::fill(slab_sliced.begin(), slab_sliced.end(), 0);
+      continue;
+    }
     if(variant == 0)
       oz_slice_rows_kernel<__nv_bfloat16><<<4096, 256, 0, stream>>>(q.x, q.R, q.K, q.Kp, S, (__nv_bfloat16*) *q.planes, *q.plane, *q.exps);
     else
@@ -448,8 +452,11 @@ ccsdt_status ccsdt_handle::ensure_tmaps(int S, int NT, int KC) {
   const long long Kv = kp_v, Ko = kp_o;
   bool ok = true;
   // A side (pair rows, 128-row boxes): rows (z, x, y) natural = z v^2 + x v + y, swapped = z v^2 + y v + x
-  ok &= encode_map(&tmaps[MAP_OVVV_NAT], sl_ovvv, (int) Kv, v, v, o, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_, KC);
-  ok &= encode_map(&tmaps[MAP_OVVV_SWP], sl_ovvv, (int) Kv, v, v, o, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM, (int) S_, KC);
+  // ovvv's occupied dimension: its slots in the direct mode (the kernel maps index -> slot)
+  ok &= encode_map(&tmaps[MAP_OVVV_NAT], sl_ovvv, (int) Kv, v, v, ovvv_nslab, P, Kv, v * Kv, v * v * Kv, pl_ovvv, TC_BM,
+                   (int) S_, KC);
+  ok &= encode_map(&tmaps[MAP_OVVV_SWP], sl_ovvv, (int) Kv, v, v, ovvv_nslab, P, v * Kv, Kv, v * v * Kv, pl_ovvv, TC_BM,
+                   (int) S_, KC);
   ok &= encode_map(&tmaps[MAP_T2H_NAT], sl_t2h, (int) Ko, v, v, o, P, Ko, v * Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_, KC);
   ok &= encode_map(&tmaps[MAP_T2H_SWP], sl_t2h, (int) Ko, v, v, o, P, v * Ko, Ko, v * v * Ko, pl_t2h, TC_BM, (int) S_, KC);
   // B side (single rows, NT-row boxes): t2 rows (xx, yy, a); ooovh rows (yy, zz, c)
@@ -608,7 +615,11 @@ ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int var
 ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* tri) {
   last_batched     = false;
   last_err_bound   = 0.0; // only the LEARNED mode estimates its error
-  if(opts->mode == CCSDT_MODE_LEARNED) return run_learned(opts, n, tri);
+  if(opts->mode == CCSDT_MODE_LEARNED) {
+    if(ovvv_direct) // its features read every occupied index's (ia|bc) exponent statistics
+      return fail(CCSDT_E_INVALID, "the learned slice count needs the whole (ia|bc); not in the Cholesky-direct mode");
+    return run_learned(opts, n, tri);
+  }
   const int S       = opts->slices;
   const int variant = opts->slice_kind;
   if(variant != 0 && variant != 1) return fail(CCSDT_E_INVALID, "unknown slice variant");
@@ -626,17 +637,14 @@ ccsdt_status ccsdt_handle::run_split(const ccsdt_opts* opts, long n, const int* 
   if(kernel_kind == 3) { // testing: FP64 contractions with the float-float energy (its own error)
     if((s = ensure_scratch())) return s;
     fp64_ff_energy = true;
-    for(long t = 0; t < n && !s; t++) {
-      const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];
-      if(i == k) {
-        if(cudaMemsetAsync(etrip + 2 * t, 0, 2 * sizeof(double), stream) != cudaSuccess) s = fail(CCSDT_E_CUDA, "memset");
-      } else
-        s = run_triplet_fp64(i, j, k, etrip + 2 * t);
-    }
+    s              = run_fp64_list(n, tri);
     fp64_ff_energy = false;
     return s;
   }
   last_batched = kernel_kind == 0 && pz_eligible(S, variant);
+  if(ovvv_direct && !last_batched)
+    return fail(CCSDT_E_INVALID, "the Cholesky-direct mode runs the split path on the persistent tcgen05 kernel only "
+                                 "(BF16 digits, default test_kernel)");
   if(last_batched) return run_batched(S, n, tri, opts->use_graph != 0, nullptr, nullptr);
   for(long t = 0; t < n; t++) {
     const int i = tri[3 * t], j = tri[3 * t + 1], k = tri[3 * t + 2];

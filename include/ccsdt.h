@@ -154,6 +154,29 @@ ccsdt_status ccsdt_upload_cholesky(ccsdt_handle* h, const double* eps_occ, const
                                    const double* t1, const double* t2, int n_chol, const double* chol_oo,
                                    const double* chol_ov, const double* chol_vv, int on_device);
 
+/* Cholesky-direct inputs: as ccsdt_upload_cholesky, but (ia|bc) is never held whole.  The handle
+ * keeps chol_ov and chol_vv on the device and forms (ia|bc) one occupied index at a time (a slab:
+ * all a, b, c; one DMMA GEMM of v x v^2 x n_chol) into a cache of max_ovvv_slabs slabs of v^3
+ * doubles, as the triplets need them: the calls visit their triplets by blocks of max_ovvv_slabs / 3
+ * occupied indices, the least recently used slab not needed by the current batch makes room, and
+ * the split path slices each slab into digit planes when it is formed.  Systems whose o v^3
+ * (ia|bc) exceeds the device memory then run, at the cost of forming slabs more than once
+ * (ccsdt_ovvv_slab_builds); max_ovvv_slabs >= o forms each slab once.  Energies equal those of
+ * ccsdt_upload_cholesky on the same vectors.  max_ovvv_slabs >= 3 (clamped to o); the split path
+ * needs the persistent tcgen05 kernel (BF16 digits) and runs batches of at most max_ovvv_slabs / 3
+ * triplets; CCSDT_MODE_LEARNED is not available in this mode (CCSDT_E_INVALID). */
+ccsdt_status ccsdt_upload_cholesky_direct(ccsdt_handle* h, const double* eps_occ, const double* eps_vir,
+                                          const double* t1, const double* t2, int n_chol, const double* chol_oo,
+                                          const double* chol_ov, const double* chol_vv, int on_device,
+                                          int max_ovvv_slabs);
+/* (ia|bc) slabs formed since the last upload (the Cholesky-direct mode; 0 otherwise). */
+long ccsdt_ovvv_slab_builds(const ccsdt_handle* h);
+/* Testing, host only: the direct mode's visiting order (order[n]: triplet ids) and the number of
+ * slabs it forms for triplets tri[3 n] run in batches of `batch` with max_ovvv_slabs slots;
+ * CCSDT_E_STATE if a batch ever found a slab it needs missing. */
+ccsdt_status ccsdt_debug_slab_schedule(int o, int max_ovvv_slabs, int batch, long n, const int* tri, long* order,
+                                       long* builds);
+
 /* Tile configurations of the persistent split-precision contraction (tcgen05 path, slices 1-8):
  *   ccsdt_tile_configs     lists the compiled ones for `slices`: *n of them, {N tile, pipeline
  *                          stages, K chunk} each in nt_st_kc[3 n] (nullable); index 0 is the default;

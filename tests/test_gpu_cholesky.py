@@ -70,3 +70,69 @@ def test_cholesky_rejects_bad_input(built):
         ft.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], Loo, Lov, bad)
     with pytest.raises(CCSDTError):                     # energy before a successful upload
         ft.energy("fp64")
+
+
+def _direct_pair(o, v, nq, seed, slabs, occ=None, vir=None):
+    """The same Cholesky system uploaded whole and in the Cholesky-direct mode."""
+    from exachem_gb300.ccsd_t import FusedTriples
+    d, L = _cholesky_system(o, v, nq, seed)
+    whole = FusedTriples(o, v, occ, vir, ts=24)
+    whole.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], *L)
+    direct = FusedTriples(o, v, occ, vir, ts=24)
+    direct.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], *L, max_ovvv_slabs=slabs)
+    return d, whole, direct
+
+
+@pytest.mark.parametrize("slabs", [3, 5, 9])
+def test_cholesky_direct_fp64_equals_whole(built, slabs):
+    """(ia|bc) formed slab by slab into a cache of 3, 5 or o slabs gives the energies of the whole
+    block bit for bit (the same GEMM per element), whatever the visiting order; small caches form
+    slabs more than once."""
+    from exachem_gb300.ccsd_t import all_triplets
+    o, v = 9, 40
+    d, whole, direct = _direct_pair(o, v, 23, 21, slabs)
+    tri = all_triplets(o)
+    w4, w5 = whole.triplet_energies(tri, "fp64")
+    g4, g5 = direct.triplet_energies(tri, "fp64")
+    assert np.array_equal(w5, g5) and np.array_equal(w4, g4)
+    builds = direct.ovvv_slab_builds()
+    assert builds == o if slabs >= o else builds > o
+    a, b = whole.energy("fp64"), direct.energy("fp64")
+    assert a["e_paren_T"] == b["e_paren_T"] and a["e_bracket_T"] == b["e_bracket_T"]
+
+
+@pytest.mark.parametrize("slabs", [6, 12])
+def test_cholesky_direct_split_equals_whole(built, slabs):
+    """The persistent split path reading its (ia|bc) digit planes from the slab cache (slices formed
+    per slab, TMA coordinates through the index -> slot table, batches of slabs / 3 triplets) gives
+    the whole block's energies bit for bit, at FP32 and float-float partial arrays."""
+    from exachem_gb300.ccsd_t import all_triplets
+    o, v = 10, 48
+    d, whole, direct = _direct_pair(o, v, 30, 22, slabs)
+    tri = all_triplets(o)
+    for S in (2, 3):
+        w4, w5 = whole.triplet_energies(tri, "ozaki", slices=S)
+        g4, g5 = direct.triplet_energies(tri, "ozaki", slices=S)
+        assert np.array_equal(w5, g5) and np.array_equal(w4, g4), S
+    assert direct.ovvv_slab_builds() > o if slabs < o else direct.ovvv_slab_builds() == o
+    # a repeated call reuses the slabs already formed (digit planes current)
+    before = direct.ovvv_slab_builds()
+    direct.triplet_energies(tri[:1], "ozaki", slices=3)
+    assert direct.ovvv_slab_builds() - before <= 3
+
+
+def test_cholesky_direct_limits(built):
+    from exachem_gb300.ccsd_t import CCSDTError, FusedTriples
+    o, v = sum(OCC), sum(VIR)
+    d, L = _cholesky_system(o, v, 8, 23)
+    ft = FusedTriples(o, v, OCC, VIR)
+    with pytest.raises(CCSDTError):                  # fewer slots than one triplet's slabs
+        ft.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], *L, max_ovvv_slabs=2)
+    ft.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], *L, max_ovvv_slabs=4)
+    with pytest.raises(CCSDTError):                  # the learned features read every slab
+        ft.energy("learned", slices=5)
+    with pytest.raises(CCSDTError):                  # the per-triplet split kernels read ovvv whole
+        ft.energy("ozaki", slices=3, legacy_mma=1)
+    r = ft.energy("ozaki", slices=3)
+    ft.upload_cholesky(d["eps_occ"], d["eps_vir"], d["t1"], d["t2"], *L)   # back to the whole block
+    assert ft.energy("ozaki", slices=3)["e_paren_T"] == r["e_paren_T"]
