@@ -340,6 +340,83 @@ def run_open_shell(args):
     return 0
 
 
+def run_cholesky_direct(args):
+    """The Cholesky-direct mode against the whole-block Cholesky upload on one system: random spatial
+    Cholesky vectors L[p][q][Q] (symmetric in p, q; n_chol = --n-chol, default 4 (o + v)) built on
+    the device, the whole (T) call in split precision (--slices) and, on --limit-triplets of them,
+    in FP64, first with (ia|bc) whole, then with caches of each --cholesky-direct size.  Reports the
+    call times, the slabs formed and the time forming them, and whether the energies are identical."""
+    import torch
+    from exachem_gb300 import ccsd_t as ct
+    from exachem_gb300.generator import generate_device
+    torch.cuda.set_device(0)
+    o, v, seed = args.o, args.v, args.seed
+    nq = args.n_chol or 4 * (o + v)
+    wl = workload_config(o, v, seed)
+    dev = generate_device(o, v, seed, device="cuda")
+    amp = {k: dev[k] for k in ("eps_occ", "eps_vir", "t1", "t2")}
+    del dev
+    torch.cuda.empty_cache()
+    g = torch.Generator(device="cuda").manual_seed(seed + 1000)
+    n = o + v
+    L = torch.empty((n, n, nq), dtype=torch.float64, device="cuda").normal_(0.0, 0.05, generator=g)
+    L = 0.5 * (L + L.transpose(0, 1))
+    Loo, Lov, Lvv = (L[:o, :o].contiguous(), L[:o, o:].contiguous(), L[o:, o:].contiguous())
+    del L
+    torch.cuda.empty_cache()
+    stream = torch.cuda.current_stream()
+    tri = triplet_list(o)
+    fp64_tri = spread_sample(tri, min(len(tri), args.limit_triplets or 8))
+    kw = {"slices": args.slices, "p_storage": args.p_storage}
+
+    def run(ft, tr, mode, **k):
+        ft.triplet_energies(tr[:1], mode, **k)           # warm: slicing, tensor maps, first slabs
+        torch.cuda.synchronize()
+        b0 = ft.ovvv_slab_builds()
+        t0 = time.perf_counter()
+        e4, e5 = ft.triplet_energies(tr, mode, **k)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, e4, e5, ft.ovvv_slab_builds() - b0
+
+    ft = ct.FusedTriples(o, v, wl["occ_tiles"], wl["vir_tiles"], device=0)
+    ft.set_stream(stream.cuda_stream)
+    ft.upload_cholesky(amp["eps_occ"], amp["eps_vir"], amp["t1"], amp["t2"], Loo, Lov, Lvv)
+    t_split, w4, w5, _ = run(ft, tri, "ozaki", **kw)
+    t_fp64, f4, f5, _ = run(ft, fp64_tri, "fp64")
+    ft.close()
+    torch.cuda.empty_cache()
+    # the time of one slab: one v x v^2 x n_chol GEMM
+    slab_flops = 2.0 * v * v * v * nq
+    rows = []
+    for C in [int(x) for x in args.cholesky_direct.split(",") if x]:
+        ft = ct.FusedTriples(o, v, wl["occ_tiles"], wl["vir_tiles"], device=0)
+        ft.set_stream(stream.cuda_stream)
+        ft.upload_cholesky(amp["eps_occ"], amp["eps_vir"], amp["t1"], amp["t2"], Loo, Lov, Lvv, max_ovvv_slabs=C)
+        ts, s4, s5, bs = run(ft, tri, "ozaki", **kw)
+        tf, g4, g5, bf = run(ft, fp64_tri, "fp64")
+        rows.append({"max_ovvv_slabs": min(C, o), "split_call_s": ts, "split_slabs_formed": bs,
+                     "split_vs_whole": ts / t_split, "split_identical": bool(np.array_equal(s5, w5) and
+                                                                             np.array_equal(s4, w4)),
+                     "fp64_sample_s": tf, "fp64_slabs_formed": bf, "fp64_vs_whole": tf / t_fp64,
+                     "fp64_identical": bool(np.array_equal(g5, f5) and np.array_equal(g4, f4)),
+                     "cache_gb": min(C, o) * v ** 3 * 8 / 1e9})
+        print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+        ft.close()
+        torch.cuda.empty_cache()
+    line = {"metric": f"(T) with (ia|bc) formed slab by slab from Cholesky vectors at o={o},v={v},n_chol={nq}: "
+                      "call time vs the whole block",
+            "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64 / bf16 digit planes",
+            "data": "synthetic (seeded amplitudes, random symmetric Cholesky vectors, built on GPU)",
+            "config": wl | {"n_chol": nq, "slices": args.slices, "triplets": int(len(tri)),
+                            "fp64_sample_triplets": int(len(fp64_tri)), "whole_ovvv_gb": o * v ** 3 * 8 / 1e9,
+                            "slab_gemm_flops": slab_flops,
+                            "timing": "host wall clock around one call after a warm-up triplet"},
+            "whole": {"split_call_s": t_split, "fp64_sample_s": t_fp64},
+            "direct": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_slice_sweep(args):
     """Split precision swept over the slice count for BF16 digits (persistent tcgen05 kernel, FP32
     level sums) and INT8 digits (mma.sync IMMA, INT32 level sums), on an evenly spread sample of
@@ -439,6 +516,9 @@ def main():
     ap.add_argument("--sweep", default=None, metavar="S1,S2,...",
                     help="slice-count sweep on a triplet sample instead of the whole call (e.g. 4,5,6,7,8)")
     ap.add_argument("--sweep-kinds", default="bf16,int8", help="digit kinds of the sweep")
+    ap.add_argument("--cholesky-direct", default=None, metavar="C1,C2,...",
+                    help="Cholesky-direct mode: whole call with (ia|bc) slab caches of these sizes vs the whole block")
+    ap.add_argument("--n-chol", type=int, default=0, help="Cholesky vectors for --cholesky-direct (0: 4 (o + v))")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -446,6 +526,8 @@ def main():
         return run_reference(args)
     if args.open_shell:
         return run_open_shell(args)
+    if args.cholesky_direct:
+        return run_cholesky_direct(args)
     if args.sweep:
         return run_slice_sweep(args)
 

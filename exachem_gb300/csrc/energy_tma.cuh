@@ -100,27 +100,29 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
   }
   __syncthreads();
 
-  // one thread issues a unit's eighteen box loads into stage st
+  // the last warp issues a unit's eighteen box loads into stage st, one per lane (lane 0 first
+  // announces the stage's bytes), so the issue is short and off the warps with prefetch extras
   auto issue = [&](int tile, int st) {
     const int3 tt     = A.tiles[tile];
     const int  rb0[3] = {tt.x * B, tt.y * B, tt.z * B};
     auto       b0f    = [&](int p) { return p == 0 ? rb0[0] : p == 1 ? rb0[1] : rb0[2]; };
     TP*        box    = reinterpret_cast<TP*>(em_dyn + st * em_stage_bytes<TP>());
-    // the stage was last read through the generic proxy; the TMA writes it through the async one
-    sm100::fence_proxy_async_smem();
-    sm100::mbar_arrive_expect_tx(&full[st], (uint32_t) em_stage_bytes<TP>());
-#pragma unroll 1
-    for(int b = 0; b < EM_BOXES; b++) {
-      const int  pass = b / 6, q = b % 6;
-      const int* P    = c_perm[q];
+    if(lane == 0) sm100::mbar_arrive_expect_tx(&full[st], (uint32_t) em_stage_bytes<TP>());
+    __syncwarp();
+    if(lane < EM_BOXES) {
+      const int  b = lane, pass = b / 6, q = b % 6;
+      const int* P = c_perm[q];
       // (slowest, middle, fastest) block positions of the pass's array: P12[a][c][b],
       // P34[b][a][c], P56[c][b][a] with a, b, c in the blocks at positions P[0], P[1], P[2]
       const int q0 = pass == 0 ? P[0] : pass == 1 ? P[1] : P[2];
       const int q1 = pass == 0 ? P[2] : pass == 1 ? P[0] : P[1];
       const int q2 = pass == 0 ? P[1] : pass == 1 ? P[2] : P[0];
+      // the stage was last read through the generic proxy; the TMA writes it through the async one
+      sm100::fence_proxy_async_smem();
       sm100::tma_load_4d(box + (size_t) b * B3, &A.pmap, &full[st], b0f(q2), b0f(q1), b0f(q0), 3 * slot + pass);
     }
   };
+  constexpr int kIssueWarp = EM_THREADS / 32 - 1;
   // every thread loads its share of a unit's singles data into registers
   auto prefetch = [&](int tile, EmPrefetch& r) {
     const int3 tt     = A.tiles[tile];
@@ -200,7 +202,7 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
   bool       failed = false;
   EmPrefetch pre{};
   if((int) blockIdx.x < A.ntiles) {
-    if(tid == 0) issue(blockIdx.x, 0);
+    if(warp == kIssueWarp) issue(blockIdx.x, 0);
     prefetch(blockIdx.x, pre);
   }
   // Pipeline: while unit n is evaluated from stage n % 2, unit n + 1's boxes are in flight into the
@@ -212,7 +214,7 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
     __syncthreads(); // stage st's singles are visible; unit n - 1's orbits are done with stage st ^ 1
     const int next = tile + gridDim.x;
     if(next < A.ntiles) {
-      if(tid == 0) issue(next, st ^ 1);
+      if(warp == kIssueWarp) issue(next, st ^ 1);
       prefetch(next, pre);
     }
     const bool ok = sm100::mbar_wait(&full[st], (n >> 1) & 1, A.spin);
