@@ -217,11 +217,11 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
       if(warp == kIssueWarp) issue(next, st ^ 1);
       prefetch(next, pre);
     }
-    const bool ok = sm100::mbar_wait(&full[st], (n >> 1) & 1, A.spin);
-    if(__syncthreads_or(!ok)) { // the boxes never arrived: give up on the call
-      failed = true;
-      break;
-    }
+    // Each thread waits for the boxes itself (the wait makes the TMA's writes visible to it).  A
+    // thread whose wait gave up evaluates nothing more and waits no more, but keeps to the loop's
+    // barriers, so no consensus is needed; the call then reports the timeout.
+    if(!failed && !sm100::mbar_wait(&full[st], (n >> 1) & 1, A.spin)) failed = true;
+    if(failed) continue;
     const EmSingles& S_ = sgl[st];
     const TP*        box = reinterpret_cast<const TP*>(em_dyn + st * em_stage_bytes<TP>());
     const int3       tt  = A.tiles[tile];
@@ -261,7 +261,7 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
       }
     }
   }
-  if(failed && tid == 0) atomicExch(A.err, 1);
+  if(failed) atomicExch(A.err, 1);
   double* part = A.part + 6 * ((long long) slot * gridDim.x + blockIdx.x);
   CSum    c4, c5;
   c4.add((double) s4.hi);
