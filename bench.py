@@ -318,6 +318,19 @@ def run_open_shell(args):
     from exachem_gb300.generator import tiles_uniform
     ref_ops, _ = ct.reference_op_count_so(*(tiles_uniform(n, 40) for n in (oa, ob, va, vb)))
     ntri = O * (O - 1) * (O - 2) // 6
+    # split-precision spin-block contractions (ccsdt_energy_spin_orbital_split) on the same inputs
+    split = []
+    for S_ in [int(x) for x in args.os_slices.split(",") if x]:
+        ct.energy_spin_orbital(oa, ob, va, vb, *dev, slices=S_)
+        ts, rs = [], None
+        for _ in range(args.steps):
+            rs = ct.energy_spin_orbital(oa, ob, va, vb, *dev, slices=S_)
+            ts.append(rs["seconds"])
+        t_ = sum(ts) / len(ts)
+        split.append({"slices": S_, "s_per_call": t_, "speedup_vs_fp64": value / t_,
+                      "rel_error_E(T)": abs(rs["e_paren_T"] - res["e_paren_T"]) / abs(res["e_paren_T"]),
+                      "rel_error_E[T]": abs(rs["e_bracket_T"] - res["e_bracket_T"]) / abs(res["e_bracket_T"]),
+                      "kernel": "oz_gemm_kernel<bf16> (mma.sync) + so_energy_kernel"})
     line = {"metric": f"(T) wall-s open-shell (UHF) FP64 at oa={oa},ob={ob},va={va},vb={vb}", "value": value,
             "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": value * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -335,7 +348,8 @@ def run_open_shell(args):
                     "d2h_bytes_per_step": 16},
             "gpu_launches": spin_orbital_launches(oa, ob, va, vb) * args.steps, "clocks": clk,
             "energies": {"e_bracket_T": res["e_bracket_T"], "e_paren_T": res["e_paren_T"],
-                         "host_equals_device": r2["e_paren_T"] == res["e_paren_T"]}}
+                         "host_equals_device": r2["e_paren_T"] == res["e_paren_T"]},
+            "split_precision": split}
     print(json.dumps(line))
     return 0
 
@@ -519,6 +533,7 @@ def main():
     ap.add_argument("--cholesky-direct", default=None, metavar="C1,C2,...",
                     help="Cholesky-direct mode: whole call with (ia|bc) slab caches of these sizes vs the whole block")
     ap.add_argument("--n-chol", type=int, default=0, help="Cholesky vectors for --cholesky-direct (0: 4 (o + v))")
+    ap.add_argument("--os-slices", default="3,4", help="--open-shell: slice counts of the split-precision calls")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

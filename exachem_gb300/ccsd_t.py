@@ -56,7 +56,7 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky",
             "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config", "ccsdt_energy_spin_orbital",
             "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so", "ccsdt_upload_cholesky_direct",
-            "ccsdt_ovvv_slab_builds", "ccsdt_debug_slab_schedule"]
+            "ccsdt_ovvv_slab_builds", "ccsdt_debug_slab_schedule", "ccsdt_energy_spin_orbital_split"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 
@@ -93,6 +93,7 @@ def load_library(path: str | os.PathLike | None = None):
     lib.ccsdt_autotune.argtypes = [vp, ctypes.c_int, dp, ip, ip]
     lib.ccsdt_set_tile_config.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.ccsdt_energy_spin_orbital.argtypes = [ctypes.c_int] * 4 + [vp] * 7 + [ctypes.c_int] * 3 + [dp, dp]
+    lib.ccsdt_energy_spin_orbital_split.argtypes = [ctypes.c_int] * 4 + [vp] * 7 + [ctypes.c_int] * 4 + [dp, dp]
     lib.ccsdt_debug_spin_orbital_plan.argtypes = [ctypes.c_int] * 7 + [ip, ctypes.POINTER(ctypes.c_longlong), ip]
     lib.ccsdt_reference_op_count_so.argtypes = [ctypes.c_int, ip] * 4 + [ctypes.c_int, dp,
                                                                          ctypes.POINTER(ctypes.c_long)]
@@ -114,7 +115,7 @@ def load_library(path: str | os.PathLike | None = None):
                  "ccsdt_triplet_error_estimates", "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end",
                  "ccsdt_upload_cholesky", "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config",
                  "ccsdt_energy_spin_orbital", "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so",
-                 "ccsdt_upload_cholesky_direct", "ccsdt_debug_slab_schedule"):
+                 "ccsdt_upload_cholesky_direct", "ccsdt_debug_slab_schedule", "ccsdt_energy_spin_orbital_split"):
         getattr(lib, name).restype = ctypes.c_int
     if path is None:
         _lib = lib
@@ -383,12 +384,13 @@ def slab_schedule(o: int, max_ovvv_slabs: int, batch: int, triplets) -> tuple[np
 
 
 def energy_spin_orbital(oa: int, ob: int, va: int, vb: int, eps_occ, eps_vir, t1, t2, v2ijab, v2ijka,
-                        v2iabc, shard_index: int = 0, shard_count: int = 1) -> dict:
+                        v2iabc, shard_index: int = 0, shard_count: int = 1, slices: int = 0) -> dict:
     """Open-shell (T) over spin orbitals (ccsdt_energy_spin_orbital): ExaChem's MO order
     (occupied alpha | beta, virtual alpha | beta), arrays t1[V][O], t2[V][V][O][O],
     v2ijab[O][O][V][V], v2ijka[O][O][O][V], v2iabc[O][V][V][V] as host numpy arrays or CUDA
     tensors (all of one kind).  shard_index / shard_count select every shard_count-th occupied
-    triplet i < j < k."""
+    triplet i < j < k.  slices > 0: split-precision contractions with that many BF16 digit planes
+    (ccsdt_energy_spin_orbital_split)."""
     lib = load_library()
     arrs = [eps_occ, eps_vir, t1, t2, v2ijab, v2ijka, v2iabc]
     kinds = {isinstance(a, np.ndarray) for a in arrs}
@@ -402,9 +404,13 @@ def energy_spin_orbital(oa: int, ob: int, va: int, vb: int, eps_occ, eps_vir, t1
     on_device = 0 if kinds == {True} else 1
     e = (ctypes.c_double * 2)()
     sec = ctypes.c_double()
-    st = lib.ccsdt_energy_spin_orbital(oa, ob, va, vb, *[_ptr(a) for a in arrs], on_device, shard_index,
-                                       shard_count, ctypes.cast(e, ctypes.POINTER(ctypes.c_double)),
-                                       ctypes.byref(sec))
+    out = ctypes.cast(e, ctypes.POINTER(ctypes.c_double))
+    if slices > 0:
+        st = lib.ccsdt_energy_spin_orbital_split(oa, ob, va, vb, *[_ptr(a) for a in arrs], on_device, shard_index,
+                                                 shard_count, slices, out, ctypes.byref(sec))
+    else:
+        st = lib.ccsdt_energy_spin_orbital(oa, ob, va, vb, *[_ptr(a) for a in arrs], on_device, shard_index,
+                                           shard_count, out, ctypes.byref(sec))
     if st:
         raise CCSDTError(st, lib.ccsdt_status_string(st).decode())
     return {"e_bracket_T": e[0], "e_paren_T": e[1], "seconds": sec.value}

@@ -11,6 +11,10 @@
 #include "ovvv_slabs.h"
 
 namespace ccsdt {
+struct OzBatch;
+// BF16-digit Ozaki GEMMs (mma.sync kernel) of up to three jobs on a stream, and its tile count
+cudaError_t oz_gemm_bf16(const OzBatch& b, int njobs, long long max_tiles, cudaStream_t st);
+long long   oz_gemm_tiles(long long M, long long N);
 // Every device allocation of the handle-based paths goes through here: cudaMalloc, except that a
 // testing countdown (ccsdt_debug_fail_alloc) can make the n-th call fail as an out-of-memory
 // cudaMalloc would (*p = nullptr, cudaErrorMemoryAllocation), so the error paths can be exercised.

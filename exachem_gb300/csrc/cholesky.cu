@@ -183,7 +183,7 @@ ccsdt_status ccsdt_handle::ensure_ovvv(const int* need, int n, bool planes) {
       if(slab_sliced[c]) continue;
       oz_slice_rows_kernel<__nv_bfloat16><<<2048, 256, 0, stream>>>(
         ovvv + c * v3, vv * vv, v, kp_v, slices_ready, (__nv_bfloat16*) sl_ovvv + (long long) c * vv * vv * kp_v,
-        pl_ovvv, ex_ovvv + (long long) c * vv * vv);
+        pl_ovvv, ex_ovvv + (long long) c * vv * vv, vv);
       cudaError_t e = cudaGetLastError();
       if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("(ia|bc) slab slicing: ") + cudaGetErrorString(e));
       slab_sliced[c] = 1;

@@ -170,7 +170,8 @@ __device__ __forceinline__ PzItem pz_decode(unsigned id, int v, int yblocks, int
 // quarter q, row = 32 q + lane) x COLS = NT / 4 columns from c_lo.  Per term it waits for the MMAs
 // (lvl_full of the term's buffer), folds the S exact levels with oz_horner in chunks of 8 columns
 // and adds (d-sum terms) or subtracts (l-sum terms) them in float-float, releases the buffer
-// (lvl_empty); finally it renormalises, scales by 2^(-7 (S + 1)) and stores the tile once.  The
+// (lvl_empty); finally it renormalises, scales by 2^(-7 (S + 1)) and stores the tile once (FP32
+// partial arrays: the fold and the term sums in FP32, one store per element).  The
 // BF16 digits carry the row scales, so the levels need no per-row or per-column factor.  Returns
 // false when a bounded wait gave up.
 template<int S, int NT, int NBUF, int KC>
@@ -201,6 +202,18 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
     // item's first term (the accumulators start from it)
     auto fold = [&](auto& rv, int c0, auto wtag, bool neg, bool first) {
       constexpr int W = decltype(wtag)::value;
+      if(P.f32_out) { // FP32 partial arrays: FP32 fold and term sums (a few roundings per element)
+#pragma unroll
+        for(int e = 0; e < W; e++) {
+          const float x = oz_horner_f32<S, W>(rv, e);
+          hi[c0 + e]    = first ? (neg ? -x : x) : (neg ? hi[c0 + e] - x : hi[c0 + e] + x);
+          if(P.tail) {
+            const float tl = __uint_as_float(rv[S - 1][e]) * kScale;
+            tsq            = fmaf(tl, tl, tsq);
+          }
+        }
+        return;
+      }
 #pragma unroll
       for(int e = 0; e < W; e++) {
         const ff    x  = oz_horner<S, W>(rv, e);
@@ -276,11 +289,11 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
     else run(true, false);
   }
   if(y < v) {
-    if(P.f32_out) { // one rounding of the float-float sum; the power-of-two scale is exact
+    if(P.f32_out) { // the FP32 sums; the power-of-two scale is exact
       float* Cf = reinterpret_cast<float*>(P.F) + e0;
 #pragma unroll
       for(int e = 0; e < COLS; e++)
-        if(n0 + e < v) Cf[(long long) (n0 + e) * v2] = (hi[e] + lo[e]) * kScale;
+        if(n0 + e < v) Cf[(long long) (n0 + e) * v2] = hi[e] * kScale;
     } else {
       float2* Cb = P.F + e0;
 #pragma unroll

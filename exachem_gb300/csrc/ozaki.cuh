@@ -130,6 +130,17 @@ __device__ __forceinline__ ff oz_horner(const uint32_t (&L)[S][W], int e) {
   return ff{hi, lo};
 }
 
+// The same fold rounded to FP32 (one rounding per level step): for partial arrays stored in FP32,
+// whose element error is then a few FP32 roundings, far below the truncation of one or two digit
+// planes.
+template<int S, int W = 16>
+__device__ __forceinline__ float oz_horner_f32(const uint32_t (&L)[S][W], int e) {
+  float x = __uint_as_float(L[0][e]);
+#pragma unroll
+  for(int l = 1; l < S; l++) x = __fmaf_rn(x, 128.f, __uint_as_float(L[l][e]));
+  return x;
+}
+
 // ---------------------------------------------------------------------------------- slicing
 // Rows of a dense FP64 array [R][K] -> S digit planes [S][R][Kp] (Kp >= K, zero padded) and
 // exponents e[R].  One warp per row.  Row r ~ 2^e[r] sum_p d_p 2^{-7 (p + 1)} with integer digits
@@ -149,13 +160,15 @@ __device__ __forceinline__ int8_t oz_digit<int8_t>(double d, int) {
   return (int8_t) (int) d;
 }
 
+// Row r of the source is x[r * ld .. r * ld + K) (ld = K for a dense array; larger to slice a
+// column range of each row).
 template<typename T>
 __global__ void oz_slice_rows_kernel(const double* __restrict__ x, long long R, int K, int Kp, int S,
-                                     T* __restrict__ out, long long plane, int* __restrict__ exps) {
+                                     T* __restrict__ out, long long plane, int* __restrict__ exps, long long ld) {
   const int       lane = threadIdx.x & 31;
   const long long warps = (long long) gridDim.x * (blockDim.x >> 5);
   for(long long r = (long long) blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < R; r += warps) {
-    const double* row = x + r * K;
+    const double* row = x + r * ld;
     double        mx  = 0.0;
     for(int k = lane; k < K; k += 32) mx = fmax(mx, fabs(row[k]));
 #pragma unroll

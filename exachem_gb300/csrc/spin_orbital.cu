@@ -36,6 +36,7 @@
 #include "../../include/ccsdt.h"
 #include "ccsdt_internal.cuh"
 #include "fp64_kernels.cuh"
+#include "ozaki.cuh"
 
 using namespace ccsdt;
 
@@ -61,10 +62,12 @@ __global__ void __launch_bounds__(256) permute4_kernel(const double* __restrict_
   }
 }
 
-// One spin block X[x - x0][(y - y0) nz + (z - z0)]; X == nullptr: the block is zero.
+// One spin block X[x - x0][(y - y0) nz + (z - z0)], FP64 (X) or float-float (Xf, the split path);
+// both null: the block is zero.
 struct SoBlock {
   const double* X;
   int           x0, y0, z0, ny, nz;
+  const float2* Xf;
 };
 
 struct SoEnergyArgs {
@@ -88,7 +91,12 @@ struct SoSpins {
 __host__ __device__ inline bool same_pair(int p, int q, int r, int s) { return p + q == r + s; }
 
 __device__ __forceinline__ double so_x(const SoBlock& b, int x, int y, int z) {
-  return b.X ? b.X[((long long) (x - b.x0) * b.ny + (y - b.y0)) * b.nz + (z - b.z0)] : 0.0;
+  const long long e = ((long long) (x - b.x0) * b.ny + (y - b.y0)) * b.nz + (z - b.z0);
+  if(b.Xf) {
+    const float2 f = b.Xf[e];
+    return (double) f.x + (double) f.y;
+  }
+  return b.X ? b.X[e] : 0.0;
 }
 
 // Energy of one triplet: W and V at every a < b < c of the triplet's spin pattern, restating
@@ -242,11 +250,71 @@ SoPlan so_plan(const SoSpins& S, int i, int j, int k) {
   return P;
 }
 
+// Digit planes (BF16, S planes) of the four contraction operands for the split path, one set per
+// spin of the contraction index: tt / vv over e of spin s (columns [vlo(s), vlo(s) + vn(s)) of
+// their rows), uu / t2 over m of spin s.  Row r of set (X, s) at X[s] + r Kp, plane stride R Kp.
+struct SoPlanes {
+  int                   S = 0;
+  const __nv_bfloat16 * tt[2] = {}, *vv[2] = {}, *uu[2] = {}, *t2[2] = {};
+  long long             Kv[2] = {}, Ko[2] = {};               // padded contraction lengths
+  long long             R_tt = 0, R_vv = 0, R_uu = 0, R_t2 = 0; // rows
+};
+
 // Launches a triplet's plan on `st` (block b into slots[b], up to three GEMM jobs per launch) and
-// fills the energy kernel's block table.
+// fills the energy kernel's block table.  With planes (pl.S > 0): BF16-digit Ozaki GEMMs with
+// float-float blocks, from the spin's digit planes.
 cudaError_t so_contract(const SoSpins& S, const SoPlan& P, const double* tt, const double* vv, const double* uu,
-                        const double* t2, double* const* slots, SoBlock (&blk)[3][3], cudaStream_t st) {
+                        const double* t2, double* const* slots, SoBlock (&blk)[3][3], cudaStream_t st,
+                        const SoPlanes& pl) {
   const long long O = S.O, V = S.V;
+  if(pl.S > 0) {
+    OzBatch   batch{};
+    int       nj = 0;
+    long long max_tiles = 0;
+    batch.S = pl.S;
+    for(int b = 0; b < P.nblk; b++) {
+      const SoPlanBlock& B = P.blk[b];
+      OzJob              J{};
+      int                nt = 0;
+      if(B.has_d) { // rows of tt (j, k, a) and vv (i, b, c); e of the spin the block's offset starts at
+        const long long e0 = B.d_a % V;
+        const int       se = (e0 == S.va && B.d_k == S.V - S.va) ? 1 : 0;
+        const long long Kp = pl.Kv[se];
+        J.t[nt++] = OzTerm{pl.tt[se] + (B.d_a / V) * Kp, nullptr, oz_plain(), pl.R_tt * Kp,
+                           pl.vv[se] + (B.d_b / V) * Kp, nullptr, OzRows{V, 1, B.nz}, pl.R_vv * Kp, (int) Kp, -1.f};
+      }
+      if(B.has_s) { // rows of uu (j, k, a) and t2 (b, c, i); m of the block's spin
+        const long long m0 = B.s_a % O;
+        const int       sm = (m0 == S.oa && B.s_k == S.O - S.oa) ? 1 : 0;
+        const long long Kp = pl.Ko[sm];
+        J.t[nt++] = OzTerm{pl.uu[sm] + (B.s_a / O) * Kp, nullptr, oz_plain(), pl.R_uu * Kp,
+                           pl.t2[sm] + (B.s_b / O) * Kp, nullptr, OzRows{V * O, O, B.nz}, pl.R_t2 * Kp, (int) Kp, -1.f};
+      }
+      J.nterms        = nt;
+      J.C             = reinterpret_cast<float2*>(slots[b]);
+      J.M             = B.nx;
+      J.N             = (long long) B.ny * B.nz;
+      J.accumulate    = 0;
+      batch.job[nj++] = J;
+      max_tiles       = std::max(max_tiles, oz_gemm_tiles(J.M, J.N));
+      if(nj == 3 || b == P.nblk - 1) {
+        const cudaError_t e = oz_gemm_bf16(batch, nj, max_tiles, st);
+        if(e != cudaSuccess) return e;
+        batch     = OzBatch{};
+        batch.S   = pl.S;
+        nj        = 0;
+        max_tiles = 0;
+      }
+    }
+    for(int p = 0; p < 3; p++)
+      for(int q = 0; q < 3; q++) {
+        const int b = P.of[p][q];
+        blk[p][q]   = b < 0 ? SoBlock{nullptr, 0, 0, 0, 0, 0, nullptr}
+                            : SoBlock{nullptr,         P.blk[b].x0, P.blk[b].y0, P.blk[b].z0, P.blk[b].ny, P.blk[b].nz,
+                                      reinterpret_cast<const float2*>(slots[b])};
+      }
+    return cudaSuccess;
+  }
   GemmBatch       batch{};
   int             nj        = 0;
   long long       max_tiles = 0;
@@ -279,8 +347,8 @@ cudaError_t so_contract(const SoSpins& S, const SoPlan& P, const double* tt, con
   for(int p = 0; p < 3; p++)
     for(int q = 0; q < 3; q++) {
       const int b = P.of[p][q];
-      blk[p][q]   = b < 0 ? SoBlock{nullptr, 0, 0, 0, 0, 0}
-                          : SoBlock{slots[b], P.blk[b].x0, P.blk[b].y0, P.blk[b].z0, P.blk[b].ny, P.blk[b].nz};
+      blk[p][q]   = b < 0 ? SoBlock{nullptr, 0, 0, 0, 0, 0, nullptr}
+                          : SoBlock{slots[b], P.blk[b].x0, P.blk[b].y0, P.blk[b].z0, P.blk[b].ny, P.blk[b].nz, nullptr};
     }
   return cudaSuccess;
 }
@@ -318,12 +386,13 @@ void launch_permute(const double* src, double* dst, long long n0, long long n1, 
 
 } // namespace
 
-extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb, const double* eps_occ,
-                                                  const double* eps_vir, const double* t1, const double* t2,
-                                                  const double* v2ijab, const double* v2ijka,
-                                                  const double* v2iabc, int on_device, int shard_index,
-                                                  int shard_count, double* energies, double* seconds) {
-  if(oa < 0 || ob < 0 || va < 0 || vb < 0 || !energies) return CCSDT_E_INVALID;
+// slices = 0: FP64 DMMA contractions; 1..6: BF16 digit planes of the operands (Ozaki GEMMs on
+// mma.sync, float-float blocks), the FP64 energy unchanged.
+static ccsdt_status so_energy(int oa, int ob, int va, int vb, const double* eps_occ, const double* eps_vir,
+                              const double* t1, const double* t2, const double* v2ijab, const double* v2ijka,
+                              const double* v2iabc, int on_device, int shard_index, int shard_count, int slices,
+                              double* energies, double* seconds) {
+  if(oa < 0 || ob < 0 || va < 0 || vb < 0 || !energies || slices < 0 || slices > 6) return CCSDT_E_INVALID;
   if(shard_count <= 1) shard_count = 1, shard_index = 0;
   if(shard_index < 0 || shard_index >= shard_count) return CCSDT_E_INVALID;
   if(oa > 4096 || ob > 4096 || va > 4096 || vb > 4096) return CCSDT_E_INVALID;
@@ -387,6 +456,36 @@ extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb
     d_ijka = stage;
   }
   launch_permute(d_ijka, uu, O, O, V, O, O * O * V, O * V, 1, V, st);
+  // split path: digit planes of tt, vv (over e) and uu, t2 (over m), per spin of the contraction index
+  SoPlanes pl;
+  if(slices > 0 && e == cudaSuccess) {
+    pl.S    = slices;
+    pl.R_tt = O * O * V, pl.R_vv = O * V * V, pl.R_uu = O * O * V, pl.R_t2 = V * V * O;
+    for(int sp = 0; sp < 2 && e == cudaSuccess; sp++) {
+      const long long nv = S.vn(sp), no = sp ? O - oa : oa, v0 = S.vlo(sp), o0 = sp ? oa : 0;
+      pl.Kv[sp] = (nv + 31) / 32 * 32, pl.Ko[sp] = (no + 31) / 32 * 32;
+      struct {
+        const double*          x;
+        long long              R, K, Kp, ld;
+        const __nv_bfloat16**  out;
+      } q[4] = {{tt + v0, pl.R_tt, nv, pl.Kv[sp], V, &pl.tt[sp]}, {vv + v0, pl.R_vv, nv, pl.Kv[sp], V, &pl.vv[sp]},
+                {uu + o0, pl.R_uu, no, pl.Ko[sp], O, &pl.uu[sp]}, {d_t2 + o0, pl.R_t2, no, pl.Ko[sp], O, &pl.t2[sp]}};
+      for(auto& c: q) {
+        if(c.K == 0 || e != cudaSuccess) continue;
+        // BF16 planes and the (unused) row exponents in one allocation of doubles
+        const long long bytes = (long long) slices * c.R * c.Kp * 2 + c.R * 4;
+        double*         buf   = M.alloc((size_t) ((bytes + 7) / 8), e);
+        if(e != cudaSuccess) break;
+        auto* planes = reinterpret_cast<__nv_bfloat16*>(buf);
+        auto* exps   = reinterpret_cast<int*>(reinterpret_cast<char*>(buf) + (long long) slices * c.R * c.Kp * 2);
+        oz_slice_rows_kernel<__nv_bfloat16><<<4096, 256, 0, st>>>(c.x, c.R, (int) c.K, (int) c.Kp, slices, planes,
+                                                                   c.R * c.Kp, exps, c.ld);
+        e      = cudaGetLastError();
+        *c.out = planes;
+      }
+    }
+    if(e != cudaSuccess) return e == cudaErrorMemoryAllocation ? CCSDT_E_OOM : CCSDT_E_CUDA;
+  }
   if(e == cudaSuccess) e = cudaMemsetAsync(part, 0, (size_t) kSoStreams * kSoGrid * 4 * sizeof(double), st);
   if(e == cudaSuccess) e = cudaGetLastError();
   if(e == cudaSuccess) e = cudaEventRecord(M.ev[1], st);
@@ -402,7 +501,7 @@ extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb
         if((long long) na * nb * nc == 0) continue;
         const int    s  = (int) (n++ % kSoStreams);
         SoEnergyArgs A{};
-        e = so_contract(S, so_plan(S, i, j, k), tt, vv, uu, d_t2, slots[s], A.blk, M.streams[s]);
+        e = so_contract(S, so_plan(S, i, j, k), tt, vv, uu, d_t2, slots[s], A.blk, M.streams[s], pl);
         if(e != cudaSuccess) break;
         A.eps_o = d_eo, A.eps_v = d_ev, A.t1 = d_t1, A.v2ijab = d_ijab;
         A.O = (int) O, A.V = (int) V, A.oa = oa, A.va = va;
@@ -442,6 +541,26 @@ extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb
   }
   if(!std::isfinite(energies[0]) || !std::isfinite(energies[1])) return CCSDT_E_NONFINITE;
   return CCSDT_OK;
+}
+
+extern "C" ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb, const double* eps_occ,
+                                                  const double* eps_vir, const double* t1, const double* t2,
+                                                  const double* v2ijab, const double* v2ijka,
+                                                  const double* v2iabc, int on_device, int shard_index,
+                                                  int shard_count, double* energies, double* seconds) {
+  return so_energy(oa, ob, va, vb, eps_occ, eps_vir, t1, t2, v2ijab, v2ijka, v2iabc, on_device, shard_index,
+                   shard_count, 0, energies, seconds);
+}
+
+extern "C" ccsdt_status ccsdt_energy_spin_orbital_split(int oa, int ob, int va, int vb, const double* eps_occ,
+                                                        const double* eps_vir, const double* t1, const double* t2,
+                                                        const double* v2ijab, const double* v2ijka,
+                                                        const double* v2iabc, int on_device, int shard_index,
+                                                        int shard_count, int slices, double* energies,
+                                                        double* seconds) {
+  if(slices < 1) return CCSDT_E_INVALID;
+  return so_energy(oa, ob, va, vb, eps_occ, eps_vir, t1, t2, v2ijab, v2ijka, v2iabc, on_device, shard_index,
+                   shard_count, slices, energies, seconds);
 }
 
 extern "C" ccsdt_status ccsdt_debug_spin_orbital_plan(int oa, int ob, int va, int vb, int i, int j, int k, int* of,

@@ -67,6 +67,7 @@ __global__ void __launch_bounds__(OZ_THREADS) oz_gemm_kernel(const __grid_consta
   using Acc = typename Tr::Acc;
   const OzJob&    J       = batch.job[blockIdx.z];
   const int       S       = batch.S;
+  if(J.nterms <= 0 || J.M <= 0 || J.N <= 0) return; // an unused job of the batch
   const long long tiles_n = (J.N + OZ_BN - 1) / OZ_BN;
   const long long m0 = (long long) (blockIdx.x / tiles_n) * OZ_BM, n0 = (long long) (blockIdx.x % tiles_n) * OZ_BN;
   if(m0 >= J.M || n0 >= J.N) return;
@@ -277,9 +278,11 @@ ccsdt_status ccsdt_handle::ensure_slices(int S, int variant) {
       continue;
     }
     if(variant == 0)
-      oz_slice_rows_kernel<__nv_bfloat16><<<4096, 256, 0, stream>>>(q.x, q.R, q.K, q.Kp, S, (__nv_bfloat16*) *q.planes, *q.plane, *q.exps);
+      oz_slice_rows_kernel<__nv_bfloat16><<<4096, 256, 0, stream>>>(q.x, q.R, q.K, q.Kp, S, (__nv_bfloat16*) *q.planes,
+                                                                     *q.plane, *q.exps, q.K);
     else
-      oz_slice_rows_kernel<int8_t><<<4096, 256, 0, stream>>>(q.x, q.R, q.K, q.Kp, S, (int8_t*) *q.planes, *q.plane, *q.exps);
+      oz_slice_rows_kernel<int8_t><<<4096, 256, 0, stream>>>(q.x, q.R, q.K, q.Kp, S, (int8_t*) *q.planes, *q.plane,
+                                                             *q.exps, q.K);
     cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("slicing: ") + cudaGetErrorString(e));
   }
@@ -561,6 +564,19 @@ static ccsdt_status launch_oz(ccsdt_handle* h, const OzBatch& b, long long M, lo
   if(e != cudaSuccess) return h->fail(CCSDT_E_CUDA, std::string("oz_gemm launch: ") + cudaGetErrorString(e));
   return CCSDT_OK;
 }
+
+// BF16-digit Ozaki GEMMs of up to three jobs (grid z = njobs) on `st`, for translation units
+// without the kernel (the open-shell split path)
+cudaError_t ccsdt::oz_gemm_bf16(const OzBatch& b, int njobs, long long max_tiles, cudaStream_t st) {
+  if(njobs < 1 || njobs > 3 || max_tiles <= 0 || max_tiles >= (1LL << 31)) return cudaErrorInvalidValue;
+  const size_t sm = oz_smem<__nv_bfloat16>(b.S);
+  cudaError_t  e  = cudaFuncSetAttribute(oz_gemm_kernel<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int) sm);
+  if(e != cudaSuccess) return e;
+  oz_gemm_kernel<__nv_bfloat16><<<dim3((unsigned) max_tiles, 1, (unsigned) njobs), OZ_THREADS, sm, st>>>(b);
+  return cudaGetLastError();
+}
+long long ccsdt::oz_gemm_tiles(long long M, long long N) { return ((M + OZ_BM - 1) / OZ_BM) * ((N + OZ_BN - 1) / OZ_BN); }
 
 ccsdt_status ccsdt_handle::run_triplet_split(int i, int j, int k, int S, int variant, double* eout) {
   const long long o = this->o, v = this->v, v2 = v * v;

@@ -314,6 +314,17 @@ ccsdt_status ccsdt_energy_spin_orbital(int oa, int ob, int va, int vb, const dou
                                        const double* v2iabc, int on_device, int shard_index,
                                        int shard_count, double* energies, double* seconds);
 
+/* The same open-shell (T) with split-precision contractions: every operand of the spin-block
+ * GEMMs cut into `slices` (1..6) BF16 digit planes carrying their rows' power-of-two scales (one
+ * set per spin of the contraction index), exact FP32 level sums on the tensor cores (mma.sync),
+ * float-float blocks; the energy is the FP64 one of ccsdt_energy_spin_orbital.  Arguments and
+ * results as there. */
+ccsdt_status ccsdt_energy_spin_orbital_split(int oa, int ob, int va, int vb, const double* eps_occ,
+                                             const double* eps_vir, const double* t1, const double* t2,
+                                             const double* v2ijab, const double* v2ijka,
+                                             const double* v2iabc, int on_device, int shard_index,
+                                             int shard_count, int slices, double* energies, double* seconds);
+
 /* Testing: the contraction plan of triplet i < j < k of an open-shell system (pure host logic).
  * of[9]: for permutation p (ijk, jik, kji) and position q ((a; b c), (b; a c), (c; b a)) the
  * block the energy reads at of[3p + q], -1 where it is zero; blocks[14 b + ...] for b < *nblk:

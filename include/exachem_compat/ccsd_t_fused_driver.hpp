@@ -395,16 +395,27 @@ CholeskyInputs gather_cholesky(const std::vector<size_t>& mo_tiles, size_t noa, 
 
 // (T) with the integral blocks built on the device from Cholesky vectors (ccsdt_upload_cholesky);
 // the amplitudes and orbital energies come from gather_amplitudes.  Returns (E[T], E(T), device s).
+// max_ovvv_slabs > 0: the Cholesky-direct mode, (ia|bc) never held whole but formed slab by slab
+// into a cache of that many v^3 slabs (ccsdt_upload_cholesky_direct); 0 takes
+// EXACHEM_GB300_OVVV_SLABS from the environment (unset or 0: (ia|bc) built whole).
 inline std::tuple<double, double, double> run_closed_shell_cholesky(const SpatialInputs& S, const CholeskyInputs& C,
-                                                                    int device, const ccsdt_opts& opts) {
+                                                                    int device, const ccsdt_opts& opts,
+                                                                    int max_ovvv_slabs = 0) {
+  if(max_ovvv_slabs <= 0) {
+    const char* e  = std::getenv("EXACHEM_GB300_OVVV_SLABS");
+    max_ovvv_slabs = e ? std::atoi(e) : 0;
+  }
   if(C.o != S.o || C.v != S.v) throw std::invalid_argument("Cholesky vectors and amplitudes differ in o / v");
   ccsdt_layout  L{S.o, S.v, (int) S.occ_tiles.size(), S.occ_tiles.data(), (int) S.vir_tiles.size(),
                  S.vir_tiles.data()};
   ccsdt_handle* h  = nullptr;
   ccsdt_status  st = ccsdt_create(&h, &L, device);
   if(st != CCSDT_OK) throw std::runtime_error(std::string("ccsdt_create: ") + ccsdt_status_string(st));
-  st = ccsdt_upload_cholesky(h, S.eps_occ.data(), S.eps_vir.data(), S.t1.data(), S.t2.data(), C.nq, C.L_oo.data(),
-                             C.L_ov.data(), C.L_vv.data(), 0);
+  st = max_ovvv_slabs > 0
+         ? ccsdt_upload_cholesky_direct(h, S.eps_occ.data(), S.eps_vir.data(), S.t1.data(), S.t2.data(), C.nq,
+                                        C.L_oo.data(), C.L_ov.data(), C.L_vv.data(), 0, max_ovvv_slabs)
+         : ccsdt_upload_cholesky(h, S.eps_occ.data(), S.eps_vir.data(), S.t1.data(), S.t2.data(), C.nq,
+                                 C.L_oo.data(), C.L_ov.data(), C.L_vv.data(), 0);
   ccsdt_result r{};
   if(st == CCSDT_OK) st = ccsdt_energy(h, &opts, &r);
   if(st != CCSDT_OK) {

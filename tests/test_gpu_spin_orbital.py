@@ -119,3 +119,34 @@ def test_open_shell_bench_line(built):
         assert k in line, k
     assert line["value"] > 0 and line["e2e"]["value"] > 0 and line["gpu_launches"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["energies"]["host_equals_device"]
+
+
+@pytest.mark.parametrize("oa,ob,va,vb,seed", [(4, 3, 6, 7, 6), (6, 4, 10, 12, 10), (3, 0, 4, 0, 1), (0, 4, 0, 5, 2)])
+def test_split_open_shell_close_to_fp64(built, oa, ob, va, vb, seed):
+    """Split-precision spin-block contractions (BF16 digit planes per spin of the contraction
+    index): the error against the FP64 path shrinks with the slice count, alpha-only and beta-only
+    systems included."""
+    arrs = open_shell_system(oa, ob, va, vb, 7, seed)
+    f4, f5 = _call(oa, ob, va, vb, arrs)
+    errs = {}
+    for S, tol in ((2, 5e-5), (3, 1e-6), (4, 5e-9), (6, 1e-11)):
+        g4, g5 = _call(oa, ob, va, vb, arrs, slices=S)
+        errs[S] = abs(g5 - f5) / abs(f5)
+        assert errs[S] <= tol and abs(g4 - f4) <= tol * abs(f4), (S, errs)
+    assert errs[4] < errs[2]
+
+
+def test_split_open_shell_larger_system(built):
+    """A ragged spin split at the size where the contraction dominates: S = 4 within 1e-9 of the
+    FP64 path, and the shards of the split path sum to its whole."""
+    import torch
+    oa, ob, va, vb = 7, 5, 60, 48
+    arrs = open_shell_system(oa, ob, va, vb, 30, 21)
+    dev = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrs]
+    f4, f5 = _call(oa, ob, va, vb, dev)
+    g4, g5 = _call(oa, ob, va, vb, dev, slices=4)
+    assert rel_close(g5, f5, 1e-9) and rel_close(g4, f4, 1e-9), (g5, f5)
+    parts = [_call(oa, ob, va, vb, dev, shard_index=s, shard_count=2, slices=4) for s in range(2)]
+    assert rel_close(parts[0][1] + parts[1][1], g5, 1e-13)
+    with pytest.raises(ccsd_t.CCSDTError):
+        _call(oa, ob, va, vb, dev, slices=7)
