@@ -44,14 +44,19 @@ struct TmaEnergyArgs {
   unsigned      spin;
 };
 
-// bytes of dynamic shared memory: the eighteen boxes of each of the two pipeline stages
+// bytes of dynamic shared memory: the eighteen boxes of each of the NST box stages
 template<typename TP>
 constexpr size_t em_stage_bytes() {
   return (size_t) EM_BOXES * ET_B * ET_B * ET_B * sizeof(TP);
 }
-template<typename TP>
+template<typename TP, int NST>
 constexpr size_t em_smem_bytes() {
-  return 2 * em_stage_bytes<TP>();
+  return NST * em_stage_bytes<TP>();
+}
+// resident CTAs per SM the shared memory allows (the launch bounds follow it)
+template<typename TP, int NST>
+constexpr int em_min_blocks() {
+  return std::is_same<TP, float>::value ? (NST == 2 ? 2 : 4) : (NST == 2 ? 1 : 2);
 }
 
 // Per-stage shared data of a unit besides the boxes: the singles' integrals and amplitudes of its
@@ -74,9 +79,12 @@ struct EmPrefetch {
   int    on;       // distinct-cube flag, threads 96..101
 };
 
-template<typename TP>
-static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::value ? 2 : 1)
+// NST = 2: unit n + 1's boxes load into the other stage while unit n is evaluated; NST = 1: one
+// stage (the load waits for the previous unit's orbits), twice the resident CTAs hiding it.
+template<typename TP, int NST>
+static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
   energy_tma_batch_kernel(const __grid_constant__ TmaEnergyArgs A) {
+  static_assert(NST == 1 || NST == 2, "one or two box stages");
   constexpr int  B = ET_B, B3 = B * B * B;
   constexpr bool kF32 = std::is_same<TP, float>::value;
   extern __shared__ __align__(128) unsigned char em_dyn[];
@@ -202,27 +210,29 @@ static __global__ void __launch_bounds__(EM_THREADS, std::is_same<TP, float>::va
   bool       failed = false;
   EmPrefetch pre{};
   if((int) blockIdx.x < A.ntiles) {
-    if(warp == kIssueWarp) issue(blockIdx.x, 0);
+    if(NST == 2 && warp == kIssueWarp) issue(blockIdx.x, 0);
     prefetch(blockIdx.x, pre);
   }
-  // Pipeline: while unit n is evaluated from stage n % 2, unit n + 1's boxes are in flight into the
-  // other stage and its singles data in registers.
+  // Pipeline: while unit n is evaluated, unit n + 1's singles data are in registers and (two
+  // stages) its boxes in flight into the other stage.  The singles always have two stages.
   int n = 0;
   for(int tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x, n++) {
-    const int st = n & 1;
-    store(pre, sgl[st]);
-    __syncthreads(); // stage st's singles are visible; unit n - 1's orbits are done with stage st ^ 1
+    const int ss = n & 1, st = NST == 2 ? ss : 0;
+    store(pre, sgl[ss]);
+    __syncthreads(); // the unit's singles are visible; unit n - 1's orbits are done with its box stage
     const int next = tile + gridDim.x;
+    if(NST == 1 && warp == kIssueWarp) issue(tile, 0);
     if(next < A.ntiles) {
-      if(warp == kIssueWarp) issue(next, st ^ 1);
+      if(NST == 2 && warp == kIssueWarp) issue(next, st ^ 1);
       prefetch(next, pre);
     }
     // Each thread waits for the boxes itself (the wait makes the TMA's writes visible to it).  A
     // thread whose wait gave up evaluates nothing more and waits no more, but keeps to the loop's
     // barriers, so no consensus is needed; the call then reports the timeout.
-    if(!failed && !sm100::mbar_wait(&full[st], (n >> 1) & 1, A.spin)) failed = true;
+    const uint32_t parity = NST == 2 ? (n >> 1) & 1 : n & 1;
+    if(!failed && !sm100::mbar_wait(&full[st], parity, A.spin)) failed = true;
     if(failed) continue;
-    const EmSingles& S_ = sgl[st];
+    const EmSingles& S_ = sgl[ss];
     const TP*        box = reinterpret_cast<const TP*>(em_dyn + st * em_stage_bytes<TP>());
     const int3       tt  = A.tiles[tile];
     const int        rbn[3] = {min(B, v - tt.x * B), min(B, v - tt.y * B), min(B, v - tt.z * B)};

@@ -137,25 +137,26 @@ int ccsdt_handle::energy_grid(bool f32) {
   return g;
 }
 
-int ccsdt_handle::energy_tma_grid(bool f32) {
-  int& g = energy_tma_grid_[f32 ? 1 : 0];
-  if(g > 0) return g;
-  int sm = 0, per = 0;
-  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
-  // the float-float boxes (72 KB) exceed the default dynamic shared-memory limit
-  if(f32) {
-    cudaFuncSetAttribute(energy_tma_batch_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) em_smem_bytes<float>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tma_batch_kernel<float>, EM_THREADS,
-                                                  em_smem_bytes<float>());
-  } else {
-    cudaFuncSetAttribute(energy_tma_batch_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int) em_smem_bytes<float2>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tma_batch_kernel<float2>, EM_THREADS,
-                                                  em_smem_bytes<float2>());
-  }
-  g = std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
+// Grid of one resident wave of the TMA energy kernel (element type, box stages); sets the kernel's
+// dynamic shared-memory limit first (the boxes exceed the default 48 KB).
+template<typename TP, int NST>
+static int tma_energy_wave(int sm) {
+  int per = 0;
+  cudaFuncSetAttribute(energy_tma_batch_kernel<TP, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int) em_smem_bytes<TP, NST>());
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tma_batch_kernel<TP, NST>, EM_THREADS,
+                                                em_smem_bytes<TP, NST>());
   cudaGetLastError();
+  return std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
+}
+
+int ccsdt_handle::energy_tma_grid(bool f32, int nst) {
+  int& g = energy_tma_grid_[(f32 ? 1 : 0) + 2 * (nst - 1)];
+  if(g > 0) return g;
+  int sm = 0;
+  cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
+  g = f32 ? (nst == 2 ? tma_energy_wave<float, 2>(sm) : tma_energy_wave<float, 1>(sm))
+          : (nst == 2 ? tma_energy_wave<float2, 2>(sm) : tma_energy_wave<float2, 1>(sm));
   return g;
 }
 
@@ -216,15 +217,20 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   if(tv[1]) cudaEventRecord(tv[1], stream);
   if(e == cudaSuccess) {
     int G = 0;
-    if(!test_energy_passes && ensure_pmap(f32)) {
+    if(test_energy_passes != 1 && ensure_pmap(f32)) {
       // the partial arrays staged by TMA, eighteen 8 x 8 x 8 boxes per work unit
       TmaEnergyArgs ta;
       ta.pmap = pmap, ta.oovv = oovv_f, ta.t1 = t1_f, ta.eo = eo, ta.ev = ev, ta.tiles = (const int3*) e_tiles;
       ta.ntiles = e_ntiles, ta.o = o, ta.v = v, ta.tri = bt_tri, ta.base = bt_ctrl + 2, ta.part = bt_part;
       ta.want_sens = sens != nullptr, ta.err = d_err, ta.spin = sm100::kSpinLimit;
-      G = std::min(e_ntiles, energy_tma_grid(f32));
-      if(f32) energy_tma_batch_kernel<float><<<dim3(G, nslots), EM_THREADS, em_smem_bytes<float>(), stream>>>(ta);
-      else energy_tma_batch_kernel<float2><<<dim3(G, nslots), EM_THREADS, em_smem_bytes<float2>(), stream>>>(ta);
+      const int nst = test_energy_passes == 2 ? 1 : 2;
+      G             = std::min(e_ntiles, energy_tma_grid(f32, nst));
+      const dim3 grid(G, nslots);
+      if(f32 && nst == 2) energy_tma_batch_kernel<float, 2><<<grid, EM_THREADS, em_smem_bytes<float, 2>(), stream>>>(ta);
+      else if(f32) energy_tma_batch_kernel<float, 1><<<grid, EM_THREADS, em_smem_bytes<float, 1>(), stream>>>(ta);
+      else if(nst == 2)
+        energy_tma_batch_kernel<float2, 2><<<grid, EM_THREADS, em_smem_bytes<float2, 2>(), stream>>>(ta);
+      else energy_tma_batch_kernel<float2, 1><<<grid, EM_THREADS, em_smem_bytes<float2, 1>(), stream>>>(ta);
     } else {
       BatchEnergyArgs ea;
       ea.base_args = TiledEnergyArgs{nullptr, nullptr, nullptr, oovv_f, t1_f, eo, ev, (const int3*) e_tiles, e_ntiles,
@@ -486,7 +492,7 @@ extern "C" ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin
 }
 
 extern "C" ccsdt_status ccsdt_debug_set_energy_kernel(ccsdt_handle* h, int passes) {
-  if(!h || passes < 0 || passes > 1) return CCSDT_E_INVALID;
+  if(!h || passes < 0 || passes > 2) return CCSDT_E_INVALID;
   h->test_energy_passes = passes;
   return CCSDT_OK;
 }
