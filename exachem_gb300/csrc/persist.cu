@@ -223,7 +223,10 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
       ta.pmap = pmap, ta.oovv = oovv_f, ta.t1 = t1_f, ta.eo = eo, ta.ev = ev, ta.tiles = (const int3*) e_tiles;
       ta.ntiles = e_ntiles, ta.o = o, ta.v = v, ta.tri = bt_tri, ta.base = bt_ctrl + 2, ta.part = bt_part;
       ta.want_sens = sens != nullptr, ta.err = d_err, ta.spin = sm100::kSpinLimit;
-      const int nst = test_energy_passes == 2 ? 1 : 2;
+      // box stages: two for FP32 boxes (2 CTAs / SM), one for float-float boxes (2 CTAs / SM rather
+      // than 1), the faster of the two for each element type on GB300; knob 2 takes the other
+      const int nst_default = f32 ? 2 : 1;
+      const int nst         = test_energy_passes == 2 ? 3 - nst_default : nst_default;
       G             = std::min(e_ntiles, energy_tma_grid(f32, nst));
       const dim3 grid(G, nslots);
       if(f32 && nst == 2) energy_tma_batch_kernel<float, 2><<<grid, EM_THREADS, em_smem_bytes<float, 2>(), stream>>>(ta);

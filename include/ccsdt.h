@@ -250,7 +250,9 @@ ccsdt_status ccsdt_debug_set_window(ccsdt_handle* h, int k);
  * staged into shared memory by TMA tensor loads where their row pitch allows (v % 4 == 0 for FP32
  * partial arrays, v even for float-float), else the pass-by-pass kernel; 1: the pass-by-pass
  * kernel always (threads load the partial arrays and sum them into swizzled cubes); 2: the TMA
- * kernel with one box stage (twice the resident CTAs) instead of two. */
+ * kernel with the other number of box stages (by default two for FP32 partial arrays - the next
+ * unit's boxes load while the current one is evaluated - and one for float-float ones, where
+ * two stages would leave one CTA per SM). */
 ccsdt_status ccsdt_debug_set_energy_kernel(ccsdt_handle* h, int passes);
 
 /* Number of kernel launches issued by the last ccsdt_energy / ccsdt_triplet_energies. */
