@@ -184,10 +184,9 @@ struct ccsdt_handle {
   CUtensorMap  pmap;
   const void*  pmap_base = nullptr;
   int          pmap_B = 0, pmap_f32 = -1;
-  int          energy_tma_grid_[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int          energy_tma_grid_[4] = {0, 0, 0, 0};
   int          test_energy_passes = 0; // testing: 1 = the pass-by-pass energy kernel even where TMA
-                                       // suits, 2 = the TMA kernel with the other number of box stages,
-                                       // 3 = the TMA kernel with 512 threads per CTA
+                                       // suits, 2 = the TMA kernel with the other number of box stages
   bool         ensure_pmap(bool f32);
-  int          energy_tma_grid(bool f32, int nst, int nth);
+  int          energy_tma_grid(bool f32, int nst);
 };

@@ -27,7 +27,7 @@
 
 namespace ccsdt {
 
-constexpr int EM_THREADS = 256, EM_BOXES = 18; // default threads per CTA (512 also compiled)
+constexpr int EM_THREADS = 256, EM_BOXES = 18;
 
 struct TmaEnergyArgs {
   CUtensorMap   pmap;      // partial arrays of the batch: dims (v, v, v, 3 slots), box 8 x 8 x 8 x 1
@@ -59,12 +59,6 @@ constexpr int em_min_blocks() {
   return std::is_same<TP, float>::value ? (NST == 2 ? 2 : 4) : (NST == 2 ? 1 : 2);
 }
 
-// A thread's share of one unit's singles data (below): positions per thread
-template<int NTH>
-constexpr int em_spos() {
-  return (6 * ET_B * ET_B + NTH - 1) / NTH;
-}
-
 // Per-stage shared data of a unit besides the boxes: the singles' integrals and amplitudes of its
 // three blocks, its virtual orbital energies, the orbit-wide part of D and the distinct-cube flags.
 struct EmSingles {
@@ -78,7 +72,7 @@ struct EmSingles {
 // A thread's share of one unit's singles data, loaded from global memory into registers while the
 // previous unit is being evaluated and stored to that unit's stage afterwards.
 struct EmPrefetch {
-  float  o[2][3];  // (jk), (ik), (ij) integrals at the thread's (up to two) singles positions
+  float  o[2][3];  // (jk), (ik), (ij) integrals at the thread's two singles positions
   float  t[3];     // t_i, t_j, t_k at (block, index) = (tid / 8, tid % 8), threads 0..23
   float2 ev;       // e_v there
   float2 dab;      // e_i + e_j + e_k - e_a - e_b, threads 64..127
@@ -87,14 +81,10 @@ struct EmPrefetch {
 
 // NST = 2: unit n + 1's boxes load into the other stage while unit n is evaluated; NST = 1: one
 // stage (the load waits for the previous unit's orbits), twice the resident CTAs hiding it.
-// NTH threads per CTA (256: two orbits per thread and unit; 512: one).
-template<typename TP, int NST, int NTH = EM_THREADS>
-static __global__ void __launch_bounds__(NTH, (em_min_blocks<TP, NST>()))
+template<typename TP, int NST>
+static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
   energy_tma_batch_kernel(const __grid_constant__ TmaEnergyArgs A) {
   static_assert(NST == 1 || NST == 2, "one or two box stages");
-  static_assert(NTH == 256 || NTH == 512, "a unit's 512 orbits spread evenly");
-  constexpr int ORB = 512 / NTH, SPOS = em_spos<NTH>();
-  static_assert(SPOS <= 2, "singles positions per thread");
   constexpr int  B = ET_B, B3 = B * B * B;
   constexpr bool kF32 = std::is_same<TP, float>::value;
   extern __shared__ __align__(128) unsigned char em_dyn[];
@@ -140,7 +130,7 @@ static __global__ void __launch_bounds__(NTH, (em_min_blocks<TP, NST>()))
       sm100::tma_load_4d(box + (size_t) b * B3, &A.pmap, &full[st], b0f(q2), b0f(q1), b0f(q0), 3 * slot + pass);
     }
   };
-  constexpr int kIssueWarp = NTH / 32 - 1;
+  constexpr int kIssueWarp = EM_THREADS / 32 - 1;
   // every thread loads its share of a unit's singles data into registers
   auto prefetch = [&](int tile, EmPrefetch& r) {
     const int3 tt     = A.tiles[tile];
@@ -149,8 +139,8 @@ static __global__ void __launch_bounds__(NTH, (em_min_blocks<TP, NST>()))
     auto       b0f    = [&](int p) { return p == 0 ? rb0[0] : p == 1 ? rb0[1] : rb0[2]; };
     auto       bnf    = [&](int p) { return p == 0 ? rbn[0] : p == 1 ? rbn[1] : rbn[2]; };
 #pragma unroll
-    for(int h = 0; h < SPOS; h++) { // the six ordered pairs of distinct blocks, 64 entries each
-      const int e = tid + h * NTH;
+    for(int h = 0; h < 2; h++) { // the six ordered pairs of distinct blocks, 64 entries each
+      const int e = tid + h * EM_THREADS;
       r.o[h][0] = r.o[h][1] = r.o[h][2] = 0.f;
       if(e < 6 * B * B) {
         const int       pi = e / (B * B), uu = pi >> 1, ww = (pi & 1) ? (uu == 2 ? 1 : 2) : (uu == 0 ? 1 : 0);
@@ -187,8 +177,8 @@ static __global__ void __launch_bounds__(NTH, (em_min_blocks<TP, NST>()))
   };
   auto store = [&](const EmPrefetch& r, EmSingles& S_) {
 #pragma unroll
-    for(int h = 0; h < SPOS; h++) {
-      const int e = tid + h * NTH;
+    for(int h = 0; h < 2; h++) {
+      const int e = tid + h * EM_THREADS;
       if(e < 6 * B * B) {
         const int pi = e / (B * B), uu = pi >> 1, ww = (pi & 1) ? (uu == 2 ? 1 : 2) : (uu == 0 ? 1 : 0);
         const int x = (e / B) % B, y = e % B;
@@ -209,12 +199,12 @@ static __global__ void __launch_bounds__(NTH, (em_min_blocks<TP, NST>()))
 
   ff    s4{0.f, 0.f}, s5{0.f, 0.f};
   float sens = 0.f;
-  // this thread's orbits of every unit (orbit warps g = warp + h NTH / 32)
+  // this thread's two orbits of every unit (warps g = warp and warp + 8)
   const int u = lane & 7, w = lane >> 3;
-  int       la_[ORB], lb_[ORB], lc_[ORB];
+  int       la_[2], lb_[2], lc_[2];
 #pragma unroll
-  for(int h = 0; h < ORB; h++) {
-    const int g = warp + (NTH / 32) * h;
+  for(int h = 0; h < 2; h++) {
+    const int g = warp + 8 * h;
     la_[h] = w + 4 * (g & 1), lb_[h] = u, lc_[h] = (u + w + (g >> 1)) & 7;
   }
   bool       failed = false;
@@ -248,7 +238,7 @@ static __global__ void __launch_bounds__(NTH, (em_min_blocks<TP, NST>()))
     const int        rbn[3] = {min(B, v - tt.x * B), min(B, v - tt.y * B), min(B, v - tt.z * B)};
     const bool       all_on = S_.slot_on[0] & S_.slot_on[1] & S_.slot_on[2] & S_.slot_on[3] & S_.slot_on[4] & S_.slot_on[5];
 #pragma unroll
-    for(int h = 0; h < ORB; h++) {
+    for(int h = 0; h < 2; h++) {
       const int la = la_[h], lb = lb_[h], lc = lc_[h];
       if(la >= rbn[0] || lb >= rbn[1] || lc >= rbn[2]) continue;
       const int loc[3] = {la, lb, lc};
@@ -288,15 +278,15 @@ static __global__ void __launch_bounds__(NTH, (em_min_blocks<TP, NST>()))
   c4.add((double) s4.lo);
   c5.add((double) s5.hi);
   c5.add((double) s5.lo);
-  block_reduce_csum<NTH>(c4, c5, part);
-  __shared__ float ssum[NTH / 32];
+  block_reduce_csum(c4, c5, part);
+  __shared__ float ssum[EM_THREADS / 32];
 #pragma unroll
   for(int off = 16; off > 0; off >>= 1) sens += __shfl_down_sync(0xffffffffu, sens, off);
   if(lane == 0) ssum[warp] = sens;
   __syncthreads();
   if(tid == 0) {
     double t = 0.0;
-    for(int q = 0; q < NTH / 32; q++) t += ssum[q];
+    for(int q = 0; q < EM_THREADS / 32; q++) t += ssum[q];
     part[4] = t;
     part[5] = 0.0;
   }

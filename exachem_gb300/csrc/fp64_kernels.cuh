@@ -145,9 +145,8 @@ struct EnergyArgs {
 
 constexpr int E_THREADS = 256;
 
-template<int NTH = E_THREADS> // threads of the block
 __device__ inline void block_reduce_csum(CSum& a, CSum& b, double* out) {
-  __shared__ double sh[4][NTH / 32];
+  __shared__ double sh[4][E_THREADS / 32];
   const int         lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   // fixed-shape tree: deterministic
 #pragma unroll
@@ -169,7 +168,7 @@ __device__ inline void block_reduce_csum(CSum& a, CSum& b, double* out) {
   __syncthreads();
   if(threadIdx.x == 0) {
     CSum ta, tb;
-    for(int q = 0; q < NTH / 32; q++) {
+    for(int q = 0; q < E_THREADS / 32; q++) {
       ta.add(sh[0][q]);
       ta.c += sh[1][q];
       tb.add(sh[2][q]);

@@ -139,26 +139,24 @@ int ccsdt_handle::energy_grid(bool f32) {
 
 // Grid of one resident wave of the TMA energy kernel (element type, box stages); sets the kernel's
 // dynamic shared-memory limit first (the boxes exceed the default 48 KB).
-template<typename TP, int NST, int NTH = EM_THREADS>
+template<typename TP, int NST>
 static int tma_energy_wave(int sm) {
   int per = 0;
-  cudaFuncSetAttribute(energy_tma_batch_kernel<TP, NST, NTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(energy_tma_batch_kernel<TP, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int) em_smem_bytes<TP, NST>());
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tma_batch_kernel<TP, NST, NTH>, NTH,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, energy_tma_batch_kernel<TP, NST>, EM_THREADS,
                                                 em_smem_bytes<TP, NST>());
   cudaGetLastError();
   return std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
 }
 
-int ccsdt_handle::energy_tma_grid(bool f32, int nst, int nth) {
-  int& g = energy_tma_grid_[(f32 ? 1 : 0) + 2 * (nst - 1) + 4 * (nth == 512)];
+int ccsdt_handle::energy_tma_grid(bool f32, int nst) {
+  int& g = energy_tma_grid_[(f32 ? 1 : 0) + 2 * (nst - 1)];
   if(g > 0) return g;
   int sm = 0;
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
-  if(nth == 512) g = f32 ? tma_energy_wave<float, 2, 512>(sm) : tma_energy_wave<float2, 1, 512>(sm);
-  else
-    g = f32 ? (nst == 2 ? tma_energy_wave<float, 2>(sm) : tma_energy_wave<float, 1>(sm))
-            : (nst == 2 ? tma_energy_wave<float2, 2>(sm) : tma_energy_wave<float2, 1>(sm));
+  g = f32 ? (nst == 2 ? tma_energy_wave<float, 2>(sm) : tma_energy_wave<float, 1>(sm))
+          : (nst == 2 ? tma_energy_wave<float2, 2>(sm) : tma_energy_wave<float2, 1>(sm));
   return g;
 }
 
@@ -229,14 +227,9 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
       // than 1), the faster of the two for each element type on GB300; knob 2 takes the other
       const int nst_default = f32 ? 2 : 1;
       const int nst         = test_energy_passes == 2 ? 3 - nst_default : nst_default;
-      const int nth         = test_energy_passes == 3 ? 512 : EM_THREADS;
-      G                     = std::min(e_ntiles, energy_tma_grid(f32, nst, nth));
+      G             = std::min(e_ntiles, energy_tma_grid(f32, nst));
       const dim3 grid(G, nslots);
-      if(nth == 512) {
-        if(f32) energy_tma_batch_kernel<float, 2, 512><<<grid, 512, em_smem_bytes<float, 2>(), stream>>>(ta);
-        else energy_tma_batch_kernel<float2, 1, 512><<<grid, 512, em_smem_bytes<float2, 1>(), stream>>>(ta);
-      } else if(f32 && nst == 2)
-        energy_tma_batch_kernel<float, 2><<<grid, EM_THREADS, em_smem_bytes<float, 2>(), stream>>>(ta);
+      if(f32 && nst == 2) energy_tma_batch_kernel<float, 2><<<grid, EM_THREADS, em_smem_bytes<float, 2>(), stream>>>(ta);
       else if(f32) energy_tma_batch_kernel<float, 1><<<grid, EM_THREADS, em_smem_bytes<float, 1>(), stream>>>(ta);
       else if(nst == 2)
         energy_tma_batch_kernel<float2, 2><<<grid, EM_THREADS, em_smem_bytes<float2, 2>(), stream>>>(ta);
@@ -502,7 +495,7 @@ extern "C" ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin
 }
 
 extern "C" ccsdt_status ccsdt_debug_set_energy_kernel(ccsdt_handle* h, int passes) {
-  if(!h || passes < 0 || passes > 3) return CCSDT_E_INVALID;
+  if(!h || passes < 0 || passes > 2) return CCSDT_E_INVALID;
   h->test_energy_passes = passes;
   return CCSDT_OK;
 }

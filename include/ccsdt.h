@@ -252,8 +252,7 @@ ccsdt_status ccsdt_debug_set_window(ccsdt_handle* h, int k);
  * kernel always (threads load the partial arrays and sum them into swizzled cubes); 2: the TMA
  * kernel with the other number of box stages (by default two for FP32 partial arrays - the next
  * unit's boxes load while the current one is evaluated - and one for float-float ones, where
- * two stages would leave one CTA per SM); 3: the TMA kernel with 512 threads per CTA (one orbit
- * per thread and unit) instead of 256. */
+ * two stages would leave one CTA per SM). */
 ccsdt_status ccsdt_debug_set_energy_kernel(ccsdt_handle* h, int passes);
 
 /* Number of kernel launches issued by the last ccsdt_energy / ccsdt_triplet_energies. */
