@@ -42,6 +42,8 @@ struct TmaEnergyArgs {
   int           want_sens;
   int*          err;       // set when a bounded wait gave up
   unsigned      spin;
+  int           skip_loads; // testing: announce each unit's bytes but issue no box load, so the
+                            // waits run out (the timeout path, CCSDT_E_TIMEOUT)
 };
 
 // bytes of dynamic shared memory: the eighteen boxes of each of the NST box stages
@@ -117,7 +119,7 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
     TP*        box    = reinterpret_cast<TP*>(em_dyn + st * em_stage_bytes<TP>());
     if(lane == 0) sm100::mbar_arrive_expect_tx(&full[st], (uint32_t) em_stage_bytes<TP>());
     __syncwarp();
-    if(lane < EM_BOXES) {
+    if(lane < EM_BOXES && !A.skip_loads) {
       const int  b = lane, pass = b / 6, q = b % 6;
       const int* P = c_perm[q];
       // (slowest, middle, fastest) block positions of the pass's array: P12[a][c][b],
@@ -221,9 +223,12 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
     store(pre, sgl[ss]);
     __syncthreads(); // the unit's singles are visible; unit n - 1's orbits are done with its box stage
     const int next = tile + gridDim.x;
-    if(NST == 1 && warp == kIssueWarp) issue(tile, 0);
+    // after a wait gave up the stages are not re-armed (their phases never completed); the issuing
+    // warp decides as one
+    const bool may_issue = warp == kIssueWarp && !__any_sync(0xffffffffu, failed);
+    if(NST == 1 && may_issue) issue(tile, 0);
     if(next < A.ntiles) {
-      if(NST == 2 && warp == kIssueWarp) issue(next, st ^ 1);
+      if(NST == 2 && may_issue) issue(next, st ^ 1);
       prefetch(next, pre);
     }
     // Each thread waits for the boxes itself (the wait makes the TMA's writes visible to it).  A

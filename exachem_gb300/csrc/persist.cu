@@ -183,8 +183,10 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   // the same windows and the energies stay bit-identical across configurations
   p.wst        = pz_window_k(S, 64) / kPzConfs[conf].KC;
   if(test_window_k > 0) p.wst = std::max(1, std::min(p.wst, test_window_k / kPzConfs[conf].KC));
-  p.spin       = test_spin_limit ? test_spin_limit : sm100::kSpinLimit;
-  p.skip_loads = test_skip_loads;
+  // the testing limit applies to the kernel whose loads the test withholds (the contraction's
+  // unless the energy's are)
+  p.spin       = test_spin_limit && test_skip_loads != 2 ? test_spin_limit : sm100::kSpinLimit;
+  p.skip_loads = test_skip_loads == 1;
   const int  NT  = kPzConfs[conf].NT;
   const long per = items_per_slot(v, NT);
   if(nitems_override <= 0) p.nitems = (unsigned) (per * nslots);
@@ -222,7 +224,9 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
       TmaEnergyArgs ta;
       ta.pmap = pmap, ta.oovv = oovv_f, ta.t1 = t1_f, ta.eo = eo, ta.ev = ev, ta.tiles = (const int3*) e_tiles;
       ta.ntiles = e_ntiles, ta.o = o, ta.v = v, ta.tri = bt_tri, ta.base = bt_ctrl + 2, ta.part = bt_part;
-      ta.want_sens = sens != nullptr, ta.err = d_err, ta.spin = sm100::kSpinLimit;
+      ta.want_sens = sens != nullptr, ta.err = d_err;
+      ta.spin       = test_spin_limit && test_skip_loads == 2 ? test_spin_limit : sm100::kSpinLimit;
+      ta.skip_loads = test_skip_loads == 2;
       // box stages: two for FP32 boxes (2 CTAs / SM), one for float-float boxes (2 CTAs / SM rather
       // than 1), the faster of the two for each element type on GB300; knob 2 takes the other
       const int nst_default = f32 ? 2 : 1;
@@ -490,7 +494,8 @@ extern "C" ccsdt_status ccsdt_set_tile_config(ccsdt_handle* h, int slices, int i
 extern "C" ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin_limit, int skip_loads) {
   if(!h) return CCSDT_E_INVALID;
   h->test_spin_limit = spin_limit;
-  h->test_skip_loads = skip_loads ? 1 : 0;
+  if(skip_loads < 0 || skip_loads > 2) return CCSDT_E_INVALID;
+  h->test_skip_loads = skip_loads;
   return CCSDT_OK;
 }
 

@@ -234,9 +234,12 @@ ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts* opts, int 
  *     (nullable) receives the number of allocations attempted since the previous call.  The
  *     calls that meet the failure return CCSDT_E_OOM and leave their handle destroyable.
  *   ccsdt_debug_set_wait_test: the split-precision persistent kernel's bounded waits give up after
- *     spin_limit polls (0: the default limit), and with skip_loads != 0 it announces each stage's
+ *     spin_limit polls (0: the default limit), and with skip_loads = 1 it announces each stage's
  *     bytes but issues no TMA load, so its stage waits run out: the call returns CCSDT_E_TIMEOUT,
- *     the kernel having released its tensor memory, and the handle stays usable. */
+ *     the kernel having released its tensor memory, and the handle stays usable.  skip_loads = 2
+ *     does the same to the TMA energy kernel (the limit then applies to its waits): it announces
+ *     each work unit's box bytes without loading them, its threads stop after their first wait
+ *     runs out, and the call returns CCSDT_E_TIMEOUT. */
 ccsdt_status ccsdt_debug_fail_alloc(long nth, long* attempts);
 ccsdt_status ccsdt_debug_set_wait_test(ccsdt_handle* h, unsigned spin_limit, int skip_loads);
 
