@@ -518,7 +518,7 @@ def main():
                     help="profiling aid: run only this many evenly spread triplets of the call (projected)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--p-storage", default="auto", choices=["auto", "ff", "f32"],
-                    help="split path: partial arrays in FP32 (auto: at 1-2 digit planes) or float-float")
+                    help="split path: partial arrays in FP32 (auto: at 1-3 digit planes) or float-float")
     ap.add_argument("--budget", type=float, default=1e-8,
                     help="learned mode: 3 sum_t sigma_t <= budget x sum_t |E(T)_t| (1e-8: two planes miss it at "
                          "o=60 v=500, three meet it)")
@@ -736,8 +736,9 @@ def main():
         nz = np.abs(f5) > 0
         entries = {}
         runs = [(f"S={s_}", "ozaki", {"slices": s_, "p_storage": args.p_storage}) for s_ in sample_slices]
-        if args.p_storage == "auto" and 2 in sample_slices:   # what the FP32 partial arrays cost in accuracy
-            runs.append(("S=2 float-float partial arrays", "ozaki", {"slices": 2, "p_storage": "ff"}))
+        for s_ in (2, 3):   # what the FP32 partial arrays cost in accuracy
+            if args.p_storage == "auto" and s_ in sample_slices:
+                runs.append((f"S={s_} float-float partial arrays", "ozaki", {"slices": s_, "p_storage": "ff"}))
         if model is not None:
             runs.append(("learned", "learned", lkw))
         for name, m_, k_ in runs:
@@ -792,9 +793,9 @@ def main():
             "config": wl | {"mode": mode, "slices": S if mode == "ozaki" else None, "tile_config": tile,
                             "partial_arrays": None if not split else (
                                 "FP32" if args.p_storage == "f32" or (args.p_storage == "auto" and mode == "ozaki"
-                                                                      and S <= 2)
+                                                                      and S <= 3)
                                 else "float-float" if mode == "ozaki" or args.p_storage == "ff"
-                                else "FP32 at 1-2 digit planes, float-float above"),
+                                else "FP32 at 1-3 digit planes, float-float above"),
                             "triplets_total": int(len(tri_all)), "triplets_timed": int(timed_trip),
                             "timed_fraction": frac,
                             "projection": None if frac >= 1 else "value = timed seconds / timed_fraction",

@@ -132,7 +132,7 @@ struct ccsdt_handle {
   bool      last_p_f32   = false;    // ... and stored its partial arrays in FP32
   int       p_storage    = 0;        // the call's opts->p_storage
   // FP32 partial arrays for S <= kPF32MaxS digit planes unless the call asks otherwise
-  static constexpr int kPF32MaxS = 2;
+  static constexpr int kPF32MaxS = 3;
   bool p_f32(int S) const { return p_storage == 2 || (p_storage == 0 && S <= kPF32MaxS); }
   double*   bt_part = nullptr;
   int       bt_B = 0, bt_order_key = -1;

@@ -82,9 +82,10 @@ typedef struct {
   int    autotune;        /* 1: ccsdt_energy / ccsdt_triplet_energies run ccsdt_autotune for each
                              slice count they use, once per handle, before the timed work      */
   int    p_storage;       /* split path: element type of the triples' partial arrays between the
-                             contraction and the energy: 0 FP32 for 1..2 digit planes (whose own
-                             contraction error is ~100x FP32's rounding), float-float otherwise;
-                             1 float-float always; 2 FP32 always                               */
+                             contraction and the energy: 0 FP32 for 1..3 digit planes (their
+                             rounding, unbiased and averaged over a triplet's v^3 elements, moves
+                             E(T) by ~1e-11 relative, far below the truncation of 3 planes),
+                             float-float from 4 planes on; 1 float-float always; 2 FP32 always */
   int    reserved[2];
 } ccsdt_opts;
 
