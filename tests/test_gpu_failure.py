@@ -93,17 +93,20 @@ def test_bounded_wait_timeout_returns_timeout_and_handle_survives(built):
     assert got["e_paren_T"] == want["e_paren_T"] and got["e_bracket_T"] == want["e_bracket_T"]
     r64 = ft.energy("fp64")
     assert abs(got["e_paren_T"] - r64["e_paren_T"]) <= 5e-8 * abs(r64["e_paren_T"])
-    # the TMA energy kernel's box waits: FP32 boxes (two stages, S = 2) and float-float ones (one
-    # stage, S = 3); no load is in flight when they run out
-    want2 = ft.energy("ozaki", slices=2)
-    for S in (2, 3):
-        assert lib.ccsdt_debug_set_wait_test(ft.h, 4096, 2) == 0
-        with pytest.raises(CCSDTError) as e:
-            ft.energy("ozaki", slices=S)
-        assert e.value.status == TIMEOUT
-        assert lib.ccsdt_debug_set_wait_test(ft.h, 0, 0) == 0
-    assert ft.energy("ozaki", slices=2)["e_paren_T"] == want2["e_paren_T"]
-    assert ft.energy("ozaki", slices=3)["e_paren_T"] == want["e_paren_T"]
     assert lib.ccsdt_debug_set_wait_test(ft.h, 0, 3) != 0
     ft.close()
     assert np.isfinite(want["e_paren_T"])
+    # the TMA energy kernel's box waits (v = 72: a row pitch TMA takes): FP32 boxes with two stages
+    # and float-float ones with one; no load is in flight when they run out
+    ft = FusedTriples(6, 72, ts=40)
+    ft.upload_dict(generate(6, 72, 6))
+    for S, store in ((2, "f32"), (4, "ff")):
+        want = ft.energy("ozaki", slices=S, p_storage=store)
+        assert lib.ccsdt_debug_set_wait_test(ft.h, 4096, 2) == 0
+        with pytest.raises(CCSDTError) as e:
+            ft.energy("ozaki", slices=S, p_storage=store)
+        assert e.value.status == TIMEOUT
+        assert lib.ccsdt_debug_set_wait_test(ft.h, 0, 0) == 0
+        got = ft.energy("ozaki", slices=S, p_storage=store)
+        assert got["e_paren_T"] == want["e_paren_T"] and got["e_bracket_T"] == want["e_bracket_T"]
+    ft.close()
