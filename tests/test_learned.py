@@ -143,7 +143,7 @@ def test_error_estimate_covers_measured_error(built):
 
 def test_batched_call_is_held_to_the_same_relative_budget(built):
     """The acceptance test is linear in the triplets (3 sum_t sigma_t <= budget sum_t |E_t|), so a
-    call that is one part of a larger computation is judged exactly as if it were the whole:
+    call that is one part of a larger computation is held to exactly the test of the whole:
     budget_triplets changes nothing."""
     from exachem_gb300 import ccsd_t as ct, learned
     from exachem_gb300.generator import generate
