@@ -4,14 +4,15 @@
 // triple X <= Y <= Z per unit, W_xyz = P12[x][z][y] + P34[y][x][z] + P56[z][y][x], every orbit
 // {a, b, c} with its six orderings), but the eighteen 8 x 8 x 8 boxes a unit needs - for each of
 // its six ordered cubes, the matching box of P12, P34 and P56 - are copied into shared memory by
-// eighteen TMA tensor loads issued by one thread, so no thread computes an address into the
-// partial arrays and out-of-range rows (v not a multiple of 8) arrive as zeros.  The orbits then
+// eighteen TMA tensor loads issued by eighteen lanes of one warp, so no thread computes an address
+// into the partial arrays and out-of-range rows (v not a multiple of 8) arrive as zeros.  The orbits then
 // read their W values from the boxes directly: cube q of the unit at its local (x, y, z) is
 // box12_q[x][z][y] + box34_q[y][x][z] + box56_q[z][y][x], summed in the order of the
 // pass-by-pass kernel, so both kernels give the same W bit for bit.
 //
-// Two pipeline stages: unit n + 1's boxes are loaded (and its singles data read into registers)
-// while unit n is evaluated.
+// Pipeline: unit n + 1's singles data are read into registers while unit n is evaluated and, with
+// two box stages (the FP32 default), its boxes load too; float-float boxes (twice the bytes) use one
+// stage, which lets two CTAs share an SM instead of one - the faster of the two on GB300.
 //
 // Lane -> orbit: warp g (16 per unit, two per thread block warp), lane (u = lane % 8, w = lane / 8)
 // takes la = w + 4 (g % 2), lb = u, lc = (u + w + g / 2) % 8.  For every one of the eighteen reads
