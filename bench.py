@@ -517,7 +517,7 @@ def main():
     ap.add_argument("--limit-triplets", type=int, default=0,
                     help="profiling aid: run only this many evenly spread triplets of the call (projected)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--p-storage", default="auto", choices=["auto", "ff", "f32"],
+    ap.add_argument("--p-storage", default="auto", choices=["auto", "ff", "f32", "f64"],
                     help="split path: partial arrays in FP32 (auto: at 1-3 digit planes) or float-float")
     ap.add_argument("--budget", type=float, default=1e-8,
                     help="learned mode: 3 sum_t sigma_t <= budget x sum_t |E(T)_t| (1e-8: two planes miss it at "
@@ -792,6 +792,7 @@ def main():
             "data": "synthetic (seeded generator, built on GPU)",
             "config": wl | {"mode": mode, "slices": S if mode == "ozaki" else None, "tile_config": tile,
                             "partial_arrays": None if not split else (
+                                "FP64 (FP64 recombination and energy)" if args.p_storage == "f64" else
                                 "FP32" if args.p_storage == "f32" or (args.p_storage == "auto" and mode == "ozaki"
                                                                       and S <= 3)
                                 else "float-float" if mode == "ozaki" or args.p_storage == "ff"

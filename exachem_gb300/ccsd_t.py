@@ -263,7 +263,8 @@ class FusedTriples:
         o.budget_triplets = budget_triplets
         o.test_kernel = legacy_mma       # 1: mma.sync slice kernel, 2: per-triplet tcgen05 kernel (testing)
         o.autotune = autotune            # 1: tune the contraction's tile configuration on first use
-        o.p_storage = {"auto": 0, "ff": 1, "f32": 2}[p_storage] if isinstance(p_storage, str) else int(p_storage)
+        o.p_storage = ({"auto": 0, "ff": 1, "f32": 2, "f64": 3}[p_storage] if isinstance(p_storage, str)
+                       else int(p_storage))
         return o
 
     def energy(self, mode="fp64", **kw) -> dict:

@@ -444,7 +444,7 @@ ccsdt_status ccsdt_handle::run_triplet_fp64(int i, int j, int k, double* eout) {
 
 static bool valid_opts(const ccsdt_opts* o) {
   return o && (o->mode == CCSDT_MODE_FP64 || o->mode == CCSDT_MODE_OZAKI || o->mode == CCSDT_MODE_LEARNED) &&
-         o->p_storage >= 0 && o->p_storage <= 2;
+         o->p_storage >= 0 && o->p_storage <= 3;
 }
 
 // opts->autotune: the slice counts this call can use on the persistent tcgen05 path, each tuned
@@ -632,7 +632,7 @@ extern "C" ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts*
     // float-float or FP32 elements
     std::vector<float2> f(n);
     const float2*       src[3] = {h->F12, h->F34, h->F56};
-    const bool          f32    = h->last_batched && h->last_p_f32;
+    const bool          f32    = h->last_batched && h->last_p_f32, f64 = h->last_batched && h->last_p_f64;
     if(h->last_batched)
       for(int q = 0; q < 3; q++)
         src[q] = f32 ? reinterpret_cast<const float2*>(reinterpret_cast<const float*>(h->bt_F) + q * n) : h->bt_F + q * n;
@@ -640,7 +640,10 @@ extern "C" ccsdt_status ccsdt_debug_triplet_w(ccsdt_handle* h, const ccsdt_opts*
       CK(cudaMemcpy(f.data(), src[q], n * (f32 ? sizeof(float) : sizeof(float2)), cudaMemcpyDeviceToHost));
       std::vector<double>& d = q == 0 ? a : q == 1 ? b : c;
       const float*         g = reinterpret_cast<const float*>(f.data());
-      for(size_t e = 0; e < n; e++) d[e] = f32 ? (double) g[e] : (double) f[e].x + (double) f[e].y;
+      if(f64)
+        std::memcpy(d.data(), f.data(), n * sizeof(double)); // FP64 elements, 8 bytes like float2
+      else
+        for(size_t e = 0; e < n; e++) d[e] = f32 ? (double) g[e] : (double) f[e].x + (double) f[e].y;
     }
   }
   // W_xyz = P12[x][z][y] + P34[y][x][z] + P56[z][y][x]

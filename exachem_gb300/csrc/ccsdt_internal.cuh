@@ -130,6 +130,7 @@ struct ccsdt_handle {
   float2*   bt_F = nullptr;          // P arrays of the batch slots
   bool      last_batched = false;    // the last split-precision call ran the persistent path
   bool      last_p_f32   = false;    // ... and stored its partial arrays in FP32
+  bool      last_p_f64   = false;    // ... or in FP64
   int       p_storage    = 0;        // the call's opts->p_storage
   // FP32 partial arrays for S <= kPF32MaxS digit planes unless the call asks otherwise
   static constexpr int kPF32MaxS = 3;
@@ -184,9 +185,9 @@ struct ccsdt_handle {
   CUtensorMap  pmap;
   const void*  pmap_base = nullptr;
   int          pmap_B = 0, pmap_f32 = -1;
-  int          energy_tma_grid_[4] = {0, 0, 0, 0};
+  int          energy_tma_grid_[6] = {0, 0, 0, 0, 0, 0};
   int          test_energy_passes = 0; // testing: 1 = the pass-by-pass energy kernel even where TMA
                                        // suits, 2 = the TMA kernel with the other number of box stages
   bool         ensure_pmap(bool f32);
-  int          energy_tma_grid(bool f32, int nst);
+  int          energy_tma_grid(int kind, int nst);
 };

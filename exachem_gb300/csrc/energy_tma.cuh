@@ -33,6 +33,7 @@ constexpr int EM_THREADS = 256, EM_BOXES = 18;
 struct TmaEnergyArgs {
   CUtensorMap   pmap;      // partial arrays of the batch: dims (v, v, v, 3 slots), box 8 x 8 x 8 x 1
   const float * oovv, *t1; // FP32 copies
+  const double *oovv_d, *t1_d; // FP64 originals (FP64 partial arrays)
   const double *eo, *ev;
   const int3*   tiles;     // sorted block triples
   int           ntiles;
@@ -64,23 +65,73 @@ constexpr int em_min_blocks() {
 
 // Per-stage shared data of a unit besides the boxes: the singles' integrals and amplitudes of its
 // three blocks, its virtual orbital energies, the orbit-wide part of D and the distinct-cube flags.
+// SS: the singles' scalar (float; double for FP64 partial arrays), ES: the orbital energies'
+// (float-float pair; double).
+template<typename SS, typename ES>
 struct EmSingles {
-  float  Ojk[3][3][ET_B * ET_B], Oik[3][3][ET_B * ET_B], Oij[3][3][ET_B * ET_B];
-  float  ti[3][ET_B], tj[3][ET_B], tk[3][ET_B];
-  float2 evs[3][ET_B];
-  float2 dab[ET_B * ET_B];
-  int    slot_on[6];
+  SS  Ojk[3][3][ET_B * ET_B], Oik[3][3][ET_B * ET_B], Oij[3][3][ET_B * ET_B];
+  SS  ti[3][ET_B], tj[3][ET_B], tk[3][ET_B];
+  ES  evs[3][ET_B];
+  ES  dab[ET_B * ET_B];
+  int slot_on[6];
 };
 
 // A thread's share of one unit's singles data, loaded from global memory into registers while the
 // previous unit is being evaluated and stored to that unit's stage afterwards.
+template<typename SS, typename ES>
 struct EmPrefetch {
-  float  o[2][3];  // (jk), (ik), (ij) integrals at the thread's two singles positions
-  float  t[3];     // t_i, t_j, t_k at (block, index) = (tid / 8, tid % 8), threads 0..23
-  float2 ev;       // e_v there
-  float2 dab;      // e_i + e_j + e_k - e_a - e_b, threads 64..127
-  int    on;       // distinct-cube flag, threads 96..101
+  SS  o[2][3]; // (jk), (ik), (ij) integrals at the thread's two singles positions
+  SS  t[3];    // t_i, t_j, t_k at (block, index) = (tid / 8, tid % 8), threads 0..23
+  ES  ev;      // e_v there
+  ES  dab;     // e_i + e_j + e_k - e_a - e_b, threads 64..127
+  int on;      // distinct-cube flag, threads 96..101
 };
+
+// FP64 partial arrays: the singles parts of V and the orbit's energy terms in FP64, compensated
+// (Kahan) FP64 sums - the precision of the plain FP64 path's energy.
+__device__ __forceinline__ void et_singles_f64(const double (*Ojk)[3][ET_B * ET_B],
+                                               const double (*Oik)[3][ET_B * ET_B],
+                                               const double (*Oij)[3][ET_B * ET_B], const double (*ti)[ET_B],
+                                               const double (*tj)[ET_B], const double (*tk)[ET_B], int la, int lb,
+                                               int lc, double (&sg)[6]) {
+  constexpr int B = ET_B;
+  const int loc[3] = {la, lb, lc};
+#pragma unroll
+  for(int q = 0; q < 6; q++) {
+    const int p0 = kPerm(q, 0), p1 = kPerm(q, 1), p2 = kPerm(q, 2);
+    const int x = loc[p0], y = loc[p1], z = loc[p2];
+    sg[q] = Ojk[p1][p2][y * B + z] * ti[p0][x] + Oik[p0][p2][x * B + z] * tj[p1][y] + Oij[p0][p1][x * B + y] * tk[p2][z];
+  }
+}
+__device__ __forceinline__ void et_orbit_values_f64(const double (&w)[6], const double (&sg)[6],
+                                                    const double (*evs)[ET_B], const double* dab, bool all_on,
+                                                    const int* slot_on, int la, int lb, int lc, int want_sens,
+                                                    CSum& s4, CSum& s5, float& sens) {
+  constexpr int B = ET_B;
+  const double ca = w[0] + w[3] + w[4], cb = w[1] + w[2] + w[5]; // the two cyclic classes
+  const double sga = sg[0] + sg[3] + sg[4], sgb = sg[1] + sg[2] + sg[5];
+  double       zy4 = 0.0, zys = 0.0;
+  float        sn  = 0.f;
+#pragma unroll
+  for(int q = 0; q < 6; q++) {
+    if(!all_on && !slot_on[q]) continue;
+    const bool   in_a = q == 0 || q == 3 || q == 4;
+    const double z    = 3.0 * w[q] + (in_a ? ca : cb);   // 4 W_q + the other two of its class
+    const double y4   = 3.0 * w[q] - (in_a ? cb : ca);   // 3 W_q - the other class
+    const double ys   = 3.0 * sg[q] - (in_a ? sgb : sga);
+    zy4 += z * y4;
+    zys += z * ys;
+    if(want_sens) {
+      const float y5 = (float) (y4 + ys), zf = (float) z;
+      sn             = fmaf(18.f * y5, y5, fmaf(12.f * zf, zf, sn));
+    }
+  }
+  const double d = dab[la * B + lb] - evs[2][lc];
+  s4.add(zy4 / d);
+  s5.add((zy4 + zys) / d);
+  const float id = (float) (1.0 / d);
+  sens           = fmaf(sn * id, id, sens);
+}
 
 // NST = 2: unit n + 1's boxes load into the other stage while unit n is evaluated; NST = 1: one
 // stage (the load waits for the previous unit's orbits), twice the resident CTAs hiding it.
@@ -89,11 +140,13 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
   energy_tma_batch_kernel(const __grid_constant__ TmaEnergyArgs A) {
   static_assert(NST == 1 || NST == 2, "one or two box stages");
   constexpr int  B = ET_B, B3 = B * B * B;
-  constexpr bool kF32 = std::is_same<TP, float>::value;
+  constexpr bool kF32 = std::is_same<TP, float>::value, kF64 = std::is_same<TP, double>::value;
+  using SS = typename std::conditional<kF64, double, float>::type;
+  using ES = typename std::conditional<kF64, double, float2>::type;
   extern __shared__ __align__(128) unsigned char em_dyn[];
   // stage st: boxes [pass][slot q][512] at em_dyn + st * em_stage_bytes (pass 0 = P12, 1 = P34, 2 = P56)
-  __shared__ EmSingles sgl[2];
-  __shared__ uint64_t  full[2];
+  __shared__ EmSingles<SS, ES> sgl[2];
+  __shared__ uint64_t          full[2];
 
   const int       slot = blockIdx.y, b0 = A.base ? *A.base : 0;
   const int*      tp   = A.tri + 4 * (b0 + slot);
@@ -101,8 +154,11 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
   const int       v = A.v, o = A.o, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long v2 = (long long) v * v;
   const ff        eijk = ff_add(ff_add(ff_from_double(A.eo[i]), ff_from_double(A.eo[j])), ff_from_double(A.eo[k]));
-  const float *   gOjk = A.oovv + ((long long) j * o + k) * v2, *gOik = A.oovv + ((long long) i * o + k) * v2,
-              *gOij = A.oovv + ((long long) i * o + j) * v2;
+  const double    eijk_d = A.eo[i] + A.eo[j] + A.eo[k];
+  const SS*       goovv  = kF64 ? reinterpret_cast<const SS*>(A.oovv_d) : reinterpret_cast<const SS*>(A.oovv);
+  const SS*       gt1    = kF64 ? reinterpret_cast<const SS*>(A.t1_d) : reinterpret_cast<const SS*>(A.t1);
+  const SS *      gOjk = goovv + ((long long) j * o + k) * v2, *gOik = goovv + ((long long) i * o + k) * v2,
+           *gOij = goovv + ((long long) i * o + j) * v2;
   if(tid == 0) {
     sm100::mbar_init(&full[0], 1);
     sm100::mbar_init(&full[1], 1);
@@ -135,7 +191,7 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
   };
   constexpr int kIssueWarp = EM_THREADS / 32 - 1;
   // every thread loads its share of a unit's singles data into registers
-  auto prefetch = [&](int tile, EmPrefetch& r) {
+  auto prefetch = [&](int tile, EmPrefetch<SS, ES>& r) {
     const int3 tt     = A.tiles[tile];
     const int  rb0[3] = {tt.x * B, tt.y * B, tt.z * B};
     const int  rbn[3] = {min(B, v - rb0[0]), min(B, v - rb0[1]), min(B, v - rb0[2])};
@@ -144,7 +200,7 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
 #pragma unroll
     for(int h = 0; h < 2; h++) { // the six ordered pairs of distinct blocks, 64 entries each
       const int e = tid + h * EM_THREADS;
-      r.o[h][0] = r.o[h][1] = r.o[h][2] = 0.f;
+      r.o[h][0] = r.o[h][1] = r.o[h][2] = SS(0);
       if(e < 6 * B * B) {
         const int       pi = e / (B * B), uu = pi >> 1, ww = (pi & 1) ? (uu == 2 ? 1 : 2) : (uu == 0 ? 1 : 0);
         const int       x = (e / B) % B, y = e % B;
@@ -156,17 +212,25 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
       const int  uu = tid / B, x = tid % B;
       const bool ok = x < bnf(uu);
       const int  a  = b0f(uu) + x;
-      r.t[0] = ok ? A.t1[(long long) i * v + a] : 0.f;
-      r.t[1] = ok ? A.t1[(long long) j * v + a] : 0.f;
-      r.t[2] = ok ? A.t1[(long long) k * v + a] : 0.f;
-      const ff e = ok ? ff_from_double(A.ev[a]) : ff{0.f, 0.f};
-      r.ev       = make_float2(e.hi, e.lo);
+      r.t[0] = ok ? gt1[(long long) i * v + a] : SS(0);
+      r.t[1] = ok ? gt1[(long long) j * v + a] : SS(0);
+      r.t[2] = ok ? gt1[(long long) k * v + a] : SS(0);
+      if constexpr(kF64) {
+        r.ev = ok ? A.ev[a] : 0.0;
+      } else {
+        const ff e = ok ? ff_from_double(A.ev[a]) : ff{0.f, 0.f};
+        r.ev       = make_float2(e.hi, e.lo);
+      }
     } else if(tid >= 64 && tid < 64 + B * B) { // a in block 0, b in block 1
       const int x = (tid - 64) / B, y = (tid - 64) % B;
-      const ff  ea = x < rbn[0] ? ff_from_double(A.ev[rb0[0] + x]) : ff{0.f, 0.f};
-      const ff  eb = y < rbn[1] ? ff_from_double(A.ev[rb0[1] + y]) : ff{0.f, 0.f};
-      const ff  d  = ff_add(ff_add(eijk, ff_neg(ea)), ff_neg(eb));
-      r.dab        = make_float2(d.hi, d.lo);
+      if constexpr(kF64) {
+        r.dab = eijk_d - (x < rbn[0] ? A.ev[rb0[0] + x] : 0.0) - (y < rbn[1] ? A.ev[rb0[1] + y] : 0.0);
+      } else {
+        const ff ea = x < rbn[0] ? ff_from_double(A.ev[rb0[0] + x]) : ff{0.f, 0.f};
+        const ff eb = y < rbn[1] ? ff_from_double(A.ev[rb0[1] + y]) : ff{0.f, 0.f};
+        const ff d  = ff_add(ff_add(eijk, ff_neg(ea)), ff_neg(eb));
+        r.dab       = make_float2(d.hi, d.lo);
+      }
       if(tid >= 96 && tid < 102) { // a cube counts once per distinct ordered block triple
         const int  t6 = tid - 96;
         const int* P  = c_perm[t6];
@@ -178,7 +242,7 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
       }
     }
   };
-  auto store = [&](const EmPrefetch& r, EmSingles& S_) {
+  auto store = [&](const EmPrefetch<SS, ES>& r, EmSingles<SS, ES>& S_) {
 #pragma unroll
     for(int h = 0; h < 2; h++) {
       const int e = tid + h * EM_THREADS;
@@ -201,6 +265,7 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
   };
 
   ff    s4{0.f, 0.f}, s5{0.f, 0.f};
+  CSum  d4, d5; // the FP64 partial arrays' sums
   float sens = 0.f;
   // this thread's two orbits of every unit (warps g = warp and warp + 8)
   const int u = lane & 7, w = lane >> 3;
@@ -210,8 +275,8 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
     const int g = warp + 8 * h;
     la_[h] = w + 4 * (g & 1), lb_[h] = u, lc_[h] = (u + w + (g >> 1)) & 7;
   }
-  bool       failed = false;
-  EmPrefetch pre{};
+  bool               failed = false;
+  EmPrefetch<SS, ES> pre{};
   if((int) blockIdx.x < A.ntiles) {
     if(NST == 2 && warp == kIssueWarp) issue(blockIdx.x, 0);
     prefetch(blockIdx.x, pre);
@@ -238,17 +303,29 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
     const uint32_t parity = NST == 2 ? (n >> 1) & 1 : n & 1;
     if(!failed && !sm100::mbar_wait(&full[st], parity, A.spin)) failed = true;
     if(failed) continue;
-    const EmSingles& S_ = sgl[ss];
-    const TP*        box = reinterpret_cast<const TP*>(em_dyn + st * em_stage_bytes<TP>());
-    const int3       tt  = A.tiles[tile];
-    const int        rbn[3] = {min(B, v - tt.x * B), min(B, v - tt.y * B), min(B, v - tt.z * B)};
-    const bool       all_on = S_.slot_on[0] & S_.slot_on[1] & S_.slot_on[2] & S_.slot_on[3] & S_.slot_on[4] & S_.slot_on[5];
+    const EmSingles<SS, ES>& S_ = sgl[ss];
+    const TP*                box = reinterpret_cast<const TP*>(em_dyn + st * em_stage_bytes<TP>());
+    const int3               tt  = A.tiles[tile];
+    const int                rbn[3] = {min(B, v - tt.x * B), min(B, v - tt.y * B), min(B, v - tt.z * B)};
+    const bool all_on = S_.slot_on[0] & S_.slot_on[1] & S_.slot_on[2] & S_.slot_on[3] & S_.slot_on[4] & S_.slot_on[5];
 #pragma unroll
     for(int h = 0; h < 2; h++) {
       const int la = la_[h], lb = lb_[h], lc = lc_[h];
       if(la >= rbn[0] || lb >= rbn[1] || lc >= rbn[2]) continue;
       const int loc[3] = {la, lb, lc};
-      float     sg[6];
+      if constexpr(kF64) {
+        double sg[6], wv[6];
+        et_singles_f64(S_.Ojk, S_.Oik, S_.Oij, S_.ti, S_.tj, S_.tk, la, lb, lc, sg);
+#pragma unroll
+        for(int q = 0; q < 6; q++) {
+          const int x = loc[kPerm(q, 0)], y = loc[kPerm(q, 1)], z = loc[kPerm(q, 2)];
+          wv[q] = box[(0 * 6 + q) * B3 + (x * B + z) * B + y] + box[(1 * 6 + q) * B3 + (y * B + x) * B + z] +
+                  box[(2 * 6 + q) * B3 + (z * B + y) * B + x];
+        }
+        et_orbit_values_f64(wv, sg, S_.evs, S_.dab, all_on, S_.slot_on, la, lb, lc, A.want_sens, d4, d5, sens);
+        continue;
+      } else {
+      float sg[6];
       et_singles(S_.Ojk, S_.Oik, S_.Oij, S_.ti, S_.tj, S_.tk, la, lb, lc, sg);
       if constexpr(kF32) {
         float wv[6];
@@ -275,15 +352,20 @@ static __global__ void __launch_bounds__(EM_THREADS, (em_min_blocks<TP, NST>()))
         }
         et_orbit_values(wv, sg, S_.evs, S_.dab, all_on, S_.slot_on, la, lb, lc, A.want_sens, s4, s5, sens);
       }
+      }
     }
   }
   if(failed) atomicExch(A.err, 1);
   double* part = A.part + 6 * ((long long) slot * gridDim.x + blockIdx.x);
   CSum    c4, c5;
-  c4.add((double) s4.hi);
-  c4.add((double) s4.lo);
-  c5.add((double) s5.hi);
-  c5.add((double) s5.lo);
+  if constexpr(kF64) {
+    c4 = d4, c5 = d5;
+  } else {
+    c4.add((double) s4.hi);
+    c4.add((double) s4.lo);
+    c5.add((double) s5.hi);
+    c5.add((double) s5.lo);
+  }
   block_reduce_csum(c4, c5, part);
   __shared__ float ssum[EM_THREADS / 32];
 #pragma unroll

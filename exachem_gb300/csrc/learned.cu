@@ -209,7 +209,7 @@ double ccsdt_handle::truncation_estimate(float tail_sq, double sens) const {
 extern "C" ccsdt_status ccsdt_triplet_error_estimates(ccsdt_handle* h, const ccsdt_opts* opts, long n, const int* tri,
                                                       double* e_bracket, double* e_paren, double* est) {
   if(!h) return CCSDT_E_INVALID;
-  if(!opts || opts->mode != CCSDT_MODE_OZAKI || opts->p_storage < 0 || opts->p_storage > 2 || n < 0 ||
+  if(!opts || opts->mode != CCSDT_MODE_OZAKI || opts->p_storage < 0 || opts->p_storage > 3 || n < 0 ||
      (n && (!tri || !e_paren || !est)))
     return h->fail(CCSDT_E_INVALID, "ccsdt_triplet_error_estimates: needs CCSDT_MODE_OZAKI and output arrays");
   if(!h->uploaded) return h->fail(CCSDT_E_STATE, "ccsdt_triplet_error_estimates before ccsdt_upload");

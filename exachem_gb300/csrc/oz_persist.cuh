@@ -66,6 +66,8 @@ struct PzParams {
   float2*         F;          // P arrays of slot s: F + s * 3 v^3 (P12, P34, P56 consecutive)
   int             f32_out;    // store P rounded to FP32 (element e at ((float*) F)[e]) instead of
                               // float-float (F[e])
+  int             f64_out;    // store P in FP64 (element e at ((double*) F)[e]): the float-float
+                              // result widened (the exact fold of S <= 4 levels equals FP64's)
   const int*      ovvv_slot;  // (ia|bc) digit planes by slot: slot of occupied index z (nullable:
                               // slot = z; the Cholesky-direct mode's slab cache otherwise)
   const unsigned* order;      // cost-ordered item ids, length nitems
@@ -289,7 +291,12 @@ __device__ __forceinline__ bool pz_epilogue_item(const PzParams& P, const PzItem
     else run(true, false);
   }
   if(y < v) {
-    if(P.f32_out) { // the FP32 sums; the power-of-two scale is exact
+    if(P.f64_out) { // the float-float sums widened to FP64 (exact: 48 significant bits at most)
+      double* Cd = reinterpret_cast<double*>(P.F) + e0;
+#pragma unroll
+      for(int e = 0; e < COLS; e++)
+        if(n0 + e < v) Cd[(long long) (n0 + e) * v2] = ((double) hi[e] + (double) lo[e]) * (double) kScale;
+    } else if(P.f32_out) { // the FP32 sums; the power-of-two scale is exact
       float* Cf = reinterpret_cast<float*>(P.F) + e0;
 #pragma unroll
       for(int e = 0; e < COLS; e++)
@@ -541,8 +548,8 @@ __global__ void __launch_bounds__(PZ_THREADS, 1) oz_persist_kernel(const __grid_
         tsq       = 0.f;
         tail_slot = tp[3];
       }
-      if(!pz_epilogue_item<S, NT, C::NBUF, KC>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full, lvl_empty,
-                                  abort_flag)) {
+      if(!pz_epilogue_item<S, NT, C::NBUF, KC>(P, w, w.nb, tp, lane_base, c_lo, row, lane, term_it, tsq, lvl_full,
+                                               lvl_empty, abort_flag)) {
         fail();
         break;
       }

@@ -150,13 +150,15 @@ static int tma_energy_wave(int sm) {
   return std::max(1, std::min(kTiledBlocks, std::max(1, per) * std::max(1, sm)));
 }
 
-int ccsdt_handle::energy_tma_grid(bool f32, int nst) {
-  int& g = energy_tma_grid_[(f32 ? 1 : 0) + 2 * (nst - 1)];
+// kind: 0 float-float, 1 FP32, 2 FP64 partial arrays
+int ccsdt_handle::energy_tma_grid(int kind, int nst) {
+  int& g = energy_tma_grid_[kind + 3 * (nst - 1)];
   if(g > 0) return g;
   int sm = 0;
   cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, device);
-  g = f32 ? (nst == 2 ? tma_energy_wave<float, 2>(sm) : tma_energy_wave<float, 1>(sm))
-          : (nst == 2 ? tma_energy_wave<float2, 2>(sm) : tma_energy_wave<float2, 1>(sm));
+  g = kind == 1   ? (nst == 2 ? tma_energy_wave<float, 2>(sm) : tma_energy_wave<float, 1>(sm))
+      : kind == 2 ? tma_energy_wave<double, 1>(sm)
+                  : (nst == 2 ? tma_energy_wave<float2, 2>(sm) : tma_energy_wave<float2, 1>(sm));
   return g;
 }
 
@@ -174,9 +176,13 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   std::memcpy(p.maps, tmaps, sizeof(p.maps));
   p.tri = bt_tri, p.base = bt_ctrl + 2, p.nslots = nslots, p.o = o, p.v = v, p.kp_v = kp_v, p.kp_o = kp_o;
   p.F = bt_F;
-  const bool f32 = p_f32(S);
+  const bool f64 = p_storage == 3, f32 = !f64 && p_f32(S);
   p.f32_out      = f32;
+  p.f64_out      = f64;
   last_p_f32     = f32;
+  last_p_f64     = f64;
+  if(f64 && !ensure_pmap(false))
+    return fail(CCSDT_E_INVALID, "FP64 partial arrays need an even v (the energy reads them through TMA)");
   p.ovvv_slot    = ovvv_direct ? d_slab_of : nullptr;
   p.order = bt_order, p.nitems = (unsigned) nitems_override, p.err = d_err, p.tail = tails;
   // windows in multiples of 64 whatever the configuration's K chunk, so every configuration folds
@@ -219,10 +225,11 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
   if(tv[1]) cudaEventRecord(tv[1], stream);
   if(e == cudaSuccess) {
     int G = 0;
-    if(test_energy_passes != 1 && ensure_pmap(f32)) {
+    if(f64 || (test_energy_passes != 1 && ensure_pmap(f32))) {
       // the partial arrays staged by TMA, eighteen 8 x 8 x 8 boxes per work unit
       TmaEnergyArgs ta;
-      ta.pmap = pmap, ta.oovv = oovv_f, ta.t1 = t1_f, ta.eo = eo, ta.ev = ev, ta.tiles = (const int3*) e_tiles;
+      ta.pmap = pmap, ta.oovv = oovv_f, ta.t1 = t1_f, ta.oovv_d = oovv, ta.t1_d = t1, ta.eo = eo, ta.ev = ev;
+      ta.tiles = (const int3*) e_tiles;
       ta.ntiles = e_ntiles, ta.o = o, ta.v = v, ta.tri = bt_tri, ta.base = bt_ctrl + 2, ta.part = bt_part;
       ta.want_sens = sens != nullptr, ta.err = d_err;
       ta.spin       = test_spin_limit && test_skip_loads == 2 ? test_spin_limit : sm100::kSpinLimit;
@@ -230,10 +237,12 @@ ccsdt_status ccsdt_handle::launch_batch(int S, int nslots, int nitems_override, 
       // box stages: two for FP32 boxes (2 CTAs / SM), one for float-float boxes (2 CTAs / SM rather
       // than 1), the faster of the two for each element type on GB300; knob 2 takes the other
       const int nst_default = f32 ? 2 : 1;
-      const int nst         = test_energy_passes == 2 ? 3 - nst_default : nst_default;
-      G             = std::min(e_ntiles, energy_tma_grid(f32, nst));
+      const int nst         = f64 ? 1 : test_energy_passes == 2 ? 3 - nst_default : nst_default;
+      G                     = std::min(e_ntiles, energy_tma_grid(f64 ? 2 : f32 ? 1 : 0, nst));
       const dim3 grid(G, nslots);
-      if(f32 && nst == 2) energy_tma_batch_kernel<float, 2><<<grid, EM_THREADS, em_smem_bytes<float, 2>(), stream>>>(ta);
+      if(f64) energy_tma_batch_kernel<double, 1><<<grid, EM_THREADS, em_smem_bytes<double, 1>(), stream>>>(ta);
+      else if(f32 && nst == 2)
+        energy_tma_batch_kernel<float, 2><<<grid, EM_THREADS, em_smem_bytes<float, 2>(), stream>>>(ta);
       else if(f32) energy_tma_batch_kernel<float, 1><<<grid, EM_THREADS, em_smem_bytes<float, 1>(), stream>>>(ta);
       else if(nst == 2)
         energy_tma_batch_kernel<float2, 2><<<grid, EM_THREADS, em_smem_bytes<float2, 2>(), stream>>>(ta);

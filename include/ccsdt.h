@@ -85,7 +85,10 @@ typedef struct {
                              contraction and the energy: 0 FP32 for 1..3 digit planes (their
                              rounding, unbiased and averaged over a triplet's v^3 elements, moves
                              E(T) by ~1e-11 relative, far below the truncation of 3 planes),
-                             float-float from 4 planes on; 1 float-float always; 2 FP32 always */
+                             float-float from 4 planes on; 1 float-float always; 2 FP32 always;
+                             3 FP64: the digit levels folded and the terms summed in FP64, the
+                             energy's W, denominator division and compensated sums in FP64
+                             (needs an even v)                                                 */
   int    reserved[2];
 } ccsdt_opts;
 

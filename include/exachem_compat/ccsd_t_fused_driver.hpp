@@ -221,7 +221,7 @@ inline std::vector<float> read_slice_model(const std::string& path) {
 // Mode from the environment: EXACHEM_GB300_MODE = fp64 (default) | ozaki | learned,
 // EXACHEM_GB300_SLICES = digit planes (ozaki, default 3) or the largest count (learned, default 5),
 // EXACHEM_GB300_BUDGET = the learned mode's energy budget (default 1e-8),
-// EXACHEM_GB300_P_STORAGE = auto (default) | ff | f32: element type of the split path's partial arrays.
+// EXACHEM_GB300_P_STORAGE = auto (default) | ff | f32 | f64: element type of the split path's partial arrays.
 inline ccsdt_opts opts_from_env() {
   ccsdt_opts  op{};
   const char* m = std::getenv("EXACHEM_GB300_MODE");
@@ -245,7 +245,8 @@ inline ccsdt_opts opts_from_env() {
   if(pst == "auto") op.p_storage = 0;
   else if(pst == "ff") op.p_storage = 1;
   else if(pst == "f32") op.p_storage = 2;
-  else throw std::invalid_argument("EXACHEM_GB300_P_STORAGE must be auto, ff or f32: " + pst);
+  else if(pst == "f64") op.p_storage = 3;
+  else throw std::invalid_argument("EXACHEM_GB300_P_STORAGE must be auto, ff, f32 or f64: " + pst);
   return op;
 }
 

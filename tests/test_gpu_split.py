@@ -214,6 +214,30 @@ def test_tma_energy_equals_pass_by_pass(built, o, v, seed):
     assert lib.ccsdt_debug_set_energy_kernel(ft.h, 3) != 0
 
 
+@pytest.mark.parametrize("o,v,seed", [(3, 10, 31), (6, 40, 0), (4, 320, 9)])
+def test_fp64_partial_arrays(built, o, v, seed):
+    """p_storage = f64: the exactly folded levels widened to FP64 partial arrays and the energy in
+    FP64 (W sums, FP64 singles, division, compensated sums).  At six planes the result sits at the
+    FP64 path's to 1e-12 even on a tiny system, where the float-float energy's FP32 singles leave a
+    floor; at S = 3 it agrees with the float-float storage to the latter's own precision."""
+    from exachem_gb300.ccsd_t import CCSDTError
+    ft = _ft(o, v, seed)
+    ref = ft.energy("fp64")
+    r6 = ft.energy("ozaki", slices=6, p_storage="f64")
+    for key in ("e_bracket_T", "e_paren_T"):
+        assert abs(r6[key] - ref[key]) <= 1e-12 * abs(ref[key]), (key, r6[key], ref[key])
+    a = ft.energy("ozaki", slices=3, p_storage="f64")
+    b = ft.energy("ozaki", slices=3, p_storage="ff")
+    assert abs(a["e_paren_T"] - b["e_paren_T"]) <= 1e-10 * abs(b["e_paren_T"])
+    if v <= 40:
+        wf = ft.triplet_w(0, 1, 2, "fp64")
+        ws = ft.triplet_w(0, 1, 2, "ozaki", slices=6, p_storage="f64")
+        assert np.abs(ws - wf).max() <= 1e-12 * np.abs(wf).max()
+    odd = _ft(3, 9, 1)
+    with pytest.raises(CCSDTError):                 # the energy reads FP64 boxes through TMA
+        odd.energy("ozaki", slices=3, p_storage="f64")
+
+
 def _set_window(ft, k):
     import ctypes
     lib = ft.lib
