@@ -534,6 +534,8 @@ def main():
                     help="Cholesky-direct mode: whole call with (ia|bc) slab caches of these sizes vs the whole block")
     ap.add_argument("--n-chol", type=int, default=0, help="Cholesky vectors for --cholesky-direct (0: 4 (o + v))")
     ap.add_argument("--os-slices", default="3,4", help="--open-shell: slice counts of the split-precision calls")
+    ap.add_argument("--graph-sample", type=int, default=768,
+                    help="triplets of the eager vs CUDA-graph comparison (split mode; 0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
@@ -724,6 +726,25 @@ def main():
     # parity sample: evenly spread triplets, the FP64 path against each slice count (and the learned
     # mode), per-triplet relative errors and the error of their sum; the FP64 time of the sample
     # also gives the plain-FP64 whole-call projection (~9 hours at this size)
+    # the per-batch launch sequence replayed from a CUDA graph (opts.use_graph) against the eager
+    # launches the timed region uses (eager there: per-launch events feed the roofline), on a sample
+    cuda_graph = None
+    if rank == 0 and mode == "ozaki" and args.graph_sample > 0:
+        gs = spread_sample(mine, min(len(mine), args.graph_sample))
+        res = {}
+        for name, g_ in (("eager", 0), ("graph", 1)):
+            ft.triplet_energies(gs[:8], mode, use_graph=g_, **kw)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r4, r5 = ft.triplet_energies(gs, mode, use_graph=g_, **kw)
+            torch.cuda.synchronize()
+            res[name] = (time.perf_counter() - t0, r4, r5)
+        cuda_graph = {"triplets": int(len(gs)), "eager_s": res["eager"][0], "graph_s": res["graph"][0],
+                      "identical": bool(np.array_equal(res["eager"][2], res["graph"][2]) and
+                                        np.array_equal(res["eager"][1], res["graph"][1])),
+                      "graph_replays": "one capture of a batch's contraction, energy, reduction and base advance, "
+                                       "replayed for every full batch"}
+
     energy_sample, fp64_proj = None, None
     if rank == 0 and split and args.sample > 0:
         samp = spread_sample(tri_all, args.sample, offset=len(tri_all) // (2 * args.sample))
@@ -803,7 +824,7 @@ def main():
                             "warmup_steps": f"{args.warmup} x {max(1, args.warm_batch)} triplets",
                             "l2": "inputs (75 GB) and per-batch scratch (12 GB) exceed L2; no flush"},
             "roofline": roof, "throughput": throughput, "cpu_baseline": cpu, "e2e": e2e,
-            "gpu_launches": launches, "clocks": clk, "energy_sample": energy_sample,
+            "gpu_launches": launches, "clocks": clk, "energy_sample": energy_sample, "cuda_graph": cuda_graph,
             "partial_energy_timed": {"e_bracket_T": esum4, "e_paren_T": esum5},
             "fp64_projected_s": fp64_proj, "speedup_vs_fp64": (fp64_proj / value) if fp64_proj else None,
             "setup": {"generate_s": t_gen, "fp64_dgemm_tflops": fp64_peak},
