@@ -120,17 +120,24 @@ def test_adapter_cholesky_gather_is_exact(tmp_path, built):
 
 
 @pytest.mark.gpu
-def test_adapter_cholesky_call_matches_oracle(tmp_path, built):
+@pytest.mark.parametrize("slabs", [None, "4"])
+def test_adapter_cholesky_call_matches_oracle(tmp_path, built, slabs):
     """The Cholesky route end to end: cholVpr blocks -> gather_cholesky -> ccsdt_upload_cholesky
-    (integral blocks built on the GPU) -> E[T], E(T) against the oracle on the same integrals."""
+    (integral blocks built on the GPU) -> E[T], E(T) against the oracle on the same integrals; with
+    EXACHEM_GB300_OVVV_SLABS the adapter takes the Cholesky-direct mode ((ia|bc) formed slab by slab
+    into a cache of that many slabs) and must give the same energies."""
+    import os
     import oracle
     exe = _compile(tmp_path, link_lib=True)
     o, v, ot, vt, ci = 8, 40, [4, 4], [16, 12, 12], [10, 14]
     d, L = _cholesky_case(o, v, sum(ci), 22)
     _write(tmp_path / "in.bin", d, ot, vt)
     _write_chol(tmp_path / "chol.bin", L, ci)
+    env = {k: x for k, x in os.environ.items() if k != "EXACHEM_GB300_OVVV_SLABS"}
+    if slabs:
+        env["EXACHEM_GB300_OVVV_SLABS"] = slabs
     subprocess.run([str(exe), str(tmp_path / "in.bin"), str(tmp_path / "out.bin"), "--chol", str(tmp_path / "chol.bin"),
-                    "--run"], check=True)
+                    "--run"], check=True, env=env)
     nq = sum(ci)
     _, extra = _read(tmp_path / "out.bin", d, extra=(o * o + o * v + v * v) * nq + 2)
     e4, e5 = oracle.energy(d)
