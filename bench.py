@@ -409,8 +409,9 @@ def run_cholesky_direct(args):
         ts, s4, s5, bs = run(ft, tri, "ozaki", **kw)
         tf, g4, g5, bf = run(ft, fp64_tri, "fp64")
         rows.append({"max_ovvv_slabs": min(C, o), "split_call_s": ts, "split_slabs_formed": bs,
-                     "split_vs_whole": ts / t_split, "split_identical": bool(np.array_equal(s5, w5) and
-                                                                             np.array_equal(s4, w4)),
+                     "split_vs_whole": ts / t_split,
+                     "split_max_rel_diff": float(np.max(np.abs(s5 - w5) / np.maximum(np.abs(w5), 1e-300))),
+                     "split_rel_diff_of_sum": float(abs(s5.sum() - w5.sum()) / abs(w5.sum())),
                      "fp64_sample_s": tf, "fp64_slabs_formed": bf, "fp64_vs_whole": tf / t_fp64,
                      "fp64_identical": bool(np.array_equal(g5, f5) and np.array_equal(g4, f4)),
                      "cache_gb": min(C, o) * v ** 3 * 8 / 1e9})

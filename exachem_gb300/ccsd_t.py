@@ -56,7 +56,8 @@ EXPORTED = ["ccsdt_create", "ccsdt_upload", "ccsdt_energy", "ccsdt_triplet_energ
             "ccsdt_upload_begin", "ccsdt_upload_blocks", "ccsdt_upload_end", "ccsdt_upload_cholesky",
             "ccsdt_tile_configs", "ccsdt_autotune", "ccsdt_set_tile_config", "ccsdt_energy_spin_orbital",
             "ccsdt_debug_spin_orbital_plan", "ccsdt_reference_op_count_so", "ccsdt_upload_cholesky_direct",
-            "ccsdt_ovvv_slab_builds", "ccsdt_debug_slab_schedule", "ccsdt_energy_spin_orbital_split"]
+            "ccsdt_ovvv_slab_builds", "ccsdt_debug_slab_schedule", "ccsdt_energy_spin_orbital_split",
+            "ccsdt_debug_set_slab_build"]
 BLOCK_KINDS = {"t2": 0, "oovv": 1, "ooov": 2, "ovvv": 3}
 
 

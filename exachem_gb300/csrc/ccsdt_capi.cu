@@ -92,7 +92,7 @@ ccsdt_handle::~ccsdt_handle() {
   for(void* p: owned_bytes) cudaFree(p);
   for(void* p: slice_bufs) cudaFree(p);
   for(void* p: {(void*) bt_F, (void*) bt_part, (void*) bt_order, (void*) bt_order_partial, (void*) bt_ctrl, (void*) bt_tri,
-                (void*) chol_ov, (void*) chol_vv, (void*) d_slab_of})
+                (void*) chol_ov, (void*) chol_vv, (void*) d_slab_of, chol_planes})
     if(p) cudaFree(p);
   if(ev0) cudaEventDestroy(ev0);
   if(ev1) cudaEventDestroy(ev1);
@@ -171,6 +171,12 @@ ccsdt_status ccsdt_handle::finish_inputs(const char* who) {
   slices_ready = 0;
   slabs.reset(o, ovvv_direct ? (int) ovvv_nslab : 0);
   slab_sliced.assign(ovvv_direct ? ovvv_nslab : 0, 0);
+  slab_exact.assign(ovvv_direct ? ovvv_nslab : 0, 0);
+  slab_forms = 0;
+  if(chol_planes) { // digit planes of earlier vectors
+    cudaFree(chol_planes);
+    chol_planes = nullptr;
+  }
   return CCSDT_OK;
 }
 

@@ -79,6 +79,11 @@ struct ccsdt_handle {
   double *          chol_ov = nullptr, *chol_vv = nullptr; // L[i][a][Q], L[b][c][Q] (direct mode)
   ccsdt::SlabCache  slabs;
   std::vector<char> slab_sliced;             // the slot's digit planes are current
+  std::vector<char> slab_exact;              // the slot's slab was formed in FP64 (else by an Ozaki GEMM)
+  bool              slab_split_build = true; // split-path calls form slabs from digit planes of the vectors
+  long              slab_forms  = 0;         // slabs formed since the upload (re-formations included)
+  void*             chol_planes = nullptr;   // BF16 digit planes of L_ov and L_vv (+ row exponents)
+  long long         chol_kq     = 0;         // their padded Q extent
   int*              d_slab_of   = nullptr;   // index -> slot table read by the contraction kernel
   // makes the slabs of need[0..n) resident (formed and, with planes, sliced into digit planes)
   // and the device table current; a no-op outside the direct mode

@@ -158,22 +158,87 @@ extern "C" ccsdt_status ccsdt_upload_cholesky_direct(ccsdt_handle* h, const doub
                          chol_vv, on_device, max_ovvv_slabs);
 }
 
-// Forms the missing slabs (index x into slot c: (x a|b c) = sum_Q L[x][a][Q] L[b][c][Q], one DMMA
-// GEMM of v x v^2 x n_chol), slices them into the digit-plane slots when `planes`, and updates
-// the device index -> slot table.  Stream-ordered: a slot is overwritten only after the kernels
-// launched before on the handle's stream have finished reading it.
+namespace {
+constexpr int kCholSlices = 6; // digit planes of the vectors for the split-path slab formation
+
+// float-float values widened to FP64 in place (element e: 8 bytes either way)
+__global__ void __launch_bounds__(256) ff_to_f64_inplace_kernel(void* p, long long n) {
+  for(long long e = (long long) blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long) gridDim.x * blockDim.x) {
+    const float2 f                     = reinterpret_cast<const float2*>(p)[e];
+    reinterpret_cast<double*>(p)[e] = (double) f.x + (double) f.y;
+  }
+}
+} // namespace
+
+// Forms the missing slabs (index x into slot c: (x a|b c) = sum_Q L[x][a][Q] L[b][c][Q], a GEMM of
+// v x v^2 x n_chol), slices them into the digit-plane slots when `planes`, and updates the device
+// index -> slot table.  FP64 calls (planes false) form slabs with FP64 DMMA and re-form any
+// resident slab that was not; split-path calls (planes true) form them, unless slab_split_build is
+// off, as an Ozaki GEMM of kCholSlices BF16 digit planes of the vectors (mma.sync, exact FP32
+// level sums, float-float result widened to FP64; relative error ~1e-12 of the slab's scale,
+// far below the (T)'s own truncation at the slice counts the split path runs).  Stream-ordered: a
+// slot is overwritten only after the kernels launched before on the handle's stream have finished
+// reading it.
 ccsdt_status ccsdt_handle::ensure_ovvv(const int* need, int n, bool planes) {
   if(!ovvv_direct) return CCSDT_OK;
   std::vector<std::pair<int, int>> todo;
   if(!slabs.require(need, n, todo))
     return fail(CCSDT_E_INVALID, "more distinct occupied indices at once than (ia|bc) slab slots");
-  const long long vv = v, v3 = vv * vv * vv;
+  const long long vv = v, v3 = vv * vv * vv, oo = o;
+  const bool      split_build = planes && slab_split_build;
+  if(!planes) // FP64 calls read exact slabs only
+    for(int q = 0; q < n; q++) {
+      const int c = slabs.slot(need[q]);
+      if(!slab_exact[c] && std::find_if(todo.begin(), todo.end(), [&](const std::pair<int, int>& t) {
+                             return t.second == c;
+                           }) == todo.end())
+        todo.emplace_back(need[q], c);
+    }
+  if(split_build && !todo.empty() && !chol_planes) { // digit planes of L_ov and L_vv, once per upload
+    chol_kq               = (n_chol + 31) / 32 * 32;
+    const long long rows  = oo * vv + vv * vv;
+    const size_t    bytes = (size_t) kCholSlices * rows * chol_kq * 2 + (size_t) rows * 4;
+    if(ccsdt::dev_malloc(&chol_planes, bytes) != cudaSuccess) {
+      chol_planes = nullptr;
+      cudaGetLastError();
+      return fail(CCSDT_E_OOM, "(ia|bc) slab formation: digit planes of the Cholesky vectors");
+    }
+    auto*     pl   = static_cast<__nv_bfloat16*>(chol_planes);
+    int*      exps = reinterpret_cast<int*>(static_cast<char*>(chol_planes) + (size_t) kCholSlices * rows * chol_kq * 2);
+    oz_slice_rows_kernel<__nv_bfloat16><<<4096, 256, 0, stream>>>(chol_ov, oo * vv, n_chol, (int) chol_kq, kCholSlices,
+                                                                   pl, rows * chol_kq, exps, n_chol);
+    oz_slice_rows_kernel<__nv_bfloat16><<<4096, 256, 0, stream>>>(chol_vv, vv * vv, n_chol, (int) chol_kq, kCholSlices,
+                                                                   pl + oo * vv * chol_kq, rows * chol_kq,
+                                                                   exps + oo * vv, n_chol);
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("Cholesky vector slicing: ") + cudaGetErrorString(e));
+    launches += 2;
+  }
   for(auto& xc: todo) {
-    cudaError_t e = gemm_abt(chol_ov + (long long) xc.first * vv * n_chol, chol_vv, ovvv + xc.second * v3, vv, vv * vv,
-                             n_chol, stream);
+    double*     slot = ovvv + xc.second * v3;
+    cudaError_t e    = cudaSuccess;
+    if(split_build) {
+      const long long rows = oo * vv + vv * vv, plane = rows * chol_kq;
+      auto*           pl   = static_cast<const __nv_bfloat16*>(chol_planes);
+      OzBatch         b{};
+      b.S      = kCholSlices;
+      b.job[0] = OzJob{{OzTerm{pl + (long long) xc.first * vv * chol_kq, nullptr, oz_plain(), plane,
+                               pl + oo * vv * chol_kq, nullptr, oz_plain(), plane, (int) chol_kq, 1.f}},
+                       1, reinterpret_cast<float2*>(slot), vv, vv * vv, 0};
+      e = oz_gemm_bf16(b, 1, oz_gemm_tiles(vv, vv * vv), stream);
+      if(e == cudaSuccess) {
+        ff_to_f64_inplace_kernel<<<4096, 256, 0, stream>>>(slot, v3);
+        e = cudaGetLastError();
+      }
+      launches += 2;
+    } else {
+      e = gemm_abt(chol_ov + (long long) xc.first * vv * n_chol, chol_vv, slot, vv, vv * vv, n_chol, stream);
+      launches++;
+    }
     if(e != cudaSuccess) return fail(CCSDT_E_CUDA, std::string("(ia|bc) slab: ") + cudaGetErrorString(e));
     slab_sliced[xc.second] = 0;
-    launches++;
+    slab_exact[xc.second]  = !split_build;
+    slab_forms++;
   }
   if(planes) {
     if(!sl_ovvv || slices_ready <= 0 || slice_variant != 0)
@@ -198,7 +263,13 @@ ccsdt_status ccsdt_handle::ensure_ovvv(const int* need, int n, bool planes) {
   return CCSDT_OK;
 }
 
-extern "C" long ccsdt_ovvv_slab_builds(const ccsdt_handle* h) { return h ? h->slabs.builds() : -1; }
+extern "C" long ccsdt_ovvv_slab_builds(const ccsdt_handle* h) { return h ? h->slab_forms : -1; }
+
+extern "C" ccsdt_status ccsdt_debug_set_slab_build(ccsdt_handle* h, int split) {
+  if(!h || split < 0 || split > 1) return CCSDT_E_INVALID;
+  h->slab_split_build = split != 0;
+  return CCSDT_OK;
+}
 
 extern "C" ccsdt_status ccsdt_debug_slab_schedule(int o, int max_ovvv_slabs, int batch, long n, const int* tri,
                                                  long* order, long* builds) {

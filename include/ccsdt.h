@@ -173,8 +173,14 @@ ccsdt_status ccsdt_upload_cholesky_direct(ccsdt_handle* h, const double* eps_occ
                                           const double* t1, const double* t2, int n_chol, const double* chol_oo,
                                           const double* chol_ov, const double* chol_vv, int on_device,
                                           int max_ovvv_slabs);
-/* (ia|bc) slabs formed since the last upload (the Cholesky-direct mode; 0 otherwise). */
+/* (ia|bc) slabs formed since the last upload (the Cholesky-direct mode; 0 otherwise).  FP64 calls
+ * form slabs with FP64 DMMA GEMMs; split-path calls form them as Ozaki GEMMs of six BF16 digit
+ * planes of the vectors (relative error ~1e-12 of the slab's scale, far below the split (T)'s own),
+ * and an FP64 call re-forms in FP64 any such slab it reads. */
 long ccsdt_ovvv_slab_builds(const ccsdt_handle* h);
+/* Testing: split-path calls form slabs with FP64 DMMA too (split = 0) or from digit planes (1, the
+ * default). */
+ccsdt_status ccsdt_debug_set_slab_build(ccsdt_handle* h, int split);
 /* Testing, host only: the direct mode's visiting order (order[n]: triplet ids) and the number of
  * slabs it forms for triplets tri[3 n] run in batches of `batch` with max_ovvv_slabs slots;
  * CCSDT_E_STATE if a batch ever found a slab it needs missing. */
