@@ -55,3 +55,15 @@ def test_adapter_reads_the_model_file(tmp_path):
     assert int(out[0]) == len(p)
     assert abs(float(out[1]) - float(p.astype(np.float64).sum())) <= 1e-6 * max(1.0, abs(float(out[1])))
     assert abs(float(out[2]) - float((p.astype(np.float64) * w).sum())) <= 1e-6 * max(1.0, abs(float(out[2])))
+
+
+def test_opts_partial_array_storage_names():
+    """The Python options map the partial-array storage names onto opts.p_storage (0 auto, 1
+    float-float, 2 FP32, 3 FP64) and reject unknown ones."""
+    import pytest
+    from exachem_gb300.ccsd_t import FusedTriples
+    for name, code in (("auto", 0), ("ff", 1), ("f32", 2), ("f64", 3)):
+        assert FusedTriples.opts("ozaki", slices=2, p_storage=name).p_storage == code
+    assert FusedTriples.opts("ozaki", p_storage=3).p_storage == 3
+    with pytest.raises(KeyError):
+        FusedTriples.opts("ozaki", p_storage="fp16")
